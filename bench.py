@@ -1,0 +1,323 @@
+"""Benchmark of the MOL right-hand side (PeleC getMOLSrcTerm path) on GB300.
+
+    python bench.py [--gpus N --steps K --warmup W] [--impl gb300|reference]
+                    [--workload c2|c1] [--precision fp64]
+
+One step = one full-level RHS evaluation of the workload (default C2: one
+128^3 box of the 9-species premixed flame, FP64).  The value is cell-RHS
+evaluations per second over the K timed steps (device-resident inputs, CUDA
+events on the launch stream, barrier + synchronize on both sides, max over
+ranks).  ``e2e`` repeats the measurement through the public API with the
+state copied from pinned host memory and the RHS copied back every step.
+Under torchrun each rank evaluates its own box (weak scaling, no data-path
+collective).  ``--impl reference`` times the CPU restatement of the
+reference path (the oracle) on the host cores with all threads.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "MOL RHS cell-evals/s, 1 GB300: FP64 vs mixed at stated error; adjoint/fwd time"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="c2", choices=["c2", "c1"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def workload(name: str, seed: int = 1):
+    from pelec_gb300 import problems
+
+    if name == "c1":
+        mech, st = problems.tgv(64, seed=0)
+        desc = "C1: Taylor-Green vortex 64^3 periodic, 1 species, GammaLaw, constant transport"
+    else:
+        mech, st, _ = problems.flame((128, 128, 128), seed=seed)
+        desc = ("C2: premixed H2/air flame 128^3, dx=1e-3 cm, 9 species (synthetic NASA-7/transport table), "
+                "ideal-mixture EOS, mixture-averaged transport, periodic x/y, foextrap z")
+    return mech, st, desc
+
+
+def alg_bytes(st) -> int:
+    """Algorithmic bytes of one RHS: the stencil footprint (+-2) read once and
+    the RHS written once, FP64: 8 NVAR [(nx+4)(ny+4)(nz+4) + nx ny nz]."""
+    nx, ny, nz = st.shape
+    nvar = st.S.shape[0]
+    return 8 * nvar * ((nx + 4) * (ny + 4) * (nz + 4) + nx * ny * nz)
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        mhz, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                mhz.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not mhz:
+            return None
+        return {"sm_mhz": statistics.median(mhz), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(mhz)}
+
+
+def cpu_baseline(st, cfg, reps: int = 3) -> dict:
+    """The oracle (CPU restatement) on a z-slab of the same state, all threads."""
+    from oracle import pyoracle
+
+    nx, ny, nz = st.shape
+    kz = min(nz, 32)
+    k0 = st.lo[2] + (nz - kz) // 2
+    lo, hi = (st.lo[0], st.lo[1], k0), (st.hi[0], st.hi[1], k0 + kz - 1)
+    threads = pyoracle.max_threads()
+    times = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        pyoracle.mol_rhs_sub(cfg, st.S, st.begin, lo, hi, st.dx, nthreads=threads)
+        times.append(time.perf_counter() - t0)
+    cells = nx * ny * kz
+    return {"value": cells / statistics.median(times), "unit": "cell-evals/s", "cores": threads, "kind": "port",
+            "sample": f"{nx}x{ny}x{kz} z-slab of the same state, median of {reps}, OpenMP {threads} threads",
+            "best_s": min(times), "median_s": statistics.median(times)}
+
+
+def traffic_from_profiles(workload_name: str):
+    path = os.path.join(ROOT, "profiles", f"dram_traffic_{workload_name}_fp64.txt")
+    if not os.path.exists(path):
+        return None
+    for ln in open(path):
+        if ln.startswith("dram_bytes_per_rhs:"):
+            return float(ln.split(":", 1)[1])
+    return None
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    from oracle import build as ob
+
+    ob.build()
+    from pelec_gb300 import problems
+
+    mech, st, desc = workload(args.workload)
+    cfg = problems.make_config(mech)
+    for _ in range(args.warmup):
+        cpu_baseline(st, cfg, reps=1)
+    vals, meds = [], []
+    t0 = time.perf_counter()
+    res = None
+    for _ in range(args.steps):
+        res = cpu_baseline(st, cfg, reps=1)
+        vals.append(res["value"])
+        meds.append(res["median_s"])
+    elapsed = time.perf_counter() - t0
+    value = statistics.median(vals)
+    cb = {"value": value, "unit": "cell-evals/s", "cores": res["cores"], "kind": "port",
+          "sample": res["sample"].replace("median of 1", f"median of {args.steps} steps")}
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "cell-evals/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": desc, "precision": "fp64", "implementation":
+                       "CPU restatement of getMOLSrcTerm (oracle/), the reference's own build is not compilable here"},
+            "cpu_baseline": cb,
+            "e2e": {"value": value, "unit": "cell-evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def run_gpu(args):
+    import numpy as np
+    import torch
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+        pg = dist
+
+    from pelec_gb300 import build as cb
+
+    cb.build()
+    from pelec_gb300 import mol, problems
+
+    mech, st, desc = workload(args.workload, seed=1 + rank)
+    cfg = problems.make_config(mech, time_passes=1)
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        from oracle import build as ob
+
+        ob.build()
+        cpu = cpu_baseline(st, problems.make_config(mech))
+
+    op = mol.MOLOperator(cfg)
+    S_h = torch.from_numpy(np.ascontiguousarray(st.S)).pin_memory()
+    S = mol.MultiFab([(st.lo, st.hi)], st.S.shape[0], st.ng, fabs=[S_h.cuda()])
+    R = mol.MultiFab([(st.lo, st.hi)], st.S.shape[0], 0)
+    R_h = torch.empty(R.fabs[0].shape, dtype=torch.float64).pin_memory()
+    stream = torch.cuda.current_stream()
+    cells = st.ncells
+
+    def barrier():
+        if pg is not None:
+            pg.barrier()
+        torch.cuda.synchronize()
+
+    def maxover(x: float) -> float:
+        if pg is None:
+            return x
+        t = torch.tensor([x], device="cuda")
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        return float(t.item())
+
+    for _ in range(max(3, args.warmup)):
+        op.rhs_level(S, R, st.dx)
+    barrier()
+    # device-resident value
+    clocks = ClockSampler(local)
+    clocks.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    e0.record(stream)
+    for _ in range(args.steps):
+        op.rhs_level(S, R, st.dx)
+    e1.record(stream)
+    barrier()
+    clk = clocks.stop()
+    t_dev = maxover(e0.elapsed_time(e1) / 1e3)
+    # per-pass device time (events recorded by the library on the same stream)
+    tc, tf = [], []
+    for _ in range(args.steps):
+        op.rhs_level(S, R, st.dx)
+        a, b = op.pass_times()
+        tc.append(a)
+        tf.append(b)
+    status = op.status()
+    # end to end through the public API: pinned host -> device -> RHS -> host
+    barrier()
+    e0.record(stream)
+    for _ in range(args.steps):
+        S.fabs[0].copy_(S_h, non_blocking=True)
+        op.rhs_level(S, R, st.dx)
+        R_h.copy_(R.fabs[0], non_blocking=True)
+    e1.record(stream)
+    barrier()
+    t_e2e = maxover(e0.elapsed_time(e1) / 1e3)
+
+    if rank != 0:
+        if pg is not None:
+            pg.destroy_process_group()
+        return 0
+    value = world * cells * args.steps / t_dev
+    ms_cell, ms_flux = statistics.mean(tc), statistics.mean(tf)
+    ms_rhs = ms_cell + ms_flux
+    ab = alg_bytes(st)
+    import json as _json
+
+    peaks = _json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    achieved = ab / (ms_rhs * 1e-3) / 1e9
+    traffic = traffic_from_profiles(args.workload)
+    line = {
+        "metric": METRIC, "value": value, "unit": "cell-evals/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * t_dev / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": desc, "boxes_per_gpu": 1, "cells_per_gpu": cells, "nspec": mech.nspec,
+                   "precision": "fp64", "l2": "inputs larger than L2 (state %.0f MB, scratch records %.0f MB)" % (
+                       st.S.nbytes / 1e6, cells * (10 + 4 * mech.nspec) * 8 * 1.1 / 1e6)},
+        "e2e": {"value": world * cells * args.steps / t_e2e, "unit": "cell-evals/s",
+                "h2d_bytes_per_step": int(S_h.numel() * 8), "d2h_bytes_per_step": int(R_h.numel() * 8)},
+        "gpu_launches": 2 * args.steps,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": achieved / hbm_peak, "traffic": traffic,
+                     "kernel": "cell_kernel + flux_kernel (one RHS)",
+                     "alg_bytes_per_rhs": ab, "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)",
+                     "binding_resource": "FP64 pipe (see profiles/)"},
+        "passes_ms": {"cell_kernel": ms_cell, "flux_kernel": ms_flux},
+        "status": {"cells": status.cells, "newton_nonconverged": status.newton_nonconverged,
+                   "nonpositive_state": status.nonpositive_state, "nonfinite_output": status.nonfinite_output},
+        "clocks": clk,
+    }
+    if cpu is not None:
+        line["cpu_baseline"] = cpu
+    print(json.dumps(line))
+    if pg is not None:
+        pg.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

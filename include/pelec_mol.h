@@ -1,0 +1,196 @@
+/*
+ * pelec_mol.h — C ABI of the GB300-native method-of-lines right-hand side.
+ *
+ * This library replaces the per-box body of PeleC's MOL operator,
+ *   void PeleC::getMOLSrcTerm(const MultiFab& S, MultiFab& MOLSrcTerm,
+ *                             Real time, Real dt, Real flux_factor)
+ * (Source/PeleC.H:523-528, Source/Diffusion.cpp:4-681, regular-box branch),
+ * for one AMR level without embedded boundaries.  The caller keeps its
+ * MultiFabs, its MFIter loop and its ghost fill; it describes each box with a
+ * pc_box_desc (an AMReX Array4 restated as plain pointers and strides) and
+ * calls pc_mol_rhs_level once per level.
+ *
+ * Conventions
+ *   - All arrays are FP64, Array4 layout: element (i,j,k,n) lives at
+ *     p[(i-begin[0]) + (j-begin[1])*jstride + (k-begin[2])*kstride + n*nstride]
+ *     (i fastest, component slowest), as amrex::Array4 (AMReX_Array4.H).
+ *   - Conserved components follow Source/IndexDefines.H:6-13,60:
+ *     URHO=0, UMX=1, UMY=2, UMZ=3, UEDEN=4, UEINT=5, UTEMP=6, UFS=7..7+nspec-1,
+ *     NVAR = 7 + nspec (NUM_ADV = NUM_AUX = NUM_LIN = 0).
+ *   - Device pointers are CUDA device addresses on the current device.
+ *     Streams are passed as void* (a cudaStream_t; NULL = legacy default).
+ *   - Every entry point returns a pc_status_code; device code never traps.
+ *     Per-call diagnostic counters are read with pc_mol_last_status.
+ *   - A handle may be used by one host thread at a time.  Calls are
+ *     asynchronous on the given stream unless stated otherwise.
+ */
+#ifndef PELEC_MOL_H
+#define PELEC_MOL_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PC_MOL_ABI_VERSION 1
+#define PC_MAX_SPECIES 9
+
+/* Return codes. */
+typedef enum pc_status_code {
+  PC_OK = 0,
+  PC_ERR_INVALID_ARGUMENT = 1, /* bad pointer, box, stride or flag value   */
+  PC_ERR_UNSUPPORTED = 2,      /* configuration with no compiled kernel     */
+  PC_ERR_CUDA = 3,             /* a CUDA runtime call failed                */
+  PC_ERR_OUT_OF_MEMORY = 4,    /* scratch allocation failed                 */
+  PC_ERR_NO_DEVICE = 5,        /* no CUDA device visible                    */
+  PC_ERR_TOO_LARGE = 6         /* request exceeds a fixed-size limit        */
+} pc_status_code;
+
+/* Equation of state (PelePhysics EosType selected at compile time in the
+ * reference, Exec/Make.PeleC:74-115). */
+typedef enum pc_eos_kind {
+  PC_EOS_GAMMA_LAW = 0, /* calorically perfect gas, p = (gamma-1) rho e     */
+  PC_EOS_IDEAL_MIX = 1  /* ideal-gas mixture with NASA-7 species thermo     */
+} pc_eos_kind;
+
+/* Transport model (PelePhysics transport(), called from
+ * Source/TransCoeff.H:30-33). */
+typedef enum pc_transport_kind {
+  PC_TRANSPORT_CONSTANT = 0, /* mu, xi, lambda, rhoD fixed                  */
+  PC_TRANSPORT_SIMPLE = 1    /* mixture-averaged, Docs Algorithms.rst:510-566 */
+} pc_transport_kind;
+
+/* Arithmetic of the right-hand side. */
+typedef enum pc_precision {
+  PC_PRECISION_FP64 = 0, /* every operation in FP64                          */
+  PC_PRECISION_MIXED = 1 /* FP32 reconstruction, Riemann and diffusion
+                            fluxes; FP64 EOS Newton solve, mass-fraction
+                            renormalisation and flux-divergence accumulation */
+} pc_precision;
+
+/* Species data.  Thermodynamics is NASA-7 per species:
+ *   cp/R = a0 + a1 T + a2 T^2 + a3 T^3 + a4 T^4
+ *   h/(R T) = a0 + a1 T/2 + a2 T^2/3 + a3 T^3/4 + a4 T^4/5 + a5/T
+ * with the low set for T < tmid and the high set otherwise.
+ * Transport fits are ln(q) = c0 + c1 L + c2 L^2 + c3 L^3, L = ln T, for the
+ * pure-species viscosity (g/cm/s), conductivity (erg/cm/s/K) and the binary
+ * diffusion coefficient (cm^2/s) at pressure diff_pref (dyn/cm^2). */
+typedef struct pc_mechanism {
+  int nspec;
+  int pad_;
+  double mw[PC_MAX_SPECIES];       /* molecular weights, g/mol              */
+  double gamma;                    /* GammaLaw ratio of specific heats      */
+  double nasa_tmid[PC_MAX_SPECIES];
+  double nasa_lo[PC_MAX_SPECIES][7];
+  double nasa_hi[PC_MAX_SPECIES][7];
+  double visc_fit[PC_MAX_SPECIES][4];
+  double cond_fit[PC_MAX_SPECIES][4];
+  double diff_fit[PC_MAX_SPECIES][PC_MAX_SPECIES][4];
+  double bulk_ratio[PC_MAX_SPECIES]; /* xi = sum_k X_k bulk_ratio_k mu_k    */
+  double diff_pref;
+  /* Constant transport (Source/TransCoeff.H with Constant transport):     */
+  double const_mu, const_xi, const_lambda, const_rhoD;
+} pc_mechanism;
+
+/* Operator configuration: the static PeleC flags that shape
+ * getMOLSrcTerm (Source/Params/_cpp_parameters; defaults in
+ * Source/Params/param_includes/pelec_defaults.H:32-57). */
+typedef struct pc_mol_config {
+  int nspec;                   /* NUM_SPECIES: 1 or 9                        */
+  int eos;                     /* pc_eos_kind                                */
+  int transport;               /* pc_transport_kind                          */
+  int precision;               /* pc_precision                               */
+  int do_hydro;                /* pelec.do_hydro (do_mol is implied)         */
+  int diffuse_vel;             /* pelec.diffuse_vel                          */
+  int diffuse_temp;            /* pelec.diffuse_temp                         */
+  int diffuse_spec;            /* pelec.diffuse_spec                         */
+  int diffuse_enth;            /* pelec.diffuse_enth                         */
+  int plm_iorder;              /* slopes are on unless == 1: getMOLSrcTerm
+                                  passes plm_iorder as mol_iorder
+                                  (Diffusion.cpp:366-368, MOL.cpp:56)        */
+  int use_laxf_flux;           /* pelec.use_laxf_flux                        */
+  int transport_harmonic_mean; /* pelec.transport_harmonic_mean              */
+  int check_output;            /* count non-finite RHS entries               */
+  int newton_max_iter;         /* cap on the EOS temperature Newton (0: 50)  */
+  int time_passes;             /* record CUDA events around each pass        */
+  int pad_;
+  pc_mechanism mech;
+} pc_mol_config;
+
+/* An amrex::Array4<Real> restated. */
+typedef struct pc_array4 {
+  double* p;           /* address of element (begin, comp 0)                 */
+  long long jstride;   /* elements between j and j+1                         */
+  long long kstride;   /* elements between k and k+1                         */
+  long long nstride;   /* elements between components                        */
+  int begin[3];        /* smallEnd of the array's box                        */
+  int end[3];          /* bigEnd + 1                                         */
+  int ncomp;
+  int pad_;
+} pc_array4;
+
+/* One box of the level: its valid region (an MFIter tilebox), the state
+ * with ghost cells (at least 2 ghost layers must be filled; PeleC fills
+ * numGrow()=4, Source/PeleC.H:877-900) and the output on the valid region. */
+typedef struct pc_box_desc {
+  int lo[3];           /* valid box smallEnd                                 */
+  int hi[3];           /* valid box bigEnd                                   */
+  pc_array4 state;     /* S, NVAR components, read only                      */
+  pc_array4 rhs;       /* MOLSrcTerm, NVAR components, written on [lo,hi]    */
+} pc_box_desc;
+
+/* Diagnostic counters accumulated over the last pc_mol_rhs_level call. */
+typedef struct pc_mol_status {
+  long long cells;                 /* valid cells evaluated                  */
+  long long newton_nonconverged;   /* cells whose T solve hit the cap        */
+  long long nonpositive_state;     /* cells with rho, p or T <= 0 or NaN     */
+  long long nonfinite_output;      /* RHS entries that are NaN or Inf        */
+  int last_error;                  /* pc_status_code of the last call        */
+  int pad_;
+} pc_mol_status;
+
+typedef struct pc_mol_handle pc_mol_handle;
+
+/* ABI version of the loaded library (PC_MOL_ABI_VERSION). */
+int pc_mol_abi_version(void);
+
+/* Human-readable text for a pc_status_code. */
+const char* pc_mol_error_string(int code);
+
+/* Create an operator for one configuration.  Validates the flags, builds
+ * the device-side species tables and allocates the diagnostic counters on
+ * the current device.  Replaces the static setup that getMOLSrcTerm reads
+ * (trans_parms, the EOS functor, PeleC static flags). */
+int pc_mol_create(pc_mol_handle** out, const pc_mol_config* cfg);
+
+/* Release the handle, its scratch and its counters. */
+void pc_mol_destroy(pc_mol_handle* h);
+
+/* MOL right-hand side of every box of one level:
+ *   rhs = -(1/V) sum_d (F_d(hi face) - F_d(lo face)),
+ * F = diffusion flux + hyperbolic flux, extensive (times face area).
+ * Replaces the MFIter loop body of getMOLSrcTerm (Diffusion.cpp:85-679,
+ * regular boxes).  dx is geom.CellSize().  The caller owns all arrays; the
+ * handle owns the scratch it grows on demand.  Asynchronous on stream. */
+int pc_mol_rhs_level(pc_mol_handle* h, const pc_box_desc* boxes, int nboxes,
+                     const double dx[3], void* stream);
+
+/* Same result as pc_mol_rhs_level computed with one kernel launch per box
+ * and per pass (the per-box launch baseline). */
+int pc_mol_rhs_level_per_box(pc_mol_handle* h, const pc_box_desc* boxes,
+                             int nboxes, const double dx[3], void* stream);
+
+/* Synchronize the handle's last stream and copy the diagnostic counters of
+ * the last rhs call into *st. */
+int pc_mol_last_status(pc_mol_handle* h, pc_mol_status* st);
+
+/* With cfg.time_passes set: synchronize and return the device time in
+ * milliseconds of each pass of the last pc_mol_rhs_level call, measured with
+ * CUDA events on the call's stream: ms[0] = cell pass (primitives, EOS,
+ * transport), ms[1] = flux pass (faces and divergence).  n >= 2. */
+int pc_mol_pass_times(pc_mol_handle* h, double* ms, int n);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PELEC_MOL_H */

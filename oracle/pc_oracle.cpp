@@ -1,0 +1,171 @@
+// pc_oracle.cpp — ORACLE (test infrastructure): extern "C" entry points of the
+// CPU restatement in pc_oracle.hpp, loaded by oracle/pyoracle.py through
+// ctypes.  Only tests/, the smoke check and bench.py's CPU-baseline leg call
+// these.  Parity status: UNPINNED (see pc_oracle.hpp).
+#include "pc_oracle.hpp"
+
+#include <omp.h>
+
+using namespace orc;
+
+namespace {
+
+Arr<double> view(const pc_array4& a) {
+  Arr<double> v;
+  v.p = a.p;
+  v.js = a.jstride;
+  v.ks = a.kstride;
+  v.ns = a.nstride;
+  for (int d = 0; d < 3; ++d) v.b[d] = a.begin[d];
+  return v;
+}
+
+bool covers(const pc_array4& a, const Box& b) {
+  for (int d = 0; d < 3; ++d)
+    if (a.begin[d] > b.lo[d] || a.end[d] - 1 < b.hi[d]) return false;
+  return true;
+}
+
+template <int NS, class EOS, class TR>
+int run_box(const pc_mol_config& cfg, const EOS& eos, const TR& tr, const pc_box_desc& bd, const double dx[3],
+            long long& fails) {
+  Box vbox;
+  for (int d = 0; d < 3; ++d) { vbox.lo[d] = bd.lo[d]; vbox.hi[d] = bd.hi[d]; }
+  // The reference computes primitives on grow(vbox, 4); the state FAB must
+  // cover it (PeleC::numGrow() = 4 without EB).
+  if (!covers(bd.state, grow(vbox, 4)) || !covers(bd.rhs, vbox)) return PC_ERR_INVALID_ARGUMENT;
+  if (bd.state.ncomp < 7 + NS || bd.rhs.ncomp < 7 + NS) return PC_ERR_INVALID_ARGUMENT;
+  Arr<double> s = view(bd.state);
+  Arr<const double> sc;
+  sc.p = s.p;
+  sc.js = s.js;
+  sc.ks = s.ks;
+  sc.ns = s.ns;
+  for (int d = 0; d < 3; ++d) sc.b[d] = s.b[d];
+  mol_rhs_box<NS>(cfg, eos, tr, vbox, sc, view(bd.rhs), dx, fails);
+  return PC_OK;
+}
+
+template <int NS>
+int dispatch(const pc_mol_config& cfg, const pc_box_desc& bd, const double dx[3], long long& fails) {
+  const int maxit = cfg.newton_max_iter > 0 ? cfg.newton_max_iter : 50;
+  if (cfg.eos == PC_EOS_GAMMA_LAW) {
+    GammaLaw<NS> eos{&cfg.mech};
+    if (cfg.transport == PC_TRANSPORT_CONSTANT)
+      return run_box<NS>(cfg, eos, ConstantTransport<NS, GammaLaw<NS>>{&cfg.mech}, bd, dx, fails);
+    return run_box<NS>(cfg, eos, SimpleTransport<NS, GammaLaw<NS>>{&cfg.mech}, bd, dx, fails);
+  }
+  IdealMix<NS> eos{&cfg.mech, maxit};
+  if (cfg.transport == PC_TRANSPORT_CONSTANT)
+    return run_box<NS>(cfg, eos, ConstantTransport<NS, IdealMix<NS>>{&cfg.mech}, bd, dx, fails);
+  return run_box<NS>(cfg, eos, SimpleTransport<NS, IdealMix<NS>>{&cfg.mech}, bd, dx, fails);
+}
+
+}  // namespace
+
+extern "C" {
+
+// RHS of each box, as getMOLSrcTerm's MFIter loop.  Host pointers.
+int oracle_mol_rhs(const pc_mol_config* cfg, const pc_box_desc* boxes, int nboxes, const double dx[3], int nthreads,
+                   long long* newton_fail) {
+  if (!cfg || !boxes || nboxes < 0 || !dx) return PC_ERR_INVALID_ARGUMENT;
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+  long long fails = 0;
+  for (int b = 0; b < nboxes; ++b) {
+    int rc;
+    if (cfg->nspec == 1)
+      rc = dispatch<1>(*cfg, boxes[b], dx, fails);
+    else if (cfg->nspec == 9)
+      rc = dispatch<9>(*cfg, boxes[b], dx, fails);
+    else
+      return PC_ERR_UNSUPPORTED;
+    if (rc != PC_OK) return rc;
+  }
+  if (newton_fail) *newton_fail = fails;
+  return PC_OK;
+}
+
+// pc_ctoprim on one cell: U[NVAR] -> q[QVAR], qaux[6].
+int oracle_ctoprim_cell(const pc_mol_config* cfg, const double* U, double* q, double* qaux, int* newton_ok) {
+  const int ns = cfg->nspec;
+  Arr<const double> u;
+  u.p = U; u.js = 1; u.ks = 1; u.ns = 1;
+  Arr<double> qa, qx;
+  qa.p = q; qa.js = 1; qa.ks = 1; qa.ns = 1;
+  qx.p = qaux; qx.js = 1; qx.ks = 1; qx.ns = 1;
+  long long fails = 0;
+  const int maxit = cfg->newton_max_iter > 0 ? cfg->newton_max_iter : 50;
+  if (ns == 1 && cfg->eos == PC_EOS_GAMMA_LAW) {
+    ctoprim<1>(0, 0, 0, u, qa, qx, GammaLaw<1>{&cfg->mech}, fails);
+  } else if (ns == 9 && cfg->eos == PC_EOS_IDEAL_MIX) {
+    ctoprim<9>(0, 0, 0, u, qa, qx, IdealMix<9>{&cfg->mech, maxit}, fails);
+  } else if (ns == 1 && cfg->eos == PC_EOS_IDEAL_MIX) {
+    ctoprim<1>(0, 0, 0, u, qa, qx, IdealMix<1>{&cfg->mech, maxit}, fails);
+  } else if (ns == 9 && cfg->eos == PC_EOS_GAMMA_LAW) {
+    ctoprim<9>(0, 0, 0, u, qa, qx, GammaLaw<9>{&cfg->mech}, fails);
+  } else {
+    return PC_ERR_UNSUPPORTED;
+  }
+  if (newton_ok) *newton_ok = fails == 0;
+  return PC_OK;
+}
+
+// Mixture-averaged or constant transport on one cell: out = [rhoD(ns), mu, xi, lambda].
+int oracle_transport_cell(const pc_mol_config* cfg, double T, double rho, const double* Y, double* out) {
+  double mu, xi, lam;
+  if (cfg->nspec == 9 && cfg->eos == PC_EOS_IDEAL_MIX) {
+    IdealMix<9> eos{&cfg->mech, 50};
+    if (cfg->transport == PC_TRANSPORT_SIMPLE)
+      SimpleTransport<9, IdealMix<9>>{&cfg->mech}.transport(eos, T, rho, Y, out, mu, xi, lam);
+    else
+      ConstantTransport<9, IdealMix<9>>{&cfg->mech}.transport(eos, T, rho, Y, out, mu, xi, lam);
+    out[9] = mu; out[10] = xi; out[11] = lam;
+    return PC_OK;
+  }
+  if (cfg->nspec == 1 && cfg->eos == PC_EOS_GAMMA_LAW) {
+    GammaLaw<1> eos{&cfg->mech};
+    ConstantTransport<1, GammaLaw<1>>{&cfg->mech}.transport(eos, T, rho, Y, out, mu, xi, lam);
+    out[1] = mu; out[2] = xi; out[3] = lam;
+    return PC_OK;
+  }
+  return PC_ERR_UNSUPPORTED;
+}
+
+// Mixture thermodynamics at (T, Y): out = [e, cv, cp, Wbar] (IdealMix only).
+int oracle_thermo(const pc_mol_config* cfg, double T, const double* Y, double* out) {
+  if (cfg->nspec != 9 || cfg->eos != PC_EOS_IDEAL_MIX) return PC_ERR_UNSUPPORTED;
+  IdealMix<9> eos{&cfg->mech, 50};
+  double e, cv, cp, cv2, wbar;
+  eos.TY2E_Cv(T, Y, e, cv);
+  eos.TY2CpCv(T, Y, cp, cv2);
+  eos.Y2WBAR(Y, wbar);
+  out[0] = e; out[1] = cv; out[2] = cp; out[3] = wbar;
+  return PC_OK;
+}
+
+// riemann() on one face: returns flux[NVAR] (UTEMP slot 0) and ustar.
+int oracle_riemann_face(const pc_mol_config* cfg, const double* left, const double* right, double cav, double* flux,
+                        double* ustar) {
+  // left/right = [rho, un, ut1, ut2, p, Y(ns)]
+  if (cfg->nspec == 9 && cfg->eos == PC_EOS_IDEAL_MIX) {
+    IdealMix<9> eos{&cfg->mech, 50};
+    for (int n = 0; n < 16; ++n) flux[n] = 0.0;
+    riemann<9>(left[0], left[1], left[2], left[3], left[4], left + 5, right[0], right[1], right[2], right[3], right[4],
+               right + 5, cav, *ustar, flux[URHO], flux + UFS, flux[UMX], flux[UMY], flux[UMZ], flux[UEDEN],
+               flux[UEINT], eos);
+    return PC_OK;
+  }
+  if (cfg->nspec == 1 && cfg->eos == PC_EOS_GAMMA_LAW) {
+    GammaLaw<1> eos{&cfg->mech};
+    for (int n = 0; n < 8; ++n) flux[n] = 0.0;
+    riemann<1>(left[0], left[1], left[2], left[3], left[4], left + 5, right[0], right[1], right[2], right[3], right[4],
+               right + 5, cav, *ustar, flux[URHO], flux + UFS, flux[UMX], flux[UMY], flux[UMZ], flux[UEDEN],
+               flux[UEINT], eos);
+    return PC_OK;
+  }
+  return PC_ERR_UNSUPPORTED;
+}
+
+int oracle_max_threads(void) { return omp_get_max_threads(); }
+
+}  // extern "C"

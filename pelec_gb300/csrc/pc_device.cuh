@@ -1,0 +1,269 @@
+// pc_device.cuh — device-side physics of the MOL right-hand side (sm_103a).
+//
+// Pointwise pieces of PeleC's getMOLSrcTerm path, restructured for a GPU
+// whose FP64 pipe is the binding resource (GB300: ~1.2 TFLOP/s FP64 against
+// ~74 TFLOP/s FP32): species sums are contracted into mixture polynomial
+// coefficients once per state, reciprocals replace repeated divisions, and
+// dead EOS evaluations of the reference are skipped.  Each function names the
+// reference code whose result it reproduces.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <math_constants.h>
+#include <stdint.h>
+
+namespace pcg {
+
+constexpr double RU = 8.31446261815324e7;  // erg/(mol K)
+
+// Conserved and primitive indices, Source/IndexDefines.H:6-23.
+enum { URHO = 0, UMX = 1, UMY = 2, UMZ = 3, UEDEN = 4, UEINT = 5, UTEMP = 6, UFS = 7 };
+
+// Source/Constants.H:10-24.
+constexpr double kSmallU = 1.0e-12;
+constexpr double kSmallNum = 1.0e-8;
+#define PCG_VERY_SMALL_NUM (2.220446049250313e-16 * 1e-100)
+
+// Device copy of the species data in the form the kernels evaluate.
+// NASA-7 coefficients are folded with R/W_k: cpc[r][n][k] = (R/W_k) a_{n,k}
+// for n = 0..5, r = 0 below tmid and 1 above.
+template <int NS>
+struct DevMech {
+  double rW[NS];     // R / W_k
+  double gamma, gm1; // GammaLaw
+  double cpk[NS];    // GammaLaw cp_k = gamma/(gamma-1) R/W_k
+  double tmid;
+  double cpc[2][6][NS];
+  double visc[NS][4], cond[NS][4], bulk[NS];
+  double diff[(NS * (NS - 1)) / 2 + 1][4];  // pairs k<j in row order
+  double inv_pref;                          // 1 / diff_pref
+  double const_mu, const_xi, const_lam, const_rhoD;
+};
+
+// Operator flags (static PeleC parameters read by getMOLSrcTerm).
+struct DevFlags {
+  int do_hydro, diffuse_vel, diffuse_temp, diffuse_spec, diffuse_enth;
+  int slopes;  // plm_iorder != 1
+  int laxf, harmonic, check_output, newton_maxit;
+};
+
+// The FP64 arithmetic below is a fixed sequence of IEEE operations: explicit
+// fma() where a fused multiply-add is meant, and otherwise separate, correctly
+// rounded multiplies, adds, divisions and square roots (this translation unit
+// is compiled without multiply-add contraction).  The CPU restatement used
+// to check the kernels evaluates the same sequence.
+
+__device__ __forceinline__ double horner4(const double c[4], double L) {
+  return fma(L, fma(L, fma(L, c[3], c[2]), c[1]), c[0]);
+}
+
+// R/Wbar = sum_k Y_k R/W_k.
+template <int NS>
+__device__ __forceinline__ double mix_rw(const DevMech<NS>& m, const double* Y) {
+  double s = 0.0;
+#pragma unroll
+  for (int k = 0; k < NS; ++k) s = fma(Y[k], m.rW[k], s);
+  return s;
+}
+
+// Y2X: X_k = Y_k (R/W_k) / (R/Wbar).
+template <int NS>
+__device__ __forceinline__ void y2x(const DevMech<NS>& m, const double* Y, double rw, double* X) {
+#pragma unroll
+  for (int k = 0; k < NS; ++k) X[k] = Y[k] * m.rW[k] / rw;
+}
+
+// ---------------------------------------------------------------------------
+// GammaLaw EOS (calorically perfect gas).
+// ---------------------------------------------------------------------------
+template <int NS>
+struct GammaLawEos {
+  static constexpr bool kIdealMix = false;
+  // REY2T: T = e (gamma-1) / (R/Wbar).
+  __device__ static double rey2t(const DevMech<NS>& m, const double* /*Y*/, double rw, double e, double /*Tguess*/,
+                                 int /*maxit*/, bool& ok) {
+    ok = true;
+    return e * m.gm1 / rw;
+  }
+  // RPY2Cs / RTY2Cs: c = sqrt(gamma p / rho).
+  __device__ static double cs_rp(const DevMech<NS>& m, const double*, double, double rho, double p) {
+    return sqrt(m.gamma * p / rho);
+  }
+  __device__ static double cs_T(const DevMech<NS>& m, const double*, double, double rho, double /*T*/, double p) {
+    return sqrt(m.gamma * p / rho);
+  }
+  // RYP2E: e = p / ((gamma-1) rho).
+  __device__ static double e_rp(const DevMech<NS>& m, const double*, double, double rho, double p) {
+    return p / (m.gm1 * rho);
+  }
+  // T2Hi: h_k = cp_k T.
+  __device__ static void hi(const DevMech<NS>& m, double T, double* h) {
+#pragma unroll
+    for (int k = 0; k < NS; ++k) h[k] = m.cpk[k] * T;
+  }
+};
+
+// ---------------------------------------------------------------------------
+// Ideal-gas mixture with NASA-7 species thermodynamics, one range split tmid.
+// Mixture coefficients C_n = sum_k Y_k (R/W_k) a_{n,k}; then
+//   cv(T) = (C0 - rw) + T (C1 + T (C2 + T (C3 + T C4)))
+//   e(T)  = C5 + T ((C0 - rw) + T (C1/2 + T (C2/3 + T (C3/4 + T C4/5)))).
+// ---------------------------------------------------------------------------
+template <int NS>
+struct IdealMixEos {
+  static constexpr bool kIdealMix = true;
+  __device__ static int range(const DevMech<NS>& m, double T) { return (T < m.tmid) ? 0 : 1; }
+  __device__ static void coefs(const DevMech<NS>& m, const double* Y, int r, double C[6]) {
+#pragma unroll
+    for (int n = 0; n < 6; ++n) {
+      double s = 0.0;
+#pragma unroll
+      for (int k = 0; k < NS; ++k) s = fma(Y[k], m.cpc[r][n][k], s);
+      C[n] = s;
+    }
+  }
+  __device__ static double cv_of(const double C[6], double rw, double T) {
+    return (C[0] - rw) + T * fma(T, fma(T, fma(T, C[4], C[3]), C[2]), C[1]);
+  }
+  __device__ static double e_of(const double C[6], double rw, double T) {
+    const double p = fma(T, fma(T, fma(T, fma(T, C[4] * 0.2, C[3] * 0.25), C[2] * (1.0 / 3.0)), C[1] * 0.5), C[0] - rw);
+    return fma(T, p, C[5]);
+  }
+  // REY2T: Newton's method on e(T) = e from the guess U(UTEMP)
+  // (Utilities.H:285).  Steps clamped to +-1000 K, T >= 10 K, stop once
+  // |T_new - T| <= 1e-12 T_new; ok=false after maxit iterations.
+  __device__ static double rey2t(const DevMech<NS>& m, const double* Y, double rw, double ein, double Tguess,
+                                 int maxit, bool& ok) {
+    double t = Tguess;
+    if (!(t > 0.0) || !isfinite(t)) t = 1000.0;
+    int r = range(m, t);
+    double C[6];
+    coefs(m, Y, r, C);
+    ok = false;
+    for (int it = 0; it < maxit; ++it) {
+      const int rn = range(m, t);
+      if (rn != r) {
+        r = rn;
+        coefs(m, Y, r, C);
+      }
+      const double e = e_of(C, rw, t);
+      const double cv = cv_of(C, rw, t);
+      double dt = (ein - e) / cv;
+      if (dt > 1000.0) dt = 1000.0;
+      if (dt < -1000.0) dt = -1000.0;
+      double tn = t + dt;
+      if (tn < 10.0) tn = 10.0;
+      const bool conv = fabs(tn - t) <= 1e-12 * tn;
+      t = tn;
+      if (conv) {
+        ok = true;
+        break;
+      }
+    }
+    return t;
+  }
+  // c^2 = (cp/cv) p / rho, cp = cv + R/Wbar, at temperature T.
+  __device__ static double cs_T(const DevMech<NS>& m, const double* Y, double rw, double rho, double T, double p) {
+    double C[6];
+    coefs(m, Y, range(m, T), C);
+    const double cv = cv_of(C, rw, T);
+    return sqrt((cv + rw) / cv * p / rho);
+  }
+  // RPY2Cs: T = p / (rho R/Wbar).
+  __device__ static double cs_rp(const DevMech<NS>& m, const double* Y, double rw, double rho, double p) {
+    return cs_T(m, Y, rw, rho, p / (rho * rw), p);
+  }
+  // RYP2E.
+  __device__ static double e_rp(const DevMech<NS>& m, const double* Y, double rw, double rho, double p) {
+    const double T = p / (rho * rw);
+    double C[6];
+    coefs(m, Y, range(m, T), C);
+    return e_of(C, rw, T);
+  }
+  // T2Hi: h_k = c5 + T (c0 + T (c1/2 + T (c2/3 + T (c3/4 + T c4/5)))), c = (R/W_k) a.
+  __device__ static void hi(const DevMech<NS>& m, double T, double* h) {
+    const int r = range(m, T);
+#pragma unroll
+    for (int k = 0; k < NS; ++k) {
+      const double p = fma(T, fma(T, fma(T, fma(T, m.cpc[r][4][k] * 0.2, m.cpc[r][3][k] * 0.25),
+                                           m.cpc[r][2][k] * (1.0 / 3.0)),
+                                  m.cpc[r][1][k] * 0.5),
+                           m.cpc[r][0][k]);
+      h[k] = fma(T, p, m.cpc[r][5][k]);
+    }
+  }
+};
+
+// ---------------------------------------------------------------------------
+// Transport (pc_transcoeff, Source/TransCoeff.H:7-37).
+// out layout: rhoD[NS], mu, xi, lambda (dComp_* of IndexDefines.H:39-42).
+// ---------------------------------------------------------------------------
+template <int NS>
+struct ConstantTransport {
+  __device__ static void eval(const DevMech<NS>& m, double, double, double, const double*, const double*, double* out) {
+#pragma unroll
+    for (int k = 0; k < NS; ++k) out[k] = m.const_rhoD;
+    out[NS] = m.const_mu;
+    out[NS + 1] = m.const_xi;
+    out[NS + 2] = m.const_lam;
+  }
+};
+
+// Mixture-averaged transport (Docs/sphinx/Algorithms.rst:540-566):
+// mu = (sum X mu_k^6)^(1/6), lambda = (sum X lambda_k^(1/4))^4,
+// xi = sum X bulk_k mu_k, rhoD_k = rho (1-Y_k) / sum_{j!=k} max(X_j,1e-15) /
+// D_kj(T,p), 1/D_kj(T,p) = exp(-fit_kj(ln T)) p / p_ref.
+template <int NS>
+struct SimpleTransport {
+  __device__ static void eval(const DevMech<NS>& m, double T, double rho, double p, const double* Y, const double* X,
+                              double* out) {
+    const double L = log(T);
+    double smu = 0.0, slam = 0.0, sxi = 0.0;
+#pragma unroll
+    for (int k = 0; k < NS; ++k) {
+      const double mk = exp(horner4(m.visc[k], L));
+      const double m2 = mk * mk;
+      smu = fma(X[k], m2 * m2 * m2, smu);
+      slam = fma(X[k], exp(0.25 * horner4(m.cond[k], L)), slam);
+      sxi = fma(X[k], m.bulk[k] * mk, sxi);
+    }
+    double s[NS];
+#pragma unroll
+    for (int k = 0; k < NS; ++k) s[k] = 0.0;
+    const double pr = p * m.inv_pref;
+    int q = 0;
+#pragma unroll
+    for (int k = 0; k < NS; ++k) {
+#pragma unroll
+      for (int j = k + 1; j < NS; ++j, ++q) {
+        const double invD = exp(-horner4(m.diff[q], L)) * pr;
+        s[k] = fma(fmax(X[j], 1e-15), invD, s[k]);
+        s[j] = fma(fmax(X[k], 1e-15), invD, s[j]);
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < NS; ++k) out[k] = (s[k] > 0.0) ? rho * (1.0 - Y[k]) / s[k] : 0.0;
+    out[NS] = exp(log(smu) * (1.0 / 6.0));
+    out[NS + 1] = sxi;
+    const double l2 = slam * slam;
+    out[NS + 2] = l2 * l2;
+  }
+};
+
+// pc_move_transcoefs_to_ec, Source/Utilities.H:322-342.
+__device__ __forceinline__ double face_coef(double a, double b, bool harmonic) {
+  if (harmonic) {
+    const double ab = a * b;
+    return (ab > 0.0) ? 2.0 * ab / (a + b) : 0.0;
+  }
+  return 0.5 * (a + b);
+}
+
+// MC-type limiter of mol_slope, Source/MOL.H:104-112.
+__device__ __forceinline__ double mc_limit(double dl, double dr) {
+  const double dcen = 0.5 * (dl + dr);
+  const double dlim = (dl * dr >= 0.0) ? 2.0 * fmin(fabs(dl), fabs(dr)) : 0.0;
+  return copysign(1.0, dcen) * fmin(dlim, fabs(dcen));
+}
+
+}  // namespace pcg

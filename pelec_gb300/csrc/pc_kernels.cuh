@@ -1,0 +1,506 @@
+// pc_kernels.cuh — the two passes of the MOL right-hand side on one level.
+//
+// Pass 1 (cell_kernel): one thread per cell of grow(valid, 2) of every box.
+//   Conserved -> primitive conversion with the EOS temperature solve
+//   (pc_ctoprim, Source/Utilities.H:239-320) and, on grow(valid, 1), the
+//   per-cell diffusion data: transport coefficients (pc_transcoeff,
+//   Source/TransCoeff.H:7-37), mole fractions (Y2X) and species enthalpies
+//   (T2Hi) used by SpeciesEnergyFlux (Source/Diffterm.H:20-75).  The record is
+//   written once per cell, structure-of-arrays, into the handle's scratch.
+//
+// Pass 2 (flux_kernel): one CTA per 8x8x4 tile of valid cells.  For each
+//   direction the CTA evaluates every face of the tile exactly once — MOL
+//   slopes (mol_slope, MOL.H:28-113), face states (MOL.cpp:69-123), the
+//   approximate Riemann solver (riemann, Riemann.H:6-200) or Lax-Friedrichs
+//   (Riemann.H:202-307), and the viscous/thermal/species diffusion flux
+//   (pc_diffusion_flux, Diffterm.H:344-461) — stages the NVAR face fluxes in
+//   shared memory and accumulates the divergence (pc_flux_div,
+//   Diffterm.H:463-484) in registers; the RHS is written once.
+//
+// The expensive per-cell work (Newton solve, ~55 exponentials of the
+// mixture-averaged transport) is done once per cell and each face flux once
+// per face: on GB300 the FP64 pipe, not HBM, bounds this computation.
+#pragma once
+
+#include "pc_device.cuh"
+
+namespace pcg {
+
+struct DevBox {
+  int lo[3], hi[3];
+  const double* S;
+  long long sj, sk, sn;
+  int sb[3];
+  int pad0;
+  double* R;
+  long long rj, rk, rn;
+  int rb[3];
+  int pad1;
+  double* rec;       // scratch records of this box: field f of cell c at rec[f*ncell + c]
+  long long ncell;   // cells of grow(valid, 2)
+  int g2lo[3];       // smallEnd of grow(valid, 2)
+  int n2[3];         // extents of grow(valid, 2)
+};
+
+struct Geo {
+  double dxinv[3];
+  double area[3];
+  double vol;
+};
+
+// Record fields (pass 1 -> pass 2).
+template <int NS>
+struct Rec {
+  static constexpr int RHO = 0, U = 1, V = 2, W = 3, P = 4, C = 5, Y = 6;
+  static constexpr int T = 6 + NS, X = 7 + NS, H = 7 + 2 * NS, D = 7 + 3 * NS;
+  static constexpr int MU = 7 + 4 * NS, XI = 8 + 4 * NS, LAM = 9 + 4 * NS;
+  static constexpr int N = 10 + 4 * NS;
+};
+
+enum { kCounterCells = 0, kCounterNewton = 1, kCounterNonpos = 2, kCounterNonfinite = 3, kNumCounters = 4 };
+
+__device__ __forceinline__ void warp_count(unsigned long long* ctr, bool pred) {
+  const unsigned m = __ballot_sync(0xffffffffu, pred);
+  if ((threadIdx.x & 31) == 0 && m) atomicAdd(ctr, (unsigned long long)__popc(m));
+}
+
+constexpr int kCellThreads = 256;
+
+// ---------------------------------------------------------------------------
+// Pass 1.
+// items[b] = (box index, first cell of the 256-cell chunk in grow(valid,2)).
+// ---------------------------------------------------------------------------
+template <int NS, class EOS, class TR>
+__global__ void __launch_bounds__(kCellThreads)
+    cell_kernel(const DevBox* __restrict__ boxes, const int2* __restrict__ items, const __grid_constant__ DevMech<NS> m,
+                const DevFlags f, unsigned long long* __restrict__ counters) {
+  using RC = Rec<NS>;
+  const int2 it = items[blockIdx.x];
+  const DevBox& b = boxes[it.x];
+  const long long c = (long long)it.y + threadIdx.x;
+  const bool active = c < b.ncell;
+  bool newton_fail = false, nonpos = false;
+  if (active) {
+    const int nx = b.n2[0], ny = b.n2[1];
+    const int i = b.g2lo[0] + (int)(c % nx);
+    const int j = b.g2lo[1] + (int)((c / nx) % ny);
+    const int k = b.g2lo[2] + (int)(c / ((long long)nx * ny));
+    const double* s = b.S + (i - b.sb[0]) + (long long)(j - b.sb[1]) * b.sj + (long long)(k - b.sb[2]) * b.sk;
+    const long long sn = b.sn;
+    // pc_ctoprim
+    const double rho = __ldg(s + URHO * sn);
+    const double rhoinv = 1.0 / rho;
+    const double vx = __ldg(s + UMX * sn) * rhoinv;
+    const double vy = __ldg(s + UMY * sn) * rhoinv;
+    const double vz = __ldg(s + UMZ * sn) * rhoinv;
+    const double kineng = 0.5 * rho * (vx * vx + vy * vy + vz * vz);
+    const double e = (__ldg(s + UEDEN * sn) - kineng) * rhoinv;
+    double Y[NS];
+#pragma unroll
+    for (int n = 0; n < NS; ++n) {
+      double y = __ldg(s + (UFS + n) * sn) / rho;
+      if (-1e-4 * 2.220446049250313e-16 < y && y < 1e-4 * 2.220446049250313e-16) y = 0.0;
+      Y[n] = y;
+    }
+    const double rw = mix_rw<NS>(m, Y);
+    bool ok = true;
+    const double T = EOS::rey2t(m, Y, rw, e, __ldg(s + UTEMP * sn), f.newton_maxit, ok);
+    const double p = rho * rw * T;  // RTY2P
+    const double cs = EOS::cs_T(m, Y, rw, rho, T, p);  // RTY2Cs
+    newton_fail = !ok;
+    nonpos = !(rho > 0.0) || !(p > 0.0) || !(T > 0.0);
+    double* r = b.rec + c;
+    const long long N = b.ncell;
+    r[RC::RHO * N] = rho;
+    r[RC::U * N] = vx;
+    r[RC::V * N] = vy;
+    r[RC::W * N] = vz;
+    r[RC::P * N] = p;
+    r[RC::C * N] = cs;
+#pragma unroll
+    for (int n = 0; n < NS; ++n) r[(RC::Y + n) * N] = Y[n];
+    const bool inner = i >= b.lo[0] - 1 && i <= b.hi[0] + 1 && j >= b.lo[1] - 1 && j <= b.hi[1] + 1 &&
+                       k >= b.lo[2] - 1 && k <= b.hi[2] + 1;
+    if (inner) {
+      // Mole fractions (Y2X) and enthalpies (T2Hi) of the cell.
+      double X[NS];
+      y2x(m, Y, rw, X);
+      double out[NS + 3];
+      TR::eval(m, T, rho, p, Y, X, out);
+      r[RC::T * N] = T;
+#pragma unroll
+      for (int n = 0; n < NS; ++n) r[(RC::X + n) * N] = X[n];
+      double h[NS];
+      EOS::hi(m, T, h);
+#pragma unroll
+      for (int n = 0; n < NS; ++n) r[(RC::H + n) * N] = h[n];
+#pragma unroll
+      for (int n = 0; n < NS + 3; ++n) r[(RC::D + n) * N] = out[n];
+    }
+  }
+  warp_count(&counters[kCounterNewton], newton_fail);
+  warp_count(&counters[kCounterNonpos], nonpos);
+}
+
+// ---------------------------------------------------------------------------
+// Face flux (extensive, times area) on the low face of cell (i,j,k) in
+// direction d; F has NVAR = 7 + NS entries.
+// ---------------------------------------------------------------------------
+template <int NS, class EOS, int d>
+__device__ __forceinline__ void hydro_face(const DevBox& b, const DevMech<NS>& m, const DevFlags& f, long long cR,
+                                           long long st, double* F) {
+  using RC = Rec<NS>;
+  const double* rec = b.rec;
+  const long long N = b.ncell;
+  const long long cL = cR - st, cLL = cL - st, cRR = cR + st;
+  auto ld = [&](int fld, long long c) { return __ldg(rec + (long long)fld * N + c); };
+  const int fun = RC::U + d;
+  const int fut1 = (d == 0) ? RC::V : RC::U;
+  const int fut2 = (d == 2) ? RC::V : RC::W;
+  const double rLL = ld(RC::RHO, cLL), rL = ld(RC::RHO, cL), rR = ld(RC::RHO, cR), rRR = ld(RC::RHO, cRR);
+  const double pLL = ld(RC::P, cLL), pL = ld(RC::P, cL), pR = ld(RC::P, cR), pRR = ld(RC::P, cRR);
+  const double uLL = ld(fun, cLL), uL = ld(fun, cL), uR = ld(fun, cR), uRR = ld(fun, cRR);
+  const double cLc = ld(RC::C, cL), cRc = ld(RC::C, cR);
+  const double t1L = ld(fut1, cL), t1R = ld(fut1, cR), t2L = ld(fut2, cL), t2R = ld(fut2, cR);
+
+  // Characteristic slopes of cells L and R (mol_slope), components 0..3.
+  double dqL[4] = {0.0, 0.0, 0.0, 0.0}, dqR[4] = {0.0, 0.0, 0.0, 0.0};
+  const bool slopes = f.slopes != 0;
+  const double dpl = pL - pLL, dpc = pR - pL, dpr = pRR - pR;
+  if (slopes) {
+    const double t1LL = ld(fut1, cLL), t1RR = ld(fut1, cRR), t2LL = ld(fut2, cLL), t2RR = ld(fut2, cRR);
+    {
+      const double a = 0.5 * dpl / cLc, bb = 0.5 * rL * (uL - uLL);
+      const double a2 = 0.5 * dpc / cLc, b2 = 0.5 * rL * (uR - uL);
+      dqL[0] = mc_limit(a - bb, a2 - b2);
+      dqL[1] = mc_limit(a + bb, a2 + b2);
+      dqL[2] = mc_limit(t1L - t1LL, t1R - t1L);
+      dqL[3] = mc_limit(t2L - t2LL, t2R - t2L);
+    }
+    {
+      const double a = 0.5 * dpc / cRc, bb = 0.5 * rR * (uR - uL);
+      const double a2 = 0.5 * dpr / cRc, b2 = 0.5 * rR * (uRR - uR);
+      dqR[0] = mc_limit(a - bb, a2 - b2);
+      dqR[1] = mc_limit(a + bb, a2 + b2);
+      dqR[2] = mc_limit(t1R - t1L, t1RR - t1R);
+      dqR[3] = mc_limit(t2R - t2L, t2RR - t2R);
+    }
+  }
+  // Face states (MOL.cpp:69-123).
+  const double unl = uL + 0.5 * ((dqL[1] - dqL[0]) / rL);
+  const double pl = pL + 0.5 * (dqL[0] + dqL[1]) * cLc;
+  const double ut1l = t1L + 0.5 * dqL[2];
+  const double ut2l = t2L + 0.5 * dqL[3];
+  const double unr = uR - 0.5 * ((dqR[1] - dqR[0]) / rR);
+  const double pr = pR - 0.5 * (dqR[0] + dqR[1]) * cRc;
+  const double ut1r = t1R - 0.5 * dqR[2];
+  const double ut2r = t2R - 0.5 * dqR[3];
+  double spl[NS], spr[NS];
+  double rl = 0.0, rr = 0.0;
+  {
+    const double sL = dqL[0] + dqL[1], sR = dqR[0] + dqR[1];
+    const double cL2 = cLc * cLc, cR2 = cRc * cRc;
+#pragma unroll
+    for (int n = 0; n < NS; ++n) {
+      const double yLL = ld(RC::Y + n, cLL), yL = ld(RC::Y + n, cL), yR = ld(RC::Y + n, cR), yRR = ld(RC::Y + n, cRR);
+      double dsL = 0.0, dsR = 0.0;
+      if (slopes) {
+        const double ryL = rL * yL, ryR = rR * yR;
+        dsL = mc_limit(ryL - rLL * yLL - yL * dpl / cL2, ryR - ryL - yL * dpc / cL2);
+        dsR = mc_limit(ryR - ryL - yR * dpc / cR2, rRR * yRR - ryR - yR * dpr / cR2);
+      }
+      spl[n] = yL * rL + 0.5 * (dsL + yL * sL / cLc);
+      spr[n] = yR * rR - 0.5 * (dsR + yR * sR / cRc);
+      rl += spl[n];
+      rr += spr[n];
+    }
+#pragma unroll
+    for (int n = 0; n < NS; ++n) {
+      spl[n] = spl[n] / rl;
+      spr[n] = spr[n] / rr;
+    }
+  }
+  const double cavg = 0.5 * (cRc + cLc);
+  double fl_rho, fl_un, fl_ut1, fl_ut2, fl_E, fl_ei;
+  double flY[NS];
+  const double rwl = mix_rw<NS>(m, spl), rwr = mix_rw<NS>(m, spr);
+  const double cl = EOS::cs_rp(m, spl, rwl, rl, pl);
+  const double cr = EOS::cs_rp(m, spr, rwr, rr, pr);
+  if (!f.laxf) {
+    // riemann(), Source/Riemann.H:42-199.
+    const double wsmall = 2.2250738585072014e-308;
+    const double wl = fmax(wsmall, cl * rl);
+    const double wr = fmax(wsmall, cr * rr);
+    const double pstar = fmax(wsmall, ((wr * pl + wl * pr) + wl * wr * (unl - unr)) / (wl + wr));
+    double ustar = ((wl * unl + wr * unr) + (pl - pr)) / (wl + wr);
+    bool mask = ustar > 0.0;
+    double rspo[NS];
+    double uo = mask ? unl : unr;
+    double po = mask ? pl : pr;
+    const bool m0 = fabs(ustar) < kSmallU * 0.5 * (fabs(unl) + fabs(unr)) || ustar == 0.0;
+    ustar = m0 ? 0.0 : ustar;
+    double ro = 0.0;
+#pragma unroll
+    for (int n = 0; n < NS; ++n) {
+      const double a = rl * spl[n], bq = rr * spr[n];
+      rspo[n] = m0 ? 0.5 * (a + bq) : (mask ? a : bq);
+      ro += rspo[n];
+    }
+    uo = m0 ? 0.5 * (unl + unr) : uo;
+    po = m0 ? 0.5 * (pl + pr) : po;
+    double Yt[NS];
+#pragma unroll
+    for (int n = 0; n < NS; ++n) Yt[n] = rspo[n] / ro;
+    const double co = EOS::cs_rp(m, Yt, mix_rw<NS>(m, Yt), ro, po);
+    const double drho = (pstar - po) / (co * co);
+    double rspstar[NS];
+    double rstar = 0.0;
+#pragma unroll
+    for (int n = 0; n < NS; ++n) {
+      rspstar[n] = fmax(0.0, rspo[n] + drho * Yt[n]);
+      rstar += rspstar[n];
+    }
+#pragma unroll
+    for (int n = 0; n < NS; ++n) Yt[n] = rspstar[n] / rstar;
+    const double cstar = EOS::cs_rp(m, Yt, mix_rw<NS>(m, Yt), rstar, pstar);
+    const double sgnm = copysign(1.0, ustar);
+    double spout = co - sgnm * uo;
+    double spin = cstar - sgnm * ustar;
+    const double ushock = 0.5 * (spin + spout);
+    mask = pstar < po;
+    spout = mask ? spout : ushock;
+    spin = mask ? spin : ushock;
+    const double scr = (fabs(spout - spin) < PCG_VERY_SMALL_NUM) ? kSmallNum * cavg : spout - spin;
+    const double frac = fmax(0.0, fmin(1.0, (1.0 + (spout + spin) / scr) * 0.5));
+    mask = ustar > 0.0;
+    double iv1 = mask ? ut1l : ut1r;
+    double iv2 = mask ? ut2l : ut2r;
+    mask = (ustar == 0.0);
+    iv1 = mask ? 0.5 * (ut1l + ut1r) : iv1;
+    iv2 = mask ? 0.5 * (ut2l + ut2r) : iv2;
+    const bool mout = spout < 0.0, min_ = spin >= 0.0;
+    double iu = frac * ustar + (1.0 - frac) * uo;
+    double gdp = frac * pstar + (1.0 - frac) * po;
+    iu = mout ? uo : iu;
+    gdp = mout ? po : gdp;
+    iu = min_ ? ustar : iu;
+    gdp = min_ ? pstar : gdp;
+    double rgd = 0.0;
+#pragma unroll
+    for (int n = 0; n < NS; ++n) {
+      double g = frac * rspstar[n] + (1.0 - frac) * rspo[n];
+      g = mout ? rspo[n] : g;
+      g = min_ ? rspstar[n] : g;
+      flY[n] = g;
+      rgd += g;
+    }
+#pragma unroll
+    for (int n = 0; n < NS; ++n) Yt[n] = flY[n] / rgd;
+    const double regd = rgd * EOS::e_rp(m, Yt, mix_rw<NS>(m, Yt), rgd, gdp);
+    fl_rho = rgd * iu;
+#pragma unroll
+    for (int n = 0; n < NS; ++n) flY[n] *= iu;
+    fl_un = fl_rho * iu + gdp;
+    fl_ut1 = fl_rho * iv1;
+    fl_ut2 = fl_rho * iv2;
+    const double rhoetot = regd + 0.5 * rgd * (iu * iu + iv1 * iv1 + iv2 * iv2);
+    fl_E = iu * (rhoetot + gdp);
+    fl_ei = iu * regd;
+  } else {
+    // laxfriedrich_flux(), Source/Riemann.H:202-307.
+    const double el = EOS::e_rp(m, spl, rwl, rl, pl);
+    const double er = EOS::e_rp(m, spr, rwr, rr, pr);
+    const double r_elt = rl * (el + 0.5 * (unl * unl + ut1l * ut1l + ut2l * ut2l));
+    const double r_ert = rr * (er + 0.5 * (unr * unr + ut1r * ut1r + ut2r * ut2r));
+    const double wsmall = 2.2250738585072014e-308;
+    const double wl = fmax(wsmall, cl * rl);
+    const double wr = fmax(wsmall, cr * rr);
+    double ustar = ((wl * unl + wr * unr) + (pl - pr)) / (wl + wr);
+    const bool m0 = fabs(ustar) < kSmallU * 0.5 * (fabs(unl) + fabs(unr)) || ustar == 0.0;
+    ustar = m0 ? 0.0 : ustar;
+    const double mw = fabs(ustar) + 0.5 * (cr + cl);
+    fl_rho = 0.0;
+#pragma unroll
+    for (int n = 0; n < NS; ++n) {
+      flY[n] = 0.5 * ((rl * unl * spl[n] + rr * unr * spr[n]) - mw * (rr * spr[n] - rl * spl[n]));
+      fl_rho += flY[n];
+    }
+    fl_un = 0.5 * ((rl * unl * unl + pl + rr * unr * unr + pr) - mw * (rr * unr - rl * unl));
+    fl_ut1 = 0.5 * ((rl * ut1l * unl + rr * ut1r * unr) - mw * (rr * ut1r - rl * ut1l));
+    fl_ut2 = 0.5 * ((rl * ut2l * unl + rr * ut2r * unr) - mw * (rr * ut2r - rl * ut2l));
+    fl_E = 0.5 * (((r_elt + pl) * unl + (r_ert + pr) * unr) - mw * (r_ert - r_elt));
+    fl_ei = 0.5 * ((rl * el * unl + rr * er * unr) - mw * (rr * er - rl * el));
+  }
+  F[URHO] += fl_rho;
+  F[UMX + d] += fl_un;
+  F[(d == 0) ? UMY : UMX] += fl_ut1;
+  F[(d == 2) ? UMY : UMZ] += fl_ut2;
+  F[UEDEN] += fl_E;
+  F[UEINT] += fl_ei;
+#pragma unroll
+  for (int n = 0; n < NS; ++n) F[UFS + n] += flY[n];
+}
+
+// pc_diffusion_flux + SpeciesEnergyFlux (Diffterm.H:20-75, 344-461), before
+// the area scaling; components switched off by the diffuse_* flags are left
+// at zero (Diffusion.cpp:321-341).
+template <int NS, class EOS, int d>
+__device__ __forceinline__ void diffusion_face(const DevBox& b, const DevFlags& f, const Geo& g, long long cR,
+                                               const long long stv[3], double* F) {
+  using RC = Rec<NS>;
+  const double* rec = b.rec;
+  const long long N = b.ncell;
+  auto ld = [&](int fld, long long c) { return __ldg(rec + (long long)fld * N + c); };
+  const long long cL = cR - stv[d];
+  const bool harm = f.harmonic != 0;
+  const double mu = face_coef(ld(RC::MU, cR), ld(RC::MU, cL), harm);
+  const double xi = face_coef(ld(RC::XI, cR), ld(RC::XI, cL), harm);
+  const double lam = face_coef(ld(RC::LAM, cR), ld(RC::LAM, cL), harm);
+  // Velocity gradients at the face.
+  double grad[3][3];  // grad[c][a] = d u_c / d x_a (only the entries used)
+  const double uR[3] = {ld(RC::U, cR), ld(RC::V, cR), ld(RC::W, cR)};
+  const double uL[3] = {ld(RC::U, cL), ld(RC::V, cL), ld(RC::W, cL)};
+#pragma unroll
+  for (int c = 0; c < 3; ++c) grad[c][d] = g.dxinv[d] * (uR[c] - uL[c]);
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    if (a == d) continue;
+    const long long sa = stv[a];
+    const double q4 = 0.25 * g.dxinv[a];
+    // components a (for div u) and d (for tau_da)
+    const int ca = RC::U + a, cd = RC::U + d;
+    grad[a][a] = (ld(ca, cR + sa) + ld(ca, cL + sa) - ld(ca, cR - sa) - ld(ca, cL - sa)) * q4;
+    grad[d][a] = (ld(cd, cR + sa) + ld(cd, cL + sa) - ld(cd, cR - sa) - ld(cd, cL - sa)) * q4;
+  }
+  const double divu = grad[0][0] + grad[1][1] + grad[2][2];
+  double tau[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    if (a == d)
+      tau[a] = mu * (2.0 * grad[d][d] - 2.0 / 3.0 * divu) + xi * divu;
+    else
+      tau[a] = mu * (grad[d][a] + grad[a][d]);
+  }
+  const double TR = ld(RC::T, cR), TL = ld(RC::T, cL);
+  const double dTdd = g.dxinv[d] * (TR - TL);
+  double fE = 0.5 * (-tau[0] * (uR[0] + uL[0]) - tau[1] * (uR[1] + uL[1]) - tau[2] * (uR[2] + uL[2])) - lam * dTdd;
+  const double A = g.area[d];
+  const bool spec = f.diffuse_spec != 0;
+  const bool ener = (f.diffuse_temp != 0) || (f.diffuse_enth != 0);
+  if (NS > 1 || spec || ener) {
+    const double pR = ld(RC::P, cR), pL = ld(RC::P, cL);
+    const double dpdx = g.dxinv[d] * (pR - pL);
+    const double dlnp = dpdx / (0.5 * (pR + pL));
+    double Vd[NS], Yf[NS], hf[NS];
+    double Vc = 0.0;
+#pragma unroll
+    for (int n = 0; n < NS; ++n) {
+      const double x1 = ld(RC::X + n, cR), x2 = ld(RC::X + n, cL);
+      const double y1 = ld(RC::Y + n, cR), y2 = ld(RC::Y + n, cL);
+      const double Xface = 0.5 * (x1 + x2);
+      Yf[n] = 0.5 * (y1 + y2);
+      hf[n] = 0.5 * (ld(RC::H + n, cR) + ld(RC::H + n, cL));
+      const double dXdx = g.dxinv[d] * (x1 - x2);
+      const double D = face_coef(ld(RC::D + n, cR), ld(RC::D + n, cL), harm);
+      Vd[n] = -D * (dXdx + (Xface - Yf[n]) * dlnp);
+      Vc += Vd[n];
+      fE += Vd[n] * hf[n];
+    }
+#pragma unroll
+    for (int n = 0; n < NS; ++n) {
+      const double v = Vd[n] - Yf[n] * Vc;
+      fE -= Yf[n] * hf[n] * Vc;
+      if (spec) F[UFS + n] = v * A;
+    }
+  }
+  if (f.diffuse_vel) {
+#pragma unroll
+    for (int a = 0; a < 3; ++a) F[UMX + a] = -tau[a] * A;
+  }
+  if (ener) F[UEDEN] = fE * A;
+}
+
+// ---------------------------------------------------------------------------
+// Pass 2.  tiles[b] = (box index, tile origin i, j, k).
+// ---------------------------------------------------------------------------
+constexpr int kTX = 8, kTY = 8, kTZ = 4, kFluxThreads = kTX * kTY * kTZ;
+constexpr int kMaxFaces = (kTX + 1) * kTY * kTZ > kTX * kTY * (kTZ + 1) ? (kTX + 1) * kTY * kTZ : kTX * kTY * (kTZ + 1);
+
+// One direction of pass 2: every face of the tile with normal d, staged in
+// shared memory, then differenced into the cell accumulators.
+template <int NS, class EOS, int d>
+__device__ __forceinline__ void dir_pass(const DevBox& b, const DevMech<NS>& m, const DevFlags& f, const Geo& g,
+                                         const int o[3], const int ext[3], const long long stv[3], bool mine, int tx,
+                                         int ty, int tz, double (*fbuf)[kMaxFaces], double* acc) {
+  constexpr int NVAR = 7 + NS;
+  const bool diff = f.diffuse_vel || f.diffuse_temp || f.diffuse_spec || f.diffuse_enth;
+  const int nf0 = ext[0] + (d == 0), nf1 = ext[1] + (d == 1), nf2 = ext[2] + (d == 2);
+  const int nfaces = nf0 * nf1 * nf2;
+  for (int fi = threadIdx.x; fi < nfaces; fi += kFluxThreads) {
+    const int fx = fi % nf0, fy = (fi / nf0) % nf1, fz = fi / (nf0 * nf1);
+    const int i = o[0] + fx, j = o[1] + fy, k = o[2] + fz;
+    const long long cR = (i - b.g2lo[0]) + (j - b.g2lo[1]) * stv[1] + (k - b.g2lo[2]) * stv[2];
+    double F[NVAR];
+#pragma unroll
+    for (int n = 0; n < NVAR; ++n) F[n] = 0.0;
+    if (diff) diffusion_face<NS, EOS, d>(b, f, g, cR, stv, F);
+    if (f.do_hydro) {
+      double H[NVAR];
+#pragma unroll
+      for (int n = 0; n < NVAR; ++n) H[n] = 0.0;
+      hydro_face<NS, EOS, d>(b, m, f, cR, stv[d], H);
+      const double A = g.area[d];
+#pragma unroll
+      for (int n = 0; n < NVAR; ++n) F[n] += H[n] * A;
+    }
+    F[UTEMP] = 0.0;
+#pragma unroll
+    for (int n = 0; n < NVAR; ++n) fbuf[n][fi] = F[n];
+  }
+  __syncthreads();
+  if (mine) {
+    const int flo = tx + nf0 * (ty + nf1 * tz);
+    const int fhi = flo + ((d == 0) ? 1 : (d == 1) ? nf0 : nf0 * nf1);
+#pragma unroll
+    for (int n = 0; n < NVAR; ++n) acc[n] += fbuf[n][flo] - fbuf[n][fhi];
+  }
+  __syncthreads();
+}
+
+template <int NS, class EOS>
+__global__ void __launch_bounds__(kFluxThreads, 1)
+    flux_kernel(const DevBox* __restrict__ boxes, const int4* __restrict__ tiles, const __grid_constant__ DevMech<NS> m,
+                const DevFlags f, const Geo g, unsigned long long* __restrict__ counters) {
+  constexpr int NVAR = 7 + NS;
+  __shared__ double fbuf[NVAR][kMaxFaces];
+  const int4 t = tiles[blockIdx.x];
+  const DevBox& b = boxes[t.x];
+  const int o[3] = {t.y, t.z, t.w};
+  const int ext[3] = {min(kTX, b.hi[0] - o[0] + 1), min(kTY, b.hi[1] - o[1] + 1), min(kTZ, b.hi[2] - o[2] + 1)};
+  const int tx = threadIdx.x % kTX, ty = (threadIdx.x / kTX) % kTY, tz = threadIdx.x / (kTX * kTY);
+  const bool mine = tx < ext[0] && ty < ext[1] && tz < ext[2];
+  const long long stv[3] = {1, b.n2[0], (long long)b.n2[0] * b.n2[1]};
+  double acc[NVAR];
+#pragma unroll
+  for (int n = 0; n < NVAR; ++n) acc[n] = 0.0;
+  dir_pass<NS, EOS, 0>(b, m, f, g, o, ext, stv, mine, tx, ty, tz, fbuf, acc);
+  dir_pass<NS, EOS, 1>(b, m, f, g, o, ext, stv, mine, tx, ty, tz, fbuf, acc);
+  dir_pass<NS, EOS, 2>(b, m, f, g, o, ext, stv, mine, tx, ty, tz, fbuf, acc);
+  bool bad = false;
+  if (mine) {
+    const int i = o[0] + tx, j = o[1] + ty, k = o[2] + tz;
+    double* r = b.R + (i - b.rb[0]) + (long long)(j - b.rb[1]) * b.rj + (long long)(k - b.rb[2]) * b.rk;
+#pragma unroll
+    for (int n = 0; n < NVAR; ++n) {
+      const double v = acc[n] / g.vol;
+      bad |= !isfinite(v);
+      r[n * b.rn] = v;
+    }
+  }
+  if (f.check_output) warp_count(&counters[kCounterNonfinite], bad);
+  if (threadIdx.x == 0) {
+    atomicAdd(&counters[kCounterCells], (unsigned long long)(ext[0] * ext[1] * ext[2]));
+  }
+}
+
+}  // namespace pcg

@@ -1,0 +1,418 @@
+// pc_mol.cu — C ABI of the GB300-native MOL right-hand side (include/pelec_mol.h).
+//
+// Host side: validation of the operator configuration and of the box
+// descriptors, the device species tables, the per-level launch layout (box
+// table, cell-chunk list of pass 1, tile list of pass 2) cached across calls
+// with the same BoxArray, the scratch that holds the per-cell records, and
+// the diagnostic counters.  Device side: pc_kernels.cuh.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "pc_kernels.cuh"
+#include "pelec_mol.h"
+
+namespace {
+
+using namespace pcg;
+
+struct Layout {
+  std::vector<DevBox> boxes;
+  std::vector<int2> items;
+  std::vector<int4> tiles;
+  std::vector<int> item_start, tile_start;  // per box, with a final sentinel
+  size_t scratch_doubles = 0;
+};
+
+}  // namespace
+
+struct pc_mol_handle {
+  pc_mol_config cfg{};
+  int device = 0;
+  int variant = 0;  // 1: NS=1 GammaLaw/Constant, 9: NS=9 IdealMix/Simple
+  DevMech<1> mech1{};
+  DevMech<9> mech9{};
+  DevFlags flags{};
+  int nrec = 0;
+  unsigned long long* d_counters = nullptr;
+  // layout cache
+  std::vector<pc_box_desc> last_boxes;
+  double last_dx[3] = {0, 0, 0};
+  Layout lay;
+  DevBox* d_boxes = nullptr;
+  size_t cap_boxes = 0;
+  int2* d_items = nullptr;
+  size_t cap_items = 0;
+  int4* d_tiles = nullptr;
+  size_t cap_tiles = 0;
+  double* scratch = nullptr;
+  size_t scratch_cap = 0;  // doubles
+  cudaStream_t last_stream = nullptr;
+  int last_error = PC_OK;
+  cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};  // pass timing (cfg.time_passes)
+  bool timed = false;
+};
+
+namespace {
+
+int cuda_fail(pc_mol_handle* h, cudaError_t e) {
+  if (e == cudaSuccess) return PC_OK;
+  if (h) h->last_error = (e == cudaErrorMemoryAllocation) ? PC_ERR_OUT_OF_MEMORY : PC_ERR_CUDA;
+  return (e == cudaErrorMemoryAllocation) ? PC_ERR_OUT_OF_MEMORY : PC_ERR_CUDA;
+}
+
+template <int NS>
+void fill_common(DevMech<NS>& d, const pc_mechanism& m) {
+  for (int k = 0; k < NS; ++k) d.rW[k] = RU / m.mw[k];
+  d.gamma = m.gamma;
+  d.gm1 = m.gamma - 1.0;
+  for (int k = 0; k < NS; ++k) d.cpk[k] = m.gamma / (m.gamma - 1.0) * RU / m.mw[k];
+  d.const_mu = m.const_mu;
+  d.const_xi = m.const_xi;
+  d.const_lam = m.const_lambda;
+  d.const_rhoD = m.const_rhoD;
+}
+
+template <int NS>
+int fill_idealmix(DevMech<NS>& d, const pc_mechanism& m) {
+  d.tmid = m.nasa_tmid[0];
+  for (int k = 0; k < NS; ++k) {
+    if (m.nasa_tmid[k] != d.tmid) return PC_ERR_UNSUPPORTED;  // one shared range split
+    const double r = RU / m.mw[k];
+    for (int n = 0; n < 6; ++n) {
+      d.cpc[0][n][k] = r * m.nasa_lo[k][n];
+      d.cpc[1][n][k] = r * m.nasa_hi[k][n];
+    }
+  }
+  return PC_OK;
+}
+
+template <int NS>
+int fill_simple(DevMech<NS>& d, const pc_mechanism& m) {
+  for (int k = 0; k < NS; ++k) {
+    for (int n = 0; n < 4; ++n) {
+      d.visc[k][n] = m.visc_fit[k][n];
+      d.cond[k][n] = m.cond_fit[k][n];
+    }
+    d.bulk[k] = m.bulk_ratio[k];
+  }
+  int q = 0;
+  for (int k = 0; k < NS; ++k)
+    for (int j = k + 1; j < NS; ++j, ++q)
+      for (int n = 0; n < 4; ++n) {
+        if (m.diff_fit[k][j][n] != m.diff_fit[j][k][n]) return PC_ERR_UNSUPPORTED;  // symmetric fits only
+        d.diff[q][n] = m.diff_fit[k][j][n];
+      }
+  if (!(m.diff_pref > 0.0)) return PC_ERR_INVALID_ARGUMENT;
+  d.inv_pref = 1.0 / m.diff_pref;
+  return PC_OK;
+}
+
+bool covers(const pc_array4& a, const int lo[3], const int hi[3], int ng) {
+  for (int d = 0; d < 3; ++d)
+    if (a.begin[d] > lo[d] - ng || a.end[d] - 1 < hi[d] + ng) return false;
+  return true;
+}
+
+int validate_box(const pc_box_desc& b, int nvar) {
+  for (int d = 0; d < 3; ++d)
+    if (b.hi[d] < b.lo[d]) return PC_ERR_INVALID_ARGUMENT;
+  if (!b.state.p || !b.rhs.p) return PC_ERR_INVALID_ARGUMENT;
+  if (b.state.ncomp < nvar || b.rhs.ncomp < nvar) return PC_ERR_INVALID_ARGUMENT;
+  if (!covers(b.state, b.lo, b.hi, 2) || !covers(b.rhs, b.lo, b.hi, 0)) return PC_ERR_INVALID_ARGUMENT;
+  const pc_array4* arrs[2] = {&b.state, &b.rhs};
+  for (const pc_array4* a : arrs) {
+    const long long nx = a->end[0] - a->begin[0], ny = a->end[1] - a->begin[1], nz = a->end[2] - a->begin[2];
+    if (a->jstride < nx || a->kstride < a->jstride * ny || a->nstride < a->kstride * nz) return PC_ERR_INVALID_ARGUMENT;
+  }
+  // Cells of grow(valid, 2) are indexed with 32-bit chunk offsets.
+  long long ncell = 1;
+  for (int d = 0; d < 3; ++d) {
+    if (b.hi[d] - b.lo[d] + 1 > 4096) return PC_ERR_TOO_LARGE;
+    ncell *= (long long)(b.hi[d] - b.lo[d] + 5);
+  }
+  if (ncell > 2000000000LL) return PC_ERR_TOO_LARGE;
+  return PC_OK;
+}
+
+void build_layout(const pc_box_desc* boxes, int nboxes, int nrec, Layout& L) {
+  L.boxes.clear();
+  L.items.clear();
+  L.tiles.clear();
+  L.item_start.clear();
+  L.tile_start.clear();
+  L.scratch_doubles = 0;
+  for (int bi = 0; bi < nboxes; ++bi) {
+    const pc_box_desc& b = boxes[bi];
+    DevBox d{};
+    for (int a = 0; a < 3; ++a) {
+      d.lo[a] = b.lo[a];
+      d.hi[a] = b.hi[a];
+      d.sb[a] = b.state.begin[a];
+      d.rb[a] = b.rhs.begin[a];
+      d.g2lo[a] = b.lo[a] - 2;
+      d.n2[a] = b.hi[a] - b.lo[a] + 5;
+    }
+    d.S = b.state.p;
+    d.sj = b.state.jstride;
+    d.sk = b.state.kstride;
+    d.sn = b.state.nstride;
+    d.R = b.rhs.p;
+    d.rj = b.rhs.jstride;
+    d.rk = b.rhs.kstride;
+    d.rn = b.rhs.nstride;
+    d.ncell = (long long)d.n2[0] * d.n2[1] * d.n2[2];
+    d.rec = reinterpret_cast<double*>(L.scratch_doubles);  // offset, rebased after allocation
+    L.scratch_doubles += (size_t)d.ncell * nrec;
+    L.scratch_doubles = (L.scratch_doubles + 31) & ~size_t(31);  // 256-byte aligned records
+    L.boxes.push_back(d);
+    L.item_start.push_back((int)L.items.size());
+    for (long long c = 0; c < d.ncell; c += kCellThreads) L.items.push_back(make_int2(bi, (int)c));
+    L.tile_start.push_back((int)L.tiles.size());
+    for (int k = b.lo[2]; k <= b.hi[2]; k += kTZ)
+      for (int j = b.lo[1]; j <= b.hi[1]; j += kTY)
+        for (int i = b.lo[0]; i <= b.hi[0]; i += kTX) L.tiles.push_back(make_int4(bi, i, j, k));
+  }
+  L.item_start.push_back((int)L.items.size());
+  L.tile_start.push_back((int)L.tiles.size());
+}
+
+template <class T>
+int ensure(pc_mol_handle* h, T*& ptr, size_t& cap, size_t n) {
+  if (n <= cap) return PC_OK;
+  if (ptr) cudaFree(ptr);
+  ptr = nullptr;
+  cap = 0;
+  cudaError_t e = cudaMalloc(&ptr, n * sizeof(T));
+  if (e != cudaSuccess) return cuda_fail(h, e);
+  cap = n;
+  return PC_OK;
+}
+
+int prepare(pc_mol_handle* h, const pc_box_desc* boxes, int nboxes, const double dx[3], cudaStream_t s) {
+  const int nvar = 7 + h->cfg.nspec;
+  for (int b = 0; b < nboxes; ++b) {
+    int rc = validate_box(boxes[b], nvar);
+    if (rc != PC_OK) return rc;
+  }
+  const bool same = (int)h->last_boxes.size() == nboxes &&
+                    std::memcmp(h->last_boxes.data(), boxes, sizeof(pc_box_desc) * nboxes) == 0 &&
+                    h->last_dx[0] == dx[0] && h->last_dx[1] == dx[1] && h->last_dx[2] == dx[2];
+  if (same) return PC_OK;
+  build_layout(boxes, nboxes, h->nrec, h->lay);
+  int rc = ensure(h, h->scratch, h->scratch_cap, h->lay.scratch_doubles);
+  if (rc != PC_OK) return rc;
+  for (auto& d : h->lay.boxes) d.rec = h->scratch + reinterpret_cast<size_t>(d.rec);
+  if ((rc = ensure(h, h->d_boxes, h->cap_boxes, h->lay.boxes.size())) != PC_OK) return rc;
+  if ((rc = ensure(h, h->d_items, h->cap_items, h->lay.items.size())) != PC_OK) return rc;
+  if ((rc = ensure(h, h->d_tiles, h->cap_tiles, h->lay.tiles.size())) != PC_OK) return rc;
+  cudaError_t e = cudaMemcpyAsync(h->d_boxes, h->lay.boxes.data(), sizeof(DevBox) * h->lay.boxes.size(),
+                                  cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(h->d_items, h->lay.items.data(), sizeof(int2) * h->lay.items.size(), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(h->d_tiles, h->lay.tiles.data(), sizeof(int4) * h->lay.tiles.size(), cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess) return cuda_fail(h, e);
+  // The uploads above read host vectors owned by the handle; a layout change
+  // waits for them before the vectors can be rebuilt.
+  e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_fail(h, e);
+  h->last_boxes.assign(boxes, boxes + nboxes);
+  for (int d = 0; d < 3; ++d) h->last_dx[d] = dx[d];
+  return PC_OK;
+}
+
+Geo make_geo(const double dx[3]) {
+  Geo g;
+  for (int d = 0; d < 3; ++d) g.dxinv[d] = 1.0 / dx[d];
+  g.area[0] = dx[1] * dx[2];
+  g.area[1] = dx[0] * dx[2];
+  g.area[2] = dx[0] * dx[1];
+  g.vol = dx[0] * dx[1] * dx[2];
+  return g;
+}
+
+template <int NS, class EOS, class TR>
+int launch(pc_mol_handle* h, const DevMech<NS>& mech, const Geo& g, int ibeg, int iend, int tbeg, int tend,
+           cudaStream_t s, bool timed) {
+  if (timed) cudaEventRecord(h->ev[0], s);
+  if (iend > ibeg)
+    cell_kernel<NS, EOS, TR><<<iend - ibeg, kCellThreads, 0, s>>>(h->d_boxes, h->d_items + ibeg, mech, h->flags,
+                                                                   h->d_counters);
+  if (timed) cudaEventRecord(h->ev[1], s);
+  if (tend > tbeg)
+    flux_kernel<NS, EOS><<<tend - tbeg, kFluxThreads, 0, s>>>(h->d_boxes, h->d_tiles + tbeg, mech, h->flags, g,
+                                                              h->d_counters);
+  if (timed) cudaEventRecord(h->ev[2], s);
+  return cuda_fail(h, cudaGetLastError());
+}
+
+int run(pc_mol_handle* h, const pc_box_desc* boxes, int nboxes, const double dx[3], void* stream, bool per_box) {
+  if (!h) return PC_ERR_INVALID_ARGUMENT;
+  if (nboxes < 0 || (nboxes > 0 && !boxes) || !dx) return h->last_error = PC_ERR_INVALID_ARGUMENT;
+  for (int d = 0; d < 3; ++d)
+    if (!(dx[d] > 0.0) || !std::isfinite(dx[d])) return h->last_error = PC_ERR_INVALID_ARGUMENT;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  int rc = cuda_fail(h, cudaSetDevice(h->device));
+  if (rc != PC_OK) return rc;
+  h->last_stream = s;
+  rc = cuda_fail(h, cudaMemsetAsync(h->d_counters, 0, sizeof(unsigned long long) * kNumCounters, s));
+  if (rc != PC_OK) return rc;
+  if (nboxes == 0) return h->last_error = PC_OK;
+  rc = prepare(h, boxes, nboxes, dx, s);
+  if (rc != PC_OK) return h->last_error = rc;
+  const Geo g = make_geo(dx);
+  const Layout& L = h->lay;
+  const bool timed = h->cfg.time_passes != 0 && !per_box;
+  h->timed = timed;
+  auto go = [&](int ib, int ie, int tb, int te) {
+    if (h->variant == 1)
+      return launch<1, GammaLawEos<1>, ConstantTransport<1>>(h, h->mech1, g, ib, ie, tb, te, s, timed);
+    return launch<9, IdealMixEos<9>, SimpleTransport<9>>(h, h->mech9, g, ib, ie, tb, te, s, timed);
+  };
+  if (!per_box) {
+    rc = go(0, (int)L.items.size(), 0, (int)L.tiles.size());
+  } else {
+    for (int b = 0; b < nboxes && rc == PC_OK; ++b)
+      rc = go(L.item_start[b], L.item_start[b + 1], L.tile_start[b], L.tile_start[b + 1]);
+  }
+  return h->last_error = rc;
+}
+
+}  // namespace
+
+extern "C" {
+
+int pc_mol_abi_version(void) { return PC_MOL_ABI_VERSION; }
+
+const char* pc_mol_error_string(int code) {
+  switch (code) {
+    case PC_OK: return "ok";
+    case PC_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case PC_ERR_UNSUPPORTED: return "unsupported configuration";
+    case PC_ERR_CUDA: return "CUDA runtime error";
+    case PC_ERR_OUT_OF_MEMORY: return "out of device memory";
+    case PC_ERR_NO_DEVICE: return "no CUDA device";
+    case PC_ERR_TOO_LARGE: return "request exceeds a fixed-size limit";
+    default: return "unknown status code";
+  }
+}
+
+int pc_mol_create(pc_mol_handle** out, const pc_mol_config* cfg) {
+  if (!out || !cfg) return PC_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  const pc_mol_config& c = *cfg;
+  if (c.nspec != c.mech.nspec) return PC_ERR_INVALID_ARGUMENT;
+  if (c.precision != PC_PRECISION_FP64 && c.precision != PC_PRECISION_MIXED) return PC_ERR_INVALID_ARGUMENT;
+  int variant = 0;
+  if (c.nspec == 1 && c.eos == PC_EOS_GAMMA_LAW && c.transport == PC_TRANSPORT_CONSTANT) variant = 1;
+  if (c.nspec == 9 && c.eos == PC_EOS_IDEAL_MIX && c.transport == PC_TRANSPORT_SIMPLE) variant = 9;
+  if (!variant) return PC_ERR_UNSUPPORTED;
+  if (c.precision == PC_PRECISION_MIXED) return PC_ERR_UNSUPPORTED;
+  for (int k = 0; k < c.nspec; ++k)
+    if (!(c.mech.mw[k] > 0.0)) return PC_ERR_INVALID_ARGUMENT;
+  if (c.eos == PC_EOS_GAMMA_LAW && !(c.mech.gamma > 1.0)) return PC_ERR_INVALID_ARGUMENT;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return PC_ERR_NO_DEVICE;
+  pc_mol_handle* h = new (std::nothrow) pc_mol_handle();
+  if (!h) return PC_ERR_OUT_OF_MEMORY;
+  h->cfg = c;
+  h->variant = variant;
+  cudaGetDevice(&h->device);
+  int rc = PC_OK;
+  if (variant == 1) {
+    fill_common(h->mech1, c.mech);
+    h->nrec = Rec<1>::N;
+  } else {
+    fill_common(h->mech9, c.mech);
+    rc = fill_idealmix(h->mech9, c.mech);
+    if (rc == PC_OK) rc = fill_simple(h->mech9, c.mech);
+    h->nrec = Rec<9>::N;
+  }
+  if (rc != PC_OK) {
+    delete h;
+    return rc;
+  }
+  h->flags.do_hydro = c.do_hydro != 0;
+  h->flags.diffuse_vel = c.diffuse_vel != 0;
+  h->flags.diffuse_temp = c.diffuse_temp != 0;
+  h->flags.diffuse_spec = c.diffuse_spec != 0;
+  h->flags.diffuse_enth = c.diffuse_enth != 0;
+  h->flags.slopes = c.plm_iorder != 1;
+  h->flags.laxf = c.use_laxf_flux != 0;
+  h->flags.harmonic = c.transport_harmonic_mean != 0;
+  h->flags.check_output = c.check_output != 0;
+  h->flags.newton_maxit = c.newton_max_iter > 0 ? c.newton_max_iter : 50;
+  if (cudaMalloc(&h->d_counters, sizeof(unsigned long long) * kNumCounters) != cudaSuccess) {
+    delete h;
+    return PC_ERR_OUT_OF_MEMORY;
+  }
+  cudaMemset(h->d_counters, 0, sizeof(unsigned long long) * kNumCounters);
+  if (c.time_passes)
+    for (auto& e : h->ev)
+      if (cudaEventCreate(&e) != cudaSuccess) {
+        pc_mol_destroy(h);
+        return PC_ERR_CUDA;
+      }
+  *out = h;
+  return PC_OK;
+}
+
+void pc_mol_destroy(pc_mol_handle* h) {
+  if (!h) return;
+  cudaSetDevice(h->device);
+  cudaDeviceSynchronize();
+  cudaFree(h->d_counters);
+  cudaFree(h->d_boxes);
+  cudaFree(h->d_items);
+  cudaFree(h->d_tiles);
+  cudaFree(h->scratch);
+  for (auto& e : h->ev)
+    if (e) cudaEventDestroy(e);
+  delete h;
+}
+
+int pc_mol_rhs_level(pc_mol_handle* h, const pc_box_desc* boxes, int nboxes, const double dx[3], void* stream) {
+  return run(h, boxes, nboxes, dx, stream, false);
+}
+
+int pc_mol_rhs_level_per_box(pc_mol_handle* h, const pc_box_desc* boxes, int nboxes, const double dx[3],
+                             void* stream) {
+  return run(h, boxes, nboxes, dx, stream, true);
+}
+
+int pc_mol_last_status(pc_mol_handle* h, pc_mol_status* st) {
+  if (!h || !st) return PC_ERR_INVALID_ARGUMENT;
+  std::memset(st, 0, sizeof(*st));
+  unsigned long long c[kNumCounters] = {0, 0, 0, 0};
+  cudaError_t e = cudaSetDevice(h->device);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->last_stream);
+  if (e == cudaSuccess) e = cudaMemcpy(c, h->d_counters, sizeof(c), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(h, e);
+  st->cells = (long long)c[kCounterCells];
+  st->newton_nonconverged = (long long)c[kCounterNewton];
+  st->nonpositive_state = (long long)c[kCounterNonpos];
+  st->nonfinite_output = (long long)c[kCounterNonfinite];
+  st->last_error = h->last_error;
+  return PC_OK;
+}
+
+int pc_mol_pass_times(pc_mol_handle* h, double* ms, int n) {
+  if (!h || !ms || n < 2) return PC_ERR_INVALID_ARGUMENT;
+  if (!h->cfg.time_passes || !h->timed) return PC_ERR_INVALID_ARGUMENT;
+  cudaError_t e = cudaSetDevice(h->device);
+  if (e == cudaSuccess) e = cudaEventSynchronize(h->ev[2]);
+  float a = 0.f, b = 0.f;
+  if (e == cudaSuccess) e = cudaEventElapsedTime(&a, h->ev[0], h->ev[1]);
+  if (e == cudaSuccess) e = cudaEventElapsedTime(&b, h->ev[1], h->ev[2]);
+  if (e != cudaSuccess) return cuda_fail(h, e);
+  ms[0] = a;
+  ms[1] = b;
+  return PC_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,165 @@
+"""Host-side mirror of PeleC's MOL operator interface over the C ABI.
+
+``PeleC::getMOLSrcTerm(const MultiFab& S, MultiFab& MOLSrcTerm, Real time,
+Real dt, Real flux_factor)`` (Source/PeleC.H:523-528, Source/Diffusion.cpp:4-681)
+is mirrored by :meth:`MOLOperator.getMOLSrcTerm` over :class:`MultiFab`, a
+minimal container of device FABs (one torch tensor per box, Array4 layout).
+The work itself is done by ``libpelec_mol.so`` (pc_mol_rhs_level); torch only
+provides device memory and streams.  There is no CPU fallback: without the
+CUDA library or a GPU every call raises.
+
+Error behaviour follows the reference, which aborts on unsupported input
+(amrex::Abort, Diffusion.cpp:272,543): a non-zero status code raises
+:class:`MOLError` carrying the library's message.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from ctypes import POINTER, c_char_p, c_double, c_int, c_void_p
+
+from . import abi
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "libpelec_mol.so")
+_lib = None
+
+
+class MOLError(RuntimeError):
+    def __init__(self, code: int, where: str):
+        super().__init__(f"{where}: {error_string(code)} (code {code})")
+        self.code = code
+
+
+def library() -> ctypes.CDLL:
+    """The CUDA library; raises if it has not been built (no fallback)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"CUDA library {LIB_PATH} is not built; run `python -m pelec_gb300.build`")
+        lib = ctypes.CDLL(LIB_PATH)
+        lib.pc_mol_abi_version.restype = c_int
+        lib.pc_mol_error_string.argtypes = [c_int]
+        lib.pc_mol_error_string.restype = c_char_p
+        lib.pc_mol_create.argtypes = [POINTER(c_void_p), POINTER(abi.PcMolConfig)]
+        lib.pc_mol_create.restype = c_int
+        lib.pc_mol_destroy.argtypes = [c_void_p]
+        lib.pc_mol_destroy.restype = None
+        for fn in (lib.pc_mol_rhs_level, lib.pc_mol_rhs_level_per_box):
+            fn.argtypes = [c_void_p, POINTER(abi.PcBoxDesc), c_int, POINTER(c_double), c_void_p]
+            fn.restype = c_int
+        lib.pc_mol_last_status.argtypes = [c_void_p, POINTER(abi.PcMolStatus)]
+        lib.pc_mol_last_status.restype = c_int
+        lib.pc_mol_pass_times.argtypes = [c_void_p, POINTER(c_double), c_int]
+        lib.pc_mol_pass_times.restype = c_int
+        if lib.pc_mol_abi_version() != abi.PC_MOL_ABI_VERSION:
+            raise RuntimeError("libpelec_mol.so ABI version does not match pelec_gb300.abi")
+        _lib = lib
+    return _lib
+
+
+def error_string(code: int) -> str:
+    try:
+        return library().pc_mol_error_string(int(code)).decode()
+    except RuntimeError:
+        return f"status {code}"
+
+
+def _check(rc: int, where: str) -> None:
+    if rc != abi.PC_OK:
+        raise MOLError(rc, where)
+
+
+class MultiFab:
+    """Device FABs of one level: ``fabs[b]`` is a float64 CUDA tensor of shape
+    (ncomp, nz+2g, ny+2g, nx+2g) for valid box ``boxes[b] = (lo, hi)``."""
+
+    def __init__(self, boxes, ncomp: int, ngrow: int, device="cuda", fabs=None):
+        import torch
+
+        self.boxes = [(tuple(lo), tuple(hi)) for lo, hi in boxes]
+        self.ncomp = ncomp
+        self.ngrow = ngrow
+        if fabs is not None:
+            self.fabs = list(fabs)
+        else:
+            self.fabs = []
+            for lo, hi in self.boxes:
+                n = [h - l + 1 + 2 * ngrow for l, h in zip(lo, hi)]
+                self.fabs.append(torch.zeros((ncomp, n[2], n[1], n[0]), dtype=torch.float64, device=device))
+
+    def array4(self, b: int) -> abi.PcArray4:
+        t = self.fabs[b]
+        if not t.is_contiguous() or t.dtype.itemsize != 8:
+            raise ValueError("FABs must be contiguous float64 tensors")
+        lo, _ = self.boxes[b]
+        return abi.array4(t.data_ptr(), t.shape, [l - self.ngrow for l in lo])
+
+    def __len__(self):
+        return len(self.boxes)
+
+
+class MOLOperator:
+    """One configured MOL right-hand side (a pc_mol_handle)."""
+
+    def __init__(self, cfg: abi.PcMolConfig):
+        lib = library()
+        self.cfg = cfg
+        h = c_void_p()
+        _check(lib.pc_mol_create(ctypes.byref(h), ctypes.byref(cfg)), "pc_mol_create")
+        self._h = h
+        self._descs = None
+        self._key = None
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) and self._h.value:
+            library().pc_mol_destroy(self._h)
+            self._h = c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _box_descs(self, S: MultiFab, R: MultiFab):
+        key = (tuple(t.data_ptr() for t in S.fabs), tuple(t.data_ptr() for t in R.fabs), tuple(S.boxes))
+        if key != self._key:
+            descs = [abi.box_desc(lo, hi, S.array4(b), R.array4(b)) for b, (lo, hi) in enumerate(S.boxes)]
+            self._descs = abi.box_array(descs)
+            self._key = key
+        return self._descs
+
+    def rhs_level(self, S: MultiFab, R: MultiFab, dx, stream=None, per_box: bool = False) -> None:
+        """pc_mol_rhs_level on torch's current stream (or ``stream``)."""
+        import torch
+
+        if len(S) != len(R):
+            raise ValueError("S and MOLSrcTerm must have the same BoxArray")
+        descs = self._box_descs(S, R)
+        st = stream if stream is not None else torch.cuda.current_stream()
+        dxa = (c_double * 3)(*[float(v) for v in dx])
+        fn = library().pc_mol_rhs_level_per_box if per_box else library().pc_mol_rhs_level
+        _check(fn(self._h, descs, len(S), dxa, c_void_p(st.cuda_stream)), fn.__name__)
+
+    def getMOLSrcTerm(self, S: MultiFab, MOLSrcTerm: MultiFab, time: float, dt: float, flux_factor: float,
+                      dx=None) -> None:
+        """Mirror of PeleC::getMOLSrcTerm on one level without EB.  ``time`` is
+        unused (Diffusion.cpp:8); ``dt`` and ``flux_factor`` only scale flux
+        register updates, which are inactive on a single level
+        (PeleC.cpp:1432-1439).  ``dx`` is geom.CellSize()."""
+        del time, dt, flux_factor
+        if dx is None:
+            raise ValueError("dx (geom.CellSize()) is required")
+        self.rhs_level(S, MOLSrcTerm, dx)
+
+    def pass_times(self):
+        """(cell pass ms, flux pass ms) of the last call (cfg.time_passes)."""
+        ms = (c_double * 2)()
+        _check(library().pc_mol_pass_times(self._h, ms, 2), "pc_mol_pass_times")
+        return float(ms[0]), float(ms[1])
+
+    def status(self) -> abi.PcMolStatus:
+        st = abi.PcMolStatus()
+        _check(library().pc_mol_last_status(self._h, ctypes.byref(st)), "pc_mol_last_status")
+        return st

@@ -1,0 +1,192 @@
+"""GPU parity of the CUDA MOL right-hand side against the oracle.
+
+Every call goes through the C ABI (libpelec_mol.so via ctypes).  The bar is
+the one stated for the plain FP64 form: per component, max|gpu - oracle| /
+max|oracle| <= 1e-12 (RTOL below).
+"""
+import numpy as np
+import pytest
+
+from conftest import rel_maxnorm
+from gpu_util import gpu_rhs
+from pelec_gb300 import abi, mechanism, problems
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-12
+
+
+def _check(gpu, ref, rtol=RTOL, what=""):
+    err = rel_maxnorm(gpu, ref)
+    assert np.all(np.isfinite(gpu)), what
+    assert err.max() <= rtol, f"{what}: per-component rel max-norm error {err}"
+    return err
+
+
+def test_tgv_64_c1_parity(cuda_lib, oracle_lib):
+    """Config C1: 64^3 periodic Taylor-Green, GammaLaw, constant transport."""
+    mech, st = problems.tgv(64, seed=0)
+    cfg = problems.make_config(mech)
+    ref, = oracle_lib.mol_rhs(cfg, [st])
+    (gpu,), status = gpu_rhs(cuda_lib, cfg, [st])
+    err = _check(gpu, ref, what="tgv64")
+    print("tgv64 rel max-norm per component:", err)
+    assert status.cells == 64 ** 3
+    assert status.newton_nonconverged == 0 and status.nonpositive_state == 0 and status.nonfinite_output == 0
+
+
+def test_flame_small_parity(cuda_lib, oracle_lib):
+    mech, st, _ = problems.flame((16, 12, 20), seed=4)
+    cfg = problems.make_config(mech)
+    ref, = oracle_lib.mol_rhs(cfg, [st])
+    (gpu,), status = gpu_rhs(cuda_lib, cfg, [st])
+    err = _check(gpu, ref, what="flame 16x12x20")
+    print("flame small rel max-norm per component:", err)
+    assert status.cells == 16 * 12 * 20
+
+
+def test_flame_128_c2_parity(cuda_lib, oracle_lib):
+    """Config C2: 128^3 flame, 9 species, periodic x/y, extrapolated z."""
+    mech, st, _ = problems.flame((128, 128, 128), seed=1)
+    cfg = problems.make_config(mech)
+    ref, = oracle_lib.mol_rhs(cfg, [st])
+    (gpu,), status = gpu_rhs(cuda_lib, cfg, [st])
+    err = _check(gpu, ref, what="flame 128^3")
+    print("flame 128^3 rel max-norm per component:", err)
+    assert status.newton_nonconverged == 0 and status.nonfinite_output == 0
+
+
+FLAG_CASES = {
+    "hydro_only": dict(diffuse=0),
+    "diffusion_only": dict(do_hydro=0),
+    "laxf": dict(use_laxf_flux=1),
+    "first_order": dict(plm_iorder=1),
+    "arithmetic_mean": dict(harmonic=0),
+    "temp_only": dict(do_hydro=0, diffuse=0, diffuse_temp=1),
+    "spec_only": dict(do_hydro=0, diffuse=0, diffuse_spec=1),
+    "vel_only": dict(do_hydro=0, diffuse=0, diffuse_vel=1),
+    "nothing": dict(do_hydro=0, diffuse=0),
+}
+
+
+@pytest.mark.parametrize("case", sorted(FLAG_CASES))
+@pytest.mark.parametrize("phys", ["tgv", "flame"])
+def test_flag_matrix(cuda_lib, oracle_lib, case, phys):
+    if phys == "tgv":
+        mech, st = problems.tgv(12, seed=7)
+    else:
+        mech, st, _ = problems.flame((10, 9, 12), seed=8)
+    cfg = problems.make_config(mech, **FLAG_CASES[case])
+    ref, = oracle_lib.mol_rhs(cfg, [st])
+    (gpu,), _ = gpu_rhs(cuda_lib, cfg, [st])
+    _check(gpu, ref, what=f"{phys}/{case}")
+
+
+def test_golden_fixtures_on_gpu(cuda_lib):
+    import os
+
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "mol_rhs_golden.npz"))
+    for case in ("tgv8", "flame6"):
+        S = np.ascontiguousarray(g[f"{case}_S"])
+        n = S.shape[-1] - 8
+        mech = mechanism.gamma_law_single() if case.startswith("tgv") else mechanism.h2_air_synthetic()
+        st = problems.BoxState(lo=(0, 0, 0), hi=(n - 1,) * 3, S=S, dx=tuple(g[f"{case}_dx"]))
+        (gpu,), _ = gpu_rhs(cuda_lib, problems.make_config(mech), [st])
+        _check(gpu, g[f"{case}_R"], what=case)
+
+
+def test_uneven_level_batched_vs_per_box(cuda_lib, oracle_lib):
+    """A BoxArray of uneven boxes: one batched launch == per-box launches
+    (bit for bit) == oracle (1e-12)."""
+    mech, boxes = problems.level_boxes(nboxes=7, seed=21, edges=(8, 16, 24))
+    cfg = problems.make_config(mech)
+    refs = oracle_lib.mol_rhs(cfg, boxes)
+    batched, st1 = gpu_rhs(cuda_lib, cfg, boxes)
+    perbox, st2 = gpu_rhs(cuda_lib, cfg, boxes, per_box=True)
+    for b, (g1, g2, r) in enumerate(zip(batched, perbox, refs)):
+        np.testing.assert_array_equal(g1, g2)
+        _check(g1, r, what=f"box {b}")
+    assert st1.cells == sum(b.ncells for b in boxes)
+
+
+def test_tiny_and_odd_boxes(cuda_lib, oracle_lib):
+    """Boxes smaller than a tile and with odd extents (ragged tiles)."""
+    mech, boxes = problems.level_boxes(nboxes=3, seed=5, edges=(24,))
+    shapes = [(1, 1, 1), (3, 5, 2), (9, 17, 5)]
+    out = []
+    for st, shp in zip(boxes, shapes):
+        nx, ny, nz = shp
+        S = np.ascontiguousarray(st.S[:, : nz + 8, : ny + 8, : nx + 8])
+        out.append(problems.BoxState(lo=st.lo, hi=tuple(l + n - 1 for l, n in zip(st.lo, shp)), S=S, dx=st.dx))
+    cfg = problems.make_config(mech)
+    refs = oracle_lib.mol_rhs(cfg, out)
+    gpus, _ = gpu_rhs(cuda_lib, cfg, out)
+    for g, r in zip(gpus, refs):
+        _check(g, r, what="tiny")
+
+
+def test_periodic_flame_conservation(cuda_lib):
+    """Fully periodic 32^3 flame: domain totals of every conserved RHS vanish
+    to round-off (Tests/test_masscons.py:20-28 checks the same totals)."""
+    mech, st, _ = problems.flame((32, 32, 32), seed=9)
+    problems.fill_ghosts(st.S, 4, ("periodic",) * 3)
+    (gpu,), _ = gpu_rhs(cuda_lib, problems.make_config(mech), [st])
+    for n in [abi.URHO, abi.UMX, abi.UMY, abi.UMZ, abi.UEDEN] + [abi.UFS + k for k in range(9)]:
+        assert abs(gpu[n].sum()) <= 1e-12 * np.abs(gpu[n]).sum(), n
+
+
+def test_negative_density_is_reported_not_trapped(cuda_lib):
+    """A corrupt ghost cell (rho < 0) is counted in the status; the call and
+    the context survive."""
+    mech, st, _ = problems.flame((8, 8, 8), seed=3)
+    S = st.S.copy()
+    S[abi.URHO, 2, 6, 6] = -abs(S[abi.URHO, 2, 6, 6])  # z ghost layer 2 (inside grow(valid,2))
+    bad = problems.BoxState(lo=st.lo, hi=st.hi, S=S, dx=st.dx)
+    (gpu,), status = gpu_rhs(cuda_lib, problems.make_config(mech), [bad])
+    assert status.nonpositive_state >= 1
+    # the context is still usable
+    (gpu2,), status2 = gpu_rhs(cuda_lib, problems.make_config(mech), [st])
+    assert status2.nonpositive_state == 0 and np.all(np.isfinite(gpu2))
+
+
+def test_invalid_arguments(cuda_lib):
+    import torch
+
+    mol = cuda_lib
+    mech, st, _ = problems.flame((8, 8, 8), seed=3)
+    op = mol.MOLOperator(problems.make_config(mech))
+    # state with a single ghost layer: rejected before any launch
+    S1 = torch.from_numpy(np.ascontiguousarray(st.S[:, 3:-3, 3:-3, 3:-3])).cuda()
+    S = mol.MultiFab([(st.lo, st.hi)], 16, 1, fabs=[S1])
+    R = mol.MultiFab([(st.lo, st.hi)], 16, 0)
+    with pytest.raises(mol.MOLError) as ei:
+        op.rhs_level(S, R, st.dx)
+    assert ei.value.code == abi.PC_ERR_INVALID_ARGUMENT
+    # a box too large for the 32-bit chunk indexing
+    with pytest.raises(mol.MOLError):
+        big = mol.MultiFab([((0, 0, 0), (5000, 0, 0))], 16, 0, fabs=[torch.zeros(16, 1, 1, 1, dtype=torch.float64,
+                                                                                        device="cuda")])
+        op.rhs_level(big, big, st.dx)
+    # unsupported physics combination
+    cfg = problems.make_config(mech)
+    cfg.eos = abi.PC_EOS_GAMMA_LAW
+    with pytest.raises(mol.MOLError) as ei:
+        mol.MOLOperator(cfg)
+    assert ei.value.code == abi.PC_ERR_UNSUPPORTED
+    # empty level: a no-op
+    op.rhs_level(mol.MultiFab([], 16, 4, fabs=[]), mol.MultiFab([], 16, 0, fabs=[]), st.dx)
+
+
+def test_getMOLSrcTerm_mirror(cuda_lib, oracle_lib):
+    """The reference-shaped entry point gives the same answer."""
+    import torch
+
+    mol = cuda_lib
+    mech, st = problems.tgv(16, seed=2)
+    cfg = problems.make_config(mech)
+    op = mol.MOLOperator(cfg)
+    S = mol.MultiFab([(st.lo, st.hi)], 8, 4, fabs=[torch.from_numpy(st.S).cuda()])
+    R = mol.MultiFab([(st.lo, st.hi)], 8, 0)
+    op.getMOLSrcTerm(S, R, time=0.0, dt=1e-6, flux_factor=0.5, dx=st.dx)
+    ref, = oracle_lib.mol_rhs(cfg, [st])
+    _check(R.fabs[0].cpu().numpy(), ref, what="getMOLSrcTerm")
