@@ -416,3 +416,171 @@ int pc_mol_pass_times(pc_mol_handle* h, double* ms, int n) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Single-box right-hand side that allocates no device memory.
+//
+// For callers that cannot call cudaMalloc while they run: code inside a CUDA
+// stream capture, code driven by an external memory pool that forbids other
+// allocations, or an application that reserves all device memory up front.
+// The per-cell records, the launch lists and the diagnostic counters of one
+// box live in g_static_scratch, a fixed array that the CUDA runtime reserves
+// when this library is loaded and that every device holds until the process
+// exits.  The kernels are the ones pc_mol_rhs_level launches.
+// ---------------------------------------------------------------------------
+#include <mutex>
+
+namespace {
+
+constexpr size_t kStaticScratchBytes = size_t(48) << 20;  // 48 MiB
+constexpr int kStaticMaxDevices = 64;
+static __device__ __align__(256) unsigned char g_static_scratch[kStaticScratchBytes];
+
+std::mutex g_static_mu;
+void* g_static_ptr[kStaticMaxDevices] = {};
+
+// Device address of g_static_scratch on the current device.  Host code may
+// not use the symbol itself (it names a host-side shadow), so the address is
+// looked up once per device, with that device current, and cached.
+int static_scratch_address(void** out) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return PC_ERR_NO_DEVICE;
+  if (dev < 0 || dev >= kStaticMaxDevices) return PC_ERR_UNSUPPORTED;
+  std::lock_guard<std::mutex> lock(g_static_mu);
+  if (!g_static_ptr[dev]) {
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_static_scratch) != cudaSuccess || !p) return PC_ERR_CUDA;
+    g_static_ptr[dev] = p;
+  }
+  *out = g_static_ptr[dev];
+  return PC_OK;
+}
+
+size_t align256(size_t n) { return (n + 255) & ~size_t(255); }
+
+// Writes the box table, the pass-1 chunk list and the pass-2 tile list of one
+// box into the static array and clears the counters.
+__global__ void static_lists_kernel(DevBox b, int nitems, int ntiles, int tiles_x, int tiles_y, DevBox* box_out,
+                                    int2* items, int4* tiles, unsigned long long* counters) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t == 0) {
+    *box_out = b;
+    for (int c = 0; c < kNumCounters; ++c) counters[c] = 0ull;
+  }
+  if (t < nitems) items[t] = make_int2(0, (int)(t * kCellThreads));
+  if (t < ntiles) {
+    const int tx = (int)(t % tiles_x), ty = (int)((t / tiles_x) % tiles_y), tz = (int)(t / ((long long)tiles_x * tiles_y));
+    tiles[t] = make_int4(0, b.lo[0] + tx * kTX, b.lo[1] + ty * kTY, b.lo[2] + tz * kTZ);
+  }
+}
+
+}  // namespace
+
+extern "C" int pc_mol_rhs_box_static(const pc_mol_config* cfg, const pc_box_desc* box, const double dx[3],
+                                     void* stream) {
+  if (!cfg || !box || !dx) return PC_ERR_INVALID_ARGUMENT;
+  const pc_mol_config& c = *cfg;
+  if (c.nspec != c.mech.nspec) return PC_ERR_INVALID_ARGUMENT;
+  if (c.precision != PC_PRECISION_FP64) return PC_ERR_UNSUPPORTED;
+  for (int d = 0; d < 3; ++d)
+    if (!(dx[d] > 0.0) || !std::isfinite(dx[d])) return PC_ERR_INVALID_ARGUMENT;
+  int variant = 0;
+  if (c.nspec == 1 && c.eos == PC_EOS_GAMMA_LAW && c.transport == PC_TRANSPORT_CONSTANT) variant = 1;
+  if (c.nspec == 9 && c.eos == PC_EOS_IDEAL_MIX && c.transport == PC_TRANSPORT_SIMPLE) variant = 9;
+  if (!variant) return PC_ERR_UNSUPPORTED;
+  for (int k = 0; k < c.nspec; ++k)
+    if (!(c.mech.mw[k] > 0.0)) return PC_ERR_INVALID_ARGUMENT;
+  if (c.eos == PC_EOS_GAMMA_LAW && !(c.mech.gamma > 1.0)) return PC_ERR_INVALID_ARGUMENT;
+  const int nvar = 7 + c.nspec;
+  int rc = validate_box(*box, nvar);
+  if (rc != PC_OK) return rc;
+
+  DevMech<1> mech1{};
+  DevMech<9> mech9{};
+  int nrec;
+  if (variant == 1) {
+    fill_common(mech1, c.mech);
+    nrec = Rec<1>::N;
+  } else {
+    fill_common(mech9, c.mech);
+    rc = fill_idealmix(mech9, c.mech);
+    if (rc == PC_OK) rc = fill_simple(mech9, c.mech);
+    if (rc != PC_OK) return rc;
+    nrec = Rec<9>::N;
+  }
+  DevFlags fl{};
+  fl.do_hydro = c.do_hydro != 0;
+  fl.diffuse_vel = c.diffuse_vel != 0;
+  fl.diffuse_temp = c.diffuse_temp != 0;
+  fl.diffuse_spec = c.diffuse_spec != 0;
+  fl.diffuse_enth = c.diffuse_enth != 0;
+  fl.slopes = c.plm_iorder != 1;
+  fl.laxf = c.use_laxf_flux != 0;
+  fl.harmonic = c.transport_harmonic_mean != 0;
+  fl.check_output = c.check_output != 0;
+  fl.newton_maxit = c.newton_max_iter > 0 ? c.newton_max_iter : 50;
+
+  // Sections of the static array: counters | box | chunk list | tile list | records.
+  int n2[3], nt[3];
+  long long ncell = 1;
+  for (int d = 0; d < 3; ++d) {
+    n2[d] = box->hi[d] - box->lo[d] + 5;
+    ncell *= n2[d];
+  }
+  nt[0] = (box->hi[0] - box->lo[0] + kTX) / kTX;
+  nt[1] = (box->hi[1] - box->lo[1] + kTY) / kTY;
+  nt[2] = (box->hi[2] - box->lo[2] + kTZ) / kTZ;
+  const long long nitems = (ncell + kCellThreads - 1) / kCellThreads;
+  const long long ntiles = (long long)nt[0] * nt[1] * nt[2];
+  const size_t off_ctr = 0;
+  const size_t off_box = align256(off_ctr + sizeof(unsigned long long) * kNumCounters);
+  const size_t off_items = align256(off_box + sizeof(DevBox));
+  const size_t off_tiles = align256(off_items + sizeof(int2) * (size_t)nitems);
+  const size_t off_rec = align256(off_tiles + sizeof(int4) * (size_t)ntiles);
+  const size_t need = off_rec + sizeof(double) * (size_t)ncell * nrec;
+  if (need > kStaticScratchBytes) return PC_ERR_TOO_LARGE;
+
+  void* basev = nullptr;
+  rc = static_scratch_address(&basev);
+  if (rc != PC_OK) return rc;
+  unsigned char* base = static_cast<unsigned char*>(basev);
+  DevBox d{};
+  for (int a = 0; a < 3; ++a) {
+    d.lo[a] = box->lo[a];
+    d.hi[a] = box->hi[a];
+    d.sb[a] = box->state.begin[a];
+    d.rb[a] = box->rhs.begin[a];
+    d.g2lo[a] = box->lo[a] - 2;
+    d.n2[a] = n2[a];
+  }
+  d.S = box->state.p;
+  d.sj = box->state.jstride;
+  d.sk = box->state.kstride;
+  d.sn = box->state.nstride;
+  d.R = box->rhs.p;
+  d.rj = box->rhs.jstride;
+  d.rk = box->rhs.kstride;
+  d.rn = box->rhs.nstride;
+  d.ncell = ncell;
+  d.rec = reinterpret_cast<double*>(base + off_rec);
+  DevBox* dbox = reinterpret_cast<DevBox*>(base + off_box);
+  int2* items = reinterpret_cast<int2*>(base + off_items);
+  int4* tiles = reinterpret_cast<int4*>(base + off_tiles);
+  unsigned long long* ctr = reinterpret_cast<unsigned long long*>(base + off_ctr);
+
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const long long nlist = nitems > ntiles ? nitems : ntiles;
+  static_lists_kernel<<<(unsigned)((nlist + 255) / 256), 256, 0, s>>>(d, (int)nitems, (int)ntiles, nt[0], nt[1], dbox,
+                                                                       items, tiles, ctr);
+  const Geo g = make_geo(dx);
+  if (variant == 1) {
+    cell_kernel<1, GammaLawEos<1>, ConstantTransport<1>><<<(unsigned)nitems, kCellThreads, 0, s>>>(dbox, items, mech1,
+                                                                                                   fl, ctr);
+    flux_kernel<1, GammaLawEos<1>><<<(unsigned)ntiles, kFluxThreads, 0, s>>>(dbox, tiles, mech1, fl, g, ctr);
+  } else {
+    cell_kernel<9, IdealMixEos<9>, SimpleTransport<9>><<<(unsigned)nitems, kCellThreads, 0, s>>>(dbox, items, mech9,
+                                                                                                 fl, ctr);
+    flux_kernel<9, IdealMixEos<9>><<<(unsigned)ntiles, kFluxThreads, 0, s>>>(dbox, tiles, mech9, fl, g, ctr);
+  }
+  return cudaGetLastError() == cudaSuccess ? PC_OK : PC_ERR_CUDA;
+}
