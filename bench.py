@@ -143,14 +143,31 @@ def cpu_baseline(st, cfg, reps: int = 3) -> dict:
             "best_s": min(times), "median_s": statistics.median(times)}
 
 
-def traffic_from_profiles(workload_name: str):
+def profile_figures(workload_name: str) -> dict:
+    """Figures from the committed ncu summary of this workload (or {})."""
     path = os.path.join(ROOT, "profiles", f"dram_traffic_{workload_name}_fp64.txt")
-    if not os.path.exists(path):
-        return None
-    for ln in open(path):
-        if ln.startswith("dram_bytes_per_rhs:"):
-            return float(ln.split(":", 1)[1])
-    return None
+    out = {}
+    if os.path.exists(path):
+        for ln in open(path):
+            if ":" in ln and not ln.startswith("#"):
+                k, v = ln.split(":", 1)
+                out[k.strip()] = float(v)
+    return out
+
+
+def fp_peaks() -> dict:
+    """FP64 / FP32 FMA rates measured live (pelec_gb300/_lib/libpc_peaks.so)."""
+    import ctypes
+
+    path = os.path.join(ROOT, "pelec_gb300", "_lib", "libpc_peaks.so")
+    try:
+        lib = ctypes.CDLL(path)
+        out = (ctypes.c_double * 2)()
+        if lib.pc_measure_fp_rates(out) != 0:
+            return {}
+        return {"fp64_fma_tflops": out[0], "fp32_fma_tflops": out[1], "source": "pc_peaks.cu, measured in this run"}
+    except OSError:
+        return {}
 
 
 def run_reference(args):
@@ -235,30 +252,40 @@ def run_gpu(args):
         pg.all_reduce(t, op=pg.ReduceOp.MAX)
         return float(t.item())
 
-    for _ in range(max(3, args.warmup)):
-        op.rhs_level(S, R, st.dx)
-    barrier()
-    # device-resident value
-    clocks = ClockSampler(local)
-    clocks.start()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    barrier()
-    e0.record(stream)
-    for _ in range(args.steps):
-        op.rhs_level(S, R, st.dx)
-    e1.record(stream)
-    barrier()
-    clk = clocks.stop()
-    t_dev = maxover(e0.elapsed_time(e1) / 1e3)
-    # per-pass device time (events recorded by the library on the same stream)
-    tc, tf = [], []
-    for _ in range(args.steps):
-        op.rhs_level(S, R, st.dx)
-        a, b = op.pass_times()
-        tc.append(a)
-        tf.append(b)
+    def timed_steps(o, with_clocks=False):
+        """K device-resident steps; returns (seconds, clock record)."""
+        for _ in range(max(3, args.warmup)):
+            o.rhs_level(S, R, st.dx)
+        clocks = ClockSampler(local) if with_clocks else None
+        if clocks:
+            clocks.start()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        barrier()
+        e0.record(stream)
+        for _ in range(args.steps):
+            o.rhs_level(S, R, st.dx)
+        e1.record(stream)
+        barrier()
+        clk = clocks.stop() if clocks else None
+        return maxover(e0.elapsed_time(e1) / 1e3), clk
+
+    def pass_times(o):
+        tc, tf = [], []
+        for _ in range(args.steps):
+            o.rhs_level(S, R, st.dx)
+            a, b = o.pass_times()
+            tc.append(a)
+            tf.append(b)
+        return statistics.mean(tc), statistics.mean(tf)
+
+    t_dev, clk = timed_steps(op, with_clocks=True)
+    ms_cell, ms_flux = pass_times(op)
     status = op.status()
+    op.rhs_level(S, R, st.dx)
+    torch.cuda.synchronize()
+    r64 = R.fabs[0].cpu().numpy()
     # end to end through the public API: pinned host -> device -> RHS -> host
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     barrier()
     e0.record(stream)
     for _ in range(args.steps):
@@ -269,12 +296,21 @@ def run_gpu(args):
     barrier()
     t_e2e = maxover(e0.elapsed_time(e1) / 1e3)
 
+    # mixed precision on the same state, error against the FP64 result
+    opm = mol.MOLOperator(problems.make_config(mech, time_passes=1, precision=1))
+    t_mix, _ = timed_steps(opm)
+    ms_cell_m, ms_flux_m = pass_times(opm)
+    opm.rhs_level(S, R, st.dx)
+    torch.cuda.synchronize()
+    r32 = R.fabs[0].cpu().numpy()
+    l2 = [float(np.sqrt(((r32[n] - r64[n]) ** 2).sum() / max((r64[n] ** 2).sum(), 1e-300))) for n in range(r64.shape[0])]
+    mx = [float(np.abs(r32[n] - r64[n]).max() / max(np.abs(r64[n]).max(), 1e-300)) for n in range(r64.shape[0])]
+
     if rank != 0:
         if pg is not None:
             pg.destroy_process_group()
         return 0
     value = world * cells * args.steps / t_dev
-    ms_cell, ms_flux = statistics.mean(tc), statistics.mean(tf)
     ms_rhs = ms_cell + ms_flux
     ab = alg_bytes(st)
     import json as _json
@@ -283,7 +319,9 @@ def run_gpu(args):
         os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
     achieved = ab / (ms_rhs * 1e-3) / 1e9
-    traffic = traffic_from_profiles(args.workload)
+    prof = profile_figures(args.workload)
+    traffic = prof.get("dram_bytes_per_rhs")
+    peaks_fp = fp_peaks()
     line = {
         "metric": METRIC, "value": value, "unit": "cell-evals/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * t_dev / args.steps, "higher_is_better": True,
@@ -298,8 +336,19 @@ def run_gpu(args):
                      "frac": achieved / hbm_peak, "traffic": traffic,
                      "kernel": "cell_kernel + flux_kernel (one RHS)",
                      "alg_bytes_per_rhs": ab, "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)",
-                     "binding_resource": "FP64 pipe (see profiles/)"},
+                     "binding_resource": "FP64 pipe",
+                     "fp64_pipe_active_pct": {"flux_kernel": prof.get("fp64_pipe_active_pct_flux_kernel"),
+                                              "cell_kernel": prof.get("fp64_pipe_active_pct_cell_kernel"),
+                                              "source": "ncu --set full, profiles/flux_kernel_c2.md, cell_kernel_c2.md"},
+                     "fp_peaks": peaks_fp},
         "passes_ms": {"cell_kernel": ms_cell, "flux_kernel": ms_flux},
+        "mixed": {"value": world * cells * args.steps / t_mix, "unit": "cell-evals/s",
+                  "ms_per_step": 1e3 * t_mix / args.steps, "speedup_vs_fp64": t_dev / t_mix,
+                  "passes_ms": {"cell_kernel": ms_cell_m, "flux_kernel": ms_flux_m},
+                  "rel_l2_vs_fp64": {"max": max(l2), "per_component": l2},
+                  "rel_max_vs_fp64": {"max": max(mx), "per_component": mx},
+                  "precision": "FP32 reconstruction/Riemann/diffusion, FP64 Newton/mass fractions/divergence"},
+        "gpu_launches_mixed": 2 * args.steps,
         "status": {"cells": status.cells, "newton_nonconverged": status.newton_nonconverged,
                    "nonpositive_state": status.nonpositive_state, "nonfinite_output": status.nonfinite_output},
         "clocks": clk,

@@ -113,6 +113,9 @@ typedef struct pc_mol_config {
   int newton_max_iter;         /* cap on the EOS temperature Newton (0: 50)  */
   int time_passes;             /* record CUDA events around each pass        */
   int pad_;
+  double mixed_p_ref;          /* PC_PRECISION_MIXED: reference pressure the
+                                  FP32 flux arithmetic is offset by, dyn/cm^2
+                                  (<= 0: 1 atm); set it near the ambient p   */
   pc_mechanism mech;
 } pc_mol_config;
 

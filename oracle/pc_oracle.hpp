@@ -213,12 +213,12 @@ struct IdealMix {
     T = t;
   }
   void RTY2P(double rho, double T, const double* Y, double& p) const { p = rho * mix_rw<NS>(m, Y) * T; }
-  // c^2 = (cp/cv) p / rho with cp = cv + R/Wbar.
+  // c^2 = (cp/cv) p / rho with cp = cv + R/Wbar, evaluated as (cp p) / (cv rho).
   double cs_at(double rho, double p, double T, const double* Y, double rw) const {
     double C[6];
     coefs(Y, range(T), C);
     const double cv = cv_of(C, rw, T);
-    return std::sqrt((cv + rw) / cv * p / rho);
+    return std::sqrt((cv + rw) * p / (cv * rho));
   }
   void RTY2Cs(double rho, double T, const double* Y, double& cs) const {
     const double rw = mix_rw<NS>(m, Y);

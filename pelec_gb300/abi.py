@@ -75,6 +75,7 @@ class PcMolConfig(ctypes.Structure):
         ("newton_max_iter", c_int),
         ("time_passes", c_int),
         ("pad_", c_int),
+        ("mixed_p_ref", c_double),
         ("mech", PcMechanism),
     ]
 

@@ -1,7 +1,18 @@
 """Build recipe of the CUDA library ``pelec_gb300/_lib/libpelec_mol.so``.
 
-One translation unit per library, compiled by nvcc for sm_103a only, with no
-torch headers: the library is a plain C ABI (include/pelec_mol.h).
+Two translation units compiled by nvcc for sm_103a only (in parallel) and
+linked into one shared library with a plain C ABI (include/pelec_mol.h), no
+torch headers:
+
+* pc_mol.cu — the ABI, the host side and the FP64 kernels, compiled with
+  ``-fmad=false``: the FP64 kernels evaluate a fixed sequence of IEEE
+  operations (explicit fma() only where written), so they reproduce the CPU
+  restatement's arithmetic exactly; host code is built without contraction
+  too.
+* pc_mol_mixed.cu — the mixed-precision kernels, with contraction on.
+
+libpc_peaks.so (pc_peaks.cu) measures the FP64/FP32 FMA rates that bench.py
+uses as roofline denominators.
 """
 from __future__ import annotations
 
@@ -13,9 +24,12 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 LIBDIR = os.path.join(HERE, "_lib")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off"]
 
 LIBS = {
-    "libpelec_mol.so": ["pc_mol.cu"],
+    "libpelec_mol.so": [("pc_mol.cu", ["-fmad=false"]), ("pc_mol_mixed.cu", ["-fmad=true"])],
+    # arithmetic peak rates for bench.py's roofline (not part of the ABI)
+    "libpc_peaks.so": [("pc_peaks.cu", ["-fmad=true"])],
 }
 
 
@@ -37,25 +51,25 @@ def _deps():
 def build(force: bool = False, verbose: bool = False) -> list:
     os.makedirs(LIBDIR, exist_ok=True)
     newest = max(os.path.getmtime(p) for p in _deps())
-    procs, outs = [], []
-    for lib, srcs in LIBS.items():
+    outs = []
+    for lib, units in LIBS.items():
         out = os.path.join(LIBDIR, lib)
         outs.append(out)
         if not force and os.path.exists(out) and os.path.getmtime(out) >= newest:
             continue
-        # -fmad=false: the FP64 kernels evaluate a fixed sequence of IEEE
-        # operations (explicit fma() only where written), so they reproduce
-        # the CPU restatement's arithmetic exactly; host code likewise.
-        cmd = [nvcc(), *ARCH, "-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC",
-               "-Xcompiler", "-ffp-contract=off", "-shared",
-               "-I", os.path.join(ROOT, "include"), "-o", out + ".tmp"]
-        if verbose:
-            cmd += ["-Xptxas", "-v"]
-        cmd += [os.path.join(CSRC, s) for s in srcs]
-        procs.append((subprocess.Popen(cmd), out))
-    for p, out in procs:
-        if p.wait() != 0:
-            raise RuntimeError(f"nvcc failed building {os.path.basename(out)}")
+        procs, objs = [], []
+        for src, flags in units:
+            obj = os.path.join(LIBDIR, os.path.splitext(src)[0] + ".o")
+            cmd = [nvcc(), *ARCH, *COMMON, *flags, "-I", os.path.join(ROOT, "include"), "-c", "-o", obj,
+                   os.path.join(CSRC, src)]
+            if verbose:
+                cmd += ["-Xptxas", "-v"]
+            procs.append(subprocess.Popen(cmd))
+            objs.append(obj)
+        for p in procs:
+            if p.wait() != 0:
+                raise RuntimeError(f"nvcc failed building {lib}")
+        subprocess.run([nvcc(), *ARCH, "-shared", "-o", out + ".tmp", *objs], check=True)
         os.replace(out + ".tmp", out)
     return outs
 

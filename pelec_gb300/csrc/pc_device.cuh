@@ -53,6 +53,27 @@ struct DevFlags {
 // is compiled without multiply-add contraction).  The CPU restatement used
 // to check the kernels evaluates the same sequence.
 
+// a / b, correctly rounded, for a divisor b shared by several quotients, given
+// y = 1.0 / b (an IEEE division).  Markstein's theorem (IBM J. Res. Dev. 34,
+// 1990): if y = RN(1/b) and q is within one ulp of a/b, the remainder
+// r = a - b q is exact in one fma and RN(q + r y) = RN(a/b).  q0 = RN(a y) can
+// be up to 1.5 ulp off, so one correction brings it within an ulp and a
+// second gives the correctly rounded quotient: 1 multiply + 4 fma instead of
+// a full division.  A zero numerator gives a*y, the correctly signed zero;
+// outside |a|, |b| in [2^-400, 2^401) (where a remainder could underflow) and
+// for infinities and NaNs it divides directly.
+__device__ __forceinline__ double div_by(double a, double b, double y) {
+  const int ha = __double2hiint(a), hb = __double2hiint(b);
+  const double q0 = a * y;
+  if (((ha & 0x7fffffff) | __double2loint(a)) == 0) return q0;  // +-0 numerator: the signed zero quotient
+  const unsigned ea = (unsigned)((ha >> 20) & 0x7ff), eb = (unsigned)((hb >> 20) & 0x7ff);
+  if (ea - 623u > 800u || eb - 623u > 800u) return a / b;
+  double r = fma(-b, q0, a);
+  const double q = fma(r, y, q0);
+  r = fma(-b, q, a);
+  return fma(r, y, q);
+}
+
 __device__ __forceinline__ double horner4(const double c[4], double L) {
   return fma(L, fma(L, fma(L, c[3], c[2]), c[1]), c[0]);
 }
@@ -113,9 +134,10 @@ template <int NS>
 struct IdealMixEos {
   static constexpr bool kIdealMix = true;
   __device__ static int range(const DevMech<NS>& m, double T) { return (T < m.tmid) ? 0 : 1; }
+  template <int NC = 6>
   __device__ static void coefs(const DevMech<NS>& m, const double* Y, int r, double C[6]) {
 #pragma unroll
-    for (int n = 0; n < 6; ++n) {
+    for (int n = 0; n < NC; ++n) {
       double s = 0.0;
 #pragma unroll
       for (int k = 0; k < NS; ++k) s = fma(Y[k], m.cpc[r][n][k], s);
@@ -165,9 +187,9 @@ struct IdealMixEos {
   // c^2 = (cp/cv) p / rho, cp = cv + R/Wbar, at temperature T.
   __device__ static double cs_T(const DevMech<NS>& m, const double* Y, double rw, double rho, double T, double p) {
     double C[6];
-    coefs(m, Y, range(m, T), C);
+    coefs<5>(m, Y, range(m, T), C);
     const double cv = cv_of(C, rw, T);
-    return sqrt((cv + rw) / cv * p / rho);
+    return sqrt((cv + rw) * p / (cv * rho));
   }
   // RPY2Cs: T = p / (rho R/Wbar).
   __device__ static double cs_rp(const DevMech<NS>& m, const double* Y, double rw, double rho, double p) {

@@ -46,6 +46,7 @@ struct Geo {
   double dxinv[3];
   double area[3];
   double vol;
+  double p_ref;  // mixed precision: pressure offset of the FP32 records
 };
 
 // Record fields (pass 1 -> pass 2).
@@ -143,12 +144,13 @@ __global__ void __launch_bounds__(kCellThreads)
 }
 
 // ---------------------------------------------------------------------------
-// Face flux (extensive, times area) on the low face of cell (i,j,k) in
-// direction d; F has NVAR = 7 + NS entries.
+// Hyperbolic flux on the low face of the cell at record index cR in
+// direction d, times the face area: F[n] = flux_n * A (Riemann.H, MOL.cpp).
+// Divisions that share a divisor use div_by (exact, see pc_device.cuh).
 // ---------------------------------------------------------------------------
 template <int NS, class EOS, int d>
 __device__ __forceinline__ void hydro_face(const DevBox& b, const DevMech<NS>& m, const DevFlags& f, long long cR,
-                                           long long st, double* F) {
+                                           long long st, double A, double* F) {
   using RC = Rec<NS>;
   const double* rec = b.rec;
   const long long N = b.ncell;
@@ -162,24 +164,25 @@ __device__ __forceinline__ void hydro_face(const DevBox& b, const DevMech<NS>& m
   const double uLL = ld(fun, cLL), uL = ld(fun, cL), uR = ld(fun, cR), uRR = ld(fun, cRR);
   const double cLc = ld(RC::C, cL), cRc = ld(RC::C, cR);
   const double t1L = ld(fut1, cL), t1R = ld(fut1, cR), t2L = ld(fut2, cL), t2R = ld(fut2, cR);
+  const double ycL = 1.0 / cLc, ycR = 1.0 / cRc;
 
-  // Characteristic slopes of cells L and R (mol_slope), components 0..3.
+  // Characteristic slopes of cells L and R (mol_slope, MOL.H:53-112).
   double dqL[4] = {0.0, 0.0, 0.0, 0.0}, dqR[4] = {0.0, 0.0, 0.0, 0.0};
   const bool slopes = f.slopes != 0;
   const double dpl = pL - pLL, dpc = pR - pL, dpr = pRR - pR;
   if (slopes) {
     const double t1LL = ld(fut1, cLL), t1RR = ld(fut1, cRR), t2LL = ld(fut2, cLL), t2RR = ld(fut2, cRR);
     {
-      const double a = 0.5 * dpl / cLc, bb = 0.5 * rL * (uL - uLL);
-      const double a2 = 0.5 * dpc / cLc, b2 = 0.5 * rL * (uR - uL);
+      const double a = div_by(0.5 * dpl, cLc, ycL), bb = 0.5 * rL * (uL - uLL);
+      const double a2 = div_by(0.5 * dpc, cLc, ycL), b2 = 0.5 * rL * (uR - uL);
       dqL[0] = mc_limit(a - bb, a2 - b2);
       dqL[1] = mc_limit(a + bb, a2 + b2);
       dqL[2] = mc_limit(t1L - t1LL, t1R - t1L);
       dqL[3] = mc_limit(t2L - t2LL, t2R - t2L);
     }
     {
-      const double a = 0.5 * dpc / cRc, bb = 0.5 * rR * (uR - uL);
-      const double a2 = 0.5 * dpr / cRc, b2 = 0.5 * rR * (uRR - uR);
+      const double a = div_by(0.5 * dpc, cRc, ycR), bb = 0.5 * rR * (uR - uL);
+      const double a2 = div_by(0.5 * dpr, cRc, ycR), b2 = 0.5 * rR * (uRR - uR);
       dqR[0] = mc_limit(a - bb, a2 - b2);
       dqR[1] = mc_limit(a + bb, a2 + b2);
       dqR[2] = mc_limit(t1R - t1L, t1RR - t1R);
@@ -200,24 +203,26 @@ __device__ __forceinline__ void hydro_face(const DevBox& b, const DevMech<NS>& m
   {
     const double sL = dqL[0] + dqL[1], sR = dqR[0] + dqR[1];
     const double cL2 = cLc * cLc, cR2 = cRc * cRc;
+    const double ycL2 = 1.0 / cL2, ycR2 = 1.0 / cR2;
 #pragma unroll
     for (int n = 0; n < NS; ++n) {
       const double yLL = ld(RC::Y + n, cLL), yL = ld(RC::Y + n, cL), yR = ld(RC::Y + n, cR), yRR = ld(RC::Y + n, cRR);
       double dsL = 0.0, dsR = 0.0;
       if (slopes) {
         const double ryL = rL * yL, ryR = rR * yR;
-        dsL = mc_limit(ryL - rLL * yLL - yL * dpl / cL2, ryR - ryL - yL * dpc / cL2);
-        dsR = mc_limit(ryR - ryL - yR * dpc / cR2, rRR * yRR - ryR - yR * dpr / cR2);
+        dsL = mc_limit(ryL - rLL * yLL - div_by(yL * dpl, cL2, ycL2), ryR - ryL - div_by(yL * dpc, cL2, ycL2));
+        dsR = mc_limit(ryR - ryL - div_by(yR * dpc, cR2, ycR2), rRR * yRR - ryR - div_by(yR * dpr, cR2, ycR2));
       }
-      spl[n] = yL * rL + 0.5 * (dsL + yL * sL / cLc);
-      spr[n] = yR * rR - 0.5 * (dsR + yR * sR / cRc);
+      spl[n] = yL * rL + 0.5 * (dsL + div_by(yL * sL, cLc, ycL));
+      spr[n] = yR * rR - 0.5 * (dsR + div_by(yR * sR, cRc, ycR));
       rl += spl[n];
       rr += spr[n];
     }
+    const double yrl = 1.0 / rl, yrr = 1.0 / rr;
 #pragma unroll
     for (int n = 0; n < NS; ++n) {
-      spl[n] = spl[n] / rl;
-      spr[n] = spr[n] / rr;
+      spl[n] = div_by(spl[n], rl, yrl);
+      spr[n] = div_by(spr[n], rr, yrr);
     }
   }
   const double cavg = 0.5 * (cRc + cLc);
@@ -231,8 +236,9 @@ __device__ __forceinline__ void hydro_face(const DevBox& b, const DevMech<NS>& m
     const double wsmall = 2.2250738585072014e-308;
     const double wl = fmax(wsmall, cl * rl);
     const double wr = fmax(wsmall, cr * rr);
-    const double pstar = fmax(wsmall, ((wr * pl + wl * pr) + wl * wr * (unl - unr)) / (wl + wr));
-    double ustar = ((wl * unl + wr * unr) + (pl - pr)) / (wl + wr);
+    const double ww = wl + wr, yww = 1.0 / ww;
+    const double pstar = fmax(wsmall, div_by((wr * pl + wl * pr) + wl * wr * (unl - unr), ww, yww));
+    double ustar = div_by((wl * unl + wr * unr) + (pl - pr), ww, yww);
     bool mask = ustar > 0.0;
     double rspo[NS];
     double uo = mask ? unl : unr;
@@ -249,8 +255,11 @@ __device__ __forceinline__ void hydro_face(const DevBox& b, const DevMech<NS>& m
     uo = m0 ? 0.5 * (unl + unr) : uo;
     po = m0 ? 0.5 * (pl + pr) : po;
     double Yt[NS];
+    {
+      const double y = 1.0 / ro;
 #pragma unroll
-    for (int n = 0; n < NS; ++n) Yt[n] = rspo[n] / ro;
+      for (int n = 0; n < NS; ++n) Yt[n] = div_by(rspo[n], ro, y);
+    }
     const double co = EOS::cs_rp(m, Yt, mix_rw<NS>(m, Yt), ro, po);
     const double drho = (pstar - po) / (co * co);
     double rspstar[NS];
@@ -260,8 +269,11 @@ __device__ __forceinline__ void hydro_face(const DevBox& b, const DevMech<NS>& m
       rspstar[n] = fmax(0.0, rspo[n] + drho * Yt[n]);
       rstar += rspstar[n];
     }
+    {
+      const double y = 1.0 / rstar;
 #pragma unroll
-    for (int n = 0; n < NS; ++n) Yt[n] = rspstar[n] / rstar;
+      for (int n = 0; n < NS; ++n) Yt[n] = div_by(rspstar[n], rstar, y);
+    }
     const double cstar = EOS::cs_rp(m, Yt, mix_rw<NS>(m, Yt), rstar, pstar);
     const double sgnm = copysign(1.0, ustar);
     double spout = co - sgnm * uo;
@@ -294,8 +306,11 @@ __device__ __forceinline__ void hydro_face(const DevBox& b, const DevMech<NS>& m
       flY[n] = g;
       rgd += g;
     }
+    {
+      const double y = 1.0 / rgd;
 #pragma unroll
-    for (int n = 0; n < NS; ++n) Yt[n] = flY[n] / rgd;
+      for (int n = 0; n < NS; ++n) Yt[n] = div_by(flY[n], rgd, y);
+    }
     const double regd = rgd * EOS::e_rp(m, Yt, mix_rw<NS>(m, Yt), rgd, gdp);
     fl_rho = rgd * iu;
 #pragma unroll
@@ -331,19 +346,22 @@ __device__ __forceinline__ void hydro_face(const DevBox& b, const DevMech<NS>& m
     fl_E = 0.5 * (((r_elt + pl) * unl + (r_ert + pr) * unr) - mw * (r_ert - r_elt));
     fl_ei = 0.5 * ((rl * el * unl + rr * er * unr) - mw * (rr * er - rl * el));
   }
-  F[URHO] += fl_rho;
-  F[UMX + d] += fl_un;
-  F[(d == 0) ? UMY : UMX] += fl_ut1;
-  F[(d == 2) ? UMY : UMZ] += fl_ut2;
-  F[UEDEN] += fl_E;
-  F[UEINT] += fl_ei;
+  F[URHO] = fl_rho * A;
+  F[UMX + d] = fl_un * A;
+  F[(d == 0) ? UMY : UMX] = fl_ut1 * A;
+  F[(d == 2) ? UMY : UMZ] = fl_ut2 * A;
+  F[UEDEN] = fl_E * A;
+  F[UEINT] = fl_ei * A;
+  F[UTEMP] = 0.0;
 #pragma unroll
-  for (int n = 0; n < NS; ++n) F[UFS + n] += flY[n];
+  for (int n = 0; n < NS; ++n) F[UFS + n] = flY[n] * A;
 }
 
-// pc_diffusion_flux + SpeciesEnergyFlux (Diffterm.H:20-75, 344-461), before
-// the area scaling; components switched off by the diffuse_* flags are left
-// at zero (Diffusion.cpp:321-341).
+// pc_diffusion_flux + SpeciesEnergyFlux (Diffterm.H:20-75, 344-461), times
+// the area, added to the hyperbolic flux already in F (the reference stores
+// the diffusion flux and adds the hyperbolic one, MOL.cpp:199-201; the sum of
+// two rounded terms does not depend on their order).  Components switched off
+// by the diffuse_* flags get no diffusion term (Diffusion.cpp:321-341).
 template <int NS, class EOS, int d>
 __device__ __forceinline__ void diffusion_face(const DevBox& b, const DevFlags& f, const Geo& g, long long cR,
                                                const long long stv[3], double* F) {
@@ -410,14 +428,14 @@ __device__ __forceinline__ void diffusion_face(const DevBox& b, const DevFlags& 
     for (int n = 0; n < NS; ++n) {
       const double v = Vd[n] - Yf[n] * Vc;
       fE -= Yf[n] * hf[n] * Vc;
-      if (spec) F[UFS + n] = v * A;
+      if (spec) F[UFS + n] += v * A;
     }
   }
   if (f.diffuse_vel) {
 #pragma unroll
-    for (int a = 0; a < 3; ++a) F[UMX + a] = -tau[a] * A;
+    for (int a = 0; a < 3; ++a) F[UMX + a] += -tau[a] * A;
   }
-  if (ener) F[UEDEN] = fE * A;
+  if (ener) F[UEDEN] += fE * A;
 }
 
 // ---------------------------------------------------------------------------
@@ -441,19 +459,13 @@ __device__ __forceinline__ void dir_pass(const DevBox& b, const DevMech<NS>& m, 
     const int i = o[0] + fx, j = o[1] + fy, k = o[2] + fz;
     const long long cR = (i - b.g2lo[0]) + (j - b.g2lo[1]) * stv[1] + (k - b.g2lo[2]) * stv[2];
     double F[NVAR];
-#pragma unroll
-    for (int n = 0; n < NVAR; ++n) F[n] = 0.0;
-    if (diff) diffusion_face<NS, EOS, d>(b, f, g, cR, stv, F);
     if (f.do_hydro) {
-      double H[NVAR];
+      hydro_face<NS, EOS, d>(b, m, f, cR, stv[d], g.area[d], F);
+    } else {
 #pragma unroll
-      for (int n = 0; n < NVAR; ++n) H[n] = 0.0;
-      hydro_face<NS, EOS, d>(b, m, f, cR, stv[d], H);
-      const double A = g.area[d];
-#pragma unroll
-      for (int n = 0; n < NVAR; ++n) F[n] += H[n] * A;
+      for (int n = 0; n < NVAR; ++n) F[n] = 0.0;
     }
-    F[UTEMP] = 0.0;
+    if (diff) diffusion_face<NS, EOS, d>(b, f, g, cR, stv, F);
 #pragma unroll
     for (int n = 0; n < NVAR; ++n) fbuf[n][fi] = F[n];
   }
@@ -468,7 +480,7 @@ __device__ __forceinline__ void dir_pass(const DevBox& b, const DevMech<NS>& m, 
 }
 
 template <int NS, class EOS>
-__global__ void __launch_bounds__(kFluxThreads, 1)
+__global__ void __launch_bounds__(kFluxThreads, 2)
     flux_kernel(const DevBox* __restrict__ boxes, const int4* __restrict__ tiles, const __grid_constant__ DevMech<NS> m,
                 const DevFlags f, const Geo g, unsigned long long* __restrict__ counters) {
   constexpr int NVAR = 7 + NS;

@@ -1,0 +1,671 @@
+// pc_mixed.cuh — mixed-precision form of the MOL right-hand side.
+//
+// Same two passes as the FP64 form (pc_kernels.cuh) with the precision split
+// of PC_PRECISION_MIXED:
+//   FP64: conserved -> primitive conversion including the cell mass
+//         fractions Y_k = rho Y_k / rho, the EOS temperature Newton solve,
+//         p = rho (R/Wbar) T, mole fractions, the Godunov-state internal
+//         energy, and the flux-divergence accumulation (each FP32
+//         face flux is widened exactly to FP64 before the differences, so the
+//         telescoping sum conserves mass, momentum and energy to FP64
+//         round-off).
+//   FP32: sound speed, transport coefficients, MOL slopes and face states
+//         (including the face mass-fraction renormalisation), the Riemann
+//         solver and its EOS calls, and the diffusion fluxes.
+// FP32 pressure is carried as p - p_ref (p_ref from the configuration): the
+// slopes, the Riemann star pressure and the pressure gradients only use
+// differences, the EOS calls add p_ref back, and the normal-momentum flux
+// drops the constant p_ref, whose divergence is zero on a uniform grid.
+// Records are FP32 except the mole fractions, kept in FP64 after the FP32
+// fields: diffusion is driven by their cell-to-cell differences, which in the
+// far field are ~1e-6 of X itself and would be lost in FP32; the differences
+// are taken in FP64 and rounded to FP32.  The internal energy of the Godunov
+// state is evaluated in FP64 (its formation-energy terms cancel to ~1e-2 of
+// their size, which FP32 cannot carry).
+#pragma once
+
+#include "pc_kernels.cuh"
+
+namespace pcg {
+
+template <int NS>
+struct MechF {
+  float rW[NS];
+  float cpc[2][6][NS];
+  float tmid;
+  float visc[NS][4], cond[NS][4], bulk[NS];
+  float diff[(NS * (NS - 1)) / 2 + 1][4];
+  float inv_pref;
+  float gamma, gm1, cpk[NS];
+  float const_mu, const_xi, const_lam, const_rhoD;
+  float p_ref;
+};
+
+template <int NS>
+__host__ MechF<NS> to_float(const DevMech<NS>& m, double p_ref) {
+  MechF<NS> f{};
+  for (int k = 0; k < NS; ++k) {
+    f.rW[k] = (float)m.rW[k];
+    f.cpk[k] = (float)m.cpk[k];
+    f.bulk[k] = (float)m.bulk[k];
+    for (int n = 0; n < 4; ++n) {
+      f.visc[k][n] = (float)m.visc[k][n];
+      f.cond[k][n] = (float)m.cond[k][n];
+    }
+    for (int r = 0; r < 2; ++r)
+      for (int n = 0; n < 6; ++n) f.cpc[r][n][k] = (float)m.cpc[r][n][k];
+  }
+  for (int q = 0; q < (NS * (NS - 1)) / 2 + 1; ++q)
+    for (int n = 0; n < 4; ++n) f.diff[q][n] = (float)m.diff[q][n];
+  f.tmid = (float)m.tmid;
+  f.inv_pref = (float)m.inv_pref;
+  f.gamma = (float)m.gamma;
+  f.gm1 = (float)m.gm1;
+  f.const_mu = (float)m.const_mu;
+  f.const_xi = (float)m.const_xi;
+  f.const_lam = (float)m.const_lam;
+  f.const_rhoD = (float)m.const_rhoD;
+  f.p_ref = (float)p_ref;
+  return f;
+}
+
+// FP64 mole fractions stored after the FP32 fields of a mixed record.
+template <int NS>
+__device__ __forceinline__ double* mixed_x(const DevBox& b) {
+  return reinterpret_cast<double*>(reinterpret_cast<float*>(b.rec) + (long long)Rec<NS>::N * b.ncell);
+}
+
+template <int NS>
+__device__ __forceinline__ float mix_rwf(const MechF<NS>& m, const float* Y) {
+  float s = 0.f;
+#pragma unroll
+  for (int k = 0; k < NS; ++k) s = fmaf(Y[k], m.rW[k], s);
+  return s;
+}
+
+// FP32 equations of state; p is the absolute pressure.
+template <int NS, bool MIX>
+struct EosF;
+
+template <int NS>
+struct EosF<NS, false> {
+  __device__ static float cs_T(const MechF<NS>& m, const float*, float, float rho, float, float p) {
+    return sqrtf(m.gamma * p / rho);
+  }
+  __device__ static float cs_rp(const MechF<NS>& m, const float*, float, float rho, float p) {
+    return sqrtf(m.gamma * p / rho);
+  }
+  __device__ static float e_rp(const MechF<NS>& m, const float*, float, float rho, float p) { return p / (m.gm1 * rho); }
+  __device__ static void hi(const MechF<NS>& m, float T, float* h) {
+#pragma unroll
+    for (int k = 0; k < NS; ++k) h[k] = m.cpk[k] * T;
+  }
+};
+
+template <int NS>
+struct EosF<NS, true> {
+  template <int NC>
+  __device__ static void coefs(const MechF<NS>& m, const float* Y, int r, float* C) {
+#pragma unroll
+    for (int n = 0; n < NC; ++n) {
+      float s = 0.f;
+#pragma unroll
+      for (int k = 0; k < NS; ++k) s = fmaf(Y[k], m.cpc[r][n][k], s);
+      C[n] = s;
+    }
+  }
+  __device__ static float cs_T(const MechF<NS>& m, const float* Y, float rw, float rho, float T, float p) {
+    float C[5];
+    coefs<5>(m, Y, T < m.tmid ? 0 : 1, C);
+    const float cv = (C[0] - rw) + T * fmaf(T, fmaf(T, fmaf(T, C[4], C[3]), C[2]), C[1]);
+    return sqrtf((cv + rw) * p / (cv * rho));
+  }
+  __device__ static float cs_rp(const MechF<NS>& m, const float* Y, float rw, float rho, float p) {
+    return cs_T(m, Y, rw, rho, p / (rho * rw), p);
+  }
+  __device__ static float e_rp(const MechF<NS>& m, const float* Y, float rw, float rho, float p) {
+    const float T = p / (rho * rw);
+    float C[6];
+    coefs<6>(m, Y, T < m.tmid ? 0 : 1, C);
+    const float q = fmaf(T, fmaf(T, fmaf(T, fmaf(T, C[4] * 0.2f, C[3] * 0.25f), C[2] * (1.f / 3.f)), C[1] * 0.5f), C[0] - rw);
+    return fmaf(T, q, C[5]);
+  }
+  __device__ static void hi(const MechF<NS>& m, float T, float* h) {
+    const int r = T < m.tmid ? 0 : 1;
+#pragma unroll
+    for (int k = 0; k < NS; ++k) {
+      const float q = fmaf(T, fmaf(T, fmaf(T, fmaf(T, m.cpc[r][4][k] * 0.2f, m.cpc[r][3][k] * 0.25f),
+                                           m.cpc[r][2][k] * (1.f / 3.f)),
+                                  m.cpc[r][1][k] * 0.5f),
+                           m.cpc[r][0][k]);
+      h[k] = fmaf(T, q, m.cpc[r][5][k]);
+    }
+  }
+};
+
+__device__ __forceinline__ float horner4f(const float c[4], float L) { return fmaf(L, fmaf(L, fmaf(L, c[3], c[2]), c[1]), c[0]); }
+
+// FP32 transport: the same formulas as SimpleTransport / ConstantTransport.
+template <int NS, bool SIMPLE>
+struct TransF {
+  __device__ static void eval(const MechF<NS>& m, float T, float rho, float p, const float* Y, const float* X, float* out) {
+    if constexpr (!SIMPLE) {
+#pragma unroll
+      for (int k = 0; k < NS; ++k) out[k] = m.const_rhoD;
+      out[NS] = m.const_mu;
+      out[NS + 1] = m.const_xi;
+      out[NS + 2] = m.const_lam;
+    } else {
+      const float L = logf(T);
+      float smu = 0.f, slam = 0.f, sxi = 0.f;
+#pragma unroll
+      for (int k = 0; k < NS; ++k) {
+        const float mk = expf(horner4f(m.visc[k], L));
+        const float m2 = mk * mk;
+        smu = fmaf(X[k], m2 * m2 * m2, smu);
+        slam = fmaf(X[k], expf(0.25f * horner4f(m.cond[k], L)), slam);
+        sxi = fmaf(X[k], m.bulk[k] * mk, sxi);
+      }
+      float s[NS];
+#pragma unroll
+      for (int k = 0; k < NS; ++k) s[k] = 0.f;
+      const float pr = p * m.inv_pref;
+      int q = 0;
+#pragma unroll
+      for (int k = 0; k < NS; ++k) {
+#pragma unroll
+        for (int j = k + 1; j < NS; ++j, ++q) {
+          const float invD = expf(-horner4f(m.diff[q], L)) * pr;
+          s[k] = fmaf(fmaxf(X[j], 1e-15f), invD, s[k]);
+          s[j] = fmaf(fmaxf(X[k], 1e-15f), invD, s[j]);
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < NS; ++k) out[k] = (s[k] > 0.f) ? rho * (1.f - Y[k]) / s[k] : 0.f;
+      out[NS] = expf(logf(smu) * (1.f / 6.f));
+      out[NS + 1] = sxi;
+      const float l2 = slam * slam;
+      out[NS + 2] = l2 * l2;
+    }
+  }
+};
+
+__device__ __forceinline__ float mc_limitf(float dl, float dr) {
+  const float dcen = 0.5f * (dl + dr);
+  const float dlim = (dl * dr >= 0.f) ? 2.f * fminf(fabsf(dl), fabsf(dr)) : 0.f;
+  return copysignf(1.f, dcen) * fminf(dlim, fabsf(dcen));
+}
+
+__device__ __forceinline__ float face_coeff(float a, float b, bool harmonic) {
+  if (harmonic) {
+    const float ab = a * b;
+    return (ab > 0.f) ? 2.f * ab / (a + b) : 0.f;
+  }
+  return 0.5f * (a + b);
+}
+
+// ---------------------------------------------------------------------------
+// Pass 1, mixed precision.  Records are FP32, in the field order of Rec<NS>
+// (P holds p - p_ref).
+// ---------------------------------------------------------------------------
+template <int NS, class EOSD, bool MIX, bool SIMPLE>
+__global__ void __launch_bounds__(kCellThreads)
+    cell_kernel_mixed(const DevBox* __restrict__ boxes, const int2* __restrict__ items,
+                      const __grid_constant__ DevMech<NS> m, const __grid_constant__ MechF<NS> mf, const DevFlags f,
+                      unsigned long long* __restrict__ counters) {
+  using RC = Rec<NS>;
+  const int2 it = items[blockIdx.x];
+  const DevBox& b = boxes[it.x];
+  const long long c = (long long)it.y + threadIdx.x;
+  bool newton_fail = false, nonpos = false;
+  if (c < b.ncell) {
+    const int nx = b.n2[0], ny = b.n2[1];
+    const int i = b.g2lo[0] + (int)(c % nx);
+    const int j = b.g2lo[1] + (int)((c / nx) % ny);
+    const int k = b.g2lo[2] + (int)(c / ((long long)nx * ny));
+    const double* s = b.S + (i - b.sb[0]) + (long long)(j - b.sb[1]) * b.sj + (long long)(k - b.sb[2]) * b.sk;
+    const long long sn = b.sn;
+    const double rho = __ldg(s + URHO * sn);
+    const double rhoinv = 1.0 / rho;
+    const double vx = __ldg(s + UMX * sn) * rhoinv;
+    const double vy = __ldg(s + UMY * sn) * rhoinv;
+    const double vz = __ldg(s + UMZ * sn) * rhoinv;
+    const double e = (__ldg(s + UEDEN * sn) - 0.5 * rho * (vx * vx + vy * vy + vz * vz)) * rhoinv;
+    double Y[NS];
+    float Yf[NS];
+#pragma unroll
+    for (int n = 0; n < NS; ++n) {
+      double y = __ldg(s + (UFS + n) * sn) * rhoinv;
+      if (-1e-4 * 2.220446049250313e-16 < y && y < 1e-4 * 2.220446049250313e-16) y = 0.0;
+      Y[n] = y;
+      Yf[n] = (float)y;
+    }
+    const double rw = mix_rw<NS>(m, Y);
+    bool ok = true;
+    const double T = EOSD::rey2t(m, Y, rw, e, __ldg(s + UTEMP * sn), f.newton_maxit, ok);
+    const double p = rho * rw * T;
+    newton_fail = !ok;
+    nonpos = !(rho > 0.0) || !(p > 0.0) || !(T > 0.0);
+    const float rhof = (float)rho, Tf = (float)T, pf = (float)p, rwf = (float)rw;
+    const float cs = EosF<NS, MIX>::cs_T(mf, Yf, rwf, rhof, Tf, pf);
+    float* r = reinterpret_cast<float*>(b.rec) + c;
+    const long long N = b.ncell;
+    r[RC::RHO * N] = rhof;
+    r[RC::U * N] = (float)vx;
+    r[RC::V * N] = (float)vy;
+    r[RC::W * N] = (float)vz;
+    r[RC::P * N] = (float)(p - (double)mf.p_ref);
+    r[RC::C * N] = cs;
+#pragma unroll
+    for (int n = 0; n < NS; ++n) r[(RC::Y + n) * N] = Yf[n];
+    const bool inner = i >= b.lo[0] - 1 && i <= b.hi[0] + 1 && j >= b.lo[1] - 1 && j <= b.hi[1] + 1 &&
+                       k >= b.lo[2] - 1 && k <= b.hi[2] + 1;
+    if (inner) {
+      float X[NS];
+      double* xr = mixed_x<NS>(b) + c;
+      const double irw = 1.0 / rw;
+#pragma unroll
+      for (int n = 0; n < NS; ++n) {
+        const double x = Y[n] * m.rW[n] * irw;
+        xr[n * N] = x;
+        X[n] = (float)x;
+      }
+      float out[NS + 3];
+      TransF<NS, SIMPLE>::eval(mf, Tf, rhof, pf, Yf, X, out);
+      r[RC::T * N] = Tf;
+      float h[NS];
+      EosF<NS, MIX>::hi(mf, Tf, h);
+#pragma unroll
+      for (int n = 0; n < NS; ++n) r[(RC::H + n) * N] = h[n];
+#pragma unroll
+      for (int n = 0; n < NS + 3; ++n) r[(RC::D + n) * N] = out[n];
+    }
+  }
+  warp_count(&counters[kCounterNewton], newton_fail);
+  warp_count(&counters[kCounterNonpos], nonpos);
+}
+
+// FP32 hyperbolic face flux (not area-scaled); normal momentum without p_ref.
+// Internal energy at (rho, Y, p) in FP64 (RYP2E), from FP32 inputs.
+template <int NS, bool MIX>
+__device__ __forceinline__ double e_rp_fp64(const DevMech<NS>& md, const float* rY, float rho, double p) {
+  const double r = (double)rho, ir = 1.0 / r;
+  double Y[NS];
+#pragma unroll
+  for (int n = 0; n < NS; ++n) Y[n] = (double)rY[n] * ir;
+  const double rw = mix_rw<NS>(md, Y);
+  if constexpr (MIX)
+    return IdealMixEos<NS>::e_rp(md, Y, rw, r, p);
+  else
+    return GammaLawEos<NS>::e_rp(md, Y, rw, r, p);
+}
+
+// FP64 internal energy from FP32 mass fractions Y (for Lax-Friedrichs sides).
+template <int NS, bool MIX>
+__device__ __forceinline__ double e_rpY_fp64(const DevMech<NS>& md, const float* Yf, float rho, double p) {
+  double Y[NS];
+#pragma unroll
+  for (int n = 0; n < NS; ++n) Y[n] = (double)Yf[n];
+  const double rw = mix_rw<NS>(md, Y);
+  if constexpr (MIX)
+    return IdealMixEos<NS>::e_rp(md, Y, rw, (double)rho, p);
+  else
+    return GammaLawEos<NS>::e_rp(md, Y, rw, (double)rho, p);
+}
+
+// The total and internal energy fluxes (FE, FEI) are returned in FP64: their
+// divergence is ~1e-3 of their size, below what an FP32 flux can resolve.
+template <int NS, bool MIX, int d>
+__device__ __forceinline__ void hydro_face_f(const DevBox& b, const MechF<NS>& m, const DevMech<NS>& md,
+                                             const DevFlags& f, long long cR, long long st, float* F, double& FE,
+                                             double& FEI) {
+  using RC = Rec<NS>;
+  using E = EosF<NS, MIX>;
+  const float* rec = reinterpret_cast<const float*>(b.rec);
+  const long long N = b.ncell;
+  const long long cL = cR - st, cLL = cL - st, cRR = cR + st;
+  auto ld = [&](int fld, long long c) { return __ldg(rec + (long long)fld * N + c); };
+  const int fun = RC::U + d;
+  const int fut1 = (d == 0) ? RC::V : RC::U;
+  const int fut2 = (d == 2) ? RC::V : RC::W;
+  const float rLL = ld(RC::RHO, cLL), rL = ld(RC::RHO, cL), rR = ld(RC::RHO, cR), rRR = ld(RC::RHO, cRR);
+  const float pLL = ld(RC::P, cLL), pL = ld(RC::P, cL), pR = ld(RC::P, cR), pRR = ld(RC::P, cRR);
+  const float uLL = ld(fun, cLL), uL = ld(fun, cL), uR = ld(fun, cR), uRR = ld(fun, cRR);
+  const float cLc = ld(RC::C, cL), cRc = ld(RC::C, cR);
+  const float t1L = ld(fut1, cL), t1R = ld(fut1, cR), t2L = ld(fut2, cL), t2R = ld(fut2, cR);
+  const float icL = 1.f / cLc, icR = 1.f / cRc;
+  float dqL[4] = {0.f, 0.f, 0.f, 0.f}, dqR[4] = {0.f, 0.f, 0.f, 0.f};
+  const bool slopes = f.slopes != 0;
+  const float dpl = pL - pLL, dpc = pR - pL, dpr = pRR - pR;
+  if (slopes) {
+    const float t1LL = ld(fut1, cLL), t1RR = ld(fut1, cRR), t2LL = ld(fut2, cLL), t2RR = ld(fut2, cRR);
+    {
+      const float a = 0.5f * dpl * icL, bb = 0.5f * rL * (uL - uLL);
+      const float a2 = 0.5f * dpc * icL, b2 = 0.5f * rL * (uR - uL);
+      dqL[0] = mc_limitf(a - bb, a2 - b2);
+      dqL[1] = mc_limitf(a + bb, a2 + b2);
+      dqL[2] = mc_limitf(t1L - t1LL, t1R - t1L);
+      dqL[3] = mc_limitf(t2L - t2LL, t2R - t2L);
+    }
+    {
+      const float a = 0.5f * dpc * icR, bb = 0.5f * rR * (uR - uL);
+      const float a2 = 0.5f * dpr * icR, b2 = 0.5f * rR * (uRR - uR);
+      dqR[0] = mc_limitf(a - bb, a2 - b2);
+      dqR[1] = mc_limitf(a + bb, a2 + b2);
+      dqR[2] = mc_limitf(t1R - t1L, t1RR - t1R);
+      dqR[3] = mc_limitf(t2R - t2L, t2RR - t2R);
+    }
+  }
+  const float unl = uL + 0.5f * (dqL[1] - dqL[0]) / rL;
+  const float pl = pL + 0.5f * (dqL[0] + dqL[1]) * cLc;  // offset pressure
+  const float ut1l = t1L + 0.5f * dqL[2];
+  const float ut2l = t2L + 0.5f * dqL[3];
+  const float unr = uR - 0.5f * (dqR[1] - dqR[0]) / rR;
+  const float pr = pR - 0.5f * (dqR[0] + dqR[1]) * cRc;
+  const float ut1r = t1R - 0.5f * dqR[2];
+  const float ut2r = t2R - 0.5f * dqR[3];
+  float spl[NS], spr[NS];
+  float rl = 0.f, rr = 0.f;
+  {
+    const float sL = (dqL[0] + dqL[1]) * icL, sR = (dqR[0] + dqR[1]) * icR;
+    const float icL2 = icL * icL, icR2 = icR * icR;
+#pragma unroll
+    for (int n = 0; n < NS; ++n) {
+      const float yLL = ld(RC::Y + n, cLL), yL = ld(RC::Y + n, cL), yR = ld(RC::Y + n, cR), yRR = ld(RC::Y + n, cRR);
+      float dsL = 0.f, dsR = 0.f;
+      if (slopes) {
+        const float ryL = rL * yL, ryR = rR * yR;
+        dsL = mc_limitf(ryL - rLL * yLL - yL * dpl * icL2, ryR - ryL - yL * dpc * icL2);
+        dsR = mc_limitf(ryR - ryL - yR * dpc * icR2, rRR * yRR - ryR - yR * dpr * icR2);
+      }
+      spl[n] = yL * rL + 0.5f * (dsL + yL * sL);
+      spr[n] = yR * rR - 0.5f * (dsR + yR * sR);
+      rl += spl[n];
+      rr += spr[n];
+    }
+    const float irl = 1.f / rl, irr = 1.f / rr;
+#pragma unroll
+    for (int n = 0; n < NS; ++n) {
+      spl[n] *= irl;
+      spr[n] *= irr;
+    }
+  }
+  const float pref = m.p_ref;
+  const float cavg = 0.5f * (cRc + cLc);
+  const float rwl = mix_rwf<NS>(m, spl), rwr = mix_rwf<NS>(m, spr);
+  const float cl = E::cs_rp(m, spl, rwl, rl, pl + pref);
+  const float cr = E::cs_rp(m, spr, rwr, rr, pr + pref);
+  float fl_rho, fl_un, fl_ut1, fl_ut2;
+  double fl_E, fl_ei;
+  float flY[NS];
+  if (!f.laxf) {
+    const float wsmall = 1.17549435e-38f;
+    const float wl = fmaxf(wsmall, cl * rl);
+    const float wr = fmaxf(wsmall, cr * rr);
+    const float iw = 1.f / (wl + wr);
+    const float pstar = fmaxf(wsmall - pref, ((wr * pl + wl * pr) + wl * wr * (unl - unr)) * iw);
+    float ustar = ((wl * unl + wr * unr) + (pl - pr)) * iw;
+    bool mask = ustar > 0.f;
+    float uo = mask ? unl : unr;
+    float po = mask ? pl : pr;
+    const bool m0 = fabsf(ustar) < 1e-12f * 0.5f * (fabsf(unl) + fabsf(unr)) || ustar == 0.f;
+    ustar = m0 ? 0.f : ustar;
+    float rspo[NS];
+    float ro = 0.f;
+#pragma unroll
+    for (int n = 0; n < NS; ++n) {
+      const float a = rl * spl[n], bq = rr * spr[n];
+      rspo[n] = m0 ? 0.5f * (a + bq) : (mask ? a : bq);
+      ro += rspo[n];
+    }
+    uo = m0 ? 0.5f * (unl + unr) : uo;
+    po = m0 ? 0.5f * (pl + pr) : po;
+    float Yt[NS];
+    {
+      const float y = 1.f / ro;
+#pragma unroll
+      for (int n = 0; n < NS; ++n) Yt[n] = rspo[n] * y;
+    }
+    const float co = E::cs_rp(m, Yt, mix_rwf<NS>(m, Yt), ro, po + pref);
+    const float drho = (pstar - po) / (co * co);
+    float rspstar[NS];
+    float rstar = 0.f;
+#pragma unroll
+    for (int n = 0; n < NS; ++n) {
+      rspstar[n] = fmaxf(0.f, rspo[n] + drho * Yt[n]);
+      rstar += rspstar[n];
+    }
+    {
+      const float y = 1.f / rstar;
+#pragma unroll
+      for (int n = 0; n < NS; ++n) Yt[n] = rspstar[n] * y;
+    }
+    const float cstar = E::cs_rp(m, Yt, mix_rwf<NS>(m, Yt), rstar, pstar + pref);
+    const float sgnm = copysignf(1.f, ustar);
+    float spout = co - sgnm * uo;
+    float spin = cstar - sgnm * ustar;
+    const float ushock = 0.5f * (spin + spout);
+    mask = pstar < po;
+    spout = mask ? spout : ushock;
+    spin = mask ? spin : ushock;
+    const float scr = (fabsf(spout - spin) < 1e-30f) ? 1e-8f * cavg : spout - spin;
+    const float frac = fmaxf(0.f, fminf(1.f, (1.f + (spout + spin) / scr) * 0.5f));
+    mask = ustar > 0.f;
+    float iv1 = mask ? ut1l : ut1r;
+    float iv2 = mask ? ut2l : ut2r;
+    mask = (ustar == 0.f);
+    iv1 = mask ? 0.5f * (ut1l + ut1r) : iv1;
+    iv2 = mask ? 0.5f * (ut2l + ut2r) : iv2;
+    const bool mout = spout < 0.f, min_ = spin >= 0.f;
+    float iu = frac * ustar + (1.f - frac) * uo;
+    float gdp = frac * pstar + (1.f - frac) * po;
+    iu = mout ? uo : iu;
+    gdp = mout ? po : gdp;
+    iu = min_ ? ustar : iu;
+    gdp = min_ ? pstar : gdp;
+    float rgd = 0.f;
+#pragma unroll
+    for (int n = 0; n < NS; ++n) {
+      float g = frac * rspstar[n] + (1.f - frac) * rspo[n];
+      g = mout ? rspo[n] : g;
+      g = min_ ? rspstar[n] : g;
+      flY[n] = g;
+      rgd += g;
+    }
+    const double gdpa = (double)gdp + (double)pref;
+    const double regd = (double)rgd * e_rp_fp64<NS, MIX>(md, flY, rgd, gdpa);
+    fl_rho = rgd * iu;
+#pragma unroll
+    for (int n = 0; n < NS; ++n) flY[n] *= iu;
+    fl_un = fl_rho * iu + gdp;  // p_ref dropped: zero divergence
+    fl_ut1 = fl_rho * iv1;
+    fl_ut2 = fl_rho * iv2;
+    const double iud = (double)iu;
+    fl_E = iud * (regd + (double)(0.5f * rgd * (iu * iu + iv1 * iv1 + iv2 * iv2)) + gdpa);
+    fl_ei = iud * regd;
+  } else {
+    const double pla = (double)pl + (double)pref, pra = (double)pr + (double)pref;
+    const double el = e_rpY_fp64<NS, MIX>(md, spl, rl, pla);
+    const double er = e_rpY_fp64<NS, MIX>(md, spr, rr, pra);
+    const double r_elt = (double)rl * (el + (double)(0.5f * (unl * unl + ut1l * ut1l + ut2l * ut2l)));
+    const double r_ert = (double)rr * (er + (double)(0.5f * (unr * unr + ut1r * ut1r + ut2r * ut2r)));
+    const float wl = fmaxf(1.17549435e-38f, cl * rl);
+    const float wr = fmaxf(1.17549435e-38f, cr * rr);
+    float ustar = ((wl * unl + wr * unr) + (pl - pr)) / (wl + wr);
+    const bool m0 = fabsf(ustar) < 1e-12f * 0.5f * (fabsf(unl) + fabsf(unr)) || ustar == 0.f;
+    ustar = m0 ? 0.f : ustar;
+    const float mw = fabsf(ustar) + 0.5f * (cr + cl);
+    fl_rho = 0.f;
+#pragma unroll
+    for (int n = 0; n < NS; ++n) {
+      flY[n] = 0.5f * ((rl * unl * spl[n] + rr * unr * spr[n]) - mw * (rr * spr[n] - rl * spl[n]));
+      fl_rho += flY[n];
+    }
+    fl_un = 0.5f * ((rl * unl * unl + pl + rr * unr * unr + pr) - mw * (rr * unr - rl * unl));
+    fl_ut1 = 0.5f * ((rl * ut1l * unl + rr * ut1r * unr) - mw * (rr * ut1r - rl * ut1l));
+    fl_ut2 = 0.5f * ((rl * ut2l * unl + rr * ut2r * unr) - mw * (rr * ut2r - rl * ut2l));
+    const double mwd = (double)mw;
+    fl_E = 0.5 * (((r_elt + pla) * (double)unl + (r_ert + pra) * (double)unr) - mwd * (r_ert - r_elt));
+    fl_ei = 0.5 * (((double)rl * el * (double)unl + (double)rr * er * (double)unr) -
+                   mwd * ((double)rr * er - (double)rl * el));
+  }
+  F[URHO] = fl_rho;
+  F[UMX + d] = fl_un;
+  F[(d == 0) ? UMY : UMX] = fl_ut1;
+  F[(d == 2) ? UMY : UMZ] = fl_ut2;
+  F[UEDEN] = 0.f;  // energy fluxes travel in FP64 (FE, FEI)
+  F[UEINT] = 0.f;
+  F[UTEMP] = 0.f;
+  FE = fl_E;
+  FEI = fl_ei;
+#pragma unroll
+  for (int n = 0; n < NS; ++n) F[UFS + n] = flY[n];
+}
+
+// FP32 diffusion flux (not area-scaled), added to F.
+template <int NS, int d>
+__device__ __forceinline__ void diffusion_face_f(const DevBox& b, const DevFlags& f, const Geo& g, long long cR,
+                                                 const long long stv[3], float* F) {
+  using RC = Rec<NS>;
+  const float* rec = reinterpret_cast<const float*>(b.rec);
+  const long long N = b.ncell;
+  auto ld = [&](int fld, long long c) { return __ldg(rec + (long long)fld * N + c); };
+  const double* xrec = mixed_x<NS>(b);
+  const long long cL = cR - stv[d];
+  const bool harm = f.harmonic != 0;
+  const float mu = face_coeff(ld(RC::MU, cR), ld(RC::MU, cL), harm);
+  const float xi = face_coeff(ld(RC::XI, cR), ld(RC::XI, cL), harm);
+  const float lam = face_coeff(ld(RC::LAM, cR), ld(RC::LAM, cL), harm);
+  float grad[3][3];
+  const float uR[3] = {ld(RC::U, cR), ld(RC::V, cR), ld(RC::W, cR)};
+  const float uL[3] = {ld(RC::U, cL), ld(RC::V, cL), ld(RC::W, cL)};
+  const float dxi = (float)g.dxinv[d];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) grad[c][d] = dxi * (uR[c] - uL[c]);
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    if (a == d) continue;
+    const long long sa = stv[a];
+    const float q4 = 0.25f * (float)g.dxinv[a];
+    const int ca = RC::U + a, cd = RC::U + d;
+    grad[a][a] = (ld(ca, cR + sa) + ld(ca, cL + sa) - ld(ca, cR - sa) - ld(ca, cL - sa)) * q4;
+    grad[d][a] = (ld(cd, cR + sa) + ld(cd, cL + sa) - ld(cd, cR - sa) - ld(cd, cL - sa)) * q4;
+  }
+  const float divu = grad[0][0] + grad[1][1] + grad[2][2];
+  float tau[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    if (a == d)
+      tau[a] = mu * (2.f * grad[d][d] - (2.f / 3.f) * divu) + xi * divu;
+    else
+      tau[a] = mu * (grad[d][a] + grad[a][d]);
+  }
+  float fE = 0.5f * (-tau[0] * (uR[0] + uL[0]) - tau[1] * (uR[1] + uL[1]) - tau[2] * (uR[2] + uL[2])) -
+             lam * dxi * (ld(RC::T, cR) - ld(RC::T, cL));
+  const bool spec = f.diffuse_spec != 0;
+  const bool ener = (f.diffuse_temp != 0) || (f.diffuse_enth != 0);
+  {
+    const float pR = ld(RC::P, cR), pL = ld(RC::P, cL);
+    // d ln p / dx from the offset pressure: p = p_ref + p'.
+    const float dlnp = dxi * (pR - pL) / (0.5f * (pR + pL) + (float)g.p_ref);
+    float Vd[NS], Yf[NS], hf[NS];
+    float Vc = 0.f;
+#pragma unroll
+    for (int n = 0; n < NS; ++n) {
+      const double x1 = __ldg(xrec + n * N + cR), x2 = __ldg(xrec + n * N + cL);
+      const float dX = (float)(x1 - x2);
+      const float Xface = (float)(0.5 * (x1 + x2));
+      const float y1 = ld(RC::Y + n, cR), y2 = ld(RC::Y + n, cL);
+      Yf[n] = 0.5f * (y1 + y2);
+      hf[n] = 0.5f * (ld(RC::H + n, cR) + ld(RC::H + n, cL));
+      const float D = face_coeff(ld(RC::D + n, cR), ld(RC::D + n, cL), harm);
+      Vd[n] = -D * (dxi * dX + (Xface - Yf[n]) * dlnp);
+      Vc += Vd[n];
+      fE += Vd[n] * hf[n];
+    }
+#pragma unroll
+    for (int n = 0; n < NS; ++n) {
+      fE -= Yf[n] * hf[n] * Vc;
+      if (spec) F[UFS + n] += Vd[n] - Yf[n] * Vc;
+    }
+  }
+  if (f.diffuse_vel) {
+#pragma unroll
+    for (int a = 0; a < 3; ++a) F[UMX + a] -= tau[a];
+  }
+  if (ener) F[UEDEN] += fE;
+}
+
+template <int NS, bool MIX, int d>
+__device__ __forceinline__ void dir_pass_mixed(const DevBox& b, const MechF<NS>& m, const DevMech<NS>& md,
+                                               const DevFlags& f, const Geo& g,
+                                               const int o[3], const int ext[3], const long long stv[3], bool mine,
+                                               int tx, int ty, int tz, double (*fbuf)[kMaxFaces], double* acc) {
+  constexpr int NVAR = 7 + NS;
+  const bool diff = f.diffuse_vel || f.diffuse_temp || f.diffuse_spec || f.diffuse_enth;
+  const int nf0 = ext[0] + (d == 0), nf1 = ext[1] + (d == 1), nf2 = ext[2] + (d == 2);
+  const int nfaces = nf0 * nf1 * nf2;
+  for (int fi = threadIdx.x; fi < nfaces; fi += kFluxThreads) {
+    const int fx = fi % nf0, fy = (fi / nf0) % nf1, fz = fi / (nf0 * nf1);
+    const int i = o[0] + fx, j = o[1] + fy, k = o[2] + fz;
+    const long long cR = (i - b.g2lo[0]) + (j - b.g2lo[1]) * stv[1] + (k - b.g2lo[2]) * stv[2];
+    float F[NVAR];
+    double FE = 0.0, FEI = 0.0;
+    if (f.do_hydro) {
+      hydro_face_f<NS, MIX, d>(b, m, md, f, cR, stv[d], F, FE, FEI);
+    } else {
+#pragma unroll
+      for (int n = 0; n < NVAR; ++n) F[n] = 0.f;
+    }
+    if (diff) diffusion_face_f<NS, d>(b, f, g, cR, stv, F);
+#pragma unroll
+    for (int n = 0; n < NVAR; ++n) fbuf[n][fi] = (double)F[n];  // exact widening
+    fbuf[UEDEN][fi] = FE + (double)F[UEDEN];
+    fbuf[UEINT][fi] = FEI;
+  }
+  __syncthreads();
+  if (mine) {
+    const int flo = tx + nf0 * (ty + nf1 * tz);
+    const int fhi = flo + ((d == 0) ? 1 : (d == 1) ? nf0 : nf0 * nf1);
+    const double s = g.dxinv[d];
+#pragma unroll
+    for (int n = 0; n < NVAR; ++n) acc[n] = fma(fbuf[n][flo] - fbuf[n][fhi], s, acc[n]);
+  }
+  __syncthreads();
+}
+
+template <int NS, bool MIX>
+__global__ void __launch_bounds__(kFluxThreads, 2)
+    flux_kernel_mixed(const DevBox* __restrict__ boxes, const int4* __restrict__ tiles,
+                      const __grid_constant__ MechF<NS> m, const __grid_constant__ DevMech<NS> md, const DevFlags f,
+                      const Geo g, unsigned long long* __restrict__ counters) {
+  constexpr int NVAR = 7 + NS;
+  __shared__ double fbuf[NVAR][kMaxFaces];
+  const int4 t = tiles[blockIdx.x];
+  const DevBox& b = boxes[t.x];
+  const int o[3] = {t.y, t.z, t.w};
+  const int ext[3] = {min(kTX, b.hi[0] - o[0] + 1), min(kTY, b.hi[1] - o[1] + 1), min(kTZ, b.hi[2] - o[2] + 1)};
+  const int tx = threadIdx.x % kTX, ty = (threadIdx.x / kTX) % kTY, tz = threadIdx.x / (kTX * kTY);
+  const bool mine = tx < ext[0] && ty < ext[1] && tz < ext[2];
+  const long long stv[3] = {1, b.n2[0], (long long)b.n2[0] * b.n2[1]};
+  double acc[NVAR];
+#pragma unroll
+  for (int n = 0; n < NVAR; ++n) acc[n] = 0.0;
+  dir_pass_mixed<NS, MIX, 0>(b, m, md, f, g, o, ext, stv, mine, tx, ty, tz, fbuf, acc);
+  dir_pass_mixed<NS, MIX, 1>(b, m, md, f, g, o, ext, stv, mine, tx, ty, tz, fbuf, acc);
+  dir_pass_mixed<NS, MIX, 2>(b, m, md, f, g, o, ext, stv, mine, tx, ty, tz, fbuf, acc);
+  bool bad = false;
+  if (mine) {
+    const int i = o[0] + tx, j = o[1] + ty, k = o[2] + tz;
+    double* r = b.R + (i - b.rb[0]) + (long long)(j - b.rb[1]) * b.rj + (long long)(k - b.rb[2]) * b.rk;
+#pragma unroll
+    for (int n = 0; n < NVAR; ++n) {
+      bad |= !isfinite(acc[n]);
+      r[n * b.rn] = acc[n];
+    }
+  }
+  if (f.check_output) warp_count(&counters[kCounterNonfinite], bad);
+  if (threadIdx.x == 0) atomicAdd(&counters[kCounterCells], (unsigned long long)(ext[0] * ext[1] * ext[2]));
+}
+
+}  // namespace pcg

@@ -16,6 +16,12 @@
 #include "pc_kernels.cuh"
 #include "pelec_mol.h"
 
+namespace pcg {
+int launch_mixed(int variant, const DevBox* boxes, const int2* items, int nitems, const int4* tiles, int ntiles,
+                 const DevMech<1>& m1, const DevMech<9>& m9, const DevFlags& f, const Geo& g, double p_ref,
+                 unsigned long long* counters, cudaStream_t s, cudaEvent_t e0, cudaEvent_t e1, cudaEvent_t e2);
+}  // namespace pcg
+
 namespace {
 
 using namespace pcg;
@@ -233,6 +239,7 @@ Geo make_geo(const double dx[3]) {
   g.area[1] = dx[0] * dx[2];
   g.area[2] = dx[0] * dx[1];
   g.vol = dx[0] * dx[1] * dx[2];
+  g.p_ref = 0.0;
   return g;
 }
 
@@ -269,7 +276,17 @@ int run(pc_mol_handle* h, const pc_box_desc* boxes, int nboxes, const double dx[
   const Layout& L = h->lay;
   const bool timed = h->cfg.time_passes != 0 && !per_box;
   h->timed = timed;
+  const bool mixed = h->cfg.precision == PC_PRECISION_MIXED;
   auto go = [&](int ib, int ie, int tb, int te) {
+    if (mixed) {
+      const double p_ref = h->cfg.mixed_p_ref > 0.0 ? h->cfg.mixed_p_ref : 1013250.0;
+      Geo gm = g;
+      gm.p_ref = p_ref;
+      const int rc = launch_mixed(h->variant, h->d_boxes, h->d_items + ib, ie - ib, h->d_tiles + tb, te - tb,
+                                  h->mech1, h->mech9, h->flags, gm, p_ref, h->d_counters, s,
+                                  timed ? h->ev[0] : nullptr, timed ? h->ev[1] : nullptr, timed ? h->ev[2] : nullptr);
+      return rc == 0 ? PC_OK : cuda_fail(h, cudaGetLastError());
+    }
     if (h->variant == 1)
       return launch<1, GammaLawEos<1>, ConstantTransport<1>>(h, h->mech1, g, ib, ie, tb, te, s, timed);
     return launch<9, IdealMixEos<9>, SimpleTransport<9>>(h, h->mech9, g, ib, ie, tb, te, s, timed);
@@ -312,7 +329,6 @@ int pc_mol_create(pc_mol_handle** out, const pc_mol_config* cfg) {
   if (c.nspec == 1 && c.eos == PC_EOS_GAMMA_LAW && c.transport == PC_TRANSPORT_CONSTANT) variant = 1;
   if (c.nspec == 9 && c.eos == PC_EOS_IDEAL_MIX && c.transport == PC_TRANSPORT_SIMPLE) variant = 9;
   if (!variant) return PC_ERR_UNSUPPORTED;
-  if (c.precision == PC_PRECISION_MIXED) return PC_ERR_UNSUPPORTED;
   for (int k = 0; k < c.nspec; ++k)
     if (!(c.mech.mw[k] > 0.0)) return PC_ERR_INVALID_ARGUMENT;
   if (c.eos == PC_EOS_GAMMA_LAW && !(c.mech.gamma > 1.0)) return PC_ERR_INVALID_ARGUMENT;

@@ -254,7 +254,7 @@ def level_boxes(nboxes: int = 400, seed: int = 3, dx: float = 1e-3, mech: Mechan
 def make_config(mech: Mechanism, precision: int = abi.PC_PRECISION_FP64, do_hydro: int = 1,
                 diffuse: int = 1, plm_iorder: int = 4, use_laxf_flux: int = 0, harmonic: int = 1,
                 check_output: int = 1, newton_max_iter: int = 50, time_passes: int = 0,
-                **flags) -> abi.PcMolConfig:
+                mixed_p_ref: float = 0.0, **flags) -> abi.PcMolConfig:
     """pc_mol_config for a mechanism; ``diffuse`` sets all four diffuse_* flags
     unless individual ones are given in ``flags``."""
     c = abi.PcMolConfig()
@@ -273,5 +273,6 @@ def make_config(mech: Mechanism, precision: int = abi.PC_PRECISION_FP64, do_hydr
     c.check_output = check_output
     c.newton_max_iter = newton_max_iter
     c.time_passes = time_passes
+    c.mixed_p_ref = mixed_p_ref
     c.mech = mech.to_ctypes()
     return c

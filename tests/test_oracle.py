@@ -169,3 +169,20 @@ def test_generators_are_deterministic():
     np.testing.assert_allclose(st.S, g["tgv8_S"], rtol=1e-14, atol=0)
     _, st, _ = problems.flame((6, 6, 6), seed=12)
     np.testing.assert_allclose(st.S, g["flame6_S"], rtol=1e-14, atol=0)
+
+
+def test_rhs_conditioning(oracle_lib):
+    """One random ulp on the input state moves the oracle's own RHS by more
+    than the 1e-12 FP64 parity bar (flame z-momentum, where the 1 atm pressure
+    flux cancels between faces): parity at that bar needs the same IEEE
+    operation sequence, not merely a correct one."""
+    from conftest import rel_maxnorm
+
+    mech, st, _ = problems.flame((16, 16, 24), seed=6)
+    cfg = problems.make_config(mech)
+    R0, = oracle_lib.mol_rhs(cfg, [st])
+    rng = np.random.default_rng(0)
+    S1 = st.S * (1.0 + 2.0 ** -52 * rng.choice([-1.0, 1.0], st.S.shape))
+    R1, = oracle_lib.mol_rhs(cfg, [problems.BoxState(lo=st.lo, hi=st.hi, S=S1, dx=st.dx)])
+    err = rel_maxnorm(R1, R0)
+    assert err.max() > 1e-11
