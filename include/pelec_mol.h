@@ -151,6 +151,25 @@ typedef struct pc_mol_status {
   int pad_;
 } pc_mol_status;
 
+/* Physical boundary conditions of a domain face (PCPhysBCType, PeleC.H, and
+ * the BCType maps of Source/Setup.cpp:34-56).  A direction is periodic when
+ * both of its faces are PC_BC_INTERIOR. */
+typedef enum pc_phys_bc {
+  PC_BC_INTERIOR = 0,   /* periodic (int_dir)                                */
+  PC_BC_OUTFLOW = 1,    /* foextrap: copy of the nearest interior cell       */
+  PC_BC_SYMMETRY = 2,   /* reflect_even; normal momentum reflect_odd         */
+  PC_BC_SLIPWALL = 3,   /* as symmetry                                       */
+  PC_BC_NOSLIPWALL = 4  /* reflect_even; all momenta reflect_odd             */
+} pc_phys_bc;
+
+/* Index-space domain of the level (geom.Domain()) and its face BCs. */
+typedef struct pc_geometry {
+  int domain_lo[3];
+  int domain_hi[3];
+  int bc_lo[3];        /* pc_phys_bc of the low face of each direction       */
+  int bc_hi[3];        /* pc_phys_bc of the high face                        */
+} pc_geometry;
+
 typedef struct pc_mol_handle pc_mol_handle;
 
 /* ABI version of the loaded library (PC_MOL_ABI_VERSION). */
@@ -191,6 +210,36 @@ int pc_mol_last_status(pc_mol_handle* h, pc_mol_status* st);
  * CUDA events on the call's stream: ms[0] = cell pass (primitives, EOS,
  * transport), ms[1] = flux pass (faces and divergence).  n >= 2. */
 int pc_mol_pass_times(pc_mol_handle* h, double* ms, int n);
+
+/* Fill ngrow ghost layers of every box's state array on one level that
+ * covers its domain: each ghost cell takes the value of the valid cell it
+ * maps to — periodic images wrap, PC_BC_OUTFLOW clamps to the nearest
+ * interior cell, reflecting faces mirror (momentum components negated as
+ * the face type says).  Replaces FillPatcherFill / FillBoundary with the
+ * physical BC fill at a single level (Source/Advance.cpp:98,132;
+ * Source/BCfill.cpp; Source/Setup.cpp:34-56).  The boxes' states must cover
+ * grow(valid, ngrow) and the valid boxes must tile the domain. */
+int pc_mol_fill_ghosts(pc_mol_handle* h, const pc_box_desc* boxes, int nboxes, const pc_geometry* geom, int ngrow,
+                       void* stream);
+
+/* dst = a*x + b*y on the valid cells of each box, all NVAR components
+ * (MultiFab::LinComb / Saxpy of the MOL advance, Advance.cpp:117,148-151).
+ * lohi holds 6 ints per box (valid lo, hi); dst may alias x or y. */
+int pc_mol_lincomb(pc_mol_handle* h, int nboxes, const int* lohi, const pc_array4* dst, double a,
+                   const pc_array4* x, double b, const pc_array4* y, void* stream);
+
+/* PeleC::computeTemp on the valid cells (PeleC.cpp:2254-2271): with the
+ * default allow_small_energy = allow_negative_energy = true,
+ * reset_internal_energy sets rho e = rho E - rho |u|^2/2 (Utilities.H:219-236)
+ * and pc_cmpTemp solves the EOS for T from U(UTEMP) (Utilities.H:67-84). */
+int pc_mol_compute_temp(pc_mol_handle* h, int nboxes, const int* lohi, const pc_array4* state, void* stream);
+
+/* PeleC::estTimeStep (PeleC.cpp:839-972, Timestep.H): min over valid cells
+ * of dx/(c+|u|) (do_hydro) and the viscous, thermal and enthalpy diffusion
+ * limits (diffuse_vel/temp/enth), times cfl, capped by max_dt.  Synchronous:
+ * returns the time step in *dt. */
+int pc_mol_est_dt(pc_mol_handle* h, const pc_box_desc* boxes, int nboxes, const double dx[3], double cfl,
+                  double max_dt, double* dt, void* stream);
 
 /* Right-hand side of ONE box without allocating any device memory.  This
  * entry point has no counterpart in the reference: it exists for callers

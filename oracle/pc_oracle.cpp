@@ -61,6 +61,18 @@ int dispatch(const pc_mol_config& cfg, const pc_box_desc& bd, const double dx[3]
   return run_box<NS>(cfg, eos, SimpleTransport<NS, IdealMix<NS>>{&cfg.mech}, bd, dx, fails);
 }
 
+template <int NS, class EOS>
+void ct_boxes(int nboxes, const int* lohi, const pc_array4* st, const EOS& eos, long long& fails) {
+  for (int i = 0; i < nboxes; ++i) {
+    Box v;
+    for (int d = 0; d < 3; ++d) {
+      v.lo[d] = lohi[6 * i + d];
+      v.hi[d] = lohi[6 * i + 3 + d];
+    }
+    compute_temp<NS>(v, view(st[i]), eos, fails);
+  }
+}
+
 }  // namespace
 
 extern "C" {
@@ -167,5 +179,89 @@ int oracle_riemann_face(const pc_mol_config* cfg, const double* left, const doub
 }
 
 int oracle_max_threads(void) { return omp_get_max_threads(); }
+
+// Ghost fill of a level covering the domain (host arrays).
+int oracle_fill_ghosts(const pc_box_desc* boxes, int nboxes, const pc_geometry* geom, int ngrow, int nvar) {
+  std::vector<FillBox> fb;
+  for (int b = 0; b < nboxes; ++b) {
+    FillBox f;
+    for (int d = 0; d < 3; ++d) {
+      f.valid.lo[d] = boxes[b].lo[d];
+      f.valid.hi[d] = boxes[b].hi[d];
+    }
+    if (!covers(boxes[b].state, grow(f.valid, ngrow))) return PC_ERR_INVALID_ARGUMENT;
+    f.S = view(boxes[b].state);
+    fb.push_back(f);
+  }
+  fill_ghosts(fb, *geom, ngrow, nvar);
+  return PC_OK;
+}
+
+// dst = a x + b y on each box's valid cells (lohi: 6 ints per box).
+int oracle_lincomb(int nboxes, const int* lohi, const pc_array4* dst, double a, const pc_array4* x, double b,
+                   const pc_array4* y, int nvar) {
+  for (int i = 0; i < nboxes; ++i) {
+    Box v;
+    for (int d = 0; d < 3; ++d) {
+      v.lo[d] = lohi[6 * i + d];
+      v.hi[d] = lohi[6 * i + 3 + d];
+    }
+    lincomb(v, nvar, view(dst[i]), a, view(x[i]), b, view(y[i]));
+  }
+  return PC_OK;
+}
+
+int oracle_compute_temp(const pc_mol_config* cfg, int nboxes, const int* lohi, const pc_array4* st,
+                        long long* newton_fail) {
+  long long fails = 0;
+  const int maxit = cfg->newton_max_iter > 0 ? cfg->newton_max_iter : 50;
+  if (cfg->nspec == 1 && cfg->eos == PC_EOS_GAMMA_LAW)
+    ct_boxes<1>(nboxes, lohi, st, GammaLaw<1>{&cfg->mech}, fails);
+  else if (cfg->nspec == 9 && cfg->eos == PC_EOS_IDEAL_MIX)
+    ct_boxes<9>(nboxes, lohi, st, IdealMix<9>{&cfg->mech, maxit}, fails);
+  else
+    return PC_ERR_UNSUPPORTED;
+  if (newton_fail) *newton_fail = fails;
+  return PC_OK;
+}
+
+// estTimeStep: dt = cfl * min(hydro, vdif, tdif, edif) capped by max_dt
+// (the limits that the configuration's flags switch on); parts[4] returns
+// the four minima.
+int oracle_est_dt(const pc_mol_config* cfg, const pc_box_desc* boxes, int nboxes, const double dx[3], double cfl,
+                  double max_dt, double* dt, double* parts) {
+  const double big = std::numeric_limits<double>::max();
+  double m4[4] = {big, big, big, big};
+  for (int b = 0; b < nboxes; ++b) {
+    Box v;
+    for (int d = 0; d < 3; ++d) {
+      v.lo[d] = boxes[b].lo[d];
+      v.hi[d] = boxes[b].hi[d];
+    }
+    double o[4];
+    if (cfg->nspec == 1 && cfg->eos == PC_EOS_GAMMA_LAW) {
+      GammaLaw<1> eos{&cfg->mech};
+      est_dt<1>(v, view(boxes[b].state), eos, ConstantTransport<1, GammaLaw<1>>{&cfg->mech}, dx, o);
+    } else if (cfg->nspec == 9 && cfg->eos == PC_EOS_IDEAL_MIX) {
+      IdealMix<9> eos{&cfg->mech, 50};
+      est_dt<9>(v, view(boxes[b].state), eos, SimpleTransport<9, IdealMix<9>>{&cfg->mech}, dx, o);
+    } else {
+      return PC_ERR_UNSUPPORTED;
+    }
+    for (int q = 0; q < 4; ++q) m4[q] = std::min(m4[q], o[q]);
+  }
+  const double mdc = max_dt / cfl;
+  double eh = mdc, ev = mdc, et = mdc, ee = mdc;
+  if (cfg->do_hydro) eh = std::min(eh, m4[0]);
+  if (cfg->diffuse_vel) ev = std::min(ev, m4[1]);
+  if (cfg->diffuse_temp) et = std::min(et, m4[2]);
+  if (cfg->diffuse_enth) ee = std::min(ee, m4[3]);
+  eh = std::min(eh, std::min(ev, std::min(et, ee)));
+  eh *= cfl;
+  *dt = std::min(max_dt, eh);
+  if (parts)
+    for (int q = 0; q < 4; ++q) parts[q] = m4[q];
+  return PC_OK;
+}
 
 }  // extern "C"

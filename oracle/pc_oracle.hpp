@@ -148,6 +148,11 @@ struct GammaLaw {
   void T2Hi(double T, double* h) const {
     for (int k = 0; k < NS; ++k) h[k] = (m->gamma / (m->gamma - 1.0) * RU / m->mw[k]) * T;
   }
+  void TY2CpCv(double, const double* Y, double& cp, double& cv) const {
+    const double rw = mix_rw<NS>(m, Y);
+    cv = rw / (m->gamma - 1.0);
+    cp = cv + rw;
+  }
 };
 
 // Ideal-gas mixture with NASA-7 species polynomials (CHEMKIN convention,
@@ -295,7 +300,9 @@ struct ConstantTransport {
 
 // Mixture-averaged transport (Docs/sphinx/Algorithms.rst:540-566):
 //   mu = (sum X_m mu_m^6)^(1/6), lambda = (sum X_m lambda_m^(1/4))^4,
-//   rhoD_m = rho (1-Y_m) / sum_{j!=m} X_j / D_mj(T,p),
+//   rhoD_m = rho (W_m/Wbar) D_m,mix, D_m,mix = (1-Y_m) / sum_{j!=m} X_j / D_mj(T,p),
+// so that the flux rhoD_m grad X_m used by SpeciesEnergyFlux is the
+// Hirschfelder-Curtiss mass flux,
 // pure-species fits ln q = sum_n c_n (ln T)^n.  D_mj(T,p) = D_mj(T) p_ref/p.
 // Mole fractions in the diffusion sum are floored at 1e-15 so a pure
 // species keeps a finite mixture coefficient.  Bulk viscosity is
@@ -333,7 +340,10 @@ struct SimpleTransport {
         const double invD = std::exp(-fit(m->diff_fit[std::min(j, k)][std::max(j, k)], L)) * pr;
         s = std::fma(std::max(X[j], 1e-15), invD, s);
       }
-      Ddiag[k] = (s > 0.0) ? rho * (1.0 - Y[k]) / s : 0.0;
+      // W_k / Wbar = (R/Wbar) / (R/W_k): rhoD_k grad X_k is then the
+      // Hirschfelder-Curtiss mass flux rho (W_k/Wbar) D_k,mix grad X_k.
+      const double wrat = mix_rw<NS>(m, Y) / (RU / m->mw[k]);
+      Ddiag[k] = (s > 0.0) ? rho * (1.0 - Y[k]) * wrat / s : 0.0;
     }
   }
 };
@@ -829,6 +839,150 @@ inline void mol_rhs_box(const pc_mol_config& cfg, const EOS& eos, const TRANS& t
   for_box(vbox, [&](int i, int j, int k) {
     for (int n = 0; n < NVAR; ++n) rhs(i, j, k, n) = Dterm(i, j, k, n);
   });
+}
+
+// ---------------------------------------------------------------------------
+// Time-advance building blocks of the MOL step (do_mol_advance,
+// Source/Advance.cpp:45-196).
+// ---------------------------------------------------------------------------
+
+// PeleC::computeTemp (PeleC.cpp:2254-2271) with the default
+// allow_small_energy = allow_negative_energy = true: reset_internal_energy
+// (pc_rst_int_e, Utilities.H:219-236) then pc_cmpTemp (Utilities.H:67-84).
+template <int NS, class EOS>
+inline void compute_temp(const Box& vbox, const Arr<double>& S, const EOS& eos, long long& fails) {
+  for_box(vbox, [&](int i, int j, int k) {
+    {
+      const double rho = S(i, j, k, URHO);
+      const double rhoInv = 1.0 / rho;
+      const double Up = S(i, j, k, UMX) * rhoInv;
+      const double Vp = S(i, j, k, UMY) * rhoInv;
+      const double Wp = S(i, j, k, UMZ) * rhoInv;
+      const double ke = 0.5 * (Up * Up + Vp * Vp + Wp * Wp) - 0.5 * 0.0 * 0.0 * 0.0 * 0.0;
+      S(i, j, k, UEINT) = S(i, j, k, UEDEN) - rho * ke;
+    }
+    const double rhoInv = 1.0 / S(i, j, k, URHO);
+    double T = S(i, j, k, UTEMP);
+    const double e = S(i, j, k, UEINT) * rhoInv;
+    double Y[NS];
+    for (int n = 0; n < NS; ++n) Y[n] = S(i, j, k, UFS + n) * rhoInv;
+    int iters = 0;
+    bool ok = true;
+    eos.REY2T(S(i, j, k, URHO), e, Y, T, iters, ok);
+    if (!ok) {
+#pragma omp atomic
+      fails += 1;
+    }
+    S(i, j, k, UTEMP) = T;
+  });
+}
+
+// MultiFab::LinComb: dst = a x + b y on vbox, NVAR components.
+inline void lincomb(const Box& vbox, int nvar, const Arr<double>& dst, double a, const Arr<double>& x, double b,
+                    const Arr<double>& y) {
+  for_box(vbox, [&](int i, int j, int k) {
+    for (int n = 0; n < nvar; ++n) dst(i, j, k, n) = a * x(i, j, k, n) + b * y(i, j, k, n);
+  });
+}
+
+// Ghost fill of one level covering the domain: every ghost cell takes the
+// value of the valid cell its index maps to (periodic wrap, foextrap clamp,
+// mirror for reflecting faces with momentum sign flips).
+struct FillBox {
+  Box valid;
+  Arr<double> S;
+};
+inline void fill_ghosts(const std::vector<FillBox>& boxes, const pc_geometry& g, int ng, int nvar) {
+  int L[3];
+  bool periodic[3];
+  for (int d = 0; d < 3; ++d) {
+    L[d] = g.domain_hi[d] - g.domain_lo[d] + 1;
+    periodic[d] = g.bc_lo[d] == PC_BC_INTERIOR && g.bc_hi[d] == PC_BC_INTERIOR;
+  }
+  for (const FillBox& b : boxes) {
+    const Box gb = grow(b.valid, ng);
+    for_box(gb, [&](int i, int j, int k) {
+      const int idx[3] = {i, j, k};
+      bool inside = true;
+      for (int d = 0; d < 3; ++d) inside = inside && idx[d] >= b.valid.lo[d] && idx[d] <= b.valid.hi[d];
+      if (inside) return;
+      int src[3];
+      double sign[3] = {1.0, 1.0, 1.0};  // momentum x, y, z
+      for (int d = 0; d < 3; ++d) {
+        int x = idx[d];
+        const int lo = g.domain_lo[d], hi = g.domain_hi[d];
+        if (x < lo || x > hi) {
+          const int bc = x < lo ? g.bc_lo[d] : g.bc_hi[d];
+          if (periodic[d]) {
+            x = x < lo ? x + L[d] : x - L[d];
+          } else if (bc == PC_BC_OUTFLOW) {
+            x = x < lo ? lo : hi;
+          } else {
+            x = x < lo ? 2 * lo - 1 - x : 2 * hi + 1 - x;
+            if (bc == PC_BC_NOSLIPWALL) {
+              for (int c = 0; c < 3; ++c) sign[c] = -sign[c];
+            } else {
+              sign[d] = -sign[d];
+            }
+          }
+        }
+        src[d] = x;
+      }
+      for (const FillBox& o : boxes) {
+        bool in = true;
+        for (int d = 0; d < 3; ++d) in = in && src[d] >= o.valid.lo[d] && src[d] <= o.valid.hi[d];
+        if (!in) continue;
+        for (int n = 0; n < nvar; ++n) {
+          double v = o.S(src[0], src[1], src[2], n);
+          if (n >= UMX && n <= UMZ) v = v * sign[n - UMX];
+          b.S(i, j, k, n) = v;
+        }
+        break;
+      }
+    });
+  }
+}
+
+// PeleC::estTimeStep (PeleC.cpp:839-972): pc_estdt_hydro / veldif / tempdif /
+// enthdif (Timestep.H:51-237) over vbox; returns the four minima.
+template <int NS, class EOS, class TRANS>
+inline void est_dt(const Box& vbox, const Arr<double>& u, const EOS& eos, const TRANS& tr, const double dx[3],
+                   double out[4]) {
+  const double big = std::numeric_limits<double>::max();
+  double dth = big, dtv = big, dtt = big, dte = big;
+  for (int k = vbox.lo[2]; k <= vbox.hi[2]; ++k)
+    for (int j = vbox.lo[1]; j <= vbox.hi[1]; ++j)
+      for (int i = vbox.lo[0]; i <= vbox.hi[0]; ++i) {
+        const double rho = u(i, j, k, URHO);
+        const double rhoInv = 1.0 / rho;
+        double Y[NS];
+        for (int n = 0; n < NS; ++n) Y[n] = u(i, j, k, UFS + n) * rhoInv;
+        const double T = u(i, j, k, UTEMP);
+        double c;
+        eos.RTY2Cs(rho, T, Y, c);
+        for (int d = 0; d < 3; ++d) {
+          const double ud = u(i, j, k, UMX + d) * rhoInv;
+          dth = std::min(dth, dx[d] / (c + std::fabs(ud)));
+        }
+        double Dd[NS], mu, xi, lam;
+        tr.transport(eos, T, rho, Y, Dd, mu, xi, lam);
+        double cp, cv;
+        eos.TY2CpCv(T, Y, cp, cv);
+        double Dv = mu * rhoInv;
+        if (Dv == 0.0) Dv = small_num();
+        double Dt = lam * (rhoInv / cv);
+        if (Dt == 0.0) Dt = small_num();
+        const double De = lam * (rhoInv / cp);
+        for (int d = 0; d < 3; ++d) {
+          dtv = std::min(dtv, 0.5 * dx[d] * dx[d] / (3 * Dv));
+          dtt = std::min(dtt, 0.5 * dx[d] * dx[d] / (3 * Dt));
+          dte = std::min(dte, 0.5 * dx[d] * dx[d] / (3 * De));
+        }
+      }
+  out[0] = dth;
+  out[1] = dtv;
+  out[2] = dtt;
+  out[3] = dte;
 }
 
 }  // namespace orc

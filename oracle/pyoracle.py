@@ -135,3 +135,84 @@ def max_threads() -> int:
 
 
 _ = (c_void_p,)
+
+
+# ---------------------------------------------------------------------------
+# Level operations of the MOL advance (oracle side).
+# ---------------------------------------------------------------------------
+def _state_descs(boxes):
+    return abi.box_array([abi.box_desc(st.lo, st.hi, abi.array4(st.S.ctypes.data, st.S.shape, st.begin),
+                                       abi.array4(st.S.ctypes.data, st.S.shape, st.begin)) for st in boxes])
+
+
+def fill_ghosts(boxes, geom: abi.PcGeometry, ngrow: int = 4) -> None:
+    """In-place ghost fill of BoxStates that tile the domain."""
+    lib = library()
+    lib.oracle_fill_ghosts.argtypes = [POINTER(abi.PcBoxDesc), c_int, POINTER(abi.PcGeometry), c_int, c_int]
+    for st in boxes:
+        assert st.S.flags.c_contiguous and st.S.dtype == np.float64
+    rc = lib.oracle_fill_ghosts(_state_descs(boxes), len(boxes), ctypes.byref(geom), ngrow, boxes[0].S.shape[0])
+    if rc != 0:
+        raise RuntimeError(f"oracle_fill_ghosts failed with code {rc}")
+
+
+def compute_temp(cfg: abi.PcMolConfig, boxes) -> int:
+    """PeleC::computeTemp on the valid cells of BoxStates (in place)."""
+    lib = library()
+    lib.oracle_compute_temp.argtypes = [POINTER(abi.PcMolConfig), c_int, POINTER(c_int), POINTER(abi.PcArray4),
+                                        POINTER(c_longlong)]
+    lohi = (c_int * (6 * len(boxes)))()
+    arrs = (abi.PcArray4 * len(boxes))()
+    for b, st in enumerate(boxes):
+        for d in range(3):
+            lohi[6 * b + d] = st.lo[d]
+            lohi[6 * b + 3 + d] = st.hi[d]
+        arrs[b] = abi.array4(st.S.ctypes.data, st.S.shape, st.begin)
+    fails = c_longlong(0)
+    rc = lib.oracle_compute_temp(ctypes.byref(cfg), len(boxes), lohi, arrs, ctypes.byref(fails))
+    if rc != 0:
+        raise RuntimeError(f"oracle_compute_temp failed with code {rc}")
+    return fails.value
+
+
+def est_dt(cfg: abi.PcMolConfig, boxes, cfl: float, max_dt: float = 1e30):
+    lib = library()
+    lib.oracle_est_dt.argtypes = [POINTER(abi.PcMolConfig), POINTER(abi.PcBoxDesc), c_int, POINTER(c_double),
+                                  c_double, c_double, POINTER(c_double), POINTER(c_double)]
+    dt = c_double(0.0)
+    parts = (c_double * 4)()
+    dx = (c_double * 3)(*boxes[0].dx)
+    rc = lib.oracle_est_dt(ctypes.byref(cfg), _state_descs(boxes), len(boxes), dx, cfl, max_dt, ctypes.byref(dt),
+                           parts)
+    if rc != 0:
+        raise RuntimeError(f"oracle_est_dt failed with code {rc}")
+    return dt.value, list(parts)
+
+
+def _valid(st):
+    g = st.ng
+    return st.S[:, g:-g, g:-g, g:-g]
+
+
+def ssprk2_step(cfg: abi.PcMolConfig, boxes, geom: abi.PcGeometry, dt: float):
+    """One MOL SSP-RK2 step (PeleC::do_mol_advance without sources) of a list
+    of BoxStates; returns the new states (the inputs keep their valid data,
+    their ghosts are refilled)."""
+    from pelec_gb300 import problems
+
+    fill_ghosts(boxes, geom, boxes[0].ng)
+    R = mol_rhs(cfg, boxes)
+    new = []
+    for st, r in zip(boxes, R):
+        S = st.S.copy()
+        _valid(problems.BoxState(st.lo, st.hi, S, st.dx))[...] = 1.0 * _valid(st) + dt * r
+        new.append(problems.BoxState(st.lo, st.hi, S, st.dx))
+    compute_temp(cfg, new)
+    fill_ghosts(new, geom, new[0].ng)
+    R = mol_rhs(cfg, new)
+    for st, old, r in zip(new, boxes, R):
+        v = _valid(st)
+        v[...] = 0.5 * v + 0.5 * _valid(old)
+        v[...] = 1.0 * v + (0.5 * dt) * r
+    compute_temp(cfg, new)
+    return new

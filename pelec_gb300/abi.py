@@ -102,6 +102,32 @@ class PcBoxDesc(ctypes.Structure):
     ]
 
 
+PC_BC_INTERIOR = 0
+PC_BC_OUTFLOW = 1
+PC_BC_SYMMETRY = 2
+PC_BC_SLIPWALL = 3
+PC_BC_NOSLIPWALL = 4
+
+
+class PcGeometry(ctypes.Structure):
+    _fields_ = [
+        ("domain_lo", c_int * 3),
+        ("domain_hi", c_int * 3),
+        ("bc_lo", c_int * 3),
+        ("bc_hi", c_int * 3),
+    ]
+
+
+def geometry(domain_lo, domain_hi, bc_lo, bc_hi) -> PcGeometry:
+    g = PcGeometry()
+    for d in range(3):
+        g.domain_lo[d] = int(domain_lo[d])
+        g.domain_hi[d] = int(domain_hi[d])
+        g.bc_lo[d] = int(bc_lo[d])
+        g.bc_hi[d] = int(bc_hi[d])
+    return g
+
+
 class PcMolStatus(ctypes.Structure):
     _fields_ = [
         ("cells", c_longlong),
@@ -146,5 +172,5 @@ def box_array(descs) -> ctypes.Array:
     return arr
 
 
-__all__ = [n for n in dir() if n.startswith(("Pc", "PC_", "U")) or n in ("array4", "box_desc", "box_array")]
+__all__ = [n for n in dir() if n.startswith(("Pc", "PC_", "U")) or n in ("array4", "box_desc", "box_array", "geometry")]
 _ = POINTER  # re-exported for callers building prototypes

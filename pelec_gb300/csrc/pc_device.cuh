@@ -233,8 +233,9 @@ struct ConstantTransport {
 
 // Mixture-averaged transport (Docs/sphinx/Algorithms.rst:540-566):
 // mu = (sum X mu_k^6)^(1/6), lambda = (sum X lambda_k^(1/4))^4,
-// xi = sum X bulk_k mu_k, rhoD_k = rho (1-Y_k) / sum_{j!=k} max(X_j,1e-15) /
-// D_kj(T,p), 1/D_kj(T,p) = exp(-fit_kj(ln T)) p / p_ref.
+// xi = sum X bulk_k mu_k, rhoD_k = rho (W_k/Wbar) (1-Y_k) /
+// sum_{j!=k} max(X_j,1e-15) / D_kj(T,p) (Hirschfelder-Curtiss mass flux
+// rhoD_k grad X_k), 1/D_kj(T,p) = exp(-fit_kj(ln T)) p / p_ref.
 template <int NS>
 struct SimpleTransport {
   __device__ static void eval(const DevMech<NS>& m, double T, double rho, double p, const double* Y, const double* X,
@@ -264,7 +265,12 @@ struct SimpleTransport {
       }
     }
 #pragma unroll
-    for (int k = 0; k < NS; ++k) out[k] = (s[k] > 0.0) ? rho * (1.0 - Y[k]) / s[k] : 0.0;
+    const double rw = mix_rw<NS>(m, Y);
+#pragma unroll
+    for (int k = 0; k < NS; ++k) {
+      const double wrat = rw / m.rW[k];  // W_k / Wbar
+      out[k] = (s[k] > 0.0) ? rho * (1.0 - Y[k]) * wrat / s[k] : 0.0;
+    }
     out[NS] = exp(log(smu) * (1.0 / 6.0));
     out[NS + 1] = sxi;
     const double l2 = slam * slam;

@@ -43,6 +43,7 @@ struct DevBox {
 };
 
 struct Geo {
+  double dxs[3];  // cell sizes
   double dxinv[3];
   double area[3];
   double vol;

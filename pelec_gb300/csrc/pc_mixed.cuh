@@ -181,7 +181,9 @@ struct TransF {
         }
       }
 #pragma unroll
-      for (int k = 0; k < NS; ++k) out[k] = (s[k] > 0.f) ? rho * (1.f - Y[k]) / s[k] : 0.f;
+      const float rw = mix_rwf<NS>(m, Y);
+#pragma unroll
+      for (int k = 0; k < NS; ++k) out[k] = (s[k] > 0.f) ? rho * (1.f - Y[k]) * (rw / m.rW[k]) / s[k] : 0.f;
       out[NS] = expf(logf(smu) * (1.f / 6.f));
       out[NS + 1] = sxi;
       const float l2 = slam * slam;

@@ -7,6 +7,7 @@
 // the diagnostic counters.  Device side: pc_kernels.cuh.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -14,6 +15,7 @@
 #include <vector>
 
 #include "pc_kernels.cuh"
+#include "pc_level.cuh"
 #include "pelec_mol.h"
 
 namespace pcg {
@@ -61,6 +63,14 @@ struct pc_mol_handle {
   int last_error = PC_OK;
   cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};  // pass timing (cfg.time_passes)
   bool timed = false;
+  // level operations: uploads cached by content (see upload())
+  struct Upload {
+    std::vector<unsigned char> host;
+    void* dev = nullptr;
+    size_t cap = 0;
+  };
+  Upload up[8];
+  unsigned long long* d_dt = nullptr;  // 4 time-step minima
 };
 
 namespace {
@@ -234,7 +244,10 @@ int prepare(pc_mol_handle* h, const pc_box_desc* boxes, int nboxes, const double
 
 Geo make_geo(const double dx[3]) {
   Geo g;
-  for (int d = 0; d < 3; ++d) g.dxinv[d] = 1.0 / dx[d];
+  for (int d = 0; d < 3; ++d) {
+    g.dxs[d] = dx[d];
+    g.dxinv[d] = 1.0 / dx[d];
+  }
   g.area[0] = dx[1] * dx[2];
   g.area[1] = dx[0] * dx[2];
   g.area[2] = dx[0] * dx[1];
@@ -389,6 +402,8 @@ void pc_mol_destroy(pc_mol_handle* h) {
   cudaFree(h->scratch);
   for (auto& e : h->ev)
     if (e) cudaEventDestroy(e);
+  for (auto& u : h->up) cudaFree(u.dev);
+  cudaFree(h->d_dt);
   delete h;
 }
 
@@ -599,4 +614,265 @@ extern "C" int pc_mol_rhs_box_static(const pc_mol_config* cfg, const pc_box_desc
     flux_kernel<9, IdealMixEos<9>><<<(unsigned)ntiles, kFluxThreads, 0, s>>>(dbox, tiles, mech9, fl, g, ctr);
   }
   return cudaGetLastError() == cudaSuccess ? PC_OK : PC_ERR_CUDA;
+}
+
+// ---------------------------------------------------------------------------
+// Level operations of the MOL advance: ghost fill, LinComb, computeTemp and
+// the time-step estimate (pc_level.cuh).
+// ---------------------------------------------------------------------------
+namespace {
+
+enum { kUpFillBoxes = 0, kUpFillItems, kUpOwner, kUpLcDst, kUpLcX, kUpLcY, kUpItems, kUpBoxes };
+
+// Copies bytes to the handle's device slot unless they equal the last upload
+// of that slot (repeated calls on the same layout launch kernels only).
+int upload(pc_mol_handle* h, int slot, const void* data, size_t bytes, cudaStream_t s, void** dev) {
+  pc_mol_handle::Upload& u = h->up[slot];
+  if (bytes == 0) {
+    *dev = u.dev;
+    return PC_OK;
+  }
+  if (u.host.size() == bytes && u.dev && std::memcmp(u.host.data(), data, bytes) == 0) {
+    *dev = u.dev;
+    return PC_OK;
+  }
+  if (bytes > u.cap) {
+    if (u.dev) {
+      cudaError_t e = cudaStreamSynchronize(s);
+      if (e != cudaSuccess) return cuda_fail(h, e);
+      cudaFree(u.dev);
+    }
+    u.dev = nullptr;
+    u.cap = 0;
+    cudaError_t e = cudaMalloc(&u.dev, bytes);
+    if (e != cudaSuccess) return cuda_fail(h, e);
+    u.cap = bytes;
+  }
+  u.host.assign(static_cast<const unsigned char*>(data), static_cast<const unsigned char*>(data) + bytes);
+  cudaError_t e = cudaMemcpyAsync(u.dev, u.host.data(), bytes, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_fail(h, e);
+  *dev = u.dev;
+  return PC_OK;
+}
+
+LevelBox level_box(const int lo[3], const int hi[3], const pc_array4& a) {
+  LevelBox b{};
+  for (int d = 0; d < 3; ++d) {
+    b.lo[d] = lo[d];
+    b.hi[d] = hi[d];
+    b.sb[d] = a.begin[d];
+  }
+  b.S = a.p;
+  b.sj = a.jstride;
+  b.sk = a.kstride;
+  b.sn = a.nstride;
+  return b;
+}
+
+bool array_ok(const pc_array4& a, const int lo[3], const int hi[3], int ng, int nvar) {
+  if (!a.p || a.ncomp < nvar) return false;
+  for (int d = 0; d < 3; ++d)
+    if (hi[d] < lo[d] || a.begin[d] > lo[d] - ng || a.end[d] - 1 < hi[d] + ng) return false;
+  const long long nx = a.end[0] - a.begin[0], ny = a.end[1] - a.begin[1], nz = a.end[2] - a.begin[2];
+  return a.jstride >= nx && a.kstride >= a.jstride * ny && a.nstride >= a.kstride * nz;
+}
+
+void chunk_items(const std::vector<long long>& ncells, std::vector<int2>& items) {
+  items.clear();
+  for (size_t b = 0; b < ncells.size(); ++b)
+    for (long long c = 0; c < ncells[b]; c += 256) items.push_back(make_int2((int)b, (int)c));
+}
+
+long long nvalid(const int lo[3], const int hi[3], int ng) {
+  long long n = 1;
+  for (int d = 0; d < 3; ++d) n *= (long long)(hi[d] - lo[d] + 1 + 2 * ng);
+  return n;
+}
+
+}  // namespace
+
+extern "C" int pc_mol_fill_ghosts(pc_mol_handle* h, const pc_box_desc* boxes, int nboxes, const pc_geometry* geom,
+                                  int ngrow, void* stream) {
+  if (!h || !geom || nboxes < 0 || (nboxes > 0 && !boxes) || ngrow < 0) return PC_ERR_INVALID_ARGUMENT;
+  if (nboxes == 0 || ngrow == 0) return PC_OK;
+  const int nvar = 7 + h->cfg.nspec;
+  FillGeom g{};
+  long long ndom = 1;
+  for (int d = 0; d < 3; ++d) {
+    g.dlo[d] = geom->domain_lo[d];
+    g.dhi[d] = geom->domain_hi[d];
+    g.len[d] = geom->domain_hi[d] - geom->domain_lo[d] + 1;
+    g.bclo[d] = geom->bc_lo[d];
+    g.bchi[d] = geom->bc_hi[d];
+    if (g.len[d] < ngrow) return PC_ERR_INVALID_ARGUMENT;
+    for (int bc : {geom->bc_lo[d], geom->bc_hi[d]})
+      if (bc < PC_BC_INTERIOR || bc > PC_BC_NOSLIPWALL) return PC_ERR_UNSUPPORTED;
+    if ((geom->bc_lo[d] == PC_BC_INTERIOR) != (geom->bc_hi[d] == PC_BC_INTERIOR)) return PC_ERR_INVALID_ARGUMENT;
+    g.periodic[d] = geom->bc_lo[d] == PC_BC_INTERIOR;
+    ndom *= g.len[d];
+  }
+  g.ng = ngrow;
+  g.nvar = nvar;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  int rc = cuda_fail(h, cudaSetDevice(h->device));
+  if (rc != PC_OK) return rc;
+  std::vector<LevelBox> lb;
+  std::vector<long long> nc;
+  for (int b = 0; b < nboxes; ++b) {
+    if (!array_ok(boxes[b].state, boxes[b].lo, boxes[b].hi, ngrow, nvar)) return h->last_error = PC_ERR_INVALID_ARGUMENT;
+    for (int d = 0; d < 3; ++d)
+      if (boxes[b].lo[d] < g.dlo[d] || boxes[b].hi[d] > g.dhi[d]) return h->last_error = PC_ERR_INVALID_ARGUMENT;
+    lb.push_back(level_box(boxes[b].lo, boxes[b].hi, boxes[b].state));
+    nc.push_back(nvalid(boxes[b].lo, boxes[b].hi, ngrow));
+  }
+  std::vector<int2> items;
+  chunk_items(nc, items);
+  // Owner of each domain cell (several boxes): the valid boxes must tile the domain.
+  void *dbox = nullptr, *ditems = nullptr, *downer = nullptr;
+  if (nboxes > 1) {
+    if (ndom > 400000000LL) return h->last_error = PC_ERR_TOO_LARGE;
+    std::vector<int> owner((size_t)ndom, -1);
+    for (int b = 0; b < nboxes; ++b)
+      for (int k = boxes[b].lo[2]; k <= boxes[b].hi[2]; ++k)
+        for (int j = boxes[b].lo[1]; j <= boxes[b].hi[1]; ++j)
+          for (int i = boxes[b].lo[0]; i <= boxes[b].hi[0]; ++i) {
+            const long long o = (i - g.dlo[0]) + (long long)(j - g.dlo[1]) * g.len[0] +
+                                (long long)(k - g.dlo[2]) * g.len[0] * g.len[1];
+            if (owner[o] >= 0) return h->last_error = PC_ERR_INVALID_ARGUMENT;  // overlapping boxes
+            owner[o] = b;
+          }
+    for (int o : owner)
+      if (o < 0) return h->last_error = PC_ERR_INVALID_ARGUMENT;  // domain not covered
+    if ((rc = upload(h, kUpOwner, owner.data(), owner.size() * sizeof(int), s, &downer)) != PC_OK) return rc;
+  } else {
+    for (int d = 0; d < 3; ++d)
+      if (boxes[0].lo[d] != g.dlo[d] || boxes[0].hi[d] != g.dhi[d]) return h->last_error = PC_ERR_INVALID_ARGUMENT;
+  }
+  if ((rc = upload(h, kUpFillBoxes, lb.data(), lb.size() * sizeof(LevelBox), s, &dbox)) != PC_OK) return rc;
+  if ((rc = upload(h, kUpFillItems, items.data(), items.size() * sizeof(int2), s, &ditems)) != PC_OK) return rc;
+  fill_ghosts_kernel<<<(unsigned)items.size(), 256, 0, s>>>(static_cast<const LevelBox*>(dbox),
+                                                            static_cast<const int2*>(ditems),
+                                                            nboxes > 1 ? static_cast<const int*>(downer) : nullptr, g);
+  return h->last_error = cuda_fail(h, cudaGetLastError());
+}
+
+extern "C" int pc_mol_lincomb(pc_mol_handle* h, int nboxes, const int* lohi, const pc_array4* dst, double a,
+                              const pc_array4* x, double b, const pc_array4* y, void* stream) {
+  if (!h || nboxes < 0 || (nboxes > 0 && (!lohi || !dst || !x || !y))) return PC_ERR_INVALID_ARGUMENT;
+  if (nboxes == 0) return PC_OK;
+  const int nvar = 7 + h->cfg.nspec;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  int rc = cuda_fail(h, cudaSetDevice(h->device));
+  if (rc != PC_OK) return rc;
+  std::vector<LevelBox> ld, lx, ly;
+  std::vector<long long> nc;
+  for (int i = 0; i < nboxes; ++i) {
+    const int* lo = lohi + 6 * i;
+    const int* hi = lohi + 6 * i + 3;
+    if (!array_ok(dst[i], lo, hi, 0, nvar) || !array_ok(x[i], lo, hi, 0, nvar) || !array_ok(y[i], lo, hi, 0, nvar))
+      return h->last_error = PC_ERR_INVALID_ARGUMENT;
+    ld.push_back(level_box(lo, hi, dst[i]));
+    lx.push_back(level_box(lo, hi, x[i]));
+    ly.push_back(level_box(lo, hi, y[i]));
+    nc.push_back(nvalid(lo, hi, 0));
+  }
+  std::vector<int2> items;
+  chunk_items(nc, items);
+  void *dd, *dx, *dy, *di;
+  if ((rc = upload(h, kUpLcDst, ld.data(), ld.size() * sizeof(LevelBox), s, &dd)) != PC_OK) return rc;
+  if ((rc = upload(h, kUpLcX, lx.data(), lx.size() * sizeof(LevelBox), s, &dx)) != PC_OK) return rc;
+  if ((rc = upload(h, kUpLcY, ly.data(), ly.size() * sizeof(LevelBox), s, &dy)) != PC_OK) return rc;
+  if ((rc = upload(h, kUpItems, items.data(), items.size() * sizeof(int2), s, &di)) != PC_OK) return rc;
+  LinCombArgs A{static_cast<const LevelBox*>(dd), static_cast<const LevelBox*>(dx), static_cast<const LevelBox*>(dy),
+                a, b, nvar};
+  lincomb_kernel<<<(unsigned)items.size(), 256, 0, s>>>(static_cast<const int2*>(di), A);
+  return h->last_error = cuda_fail(h, cudaGetLastError());
+}
+
+extern "C" int pc_mol_compute_temp(pc_mol_handle* h, int nboxes, const int* lohi, const pc_array4* state,
+                                   void* stream) {
+  if (!h || nboxes < 0 || (nboxes > 0 && (!lohi || !state))) return PC_ERR_INVALID_ARGUMENT;
+  if (nboxes == 0) return PC_OK;
+  const int nvar = 7 + h->cfg.nspec;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  int rc = cuda_fail(h, cudaSetDevice(h->device));
+  if (rc != PC_OK) return rc;
+  std::vector<LevelBox> lb;
+  std::vector<long long> nc;
+  for (int i = 0; i < nboxes; ++i) {
+    const int* lo = lohi + 6 * i;
+    const int* hi = lohi + 6 * i + 3;
+    if (!array_ok(state[i], lo, hi, 0, nvar)) return h->last_error = PC_ERR_INVALID_ARGUMENT;
+    lb.push_back(level_box(lo, hi, state[i]));
+    nc.push_back(nvalid(lo, hi, 0));
+  }
+  std::vector<int2> items;
+  chunk_items(nc, items);
+  void *db, *di;
+  if ((rc = upload(h, kUpBoxes, lb.data(), lb.size() * sizeof(LevelBox), s, &db)) != PC_OK) return rc;
+  if ((rc = upload(h, kUpItems, items.data(), items.size() * sizeof(int2), s, &di)) != PC_OK) return rc;
+  h->last_stream = s;
+  cudaMemsetAsync(h->d_counters, 0, sizeof(unsigned long long) * kNumCounters, s);
+  const int maxit = h->flags.newton_maxit;
+  if (h->variant == 1)
+    compute_temp_kernel<1, GammaLawEos<1>><<<(unsigned)items.size(), 256, 0, s>>>(
+        static_cast<const LevelBox*>(db), static_cast<const int2*>(di), h->mech1, maxit, h->d_counters);
+  else
+    compute_temp_kernel<9, IdealMixEos<9>><<<(unsigned)items.size(), 256, 0, s>>>(
+        static_cast<const LevelBox*>(db), static_cast<const int2*>(di), h->mech9, maxit, h->d_counters);
+  return h->last_error = cuda_fail(h, cudaGetLastError());
+}
+
+extern "C" int pc_mol_est_dt(pc_mol_handle* h, const pc_box_desc* boxes, int nboxes, const double dx[3], double cfl,
+                             double max_dt, double* dt, void* stream) {
+  if (!h || !dx || !dt || nboxes < 0 || (nboxes > 0 && !boxes) || !(cfl > 0.0) || !(max_dt > 0.0))
+    return PC_ERR_INVALID_ARGUMENT;
+  const int nvar = 7 + h->cfg.nspec;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  int rc = cuda_fail(h, cudaSetDevice(h->device));
+  if (rc != PC_OK) return rc;
+  if (!h->d_dt && (rc = cuda_fail(h, cudaMalloc(&h->d_dt, 4 * sizeof(unsigned long long)))) != PC_OK) return rc;
+  std::vector<LevelBox> lb;
+  std::vector<long long> nc;
+  for (int i = 0; i < nboxes; ++i) {
+    if (!array_ok(boxes[i].state, boxes[i].lo, boxes[i].hi, 0, nvar)) return h->last_error = PC_ERR_INVALID_ARGUMENT;
+    lb.push_back(level_box(boxes[i].lo, boxes[i].hi, boxes[i].state));
+    nc.push_back(nvalid(boxes[i].lo, boxes[i].hi, 0));
+  }
+  std::vector<int2> items;
+  chunk_items(nc, items);
+  const unsigned long long inf[4] = {0x7ff0000000000000ull, 0x7ff0000000000000ull, 0x7ff0000000000000ull,
+                                     0x7ff0000000000000ull};
+  cudaError_t e = cudaMemcpyAsync(h->d_dt, inf, sizeof(inf), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_fail(h, e);
+  if (!items.empty()) {
+    void *db, *di;
+    if ((rc = upload(h, kUpBoxes, lb.data(), lb.size() * sizeof(LevelBox), s, &db)) != PC_OK) return rc;
+    if ((rc = upload(h, kUpItems, items.data(), items.size() * sizeof(int2), s, &di)) != PC_OK) return rc;
+    const Geo g = make_geo(dx);
+    if (h->variant == 1)
+      est_dt_kernel<1, GammaLawEos<1>, ConstantTransport<1>><<<(unsigned)items.size(), 256, 0, s>>>(
+          static_cast<const LevelBox*>(db), static_cast<const int2*>(di), h->mech1, g, h->d_dt);
+    else
+      est_dt_kernel<9, IdealMixEos<9>, SimpleTransport<9>><<<(unsigned)items.size(), 256, 0, s>>>(
+          static_cast<const LevelBox*>(db), static_cast<const int2*>(di), h->mech9, g, h->d_dt);
+  }
+  unsigned long long bits[4];
+  e = cudaMemcpyAsync(bits, h->d_dt, sizeof(bits), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_fail(h, e);
+  double m4[4];
+  std::memcpy(m4, bits, sizeof(m4));
+  const double mdc = max_dt / cfl;
+  double eh = mdc, ev = mdc, et = mdc, ee = mdc;
+  if (h->cfg.do_hydro) eh = std::min(eh, m4[0]);
+  if (h->cfg.diffuse_vel) ev = std::min(ev, m4[1]);
+  if (h->cfg.diffuse_temp) et = std::min(et, m4[2]);
+  if (h->cfg.diffuse_enth) ee = std::min(ee, m4[3]);
+  eh = std::min(eh, std::min(ev, std::min(et, ee)));
+  eh *= cfl;
+  *dt = std::min(max_dt, eh);
+  return h->last_error = PC_OK;
 }

@@ -52,6 +52,17 @@ def library() -> ctypes.CDLL:
         lib.pc_mol_last_status.restype = c_int
         lib.pc_mol_pass_times.argtypes = [c_void_p, POINTER(c_double), c_int]
         lib.pc_mol_pass_times.restype = c_int
+        lib.pc_mol_fill_ghosts.argtypes = [c_void_p, POINTER(abi.PcBoxDesc), c_int, POINTER(abi.PcGeometry), c_int,
+                                           c_void_p]
+        lib.pc_mol_fill_ghosts.restype = c_int
+        lib.pc_mol_lincomb.argtypes = [c_void_p, c_int, POINTER(c_int), POINTER(abi.PcArray4), c_double,
+                                       POINTER(abi.PcArray4), c_double, POINTER(abi.PcArray4), c_void_p]
+        lib.pc_mol_lincomb.restype = c_int
+        lib.pc_mol_compute_temp.argtypes = [c_void_p, c_int, POINTER(c_int), POINTER(abi.PcArray4), c_void_p]
+        lib.pc_mol_compute_temp.restype = c_int
+        lib.pc_mol_est_dt.argtypes = [c_void_p, POINTER(abi.PcBoxDesc), c_int, POINTER(c_double), c_double, c_double,
+                                      POINTER(c_double), c_void_p]
+        lib.pc_mol_est_dt.restype = c_int
         if lib.pc_mol_abi_version() != abi.PC_MOL_ABI_VERSION:
             raise RuntimeError("libpelec_mol.so ABI version does not match pelec_gb300.abi")
         _lib = lib
@@ -158,6 +169,57 @@ class MOLOperator:
         ms = (c_double * 2)()
         _check(library().pc_mol_pass_times(self._h, ms, 2), "pc_mol_pass_times")
         return float(ms[0]), float(ms[1])
+
+    # ---- level operations of the MOL advance ----
+    @staticmethod
+    def _stream(stream):
+        import torch
+
+        return c_void_p((stream if stream is not None else torch.cuda.current_stream()).cuda_stream)
+
+    @staticmethod
+    def _lohi(mf: MultiFab):
+        arr = (c_int * (6 * len(mf)))()
+        for b, (lo, hi) in enumerate(mf.boxes):
+            for d in range(3):
+                arr[6 * b + d] = lo[d]
+                arr[6 * b + 3 + d] = hi[d]
+        return arr
+
+    @staticmethod
+    def _arrays(mf: MultiFab):
+        arr = (abi.PcArray4 * len(mf))()
+        for b in range(len(mf)):
+            arr[b] = mf.array4(b)
+        return arr
+
+    def fill_ghosts(self, S: MultiFab, geom: abi.PcGeometry, ngrow: int | None = None, stream=None) -> None:
+        """Fill S's ghost cells from the level's valid data and the domain BCs
+        (FillPatcherFill at a single level)."""
+        descs = abi.box_array([abi.box_desc(lo, hi, S.array4(b), S.array4(b)) for b, (lo, hi) in enumerate(S.boxes)])
+        ng = S.ngrow if ngrow is None else ngrow
+        _check(library().pc_mol_fill_ghosts(self._h, descs, len(S), ctypes.byref(geom), ng, self._stream(stream)),
+               "pc_mol_fill_ghosts")
+
+    def lincomb(self, dst: MultiFab, a: float, x: MultiFab, b: float, y: MultiFab, stream=None) -> None:
+        """dst = a x + b y on the valid cells (MultiFab::LinComb)."""
+        _check(library().pc_mol_lincomb(self._h, len(dst), self._lohi(dst), self._arrays(dst), float(a),
+                                        self._arrays(x), float(b), self._arrays(y), self._stream(stream)),
+               "pc_mol_lincomb")
+
+    def compute_temp(self, S: MultiFab, stream=None) -> None:
+        """PeleC::computeTemp on the valid cells."""
+        _check(library().pc_mol_compute_temp(self._h, len(S), self._lohi(S), self._arrays(S), self._stream(stream)),
+               "pc_mol_compute_temp")
+
+    def est_dt(self, S: MultiFab, dx, cfl: float, max_dt: float = 1e30, stream=None) -> float:
+        """PeleC::estTimeStep (synchronous)."""
+        descs = abi.box_array([abi.box_desc(lo, hi, S.array4(b), S.array4(b)) for b, (lo, hi) in enumerate(S.boxes)])
+        out = c_double(0.0)
+        dxa = (c_double * 3)(*[float(v) for v in dx])
+        _check(library().pc_mol_est_dt(self._h, descs, len(S), dxa, float(cfl), float(max_dt), ctypes.byref(out),
+                                       self._stream(stream)), "pc_mol_est_dt")
+        return out.value
 
     def status(self) -> abi.PcMolStatus:
         st = abi.PcMolStatus()
