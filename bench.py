@@ -1,7 +1,7 @@
 """Benchmark of the MOL right-hand side (PeleC getMOLSrcTerm path) on GB300.
 
     python bench.py [--gpus N --steps K --warmup W] [--impl gb300|reference]
-                    [--workload c2|c1] [--precision fp64]
+                    [--workload c2|c1] [--precision fp64] [--no-level]
 
 One step = one full-level RHS evaluation of the workload (default C2: one
 128^3 box of the 9-species premixed flame, FP64).  The value is cell-RHS
@@ -10,8 +10,11 @@ events on the launch stream, barrier + synchronize on both sides, max over
 ranks).  ``e2e`` repeats the measurement through the public API with the
 state copied from pinned host memory and the RHS copied back every step.
 Under torchrun each rank evaluates its own box (weak scaling, no data-path
-collective).  ``--impl reference`` times the CPU restatement of the
-reference path (the oracle) on the host cores with all threads.
+collective).  ``level_c3`` adds the batched-level measurement (400 uneven
+boxes: per-box launches vs one batched launch vs the autotuned tile shape vs
+a CUDA-graph replay, FP64 and mixed), outside the headline's timed region.
+``--impl reference`` times the CPU restatement of the reference path (the
+oracle) on the host cores with all threads.
 """
 from __future__ import annotations
 
@@ -39,6 +42,7 @@ def parse():
     ap.add_argument("--workload", default="c2", choices=["c2", "c1"])
     ap.add_argument("--precision", default="fp64", choices=["fp64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-level", action="store_true", help="skip the 400-box batched-level measurement")
     return ap.parse_args()
 
 
@@ -168,6 +172,102 @@ def fp_peaks() -> dict:
         return {"fp64_fma_tflops": out[0], "fp32_fma_tflops": out[1], "source": "pc_peaks.cu, measured in this run"}
     except OSError:
         return {}
+
+
+def bench_level(args, rank: int, local: int, maxover, barrier) -> dict:
+    """C3: 400 uneven boxes (edges from {8,16,24,32,48,64} per axis, seeded),
+    9 species.  Times one RHS of the whole level per step as (a) one launch per
+    box and pass, (b) one batched launch per pass at the default tile shape,
+    (c) batched at the autotuned shape, (d) a CUDA-graph replay of (c), for
+    FP64 and for mixed precision; plus the oracle on a sample of the boxes."""
+    import numpy as np
+    import torch
+
+    from pelec_gb300 import mol, problems
+
+    mech, boxes = problems.level_boxes(400, seed=3 + 1000 * rank)
+    cells = sum(b.ncells for b in boxes)
+    S = mol.MultiFab([(b.lo, b.hi) for b in boxes], boxes[0].S.shape[0], boxes[0].ng,
+                     fabs=[torch.from_numpy(b.S).cuda() for b in boxes])
+    R = mol.MultiFab(S.boxes, S.ncomp, 0)
+    dx = boxes[0].dx
+    stream = torch.cuda.current_stream()
+    steps = max(1, min(args.steps, 10))
+
+    def timed(fn):
+        for _ in range(max(3, args.warmup)):
+            fn()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        barrier()
+        e0.record(stream)
+        for _ in range(steps):
+            fn()
+        e1.record(stream)
+        barrier()
+        return maxover(e0.elapsed_time(e1) / 1e3) / steps
+
+    out = {"workload": "C3: %d boxes, edges per axis from {8,16,24,32,48,64} (seeded), %d cells, 9-species flame "
+                       "at per-box seeded offsets" % (len(boxes), cells),
+           "cells": cells, "steps": steps, "unit": "cell-evals/s"}
+    ref = None
+    for prec, name in ((abi_precision(0), "fp64"), (abi_precision(1), "mixed")):
+        op = mol.MOLOperator(problems.make_config(mech, precision=prec))
+        res = {}
+        t_per_box = timed(lambda: op.rhs_level(S, R, dx, per_box=True))
+        op.set_tile(0)
+        t_default = timed(lambda: op.rhs_level(S, R, dx))
+        op.set_tile(-1)
+        best, ms = op.autotune(S, R, dx, reps=3)
+        t_tuned = timed(lambda: op.rhs_level(S, R, dx))
+        torch.cuda.synchronize()
+        r = [t.cpu().numpy() for t in R.fabs]
+        g = op.graph(S, R, dx)
+        t_graph = timed(g.launch)
+        g.close()
+        res["per_box"] = {"value": cells / t_per_box, "ms_per_step": 1e3 * t_per_box,
+                          "gpu_launches_per_step": 2 * len(boxes)}
+        res["batched_default_tile"] = {"value": cells / t_default, "ms_per_step": 1e3 * t_default,
+                                       "tile": mol.MOLOperator.tile_shape(0), "gpu_launches_per_step": 2}
+        res["batched_autotuned"] = {"value": cells / t_tuned, "ms_per_step": 1e3 * t_tuned,
+                                    "tile": mol.MOLOperator.tile_shape(best), "gpu_launches_per_step": 2,
+                                    "autotune_ms_per_shape": {"x".join(map(str, mol.MOLOperator.tile_shape(t)[:3])): v
+                                                              for t, v in enumerate(ms)}}
+        res["graph"] = {"value": cells / t_graph, "ms_per_step": 1e3 * t_graph, "gpu_launches_per_step": 2,
+                        "note": "one cudaGraphLaunch of the autotuned batched RHS"}
+        res["speedup_graph_vs_per_box"] = t_per_box / t_graph
+        if prec == 0:
+            ref = r
+        else:
+            num = np.zeros(S.ncomp)
+            den = np.zeros(S.ncomp)
+            for a, b in zip(r, ref):
+                num += ((a - b) ** 2).sum(axis=(1, 2, 3))
+                den += (b ** 2).sum(axis=(1, 2, 3))
+            l2 = np.sqrt(num / np.maximum(den, 1e-300))
+            res["rel_l2_vs_fp64"] = {"max": float(l2.max()), "per_component": [float(v) for v in l2]}
+        out[name] = res
+        op.close()
+    out["mixed_speedup_vs_fp64_graph"] = out["fp64"]["graph"]["ms_per_step"] / out["mixed"]["graph"]["ms_per_step"]
+    if rank == 0 and not args.no_cpu_baseline:
+        from oracle import pyoracle
+
+        cfg = problems.make_config(mech)
+        sample = boxes[:40]
+        ncs = sum(b.ncells for b in sample)
+        t0 = time.perf_counter()
+        pyoracle.mol_rhs(cfg, sample, nthreads=pyoracle.max_threads())
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": ncs / dt, "unit": "cell-evals/s", "cores": pyoracle.max_threads(),
+                               "kind": "port", "sample": f"first 40 of the 400 boxes ({ncs} cells), one pass"}
+    del S, R
+    torch.cuda.empty_cache()
+    return out
+
+
+def abi_precision(mixed: int) -> int:
+    from pelec_gb300 import abi
+
+    return abi.PC_PRECISION_MIXED if mixed else abi.PC_PRECISION_FP64
 
 
 def run_reference(args):
@@ -306,6 +406,8 @@ def run_gpu(args):
     l2 = [float(np.sqrt(((r32[n] - r64[n]) ** 2).sum() / max((r64[n] ** 2).sum(), 1e-300))) for n in range(r64.shape[0])]
     mx = [float(np.abs(r32[n] - r64[n]).max() / max(np.abs(r64[n]).max(), 1e-300)) for n in range(r64.shape[0])]
 
+    level = None if args.no_level else bench_level(args, rank, local, maxover, barrier)
+
     if rank != 0:
         if pg is not None:
             pg.destroy_process_group()
@@ -355,6 +457,8 @@ def run_gpu(args):
     }
     if cpu is not None:
         line["cpu_baseline"] = cpu
+    if level is not None:
+        line["level_c3"] = level
     print(json.dumps(line))
     if pg is not None:
         pg.destroy_process_group()

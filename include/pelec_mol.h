@@ -211,6 +211,40 @@ int pc_mol_last_status(pc_mol_handle* h, pc_mol_status* st);
  * transport), ms[1] = flux pass (faces and divergence).  n >= 2. */
 int pc_mol_pass_times(pc_mol_handle* h, double* ms, int n);
 
+/* Tile shapes of the flux pass (one thread per cell of a tile; every shape
+ * gives bit-identical FP64 results).  The reference's counterpart is the
+ * MFIter tile size and the launch shape of its GPU loops (hydro_tile_size,
+ * Diffusion.cpp:81-86; amrex::ParallelFor block size), which are fixed. */
+#define PC_NUM_TILES 4
+enum {
+  PC_TILE_8x8x4 = 0,   /* 256 threads, 2 CTAs/SM (default)                   */
+  PC_TILE_8x8x8 = 1,   /* 512 threads, 1 CTA/SM                               */
+  PC_TILE_16x8x4 = 2,  /* 512 threads, 1 CTA/SM                               */
+  PC_TILE_8x4x4 = 3    /* 128 threads, 4 CTAs/SM                              */
+};
+
+/* shape[0..3] = tile extents x, y, z and threads per CTA of tile t. */
+int pc_mol_tile_shape(int t, int shape[4]);
+
+/* Force tile shape t for the following calls, or t = -1 to return to the
+ * automatic choice (the autotune cache entry of the BoxArray's box-size
+ * histogram, else PC_TILE_8x8x4). */
+int pc_mol_set_tile(pc_mol_handle* h, int t);
+
+/* The tile shape that the last rhs call used. */
+int pc_mol_current_tile(pc_mol_handle* h, int* t);
+
+/* Autotuner: time pc_mol_rhs_level on this BoxArray at every tile shape
+ * (one warm-up, then reps timed calls each, CUDA events on stream), keep the
+ * fastest in the handle's cache under the BoxArray's box-size histogram (the
+ * species count and precision are the handle's) and return it in *best.
+ * ms[t] receives the mean time per call of shape t when ms is not NULL and
+ * n_ms >= PC_NUM_TILES.  Writes the RHS into the boxes' rhs arrays (every
+ * shape gives the same values).  Synchronous; not to be called during a
+ * stream capture. */
+int pc_mol_autotune(pc_mol_handle* h, const pc_box_desc* boxes, int nboxes, const double dx[3], int reps,
+                    int* best, double* ms, int n_ms, void* stream);
+
 /* Fill ngrow ghost layers of every box's state array on one level that
  * covers its domain: each ghost cell takes the value of the valid cell it
  * maps to — periodic images wrap, PC_BC_OUTFLOW clamps to the nearest
@@ -233,6 +267,23 @@ int pc_mol_lincomb(pc_mol_handle* h, int nboxes, const int* lohi, const pc_array
  * reset_internal_energy sets rho e = rho E - rho |u|^2/2 (Utilities.H:219-236)
  * and pc_cmpTemp solves the EOS for T from U(UTEMP) (Utilities.H:67-84). */
 int pc_mol_compute_temp(pc_mol_handle* h, int nboxes, const int* lohi, const pc_array4* state, void* stream);
+
+/* A CUDA graph of one level's RHS, optionally preceded by its ghost fill
+ * (FillPatcherFill + getMOLSrcTerm of Advance.cpp:98-100), captured once and
+ * replayed with one launch.  The layout (boxes, array pointers, dx, fill
+ * geometry when not NULL, tile shape) is fixed at creation; each replay
+ * reads the arrays' current contents.  The graph owns a private copy of h
+ * (configuration, tile choice and autotune cache as they are at creation)
+ * with its own scratch and counters, so later calls through h do not
+ * disturb it; pc_mol_graph_status reads the counters of the last replay.
+ * Creation runs the sequence once uncaptured on an internal stream (uploads,
+ * scratch) and synchronizes. */
+typedef struct pc_mol_graph pc_mol_graph;
+int pc_mol_graph_create(pc_mol_handle* h, const pc_box_desc* boxes, int nboxes, const double dx[3],
+                        const pc_geometry* fill_geom, int ngrow, pc_mol_graph** out);
+int pc_mol_graph_launch(pc_mol_graph* g, void* stream);
+int pc_mol_graph_status(pc_mol_graph* g, pc_mol_status* st);
+void pc_mol_graph_destroy(pc_mol_graph* g);
 
 /* PeleC::estTimeStep (PeleC.cpp:839-972, Timestep.H): min over valid cells
  * of dx/(c+|u|) (do_hydro) and the viscous, thermal and enthalpy diffusion

@@ -108,6 +108,9 @@ PC_BC_SYMMETRY = 2
 PC_BC_SLIPWALL = 3
 PC_BC_NOSLIPWALL = 4
 
+# flux-pass tile shapes (PC_TILE_*): 8x8x4, 8x8x8, 16x8x4, 8x4x4
+PC_NUM_TILES = 4
+
 
 class PcGeometry(ctypes.Structure):
     _fields_ = [

@@ -1,6 +1,6 @@
 """Build recipe of the CUDA library ``pelec_gb300/_lib/libpelec_mol.so``.
 
-Two translation units compiled by nvcc for sm_103a only (in parallel) and
+Four translation units compiled by nvcc for sm_103a only (in parallel) and
 linked into one shared library with a plain C ABI (include/pelec_mol.h), no
 torch headers:
 
@@ -10,6 +10,8 @@ torch headers:
   restatement's arithmetic exactly; host code is built without contraction
   too.
 * pc_mol_mixed.cu — the mixed-precision kernels, with contraction on.
+* pc_tiles_fp64.cu / pc_tiles_mixed.cu — the flux pass of each precision at
+  the tile shapes other than the default, compiled like the unit above them.
 
 libpc_peaks.so (pc_peaks.cu) measures the FP64/FP32 FMA rates that bench.py
 uses as roofline denominators.
@@ -27,7 +29,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off"]
 
 LIBS = {
-    "libpelec_mol.so": [("pc_mol.cu", ["-fmad=false"]), ("pc_mol_mixed.cu", ["-fmad=true"])],
+    "libpelec_mol.so": [("pc_mol.cu", ["-fmad=false"]), ("pc_mol_mixed.cu", ["-fmad=true"]),
+                        ("pc_tiles_fp64.cu", ["-fmad=false"]), ("pc_tiles_mixed.cu", ["-fmad=true"])],
     # arithmetic peak rates for bench.py's roofline (not part of the ABI)
     "libpc_peaks.so": [("pc_peaks.cu", ["-fmad=true"])],
 }

@@ -264,7 +264,6 @@ struct SimpleTransport {
         s[j] = fma(fmax(X[k], 1e-15), invD, s[j]);
       }
     }
-#pragma unroll
     const double rw = mix_rw<NS>(m, Y);
 #pragma unroll
     for (int k = 0; k < NS; ++k) {

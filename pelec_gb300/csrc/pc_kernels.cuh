@@ -442,20 +442,40 @@ __device__ __forceinline__ void diffusion_face(const DevBox& b, const DevFlags& 
 // ---------------------------------------------------------------------------
 // Pass 2.  tiles[b] = (box index, tile origin i, j, k).
 // ---------------------------------------------------------------------------
-constexpr int kTX = 8, kTY = 8, kTZ = 4, kFluxThreads = kTX * kTY * kTZ;
-constexpr int kMaxFaces = (kTX + 1) * kTY * kTZ > kTX * kTY * (kTZ + 1) ? (kTX + 1) * kTY * kTZ : kTX * kTY * (kTZ + 1);
+// Tile of the flux pass: TX x TY x TZ cells, one thread per cell, MINB CTAs
+// per SM requested from the register allocator.  The face buffer holds
+// NVAR x MAXF doubles; tiles whose buffer exceeds the 48 KB of static shared
+// memory use dynamic shared memory (DYN).
+template <int TX_, int TY_, int TZ_, int MINB_>
+struct Tile {
+  static constexpr int TX = TX_, TY = TY_, TZ = TZ_, MINB = MINB_, NT = TX_ * TY_ * TZ_;
+  static constexpr int F0 = (TX_ + 1) * TY_ * TZ_, F1 = TX_ * (TY_ + 1) * TZ_, F2 = TX_ * TY_ * (TZ_ + 1);
+  static constexpr int MAXF = F0 > F1 ? (F0 > F2 ? F0 : F2) : (F1 > F2 ? F1 : F2);
+  static constexpr bool DYN = TX_ * TY_ * TZ_ > 256;
+};
+// The tile shapes the level autotuner chooses from (index = PC_TILE_* order).
+using TileDefault = Tile<8, 8, 4, 2>;
+using TileCube = Tile<8, 8, 8, 1>;
+using TileLong = Tile<16, 8, 4, 1>;
+using TileSmall = Tile<8, 4, 4, 4>;
+constexpr int kNumTiles = 4;
+__host__ __device__ constexpr int tile_extent(int t, int d) {
+  return t == 1 ? 8 : t == 2 ? (d == 0 ? 16 : d == 1 ? 8 : 4) : t == 3 ? (d == 0 ? 8 : 4) : (d == 2 ? 4 : 8);
+}
+constexpr int kTX = TileDefault::TX, kTY = TileDefault::TY, kTZ = TileDefault::TZ, kFluxThreads = TileDefault::NT;
+constexpr int kMaxFaces = TileDefault::MAXF;
 
 // One direction of pass 2: every face of the tile with normal d, staged in
 // shared memory, then differenced into the cell accumulators.
-template <int NS, class EOS, int d>
+template <int NS, class EOS, int d, class TL>
 __device__ __forceinline__ void dir_pass(const DevBox& b, const DevMech<NS>& m, const DevFlags& f, const Geo& g,
                                          const int o[3], const int ext[3], const long long stv[3], bool mine, int tx,
-                                         int ty, int tz, double (*fbuf)[kMaxFaces], double* acc) {
+                                         int ty, int tz, double* fbuf, double* acc) {
   constexpr int NVAR = 7 + NS;
   const bool diff = f.diffuse_vel || f.diffuse_temp || f.diffuse_spec || f.diffuse_enth;
   const int nf0 = ext[0] + (d == 0), nf1 = ext[1] + (d == 1), nf2 = ext[2] + (d == 2);
   const int nfaces = nf0 * nf1 * nf2;
-  for (int fi = threadIdx.x; fi < nfaces; fi += kFluxThreads) {
+  for (int fi = threadIdx.x; fi < nfaces; fi += TL::NT) {
     const int fx = fi % nf0, fy = (fi / nf0) % nf1, fz = fi / (nf0 * nf1);
     const int i = o[0] + fx, j = o[1] + fy, k = o[2] + fz;
     const long long cR = (i - b.g2lo[0]) + (j - b.g2lo[1]) * stv[1] + (k - b.g2lo[2]) * stv[2];
@@ -468,37 +488,44 @@ __device__ __forceinline__ void dir_pass(const DevBox& b, const DevMech<NS>& m, 
     }
     if (diff) diffusion_face<NS, EOS, d>(b, f, g, cR, stv, F);
 #pragma unroll
-    for (int n = 0; n < NVAR; ++n) fbuf[n][fi] = F[n];
+    for (int n = 0; n < NVAR; ++n) fbuf[n * TL::MAXF + fi] = F[n];
   }
   __syncthreads();
   if (mine) {
     const int flo = tx + nf0 * (ty + nf1 * tz);
     const int fhi = flo + ((d == 0) ? 1 : (d == 1) ? nf0 : nf0 * nf1);
 #pragma unroll
-    for (int n = 0; n < NVAR; ++n) acc[n] += fbuf[n][flo] - fbuf[n][fhi];
+    for (int n = 0; n < NVAR; ++n) acc[n] += fbuf[n * TL::MAXF + flo] - fbuf[n * TL::MAXF + fhi];
   }
   __syncthreads();
 }
 
-template <int NS, class EOS>
-__global__ void __launch_bounds__(kFluxThreads, 2)
+template <int NS, class EOS, class TL = TileDefault>
+__global__ void __launch_bounds__(TL::NT, TL::MINB)
     flux_kernel(const DevBox* __restrict__ boxes, const int4* __restrict__ tiles, const __grid_constant__ DevMech<NS> m,
                 const DevFlags f, const Geo g, unsigned long long* __restrict__ counters) {
   constexpr int NVAR = 7 + NS;
-  __shared__ double fbuf[NVAR][kMaxFaces];
+  double* fbuf;
+  if constexpr (TL::DYN) {
+    extern __shared__ double flux_dyn_smem[];
+    fbuf = flux_dyn_smem;
+  } else {
+    __shared__ double flux_static_smem[NVAR * TL::MAXF];
+    fbuf = flux_static_smem;
+  }
   const int4 t = tiles[blockIdx.x];
   const DevBox& b = boxes[t.x];
   const int o[3] = {t.y, t.z, t.w};
-  const int ext[3] = {min(kTX, b.hi[0] - o[0] + 1), min(kTY, b.hi[1] - o[1] + 1), min(kTZ, b.hi[2] - o[2] + 1)};
-  const int tx = threadIdx.x % kTX, ty = (threadIdx.x / kTX) % kTY, tz = threadIdx.x / (kTX * kTY);
+  const int ext[3] = {min(TL::TX, b.hi[0] - o[0] + 1), min(TL::TY, b.hi[1] - o[1] + 1), min(TL::TZ, b.hi[2] - o[2] + 1)};
+  const int tx = threadIdx.x % TL::TX, ty = (threadIdx.x / TL::TX) % TL::TY, tz = threadIdx.x / (TL::TX * TL::TY);
   const bool mine = tx < ext[0] && ty < ext[1] && tz < ext[2];
   const long long stv[3] = {1, b.n2[0], (long long)b.n2[0] * b.n2[1]};
   double acc[NVAR];
 #pragma unroll
   for (int n = 0; n < NVAR; ++n) acc[n] = 0.0;
-  dir_pass<NS, EOS, 0>(b, m, f, g, o, ext, stv, mine, tx, ty, tz, fbuf, acc);
-  dir_pass<NS, EOS, 1>(b, m, f, g, o, ext, stv, mine, tx, ty, tz, fbuf, acc);
-  dir_pass<NS, EOS, 2>(b, m, f, g, o, ext, stv, mine, tx, ty, tz, fbuf, acc);
+  dir_pass<NS, EOS, 0, TL>(b, m, f, g, o, ext, stv, mine, tx, ty, tz, fbuf, acc);
+  dir_pass<NS, EOS, 1, TL>(b, m, f, g, o, ext, stv, mine, tx, ty, tz, fbuf, acc);
+  dir_pass<NS, EOS, 2, TL>(b, m, f, g, o, ext, stv, mine, tx, ty, tz, fbuf, acc);
   bool bad = false;
   if (mine) {
     const int i = o[0] + tx, j = o[1] + ty, k = o[2] + tz;

@@ -16,10 +16,11 @@
 // slopes, the Riemann star pressure and the pressure gradients only use
 // differences, the EOS calls add p_ref back, and the normal-momentum flux
 // drops the constant p_ref, whose divergence is zero on a uniform grid.
-// Records are FP32 except the mole fractions, kept in FP64 after the FP32
-// fields: diffusion is driven by their cell-to-cell differences, which in the
-// far field are ~1e-6 of X itself and would be lost in FP32; the differences
-// are taken in FP64 and rounded to FP32.  The internal energy of the Godunov
+// Records are FP32 except the mole fractions and the temperature, kept in
+// FP64 after the FP32 fields: diffusion is driven by their cell-to-cell
+// differences, which in the far field are ~1e-6 of X itself and would be lost
+// in FP32, and whose second differences (the conduction term of the energy
+// RHS) are ~1e-3 of T; the differences are taken in FP64 and rounded to FP32.  The internal energy of the Godunov
 // state is evaluated in FP64 (its formation-energy terms cancel to ~1e-2 of
 // their size, which FP32 cannot carry).
 #pragma once
@@ -69,7 +70,11 @@ __host__ MechF<NS> to_float(const DevMech<NS>& m, double p_ref) {
   return f;
 }
 
-// FP64 mole fractions stored after the FP32 fields of a mixed record.
+// FP64 mole fractions, then the FP64 temperature, stored after the FP32
+// fields of a mixed record.  Both enter the diffusion fluxes only through
+// differences between neighbouring cells, which FP32 values would resolve
+// to no better than 1e-4 K / 1e-7 (the flame's second differences of T are
+// a few K per cell).
 template <int NS>
 __device__ __forceinline__ double* mixed_x(const DevBox& b) {
   return reinterpret_cast<double*>(reinterpret_cast<float*>(b.rec) + (long long)Rec<NS>::N * b.ncell);
@@ -180,7 +185,6 @@ struct TransF {
           s[j] = fmaf(fmaxf(X[k], 1e-15f), invD, s[j]);
         }
       }
-#pragma unroll
       const float rw = mix_rwf<NS>(m, Y);
 #pragma unroll
       for (int k = 0; k < NS; ++k) out[k] = (s[k] > 0.f) ? rho * (1.f - Y[k]) * (rw / m.rW[k]) / s[k] : 0.f;
@@ -272,6 +276,7 @@ __global__ void __launch_bounds__(kCellThreads)
         xr[n * N] = x;
         X[n] = (float)x;
       }
+      xr[NS * N] = T;
       float out[NS + 3];
       TransF<NS, SIMPLE>::eval(mf, Tf, rhof, pf, Yf, X, out);
       r[RC::T * N] = Tf;
@@ -562,8 +567,9 @@ __device__ __forceinline__ void diffusion_face_f(const DevBox& b, const DevFlags
     else
       tau[a] = mu * (grad[d][a] + grad[a][d]);
   }
+  const float dT = (float)(__ldg(xrec + NS * N + cR) - __ldg(xrec + NS * N + cL));
   float fE = 0.5f * (-tau[0] * (uR[0] + uL[0]) - tau[1] * (uR[1] + uL[1]) - tau[2] * (uR[2] + uL[2])) -
-             lam * dxi * (ld(RC::T, cR) - ld(RC::T, cL));
+             lam * dxi * dT;
   const bool spec = f.diffuse_spec != 0;
   const bool ener = (f.diffuse_temp != 0) || (f.diffuse_enth != 0);
   {
@@ -598,16 +604,16 @@ __device__ __forceinline__ void diffusion_face_f(const DevBox& b, const DevFlags
   if (ener) F[UEDEN] += fE;
 }
 
-template <int NS, bool MIX, int d>
+template <int NS, bool MIX, int d, class TL>
 __device__ __forceinline__ void dir_pass_mixed(const DevBox& b, const MechF<NS>& m, const DevMech<NS>& md,
                                                const DevFlags& f, const Geo& g,
                                                const int o[3], const int ext[3], const long long stv[3], bool mine,
-                                               int tx, int ty, int tz, double (*fbuf)[kMaxFaces], double* acc) {
+                                               int tx, int ty, int tz, double* fbuf, double* acc) {
   constexpr int NVAR = 7 + NS;
   const bool diff = f.diffuse_vel || f.diffuse_temp || f.diffuse_spec || f.diffuse_enth;
   const int nf0 = ext[0] + (d == 0), nf1 = ext[1] + (d == 1), nf2 = ext[2] + (d == 2);
   const int nfaces = nf0 * nf1 * nf2;
-  for (int fi = threadIdx.x; fi < nfaces; fi += kFluxThreads) {
+  for (int fi = threadIdx.x; fi < nfaces; fi += TL::NT) {
     const int fx = fi % nf0, fy = (fi / nf0) % nf1, fz = fi / (nf0 * nf1);
     const int i = o[0] + fx, j = o[1] + fy, k = o[2] + fz;
     const long long cR = (i - b.g2lo[0]) + (j - b.g2lo[1]) * stv[1] + (k - b.g2lo[2]) * stv[2];
@@ -621,9 +627,9 @@ __device__ __forceinline__ void dir_pass_mixed(const DevBox& b, const MechF<NS>&
     }
     if (diff) diffusion_face_f<NS, d>(b, f, g, cR, stv, F);
 #pragma unroll
-    for (int n = 0; n < NVAR; ++n) fbuf[n][fi] = (double)F[n];  // exact widening
-    fbuf[UEDEN][fi] = FE + (double)F[UEDEN];
-    fbuf[UEINT][fi] = FEI;
+    for (int n = 0; n < NVAR; ++n) fbuf[n * TL::MAXF + fi] = (double)F[n];  // exact widening
+    fbuf[UEDEN * TL::MAXF + fi] = FE + (double)F[UEDEN];
+    fbuf[UEINT * TL::MAXF + fi] = FEI;
   }
   __syncthreads();
   if (mine) {
@@ -631,31 +637,38 @@ __device__ __forceinline__ void dir_pass_mixed(const DevBox& b, const MechF<NS>&
     const int fhi = flo + ((d == 0) ? 1 : (d == 1) ? nf0 : nf0 * nf1);
     const double s = g.dxinv[d];
 #pragma unroll
-    for (int n = 0; n < NVAR; ++n) acc[n] = fma(fbuf[n][flo] - fbuf[n][fhi], s, acc[n]);
+    for (int n = 0; n < NVAR; ++n) acc[n] = fma(fbuf[n * TL::MAXF + flo] - fbuf[n * TL::MAXF + fhi], s, acc[n]);
   }
   __syncthreads();
 }
 
-template <int NS, bool MIX>
-__global__ void __launch_bounds__(kFluxThreads, 2)
+template <int NS, bool MIX, class TL = TileDefault>
+__global__ void __launch_bounds__(TL::NT, TL::MINB)
     flux_kernel_mixed(const DevBox* __restrict__ boxes, const int4* __restrict__ tiles,
                       const __grid_constant__ MechF<NS> m, const __grid_constant__ DevMech<NS> md, const DevFlags f,
                       const Geo g, unsigned long long* __restrict__ counters) {
   constexpr int NVAR = 7 + NS;
-  __shared__ double fbuf[NVAR][kMaxFaces];
+  double* fbuf;
+  if constexpr (TL::DYN) {
+    extern __shared__ double flux_dyn_smem[];
+    fbuf = flux_dyn_smem;
+  } else {
+    __shared__ double flux_static_smem[NVAR * TL::MAXF];
+    fbuf = flux_static_smem;
+  }
   const int4 t = tiles[blockIdx.x];
   const DevBox& b = boxes[t.x];
   const int o[3] = {t.y, t.z, t.w};
-  const int ext[3] = {min(kTX, b.hi[0] - o[0] + 1), min(kTY, b.hi[1] - o[1] + 1), min(kTZ, b.hi[2] - o[2] + 1)};
-  const int tx = threadIdx.x % kTX, ty = (threadIdx.x / kTX) % kTY, tz = threadIdx.x / (kTX * kTY);
+  const int ext[3] = {min(TL::TX, b.hi[0] - o[0] + 1), min(TL::TY, b.hi[1] - o[1] + 1), min(TL::TZ, b.hi[2] - o[2] + 1)};
+  const int tx = threadIdx.x % TL::TX, ty = (threadIdx.x / TL::TX) % TL::TY, tz = threadIdx.x / (TL::TX * TL::TY);
   const bool mine = tx < ext[0] && ty < ext[1] && tz < ext[2];
   const long long stv[3] = {1, b.n2[0], (long long)b.n2[0] * b.n2[1]};
   double acc[NVAR];
 #pragma unroll
   for (int n = 0; n < NVAR; ++n) acc[n] = 0.0;
-  dir_pass_mixed<NS, MIX, 0>(b, m, md, f, g, o, ext, stv, mine, tx, ty, tz, fbuf, acc);
-  dir_pass_mixed<NS, MIX, 1>(b, m, md, f, g, o, ext, stv, mine, tx, ty, tz, fbuf, acc);
-  dir_pass_mixed<NS, MIX, 2>(b, m, md, f, g, o, ext, stv, mine, tx, ty, tz, fbuf, acc);
+  dir_pass_mixed<NS, MIX, 0, TL>(b, m, md, f, g, o, ext, stv, mine, tx, ty, tz, fbuf, acc);
+  dir_pass_mixed<NS, MIX, 1, TL>(b, m, md, f, g, o, ext, stv, mine, tx, ty, tz, fbuf, acc);
+  dir_pass_mixed<NS, MIX, 2, TL>(b, m, md, f, g, o, ext, stv, mine, tx, ty, tz, fbuf, acc);
   bool bad = false;
   if (mine) {
     const int i = o[0] + tx, j = o[1] + ty, k = o[2] + tz;

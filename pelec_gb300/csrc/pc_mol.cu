@@ -11,6 +11,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <new>
 #include <vector>
 
@@ -19,9 +20,12 @@
 #include "pelec_mol.h"
 
 namespace pcg {
-int launch_mixed(int variant, const DevBox* boxes, const int2* items, int nitems, const int4* tiles, int ntiles,
-                 const DevMech<1>& m1, const DevMech<9>& m9, const DevFlags& f, const Geo& g, double p_ref,
+int launch_mixed(int variant, int tile, const DevBox* boxes, const int2* items, int nitems, const int4* tiles,
+                 int ntiles, const DevMech<1>& m1, const DevMech<9>& m9, const DevFlags& f, const Geo& g, double p_ref,
                  unsigned long long* counters, cudaStream_t s, cudaEvent_t e0, cudaEvent_t e1, cudaEvent_t e2);
+cudaError_t launch_flux_fp64_tile(int tile, int variant, const DevBox* boxes, const int4* tiles, int ntiles,
+                                  const DevMech<1>& m1, const DevMech<9>& m9, const DevFlags& f, const Geo& g,
+                                  unsigned long long* counters, cudaStream_t s);
 }  // namespace pcg
 
 namespace {
@@ -50,7 +54,13 @@ struct pc_mol_handle {
   // layout cache
   std::vector<pc_box_desc> last_boxes;
   double last_dx[3] = {0, 0, 0};
+  int lay_tile = -1;  // tile shape the cached layout was built for
   Layout lay;
+  // flux-pass tile shape: forced by pc_mol_set_tile (>= 0), else looked up in
+  // the autotune cache by the BoxArray's box-size multiset, else 0
+  int tile_forced = -1;
+  int tile = 0;
+  std::map<std::vector<int>, int> tune_cache;
   DevBox* d_boxes = nullptr;
   size_t cap_boxes = 0;
   int2* d_items = nullptr;
@@ -155,7 +165,8 @@ int validate_box(const pc_box_desc& b, int nvar) {
   return PC_OK;
 }
 
-void build_layout(const pc_box_desc* boxes, int nboxes, int nrec, Layout& L) {
+void build_layout(const pc_box_desc* boxes, int nboxes, int nrec, int tile, Layout& L) {
+  const int TX = tile_extent(tile, 0), TY = tile_extent(tile, 1), TZ = tile_extent(tile, 2);
   L.boxes.clear();
   L.items.clear();
   L.tiles.clear();
@@ -189,9 +200,9 @@ void build_layout(const pc_box_desc* boxes, int nboxes, int nrec, Layout& L) {
     L.item_start.push_back((int)L.items.size());
     for (long long c = 0; c < d.ncell; c += kCellThreads) L.items.push_back(make_int2(bi, (int)c));
     L.tile_start.push_back((int)L.tiles.size());
-    for (int k = b.lo[2]; k <= b.hi[2]; k += kTZ)
-      for (int j = b.lo[1]; j <= b.hi[1]; j += kTY)
-        for (int i = b.lo[0]; i <= b.hi[0]; i += kTX) L.tiles.push_back(make_int4(bi, i, j, k));
+    for (int k = b.lo[2]; k <= b.hi[2]; k += TZ)
+      for (int j = b.lo[1]; j <= b.hi[1]; j += TY)
+        for (int i = b.lo[0]; i <= b.hi[0]; i += TX) L.tiles.push_back(make_int4(bi, i, j, k));
   }
   L.item_start.push_back((int)L.items.size());
   L.tile_start.push_back((int)L.tiles.size());
@@ -209,17 +220,46 @@ int ensure(pc_mol_handle* h, T*& ptr, size_t& cap, size_t n) {
   return PC_OK;
 }
 
+// Autotune key of a BoxArray: its multiset of box extents (the box-size
+// histogram); the handle fixes the species count and the precision.
+std::vector<int> tune_key(const pc_box_desc* boxes, int nboxes) {
+  std::vector<int> k;
+  k.reserve(3 * (size_t)nboxes);
+  std::vector<long long> ext(nboxes);
+  for (int b = 0; b < nboxes; ++b) {
+    long long e = 0;
+    for (int d = 2; d >= 0; --d) e = e * 8192 + (boxes[b].hi[d] - boxes[b].lo[d] + 1);
+    ext[b] = e;
+  }
+  std::sort(ext.begin(), ext.end());
+  for (long long e : ext) {
+    k.push_back((int)(e % 8192));
+    k.push_back((int)((e / 8192) % 8192));
+    k.push_back((int)(e / (8192LL * 8192)));
+  }
+  return k;
+}
+
+int choose_tile(pc_mol_handle* h, const pc_box_desc* boxes, int nboxes) {
+  if (h->tile_forced >= 0) return h->tile_forced;
+  if (h->tune_cache.empty()) return 0;
+  auto it = h->tune_cache.find(tune_key(boxes, nboxes));
+  return it == h->tune_cache.end() ? 0 : it->second;
+}
+
 int prepare(pc_mol_handle* h, const pc_box_desc* boxes, int nboxes, const double dx[3], cudaStream_t s) {
   const int nvar = 7 + h->cfg.nspec;
   for (int b = 0; b < nboxes; ++b) {
     int rc = validate_box(boxes[b], nvar);
     if (rc != PC_OK) return rc;
   }
-  const bool same = (int)h->last_boxes.size() == nboxes &&
-                    std::memcmp(h->last_boxes.data(), boxes, sizeof(pc_box_desc) * nboxes) == 0 &&
-                    h->last_dx[0] == dx[0] && h->last_dx[1] == dx[1] && h->last_dx[2] == dx[2];
-  if (same) return PC_OK;
-  build_layout(boxes, nboxes, h->nrec, h->lay);
+  const bool same_boxes = (int)h->last_boxes.size() == nboxes &&
+                          std::memcmp(h->last_boxes.data(), boxes, sizeof(pc_box_desc) * nboxes) == 0 &&
+                          h->last_dx[0] == dx[0] && h->last_dx[1] == dx[1] && h->last_dx[2] == dx[2];
+  if (!same_boxes) h->tile = choose_tile(h, boxes, nboxes);
+  if (same_boxes && h->lay_tile == h->tile) return PC_OK;
+  h->lay_tile = -1;
+  build_layout(boxes, nboxes, h->nrec, h->tile, h->lay);
   int rc = ensure(h, h->scratch, h->scratch_cap, h->lay.scratch_doubles);
   if (rc != PC_OK) return rc;
   for (auto& d : h->lay.boxes) d.rec = h->scratch + reinterpret_cast<size_t>(d.rec);
@@ -239,6 +279,7 @@ int prepare(pc_mol_handle* h, const pc_box_desc* boxes, int nboxes, const double
   if (e != cudaSuccess) return cuda_fail(h, e);
   h->last_boxes.assign(boxes, boxes + nboxes);
   for (int d = 0; d < 3; ++d) h->last_dx[d] = dx[d];
+  h->lay_tile = h->tile;
   return PC_OK;
 }
 
@@ -264,6 +305,13 @@ int launch(pc_mol_handle* h, const DevMech<NS>& mech, const Geo& g, int ibeg, in
     cell_kernel<NS, EOS, TR><<<iend - ibeg, kCellThreads, 0, s>>>(h->d_boxes, h->d_items + ibeg, mech, h->flags,
                                                                    h->d_counters);
   if (timed) cudaEventRecord(h->ev[1], s);
+  if (h->lay_tile != 0) {
+    const cudaError_t e = launch_flux_fp64_tile(h->lay_tile, h->variant, h->d_boxes, h->d_tiles + tbeg, tend - tbeg,
+                                                h->mech1, h->mech9, h->flags, g, h->d_counters, s);
+    if (timed) cudaEventRecord(h->ev[2], s);
+    if (e != cudaSuccess) return cuda_fail(h, e);
+    return cuda_fail(h, cudaGetLastError());
+  }
   if (tend > tbeg)
     flux_kernel<NS, EOS><<<tend - tbeg, kFluxThreads, 0, s>>>(h->d_boxes, h->d_tiles + tbeg, mech, h->flags, g,
                                                               h->d_counters);
@@ -295,7 +343,7 @@ int run(pc_mol_handle* h, const pc_box_desc* boxes, int nboxes, const double dx[
       const double p_ref = h->cfg.mixed_p_ref > 0.0 ? h->cfg.mixed_p_ref : 1013250.0;
       Geo gm = g;
       gm.p_ref = p_ref;
-      const int rc = launch_mixed(h->variant, h->d_boxes, h->d_items + ib, ie - ib, h->d_tiles + tb, te - tb,
+      const int rc = launch_mixed(h->variant, h->lay_tile, h->d_boxes, h->d_items + ib, ie - ib, h->d_tiles + tb, te - tb,
                                   h->mech1, h->mech9, h->flags, gm, p_ref, h->d_counters, s,
                                   timed ? h->ev[0] : nullptr, timed ? h->ev[1] : nullptr, timed ? h->ev[2] : nullptr);
       return rc == 0 ? PC_OK : cuda_fail(h, cudaGetLastError());
@@ -444,6 +492,69 @@ int pc_mol_pass_times(pc_mol_handle* h, double* ms, int n) {
   ms[0] = a;
   ms[1] = b;
   return PC_OK;
+}
+
+int pc_mol_tile_shape(int t, int shape[4]) {
+  if (t < 0 || t >= kNumTiles || !shape) return PC_ERR_INVALID_ARGUMENT;
+  shape[0] = tile_extent(t, 0);
+  shape[1] = tile_extent(t, 1);
+  shape[2] = tile_extent(t, 2);
+  shape[3] = shape[0] * shape[1] * shape[2];
+  return PC_OK;
+}
+
+int pc_mol_set_tile(pc_mol_handle* h, int t) {
+  if (!h || t < -1 || t >= kNumTiles) return PC_ERR_INVALID_ARGUMENT;
+  h->tile_forced = t;
+  h->last_boxes.clear();  // the next call chooses again
+  return PC_OK;
+}
+
+int pc_mol_current_tile(pc_mol_handle* h, int* t) {
+  if (!h || !t) return PC_ERR_INVALID_ARGUMENT;
+  *t = h->lay_tile >= 0 ? h->lay_tile : h->tile;
+  return PC_OK;
+}
+
+int pc_mol_autotune(pc_mol_handle* h, const pc_box_desc* boxes, int nboxes, const double dx[3], int reps, int* best,
+                    double* ms, int n_ms, void* stream) {
+  if (!h || !best || nboxes <= 0 || !boxes || reps <= 0) return PC_ERR_INVALID_ARGUMENT;
+  if (ms && n_ms < kNumTiles) return PC_ERR_INVALID_ARGUMENT;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  int rc = cuda_fail(h, cudaSetDevice(h->device));
+  if (rc != PC_OK) return rc;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+    if (e0) cudaEventDestroy(e0);
+    return h->last_error = PC_ERR_CUDA;
+  }
+  const int saved = h->tile_forced;
+  double tbest = 0.0;
+  int ibest = 0;
+  for (int t = 0; t < kNumTiles && rc == PC_OK; ++t) {
+    h->tile_forced = t;
+    rc = run(h, boxes, nboxes, dx, stream, false);  // warm-up, builds the layout of shape t
+    if (rc == PC_OK) rc = cuda_fail(h, cudaEventRecord(e0, s));
+    for (int r = 0; r < reps && rc == PC_OK; ++r) rc = run(h, boxes, nboxes, dx, stream, false);
+    if (rc == PC_OK) rc = cuda_fail(h, cudaEventRecord(e1, s));
+    if (rc == PC_OK) rc = cuda_fail(h, cudaEventSynchronize(e1));
+    float el = 0.f;
+    if (rc == PC_OK) rc = cuda_fail(h, cudaEventElapsedTime(&el, e0, e1));
+    const double per = (double)el / reps;
+    if (ms) ms[t] = per;
+    if (rc == PC_OK && (t == 0 || per < tbest)) {
+      tbest = per;
+      ibest = t;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  h->tile_forced = saved;
+  h->last_boxes.clear();
+  if (rc != PC_OK) return h->last_error = rc;
+  h->tune_cache[tune_key(boxes, nboxes)] = ibest;
+  *best = ibest;
+  return h->last_error = PC_OK;
 }
 
 }  // extern "C"
@@ -875,4 +986,84 @@ extern "C" int pc_mol_est_dt(pc_mol_handle* h, const pc_box_desc* boxes, int nbo
   eh *= cfl;
   *dt = std::min(max_dt, eh);
   return h->last_error = PC_OK;
+}
+
+// ---------------------------------------------------------------------------
+// CUDA graph of (ghost fill +) RHS.
+// ---------------------------------------------------------------------------
+struct pc_mol_graph {
+  pc_mol_handle* h = nullptr;  // private handle: its layout, scratch and counters belong to the graph
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+};
+
+extern "C" int pc_mol_graph_create(pc_mol_handle* parent, const pc_box_desc* boxes, int nboxes, const double dx[3],
+                                   const pc_geometry* fill_geom, int ngrow, pc_mol_graph** out) {
+  if (!parent || !out || nboxes <= 0 || !boxes || !dx) return PC_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  int rc = cuda_fail(parent, cudaSetDevice(parent->device));
+  if (rc != PC_OK) return rc;
+  // The captured kernels read the box table, tile list and record scratch of
+  // the handle they were launched through; a private handle keeps them alive
+  // and unchanged for the graph's lifetime whatever the caller's handle does.
+  pc_mol_config cfg = parent->cfg;
+  cfg.time_passes = 0;
+  pc_mol_graph* g = new (std::nothrow) pc_mol_graph();
+  if (!g) return parent->last_error = PC_ERR_OUT_OF_MEMORY;
+  rc = pc_mol_create(&g->h, &cfg);
+  if (rc != PC_OK) {
+    delete g;
+    return parent->last_error = rc;
+  }
+  pc_mol_handle* h = g->h;
+  h->tile_forced = parent->tile_forced;
+  h->tune_cache = parent->tune_cache;
+  cudaStream_t s = nullptr;
+  rc = cuda_fail(h, cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+  auto seq = [&]() -> int {
+    int r = PC_OK;
+    if (fill_geom) r = pc_mol_fill_ghosts(h, boxes, nboxes, fill_geom, ngrow, s);
+    if (r == PC_OK) r = run(h, boxes, nboxes, dx, s, false);
+    return r;
+  };
+  // One uncaptured pass performs every upload and allocation.
+  if (rc == PC_OK) rc = seq();
+  if (rc == PC_OK) rc = cuda_fail(h, cudaStreamSynchronize(s));
+  if (rc == PC_OK) rc = cuda_fail(h, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+  if (rc == PC_OK) {
+    const int r1 = seq();
+    const cudaError_t e = cudaStreamEndCapture(s, &g->graph);
+    rc = r1 != PC_OK ? r1 : cuda_fail(h, e);
+  }
+  if (rc == PC_OK) rc = cuda_fail(h, cudaGraphInstantiate(&g->exec, g->graph, 0));
+  if (s) cudaStreamDestroy(s);
+  if (rc != PC_OK) {
+    pc_mol_graph_destroy(g);
+    return parent->last_error = rc;
+  }
+  *out = g;
+  return PC_OK;
+}
+
+extern "C" int pc_mol_graph_launch(pc_mol_graph* g, void* stream) {
+  if (!g || !g->exec) return PC_ERR_INVALID_ARGUMENT;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  int rc = cuda_fail(g->h, cudaSetDevice(g->h->device));
+  if (rc != PC_OK) return rc;
+  g->h->last_stream = s;
+  return g->h->last_error = cuda_fail(g->h, cudaGraphLaunch(g->exec, s));
+}
+
+extern "C" int pc_mol_graph_status(pc_mol_graph* g, pc_mol_status* st) {
+  if (!g) return PC_ERR_INVALID_ARGUMENT;
+  return pc_mol_last_status(g->h, st);
+}
+
+extern "C" void pc_mol_graph_destroy(pc_mol_graph* g) {
+  if (!g) return;
+  if (g->h) cudaSetDevice(g->h->device);
+  if (g->exec) cudaGraphExecDestroy(g->exec);
+  if (g->graph) cudaGraphDestroy(g->graph);
+  pc_mol_destroy(g->h);
+  delete g;
 }

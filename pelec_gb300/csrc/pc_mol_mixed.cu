@@ -5,10 +5,30 @@
 
 namespace pcg {
 
-int launch_mixed(int variant, const DevBox* boxes, const int2* items, int nitems, const int4* tiles, int ntiles,
-                 const DevMech<1>& m1, const DevMech<9>& m9, const DevFlags& f, const Geo& g, double p_ref,
+cudaError_t launch_flux_mixed_tile(int tile, int variant, const DevBox* boxes, const int4* tiles, int ntiles,
+                                   const DevMech<1>& m1, const DevMech<9>& m9, const DevFlags& f, const Geo& g,
+                                   double p_ref, unsigned long long* counters, cudaStream_t s);
+
+// Cell pass, then the flux pass at tile shape `tile` (0 = 8x8x4, launched
+// here; the others in pc_tiles_mixed.cu).
+int launch_mixed(int variant, int tile, const DevBox* boxes, const int2* items, int nitems, const int4* tiles,
+                 int ntiles, const DevMech<1>& m1, const DevMech<9>& m9, const DevFlags& f, const Geo& g, double p_ref,
                  unsigned long long* counters, cudaStream_t s, cudaEvent_t e0, cudaEvent_t e1, cudaEvent_t e2) {
   if (e0) cudaEventRecord(e0, s);
+  if (tile != 0) {
+    if (nitems > 0) {
+      if (variant == 1)
+        cell_kernel_mixed<1, GammaLawEos<1>, false, false><<<nitems, kCellThreads, 0, s>>>(
+            boxes, items, m1, to_float(m1, p_ref), f, counters);
+      else
+        cell_kernel_mixed<9, IdealMixEos<9>, true, true><<<nitems, kCellThreads, 0, s>>>(
+            boxes, items, m9, to_float(m9, p_ref), f, counters);
+    }
+    if (e1) cudaEventRecord(e1, s);
+    const cudaError_t e = launch_flux_mixed_tile(tile, variant, boxes, tiles, ntiles, m1, m9, f, g, p_ref, counters, s);
+    if (e2) cudaEventRecord(e2, s);
+    return e == cudaSuccess && cudaGetLastError() == cudaSuccess ? 0 : 3;
+  }
   if (variant == 1) {
     const MechF<1> mf = to_float(m1, p_ref);
     if (nitems > 0)

@@ -1,0 +1,46 @@
+// pc_tiles_fp64.cu — the FP64 flux pass at the tile shapes other than the
+// default 8x8x4 (which pc_mol.cu launches itself).  Same arithmetic as
+// pc_mol.cu (compiled without multiply-add contraction): the tile shape only
+// changes which thread evaluates a face, never the operations on it, so every
+// shape gives bit-identical results.
+#include "pc_kernels.cuh"
+
+namespace pcg {
+
+namespace {
+
+template <int NS, class EOS, class TL>
+cudaError_t flux_at(const DevBox* boxes, const int4* tiles, int ntiles, const DevMech<NS>& m, const DevFlags& f,
+                    const Geo& g, unsigned long long* counters, cudaStream_t s) {
+  constexpr size_t smem = TL::DYN ? sizeof(double) * (7 + NS) * TL::MAXF : 0;
+  if (TL::DYN) {
+    const cudaError_t e =
+        cudaFuncSetAttribute(flux_kernel<NS, EOS, TL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
+  flux_kernel<NS, EOS, TL><<<ntiles, TL::NT, smem, s>>>(boxes, tiles, m, f, g, counters);
+  return cudaGetLastError();
+}
+
+template <int NS, class EOS>
+cudaError_t flux_tile(int tile, const DevBox* boxes, const int4* tiles, int ntiles, const DevMech<NS>& m,
+                      const DevFlags& f, const Geo& g, unsigned long long* counters, cudaStream_t s) {
+  switch (tile) {
+    case 1: return flux_at<NS, EOS, TileCube>(boxes, tiles, ntiles, m, f, g, counters, s);
+    case 2: return flux_at<NS, EOS, TileLong>(boxes, tiles, ntiles, m, f, g, counters, s);
+    case 3: return flux_at<NS, EOS, TileSmall>(boxes, tiles, ntiles, m, f, g, counters, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+}  // namespace
+
+cudaError_t launch_flux_fp64_tile(int tile, int variant, const DevBox* boxes, const int4* tiles, int ntiles,
+                                  const DevMech<1>& m1, const DevMech<9>& m9, const DevFlags& f, const Geo& g,
+                                  unsigned long long* counters, cudaStream_t s) {
+  if (ntiles <= 0) return cudaSuccess;
+  if (variant == 1) return flux_tile<1, GammaLawEos<1>>(tile, boxes, tiles, ntiles, m1, f, g, counters, s);
+  return flux_tile<9, IdealMixEos<9>>(tile, boxes, tiles, ntiles, m9, f, g, counters, s);
+}
+
+}  // namespace pcg

@@ -63,6 +63,24 @@ def library() -> ctypes.CDLL:
         lib.pc_mol_est_dt.argtypes = [c_void_p, POINTER(abi.PcBoxDesc), c_int, POINTER(c_double), c_double, c_double,
                                       POINTER(c_double), c_void_p]
         lib.pc_mol_est_dt.restype = c_int
+        lib.pc_mol_graph_create.argtypes = [c_void_p, POINTER(abi.PcBoxDesc), c_int, POINTER(c_double),
+                                            POINTER(abi.PcGeometry), c_int, POINTER(c_void_p)]
+        lib.pc_mol_graph_create.restype = c_int
+        lib.pc_mol_graph_launch.argtypes = [c_void_p, c_void_p]
+        lib.pc_mol_graph_launch.restype = c_int
+        lib.pc_mol_graph_destroy.argtypes = [c_void_p]
+        lib.pc_mol_graph_destroy.restype = None
+        lib.pc_mol_graph_status.argtypes = [c_void_p, POINTER(abi.PcMolStatus)]
+        lib.pc_mol_graph_status.restype = c_int
+        lib.pc_mol_tile_shape.argtypes = [c_int, POINTER(c_int)]
+        lib.pc_mol_tile_shape.restype = c_int
+        lib.pc_mol_set_tile.argtypes = [c_void_p, c_int]
+        lib.pc_mol_set_tile.restype = c_int
+        lib.pc_mol_current_tile.argtypes = [c_void_p, POINTER(c_int)]
+        lib.pc_mol_current_tile.restype = c_int
+        lib.pc_mol_autotune.argtypes = [c_void_p, POINTER(abi.PcBoxDesc), c_int, POINTER(c_double), c_int,
+                                        POINTER(c_int), POINTER(c_double), c_int, c_void_p]
+        lib.pc_mol_autotune.restype = c_int
         if lib.pc_mol_abi_version() != abi.PC_MOL_ABI_VERSION:
             raise RuntimeError("libpelec_mol.so ABI version does not match pelec_gb300.abi")
         _lib = lib
@@ -221,7 +239,74 @@ class MOLOperator:
                                        self._stream(stream)), "pc_mol_est_dt")
         return out.value
 
+    def graph(self, S: MultiFab, R: MultiFab, dx, geom: abi.PcGeometry | None = None,
+              ngrow: int | None = None) -> "LevelGraph":
+        """CUDA graph of (ghost fill +) RHS on fixed arrays; replay with .launch()."""
+        return LevelGraph(self, S, R, dx, geom, S.ngrow if ngrow is None else ngrow)
+
+    # ---- flux-pass tile shape ----
+    @staticmethod
+    def tile_shape(t: int):
+        """(tx, ty, tz, threads) of tile shape t."""
+        out = (c_int * 4)()
+        _check(library().pc_mol_tile_shape(int(t), out), "pc_mol_tile_shape")
+        return tuple(out)
+
+    def set_tile(self, t: int) -> None:
+        """Force tile shape t (-1: automatic, from the autotune cache)."""
+        _check(library().pc_mol_set_tile(self._h, int(t)), "pc_mol_set_tile")
+
+    def current_tile(self) -> int:
+        out = c_int(0)
+        _check(library().pc_mol_current_tile(self._h, ctypes.byref(out)), "pc_mol_current_tile")
+        return out.value
+
+    def autotune(self, S: MultiFab, R: MultiFab, dx, reps: int = 3, stream=None):
+        """Time every tile shape on this BoxArray, cache the fastest for its
+        box-size histogram; returns (best, [ms per call of each shape])."""
+        descs = self._box_descs(S, R)
+        dxa = (c_double * 3)(*[float(v) for v in dx])
+        best = c_int(0)
+        ms = (c_double * abi.PC_NUM_TILES)()
+        _check(library().pc_mol_autotune(self._h, descs, len(S), dxa, int(reps), ctypes.byref(best), ms,
+                                         abi.PC_NUM_TILES, self._stream(stream)), "pc_mol_autotune")
+        return best.value, list(ms)
+
     def status(self) -> abi.PcMolStatus:
         st = abi.PcMolStatus()
         _check(library().pc_mol_last_status(self._h, ctypes.byref(st)), "pc_mol_last_status")
         return st
+
+
+class LevelGraph:
+    """pc_mol_graph: one launch replays the captured ghost fill and RHS."""
+
+    def __init__(self, op: MOLOperator, S: MultiFab, R: MultiFab, dx, geom, ngrow: int):
+        self._op = op  # keeps the handle alive
+        self._keep = (S, R)
+        descs = abi.box_array([abi.box_desc(lo, hi, S.array4(b), R.array4(b)) for b, (lo, hi) in enumerate(S.boxes)])
+        dxa = (c_double * 3)(*[float(v) for v in dx])
+        g = c_void_p()
+        _check(library().pc_mol_graph_create(op._h, descs, len(S), dxa, ctypes.byref(geom) if geom is not None else None,
+                                             int(ngrow), ctypes.byref(g)), "pc_mol_graph_create")
+        self._g = g
+
+    def launch(self, stream=None) -> None:
+        _check(library().pc_mol_graph_launch(self._g, MOLOperator._stream(stream)), "pc_mol_graph_launch")
+
+    def status(self) -> abi.PcMolStatus:
+        """Counters of the last replay (synchronizes its stream)."""
+        st = abi.PcMolStatus()
+        _check(library().pc_mol_graph_status(self._g, ctypes.byref(st)), "pc_mol_graph_status")
+        return st
+
+    def close(self) -> None:
+        if getattr(self, "_g", None) and self._g.value:
+            library().pc_mol_graph_destroy(self._g)
+            self._g = c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,140 @@
+"""GPU tests of the batched-level machinery: every flux-pass tile shape gives
+the same RHS bit for bit (and the oracle's to 1e-12), the autotuner caches
+its choice per box-size histogram, and a captured CUDA graph of ghost fill +
+RHS replays to the direct calls' result.
+"""
+import numpy as np
+import pytest
+
+from conftest import rel_maxnorm
+from gpu_util import to_multifab
+from pelec_gb300 import abi, problems
+
+pytestmark = pytest.mark.gpu
+
+
+def _rhs_at_tile(mol, op, boxes, tile):
+    import torch
+
+    op.set_tile(tile)
+    S = to_multifab(mol, boxes, boxes[0].ng)
+    R = mol.MultiFab([(st.lo, st.hi) for st in boxes], boxes[0].S.shape[0], 0)
+    for t in R.fabs:
+        t.fill_(np.nan)
+    op.rhs_level(S, R, boxes[0].dx)
+    torch.cuda.synchronize()
+    assert op.current_tile() == tile
+    return [t.cpu().numpy() for t in R.fabs]
+
+
+def _ragged_level():
+    """Uneven boxes plus boxes smaller than every tile and with odd extents."""
+    mech, boxes = problems.level_boxes(nboxes=6, seed=31, edges=(8, 12, 16, 24))
+    _, big = problems.level_boxes(nboxes=3, seed=32, edges=(24,))
+    for st, shp in zip(big, [(1, 1, 1), (3, 5, 2), (17, 9, 5)]):
+        nx, ny, nz = shp
+        S = np.ascontiguousarray(st.S[:, : nz + 8, : ny + 8, : nx + 8])
+        lo = (st.lo[0] + 10000, 0, 0)  # disjoint from the first boxes
+        boxes.append(problems.BoxState(lo=lo, hi=tuple(l + n - 1 for l, n in zip(lo, shp)), S=S, dx=st.dx))
+    return mech, boxes
+
+
+@pytest.mark.parametrize("precision", [abi.PC_PRECISION_FP64, abi.PC_PRECISION_MIXED])
+def test_every_tile_shape_gives_identical_rhs(cuda_lib, oracle_lib, precision):
+    mol = cuda_lib
+    mech, boxes = _ragged_level()
+    cfg = problems.make_config(mech, precision=precision)
+    op = mol.MOLOperator(cfg)
+    outs = [_rhs_at_tile(mol, op, boxes, t) for t in range(abi.PC_NUM_TILES)]
+    for t in range(1, abi.PC_NUM_TILES):
+        for b, (g0, gt) in enumerate(zip(outs[0], outs[t])):
+            np.testing.assert_array_equal(gt, g0, err_msg=f"tile {t} box {b}")
+    if precision == abi.PC_PRECISION_FP64:
+        refs = oracle_lib.mol_rhs(cfg, boxes)
+        for g, r in zip(outs[2], refs):
+            assert rel_maxnorm(g, r).max() <= 1e-12
+
+
+def test_every_tile_shape_single_species(cuda_lib, oracle_lib):
+    mol = cuda_lib
+    mech, st = problems.tgv(20, seed=33)
+    cfg = problems.make_config(mech)
+    op = mol.MOLOperator(cfg)
+    outs = [_rhs_at_tile(mol, op, [st], t)[0] for t in range(abi.PC_NUM_TILES)]
+    for t in range(1, abi.PC_NUM_TILES):
+        np.testing.assert_array_equal(outs[t], outs[0])
+    ref, = oracle_lib.mol_rhs(cfg, [st])
+    assert rel_maxnorm(outs[3], ref).max() <= 1e-12
+
+
+def test_autotune_caches_choice_per_histogram(cuda_lib):
+    import torch
+
+    mol = cuda_lib
+    mech, boxes = _ragged_level()
+    cfg = problems.make_config(mech)
+    op = mol.MOLOperator(cfg)
+    S = to_multifab(mol, boxes, boxes[0].ng)
+    R = mol.MultiFab(S.boxes, S.ncomp, 0)
+    best, ms = op.autotune(S, R, boxes[0].dx, reps=2)
+    assert 0 <= best < abi.PC_NUM_TILES
+    assert all(m > 0 for m in ms) and ms[best] == min(ms)
+    ref = [t.clone() for t in R.fabs]
+    R2 = mol.MultiFab(S.boxes, S.ncomp, 0)
+    op.rhs_level(S, R2, boxes[0].dx)
+    torch.cuda.synchronize()
+    assert op.current_tile() == best  # looked up by the histogram
+    for a, b in zip(R2.fabs, ref):
+        assert torch.equal(a, b)
+    # a different BoxArray falls back to the default shape
+    op.rhs_level(to_multifab(mol, boxes[:2], 4), mol.MultiFab(S.boxes[:2], S.ncomp, 0), boxes[0].dx)
+    torch.cuda.synchronize()
+    assert op.current_tile() == 0
+
+
+def test_graph_replay_equals_direct_calls(cuda_lib):
+    """Graph of ghost fill + RHS on a 2x2x2 split periodic flame: the replay
+    equals fill_ghosts + rhs_level, reads the arrays' current contents on
+    every replay, and is not disturbed by later calls through the handle."""
+    import torch
+
+    from test_gpu_advance import _split
+
+    mol = cuda_lib
+    mech, st, _ = problems.flame((24, 16, 16), seed=34)
+    cfg = problems.make_config(mech)
+    geom = abi.geometry((0, 0, 0), (23, 15, 15), (0, 0, 0), (0, 0, 0))
+    boxes = _split(st, 2)
+    op = mol.MOLOperator(cfg)
+
+    def direct(S):
+        Sd = mol.MultiFab(S.boxes, S.ncomp, S.ngrow, fabs=[t.clone() for t in S.fabs])
+        R = mol.MultiFab(S.boxes, S.ncomp, 0)
+        op.fill_ghosts(Sd, geom)
+        op.rhs_level(Sd, R, st.dx)
+        torch.cuda.synchronize()
+        return R
+
+    S = to_multifab(mol, boxes, 4)
+    Rg = mol.MultiFab(S.boxes, S.ncomp, 0)
+    g = op.graph(S, Rg, st.dx, geom)
+    want = direct(S)
+    for t in Rg.fabs:
+        t.fill_(np.nan)
+    g.launch()
+    torch.cuda.synchronize()
+    for a, b in zip(Rg.fabs, want.fabs):
+        assert torch.equal(a, b)
+    assert g.status().cells == 24 * 16 * 16
+    # change the state in place, use the handle on another BoxArray, replay
+    for t in S.fabs:
+        t[abi.URHO] *= 1.001
+        t[abi.UEDEN] *= 1.001
+    other = to_multifab(mol, boxes[:1], 4)
+    op.rhs_level(other, mol.MultiFab(other.boxes, other.ncomp, 0), st.dx)
+    want2 = direct(S)
+    g.launch()
+    torch.cuda.synchronize()
+    for a, b in zip(Rg.fabs, want2.fabs):
+        assert torch.equal(a, b)
+    g.close()
