@@ -285,6 +285,33 @@ int pc_mol_graph_launch(pc_mol_graph* g, void* stream);
 int pc_mol_graph_status(pc_mol_graph* g, pc_mol_status* st);
 void pc_mol_graph_destroy(pc_mol_graph* g);
 
+/* Vector-Jacobian product of the RHS (reverse mode, hand-written):
+ *   state_bar = (d rhs / d state)^T rhs_bar
+ * for PC_PRECISION_FP64 with the Riemann solver of riemann() (use_laxf_flux
+ * = 0).  boxes as for pc_mol_rhs_level (their rhs arrays are not touched);
+ * rhs_bar[b] covers the valid box, state_bar[b] covers grow(valid, 2) and
+ * receives the cotangent of every state entry the RHS reads there (the
+ * ghost entries included; UEINT and UTEMP get 0: the RHS does not read
+ * UEINT, and UTEMP only as the Newton guess).  The EOS temperature solve is
+ * differentiated by the implicit-function theorem; at the kinks of the
+ * limiters and Riemann switches the derivative of the branch the forward
+ * pass took is used.  The reference has no adjoint; this is the entry point
+ * a differentiable getMOLSrcTerm would bind.  Asynchronous on stream. */
+int pc_mol_rhs_vjp(pc_mol_handle* h, const pc_box_desc* boxes, int nboxes, const double dx[3],
+                   const pc_array4* rhs_bar, pc_array4* state_bar, void* stream);
+
+/* Jacobian-vector product of the RHS (forward mode, dual numbers):
+ *   rhs_dot = (d rhs / d state) state_dot,
+ * and the RHS itself into boxes[b].rhs (bit for bit the pc_mol_rhs_level
+ * result).  PC_PRECISION_FP64 only.  state_dot[b] covers grow(valid, 2)
+ * (UEINT and UTEMP entries are ignored), rhs_dot[b] the valid box.  Uses
+ * the derivative of the branch the forward takes and the implicit-function
+ * theorem for the EOS temperature solve, like pc_mol_rhs_vjp, so
+ * <rhs_bar, JVP(v)> = <VJP(rhs_bar), v> to round-off.  No counterpart in the
+ * reference.  Asynchronous on stream. */
+int pc_mol_rhs_jvp(pc_mol_handle* h, const pc_box_desc* boxes, int nboxes, const double dx[3],
+                   const pc_array4* state_dot, pc_array4* rhs_dot, void* stream);
+
 /* PeleC::estTimeStep (PeleC.cpp:839-972, Timestep.H): min over valid cells
  * of dx/(c+|u|) (do_hydro) and the viscous, thermal and enthalpy diffusion
  * limits (diffuse_vel/temp/enth), times cfl, capped by max_dt.  Synchronous:

@@ -1,6 +1,6 @@
 """Build recipe of the CUDA library ``pelec_gb300/_lib/libpelec_mol.so``.
 
-Four translation units compiled by nvcc for sm_103a only (in parallel) and
+Six translation units compiled by nvcc for sm_103a only (in parallel) and
 linked into one shared library with a plain C ABI (include/pelec_mol.h), no
 torch headers:
 
@@ -12,6 +12,10 @@ torch headers:
 * pc_mol_mixed.cu — the mixed-precision kernels, with contraction on.
 * pc_tiles_fp64.cu / pc_tiles_mixed.cu — the flux pass of each precision at
   the tile shapes other than the default, compiled like the unit above them.
+* pc_adjoint.cu — the vector-Jacobian product passes, without contraction
+  (their re-evaluated forward quantities must be the forward's own).
+* pc_tangent.cu — the Jacobian-vector product (the forward passes on dual
+  numbers), without contraction for the same reason.
 
 libpc_peaks.so (pc_peaks.cu) measures the FP64/FP32 FMA rates that bench.py
 uses as roofline denominators.
@@ -30,7 +34,8 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler",
 
 LIBS = {
     "libpelec_mol.so": [("pc_mol.cu", ["-fmad=false"]), ("pc_mol_mixed.cu", ["-fmad=true"]),
-                        ("pc_tiles_fp64.cu", ["-fmad=false"]), ("pc_tiles_mixed.cu", ["-fmad=true"])],
+                        ("pc_tiles_fp64.cu", ["-fmad=false"]), ("pc_tiles_mixed.cu", ["-fmad=true"]),
+                        ("pc_adjoint.cu", ["-fmad=false"]), ("pc_tangent.cu", ["-fmad=false"])],
     # arithmetic peak rates for bench.py's roofline (not part of the ABI)
     "libpc_peaks.so": [("pc_peaks.cu", ["-fmad=true"])],
 }

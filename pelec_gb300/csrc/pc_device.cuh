@@ -74,22 +74,25 @@ __device__ __forceinline__ double div_by(double a, double b, double y) {
   return fma(r, y, q);
 }
 
-__device__ __forceinline__ double horner4(const double c[4], double L) {
+// The functions below are templates on the scalar type R: double for the
+// RHS, Dual (pc_dual.cuh) for its forward-mode tangent.
+template <class R>
+__device__ __forceinline__ R horner4(const double c[4], R L) {
   return fma(L, fma(L, fma(L, c[3], c[2]), c[1]), c[0]);
 }
 
 // R/Wbar = sum_k Y_k R/W_k.
-template <int NS>
-__device__ __forceinline__ double mix_rw(const DevMech<NS>& m, const double* Y) {
-  double s = 0.0;
+template <int NS, class R>
+__device__ __forceinline__ R mix_rw(const DevMech<NS>& m, const R* Y) {
+  R s = 0.0;
 #pragma unroll
   for (int k = 0; k < NS; ++k) s = fma(Y[k], m.rW[k], s);
   return s;
 }
 
 // Y2X: X_k = Y_k (R/W_k) / (R/Wbar).
-template <int NS>
-__device__ __forceinline__ void y2x(const DevMech<NS>& m, const double* Y, double rw, double* X) {
+template <int NS, class R>
+__device__ __forceinline__ void y2x(const DevMech<NS>& m, const R* Y, R rw, R* X) {
 #pragma unroll
   for (int k = 0; k < NS; ++k) X[k] = Y[k] * m.rW[k] / rw;
 }
@@ -101,24 +104,29 @@ template <int NS>
 struct GammaLawEos {
   static constexpr bool kIdealMix = false;
   // REY2T: T = e (gamma-1) / (R/Wbar).
-  __device__ static double rey2t(const DevMech<NS>& m, const double* /*Y*/, double rw, double e, double /*Tguess*/,
-                                 int /*maxit*/, bool& ok) {
+  template <class R>
+  __device__ static R rey2t(const DevMech<NS>& m, const R* /*Y*/, R rw, R e, double /*Tguess*/, int /*maxit*/,
+                            bool& ok) {
     ok = true;
     return e * m.gm1 / rw;
   }
   // RPY2Cs / RTY2Cs: c = sqrt(gamma p / rho).
-  __device__ static double cs_rp(const DevMech<NS>& m, const double*, double, double rho, double p) {
+  template <class R>
+  __device__ static R cs_rp(const DevMech<NS>& m, const R*, R, R rho, R p) {
     return sqrt(m.gamma * p / rho);
   }
-  __device__ static double cs_T(const DevMech<NS>& m, const double*, double, double rho, double /*T*/, double p) {
+  template <class R>
+  __device__ static R cs_T(const DevMech<NS>& m, const R*, R, R rho, R /*T*/, R p) {
     return sqrt(m.gamma * p / rho);
   }
   // RYP2E: e = p / ((gamma-1) rho).
-  __device__ static double e_rp(const DevMech<NS>& m, const double*, double, double rho, double p) {
+  template <class R>
+  __device__ static R e_rp(const DevMech<NS>& m, const R*, R, R rho, R p) {
     return p / (m.gm1 * rho);
   }
   // T2Hi: h_k = cp_k T.
-  __device__ static void hi(const DevMech<NS>& m, double T, double* h) {
+  template <class R>
+  __device__ static void hi(const DevMech<NS>& m, R T, R* h) {
 #pragma unroll
     for (int k = 0; k < NS; ++k) h[k] = m.cpk[k] * T;
   }
@@ -133,22 +141,27 @@ struct GammaLawEos {
 template <int NS>
 struct IdealMixEos {
   static constexpr bool kIdealMix = true;
-  __device__ static int range(const DevMech<NS>& m, double T) { return (T < m.tmid) ? 0 : 1; }
-  template <int NC = 6>
-  __device__ static void coefs(const DevMech<NS>& m, const double* Y, int r, double C[6]) {
+  template <class R>
+  __device__ static int range(const DevMech<NS>& m, R T) {
+    return (T < m.tmid) ? 0 : 1;
+  }
+  template <int NC = 6, class R>
+  __device__ static void coefs(const DevMech<NS>& m, const R* Y, int r, R C[6]) {
 #pragma unroll
     for (int n = 0; n < NC; ++n) {
-      double s = 0.0;
+      R s = 0.0;
 #pragma unroll
       for (int k = 0; k < NS; ++k) s = fma(Y[k], m.cpc[r][n][k], s);
       C[n] = s;
     }
   }
-  __device__ static double cv_of(const double C[6], double rw, double T) {
+  template <class R>
+  __device__ static R cv_of(const R C[6], R rw, R T) {
     return (C[0] - rw) + T * fma(T, fma(T, fma(T, C[4], C[3]), C[2]), C[1]);
   }
-  __device__ static double e_of(const double C[6], double rw, double T) {
-    const double p = fma(T, fma(T, fma(T, fma(T, C[4] * 0.2, C[3] * 0.25), C[2] * (1.0 / 3.0)), C[1] * 0.5), C[0] - rw);
+  template <class R>
+  __device__ static R e_of(const R C[6], R rw, R T) {
+    const R p = fma(T, fma(T, fma(T, fma(T, C[4] * 0.2, C[3] * 0.25), C[2] * (1.0 / 3.0)), C[1] * 0.5), C[0] - rw);
     return fma(T, p, C[5]);
   }
   // REY2T: Newton's method on e(T) = e from the guess U(UTEMP)
@@ -185,29 +198,33 @@ struct IdealMixEos {
     return t;
   }
   // c^2 = (cp/cv) p / rho, cp = cv + R/Wbar, at temperature T.
-  __device__ static double cs_T(const DevMech<NS>& m, const double* Y, double rw, double rho, double T, double p) {
-    double C[6];
+  template <class R>
+  __device__ static R cs_T(const DevMech<NS>& m, const R* Y, R rw, R rho, R T, R p) {
+    R C[6];
     coefs<5>(m, Y, range(m, T), C);
-    const double cv = cv_of(C, rw, T);
+    const R cv = cv_of(C, rw, T);
     return sqrt((cv + rw) * p / (cv * rho));
   }
   // RPY2Cs: T = p / (rho R/Wbar).
-  __device__ static double cs_rp(const DevMech<NS>& m, const double* Y, double rw, double rho, double p) {
+  template <class R>
+  __device__ static R cs_rp(const DevMech<NS>& m, const R* Y, R rw, R rho, R p) {
     return cs_T(m, Y, rw, rho, p / (rho * rw), p);
   }
   // RYP2E.
-  __device__ static double e_rp(const DevMech<NS>& m, const double* Y, double rw, double rho, double p) {
-    const double T = p / (rho * rw);
-    double C[6];
+  template <class R>
+  __device__ static R e_rp(const DevMech<NS>& m, const R* Y, R rw, R rho, R p) {
+    const R T = p / (rho * rw);
+    R C[6];
     coefs(m, Y, range(m, T), C);
     return e_of(C, rw, T);
   }
   // T2Hi: h_k = c5 + T (c0 + T (c1/2 + T (c2/3 + T (c3/4 + T c4/5)))), c = (R/W_k) a.
-  __device__ static void hi(const DevMech<NS>& m, double T, double* h) {
+  template <class R>
+  __device__ static void hi(const DevMech<NS>& m, R T, R* h) {
     const int r = range(m, T);
 #pragma unroll
     for (int k = 0; k < NS; ++k) {
-      const double p = fma(T, fma(T, fma(T, fma(T, m.cpc[r][4][k] * 0.2, m.cpc[r][3][k] * 0.25),
+      const R p = fma(T, fma(T, fma(T, fma(T, m.cpc[r][4][k] * 0.2, m.cpc[r][3][k] * 0.25),
                                            m.cpc[r][2][k] * (1.0 / 3.0)),
                                   m.cpc[r][1][k] * 0.5),
                            m.cpc[r][0][k]);
@@ -222,7 +239,8 @@ struct IdealMixEos {
 // ---------------------------------------------------------------------------
 template <int NS>
 struct ConstantTransport {
-  __device__ static void eval(const DevMech<NS>& m, double, double, double, const double*, const double*, double* out) {
+  template <class R>
+  __device__ static void eval(const DevMech<NS>& m, R, R, R, const R*, const R*, R* out) {
 #pragma unroll
     for (int k = 0; k < NS; ++k) out[k] = m.const_rhoD;
     out[NS] = m.const_mu;
@@ -238,58 +256,60 @@ struct ConstantTransport {
 // rhoD_k grad X_k), 1/D_kj(T,p) = exp(-fit_kj(ln T)) p / p_ref.
 template <int NS>
 struct SimpleTransport {
-  __device__ static void eval(const DevMech<NS>& m, double T, double rho, double p, const double* Y, const double* X,
-                              double* out) {
-    const double L = log(T);
-    double smu = 0.0, slam = 0.0, sxi = 0.0;
+  template <class R>
+  __device__ static void eval(const DevMech<NS>& m, R T, R rho, R p, const R* Y, const R* X, R* out) {
+    const R L = log(T);
+    R smu = 0.0, slam = 0.0, sxi = 0.0;
 #pragma unroll
     for (int k = 0; k < NS; ++k) {
-      const double mk = exp(horner4(m.visc[k], L));
-      const double m2 = mk * mk;
+      const R mk = exp(horner4(m.visc[k], L));
+      const R m2 = mk * mk;
       smu = fma(X[k], m2 * m2 * m2, smu);
       slam = fma(X[k], exp(0.25 * horner4(m.cond[k], L)), slam);
       sxi = fma(X[k], m.bulk[k] * mk, sxi);
     }
-    double s[NS];
+    R s[NS];
 #pragma unroll
     for (int k = 0; k < NS; ++k) s[k] = 0.0;
-    const double pr = p * m.inv_pref;
+    const R pr = p * m.inv_pref;
     int q = 0;
 #pragma unroll
     for (int k = 0; k < NS; ++k) {
 #pragma unroll
       for (int j = k + 1; j < NS; ++j, ++q) {
-        const double invD = exp(-horner4(m.diff[q], L)) * pr;
+        const R invD = exp(-horner4(m.diff[q], L)) * pr;
         s[k] = fma(fmax(X[j], 1e-15), invD, s[k]);
         s[j] = fma(fmax(X[k], 1e-15), invD, s[j]);
       }
     }
-    const double rw = mix_rw<NS>(m, Y);
+    const R rw = mix_rw<NS>(m, Y);
 #pragma unroll
     for (int k = 0; k < NS; ++k) {
-      const double wrat = rw / m.rW[k];  // W_k / Wbar
+      const R wrat = rw / m.rW[k];  // W_k / Wbar
       out[k] = (s[k] > 0.0) ? rho * (1.0 - Y[k]) * wrat / s[k] : 0.0;
     }
     out[NS] = exp(log(smu) * (1.0 / 6.0));
     out[NS + 1] = sxi;
-    const double l2 = slam * slam;
+    const R l2 = slam * slam;
     out[NS + 2] = l2 * l2;
   }
 };
 
 // pc_move_transcoefs_to_ec, Source/Utilities.H:322-342.
-__device__ __forceinline__ double face_coef(double a, double b, bool harmonic) {
+template <class R>
+__device__ __forceinline__ R face_coef(R a, R b, bool harmonic) {
   if (harmonic) {
-    const double ab = a * b;
+    const R ab = a * b;
     return (ab > 0.0) ? 2.0 * ab / (a + b) : 0.0;
   }
   return 0.5 * (a + b);
 }
 
 // MC-type limiter of mol_slope, Source/MOL.H:104-112.
-__device__ __forceinline__ double mc_limit(double dl, double dr) {
-  const double dcen = 0.5 * (dl + dr);
-  const double dlim = (dl * dr >= 0.0) ? 2.0 * fmin(fabs(dl), fabs(dr)) : 0.0;
+template <class R>
+__device__ __forceinline__ R mc_limit(R dl, R dr) {
+  const R dcen = 0.5 * (dl + dr);
+  const R dlim = (dl * dr >= 0.0) ? 2.0 * fmin(fabs(dl), fabs(dr)) : R(0.0);
   return copysign(1.0, dcen) * fmin(dlim, fabs(dcen));
 }
 

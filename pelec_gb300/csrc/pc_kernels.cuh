@@ -59,6 +59,32 @@ struct Rec {
   static constexpr int N = 10 + 4 * NS;
 };
 
+// Loads of record fields in the flux pass (a Dual specialisation reads
+// value and tangent records).
+template <class R>
+struct RecAcc;
+template <>
+struct RecAcc<double> {
+  const double* p;
+  long long N;
+  __device__ __forceinline__ double ld(int fld, long long c) const { return __ldg(p + (long long)fld * N + c); }
+};
+
+// Tangent arrays of one box for the Jacobian-vector product: the state
+// direction Sd (covering grow(valid, 2)), the RHS tangent Rd (valid box) and
+// the tangent records trec (same layout as rec).
+struct TanBox {
+  const double* Sd;
+  long long sj, sk, sn;
+  int sb[3];
+  int pad0;
+  double* Rd;
+  long long rj, rk, rn;
+  int rb[3];
+  int pad1;
+  double* trec;
+};
+
 enum { kCounterCells = 0, kCounterNewton = 1, kCounterNonpos = 2, kCounterNonfinite = 3, kNumCounters = 4 };
 
 __device__ __forceinline__ void warp_count(unsigned long long* ctr, bool pred) {
@@ -72,73 +98,104 @@ constexpr int kCellThreads = 256;
 // Pass 1.
 // items[b] = (box index, first cell of the 256-cell chunk in grow(valid,2)).
 // ---------------------------------------------------------------------------
+// The EOS temperature solve of the cell pass (a Dual overload differentiates
+// it by the implicit-function theorem).
+template <class EOS, int NS>
+__device__ __forceinline__ double rey2t_of(const DevMech<NS>& m, const double* Y, double rw, double e, double Tguess,
+                                           int maxit, bool& ok) {
+  return EOS::rey2t(m, Y, rw, e, Tguess, maxit, ok);
+}
+
+// pc_ctoprim and the per-cell diffusion data of one cell, generic in the
+// scalar type: U holds the conserved components, Tguess the Newton guess
+// U(UTEMP); st(field, value) writes a record field.  inner: the cell lies in
+// grow(valid, 1), where the diffusion fluxes need T, X, h and the transport
+// coefficients.
+template <int NS, class EOS, class TR, class R, class Store>
+__device__ __forceinline__ void cell_record(const DevMech<NS>& m, const DevFlags& f, const R* U, double Tguess,
+                                            bool inner, Store st, bool& newton_fail, bool& nonpos) {
+  using RC = Rec<NS>;
+  const R rho = U[URHO];
+  const R rhoinv = 1.0 / rho;
+  const R vx = U[UMX] * rhoinv;
+  const R vy = U[UMY] * rhoinv;
+  const R vz = U[UMZ] * rhoinv;
+  const R kineng = 0.5 * rho * (vx * vx + vy * vy + vz * vz);
+  const R e = (U[UEDEN] - kineng) * rhoinv;
+  R Y[NS];
+#pragma unroll
+  for (int n = 0; n < NS; ++n) {
+    R y = U[UFS + n] / rho;
+    if (-1e-4 * 2.220446049250313e-16 < y && y < 1e-4 * 2.220446049250313e-16) y = 0.0;
+    Y[n] = y;
+  }
+  const R rw = mix_rw<NS>(m, Y);
+  bool ok = true;
+  const R T = rey2t_of<EOS>(m, Y, rw, e, Tguess, f.newton_maxit, ok);
+  const R p = rho * rw * T;                      // RTY2P
+  const R cs = EOS::cs_T(m, Y, rw, rho, T, p);  // RTY2Cs
+  newton_fail = !ok;
+  nonpos = !(rho > 0.0) || !(p > 0.0) || !(T > 0.0);
+  st(RC::RHO, rho);
+  st(RC::U, vx);
+  st(RC::V, vy);
+  st(RC::W, vz);
+  st(RC::P, p);
+  st(RC::C, cs);
+#pragma unroll
+  for (int n = 0; n < NS; ++n) st(RC::Y + n, Y[n]);
+  if (inner) {
+    // Mole fractions (Y2X) and enthalpies (T2Hi) of the cell.
+    R X[NS];
+    y2x(m, Y, rw, X);
+    R out[NS + 3];
+    TR::eval(m, T, rho, p, Y, X, out);
+    st(RC::T, T);
+#pragma unroll
+    for (int n = 0; n < NS; ++n) st(RC::X + n, X[n]);
+    R h[NS];
+    EOS::hi(m, T, h);
+#pragma unroll
+    for (int n = 0; n < NS; ++n) st(RC::H + n, h[n]);
+#pragma unroll
+    for (int n = 0; n < NS + 3; ++n) st(RC::D + n, out[n]);
+  }
+}
+
+// Cell (i, j, k) of record index c in grow(valid, 2) of box b.
+__device__ __forceinline__ void cell_index(const DevBox& b, long long c, int& i, int& j, int& k) {
+  const int nx = b.n2[0], ny = b.n2[1];
+  i = b.g2lo[0] + (int)(c % nx);
+  j = b.g2lo[1] + (int)((c / nx) % ny);
+  k = b.g2lo[2] + (int)(c / ((long long)nx * ny));
+}
+
+__device__ __forceinline__ bool in_grow1(const DevBox& b, int i, int j, int k) {
+  return i >= b.lo[0] - 1 && i <= b.hi[0] + 1 && j >= b.lo[1] - 1 && j <= b.hi[1] + 1 && k >= b.lo[2] - 1 &&
+         k <= b.hi[2] + 1;
+}
+
 template <int NS, class EOS, class TR>
 __global__ void __launch_bounds__(kCellThreads)
     cell_kernel(const DevBox* __restrict__ boxes, const int2* __restrict__ items, const __grid_constant__ DevMech<NS> m,
                 const DevFlags f, unsigned long long* __restrict__ counters) {
-  using RC = Rec<NS>;
+  constexpr int NVAR = 7 + NS;
   const int2 it = items[blockIdx.x];
   const DevBox& b = boxes[it.x];
   const long long c = (long long)it.y + threadIdx.x;
-  const bool active = c < b.ncell;
   bool newton_fail = false, nonpos = false;
-  if (active) {
-    const int nx = b.n2[0], ny = b.n2[1];
-    const int i = b.g2lo[0] + (int)(c % nx);
-    const int j = b.g2lo[1] + (int)((c / nx) % ny);
-    const int k = b.g2lo[2] + (int)(c / ((long long)nx * ny));
+  if (c < b.ncell) {
+    int i, j, k;
+    cell_index(b, c, i, j, k);
     const double* s = b.S + (i - b.sb[0]) + (long long)(j - b.sb[1]) * b.sj + (long long)(k - b.sb[2]) * b.sk;
     const long long sn = b.sn;
-    // pc_ctoprim
-    const double rho = __ldg(s + URHO * sn);
-    const double rhoinv = 1.0 / rho;
-    const double vx = __ldg(s + UMX * sn) * rhoinv;
-    const double vy = __ldg(s + UMY * sn) * rhoinv;
-    const double vz = __ldg(s + UMZ * sn) * rhoinv;
-    const double kineng = 0.5 * rho * (vx * vx + vy * vy + vz * vz);
-    const double e = (__ldg(s + UEDEN * sn) - kineng) * rhoinv;
-    double Y[NS];
+    double U[NVAR];
 #pragma unroll
-    for (int n = 0; n < NS; ++n) {
-      double y = __ldg(s + (UFS + n) * sn) / rho;
-      if (-1e-4 * 2.220446049250313e-16 < y && y < 1e-4 * 2.220446049250313e-16) y = 0.0;
-      Y[n] = y;
-    }
-    const double rw = mix_rw<NS>(m, Y);
-    bool ok = true;
-    const double T = EOS::rey2t(m, Y, rw, e, __ldg(s + UTEMP * sn), f.newton_maxit, ok);
-    const double p = rho * rw * T;  // RTY2P
-    const double cs = EOS::cs_T(m, Y, rw, rho, T, p);  // RTY2Cs
-    newton_fail = !ok;
-    nonpos = !(rho > 0.0) || !(p > 0.0) || !(T > 0.0);
+    for (int n = 0; n < NVAR; ++n) U[n] = (n == UEINT || n == UTEMP) ? 0.0 : __ldg(s + n * sn);
     double* r = b.rec + c;
     const long long N = b.ncell;
-    r[RC::RHO * N] = rho;
-    r[RC::U * N] = vx;
-    r[RC::V * N] = vy;
-    r[RC::W * N] = vz;
-    r[RC::P * N] = p;
-    r[RC::C * N] = cs;
-#pragma unroll
-    for (int n = 0; n < NS; ++n) r[(RC::Y + n) * N] = Y[n];
-    const bool inner = i >= b.lo[0] - 1 && i <= b.hi[0] + 1 && j >= b.lo[1] - 1 && j <= b.hi[1] + 1 &&
-                       k >= b.lo[2] - 1 && k <= b.hi[2] + 1;
-    if (inner) {
-      // Mole fractions (Y2X) and enthalpies (T2Hi) of the cell.
-      double X[NS];
-      y2x(m, Y, rw, X);
-      double out[NS + 3];
-      TR::eval(m, T, rho, p, Y, X, out);
-      r[RC::T * N] = T;
-#pragma unroll
-      for (int n = 0; n < NS; ++n) r[(RC::X + n) * N] = X[n];
-      double h[NS];
-      EOS::hi(m, T, h);
-#pragma unroll
-      for (int n = 0; n < NS; ++n) r[(RC::H + n) * N] = h[n];
-#pragma unroll
-      for (int n = 0; n < NS + 3; ++n) r[(RC::D + n) * N] = out[n];
-    }
+    cell_record<NS, EOS, TR>(m, f, U, __ldg(s + UTEMP * sn), in_grow1(b, i, j, k),
+                             [&](int fld, double v) { r[fld * N] = v; }, newton_fail, nonpos);
   }
   warp_count(&counters[kCounterNewton], newton_fail);
   warp_count(&counters[kCounterNonpos], nonpos);
@@ -149,41 +206,39 @@ __global__ void __launch_bounds__(kCellThreads)
 // direction d, times the face area: F[n] = flux_n * A (Riemann.H, MOL.cpp).
 // Divisions that share a divisor use div_by (exact, see pc_device.cuh).
 // ---------------------------------------------------------------------------
-template <int NS, class EOS, int d>
-__device__ __forceinline__ void hydro_face(const DevBox& b, const DevMech<NS>& m, const DevFlags& f, long long cR,
-                                           long long st, double A, double* F) {
+template <int NS, class EOS, int d, class R>
+__device__ __forceinline__ void hydro_face(const RecAcc<R>& ra, const DevMech<NS>& m, const DevFlags& f, long long cR,
+                                           long long st, double A, R* F) {
   using RC = Rec<NS>;
-  const double* rec = b.rec;
-  const long long N = b.ncell;
   const long long cL = cR - st, cLL = cL - st, cRR = cR + st;
-  auto ld = [&](int fld, long long c) { return __ldg(rec + (long long)fld * N + c); };
+  auto ld = [&](int fld, long long c) { return ra.ld(fld, c); };
   const int fun = RC::U + d;
   const int fut1 = (d == 0) ? RC::V : RC::U;
   const int fut2 = (d == 2) ? RC::V : RC::W;
-  const double rLL = ld(RC::RHO, cLL), rL = ld(RC::RHO, cL), rR = ld(RC::RHO, cR), rRR = ld(RC::RHO, cRR);
-  const double pLL = ld(RC::P, cLL), pL = ld(RC::P, cL), pR = ld(RC::P, cR), pRR = ld(RC::P, cRR);
-  const double uLL = ld(fun, cLL), uL = ld(fun, cL), uR = ld(fun, cR), uRR = ld(fun, cRR);
-  const double cLc = ld(RC::C, cL), cRc = ld(RC::C, cR);
-  const double t1L = ld(fut1, cL), t1R = ld(fut1, cR), t2L = ld(fut2, cL), t2R = ld(fut2, cR);
-  const double ycL = 1.0 / cLc, ycR = 1.0 / cRc;
+  const R rLL = ld(RC::RHO, cLL), rL = ld(RC::RHO, cL), rR = ld(RC::RHO, cR), rRR = ld(RC::RHO, cRR);
+  const R pLL = ld(RC::P, cLL), pL = ld(RC::P, cL), pR = ld(RC::P, cR), pRR = ld(RC::P, cRR);
+  const R uLL = ld(fun, cLL), uL = ld(fun, cL), uR = ld(fun, cR), uRR = ld(fun, cRR);
+  const R cLc = ld(RC::C, cL), cRc = ld(RC::C, cR);
+  const R t1L = ld(fut1, cL), t1R = ld(fut1, cR), t2L = ld(fut2, cL), t2R = ld(fut2, cR);
+  const R ycL = 1.0 / cLc, ycR = 1.0 / cRc;
 
   // Characteristic slopes of cells L and R (mol_slope, MOL.H:53-112).
-  double dqL[4] = {0.0, 0.0, 0.0, 0.0}, dqR[4] = {0.0, 0.0, 0.0, 0.0};
+  R dqL[4] = {0.0, 0.0, 0.0, 0.0}, dqR[4] = {0.0, 0.0, 0.0, 0.0};
   const bool slopes = f.slopes != 0;
-  const double dpl = pL - pLL, dpc = pR - pL, dpr = pRR - pR;
+  const R dpl = pL - pLL, dpc = pR - pL, dpr = pRR - pR;
   if (slopes) {
-    const double t1LL = ld(fut1, cLL), t1RR = ld(fut1, cRR), t2LL = ld(fut2, cLL), t2RR = ld(fut2, cRR);
+    const R t1LL = ld(fut1, cLL), t1RR = ld(fut1, cRR), t2LL = ld(fut2, cLL), t2RR = ld(fut2, cRR);
     {
-      const double a = div_by(0.5 * dpl, cLc, ycL), bb = 0.5 * rL * (uL - uLL);
-      const double a2 = div_by(0.5 * dpc, cLc, ycL), b2 = 0.5 * rL * (uR - uL);
+      const R a = div_by(0.5 * dpl, cLc, ycL), bb = 0.5 * rL * (uL - uLL);
+      const R a2 = div_by(0.5 * dpc, cLc, ycL), b2 = 0.5 * rL * (uR - uL);
       dqL[0] = mc_limit(a - bb, a2 - b2);
       dqL[1] = mc_limit(a + bb, a2 + b2);
       dqL[2] = mc_limit(t1L - t1LL, t1R - t1L);
       dqL[3] = mc_limit(t2L - t2LL, t2R - t2L);
     }
     {
-      const double a = div_by(0.5 * dpc, cRc, ycR), bb = 0.5 * rR * (uR - uL);
-      const double a2 = div_by(0.5 * dpr, cRc, ycR), b2 = 0.5 * rR * (uRR - uR);
+      const R a = div_by(0.5 * dpc, cRc, ycR), bb = 0.5 * rR * (uR - uL);
+      const R a2 = div_by(0.5 * dpr, cRc, ycR), b2 = 0.5 * rR * (uRR - uR);
       dqR[0] = mc_limit(a - bb, a2 - b2);
       dqR[1] = mc_limit(a + bb, a2 + b2);
       dqR[2] = mc_limit(t1R - t1L, t1RR - t1R);
@@ -191,26 +246,26 @@ __device__ __forceinline__ void hydro_face(const DevBox& b, const DevMech<NS>& m
     }
   }
   // Face states (MOL.cpp:69-123).
-  const double unl = uL + 0.5 * ((dqL[1] - dqL[0]) / rL);
-  const double pl = pL + 0.5 * (dqL[0] + dqL[1]) * cLc;
-  const double ut1l = t1L + 0.5 * dqL[2];
-  const double ut2l = t2L + 0.5 * dqL[3];
-  const double unr = uR - 0.5 * ((dqR[1] - dqR[0]) / rR);
-  const double pr = pR - 0.5 * (dqR[0] + dqR[1]) * cRc;
-  const double ut1r = t1R - 0.5 * dqR[2];
-  const double ut2r = t2R - 0.5 * dqR[3];
-  double spl[NS], spr[NS];
-  double rl = 0.0, rr = 0.0;
+  const R unl = uL + 0.5 * ((dqL[1] - dqL[0]) / rL);
+  const R pl = pL + 0.5 * (dqL[0] + dqL[1]) * cLc;
+  const R ut1l = t1L + 0.5 * dqL[2];
+  const R ut2l = t2L + 0.5 * dqL[3];
+  const R unr = uR - 0.5 * ((dqR[1] - dqR[0]) / rR);
+  const R pr = pR - 0.5 * (dqR[0] + dqR[1]) * cRc;
+  const R ut1r = t1R - 0.5 * dqR[2];
+  const R ut2r = t2R - 0.5 * dqR[3];
+  R spl[NS], spr[NS];
+  R rl = 0.0, rr = 0.0;
   {
-    const double sL = dqL[0] + dqL[1], sR = dqR[0] + dqR[1];
-    const double cL2 = cLc * cLc, cR2 = cRc * cRc;
-    const double ycL2 = 1.0 / cL2, ycR2 = 1.0 / cR2;
+    const R sL = dqL[0] + dqL[1], sR = dqR[0] + dqR[1];
+    const R cL2 = cLc * cLc, cR2 = cRc * cRc;
+    const R ycL2 = 1.0 / cL2, ycR2 = 1.0 / cR2;
 #pragma unroll
     for (int n = 0; n < NS; ++n) {
-      const double yLL = ld(RC::Y + n, cLL), yL = ld(RC::Y + n, cL), yR = ld(RC::Y + n, cR), yRR = ld(RC::Y + n, cRR);
-      double dsL = 0.0, dsR = 0.0;
+      const R yLL = ld(RC::Y + n, cLL), yL = ld(RC::Y + n, cL), yR = ld(RC::Y + n, cR), yRR = ld(RC::Y + n, cRR);
+      R dsL = 0.0, dsR = 0.0;
       if (slopes) {
-        const double ryL = rL * yL, ryR = rR * yR;
+        const R ryL = rL * yL, ryR = rR * yR;
         dsL = mc_limit(ryL - rLL * yLL - div_by(yL * dpl, cL2, ycL2), ryR - ryL - div_by(yL * dpc, cL2, ycL2));
         dsR = mc_limit(ryR - ryL - div_by(yR * dpc, cR2, ycR2), rRR * yRR - ryR - div_by(yR * dpr, cR2, ycR2));
       }
@@ -219,122 +274,122 @@ __device__ __forceinline__ void hydro_face(const DevBox& b, const DevMech<NS>& m
       rl += spl[n];
       rr += spr[n];
     }
-    const double yrl = 1.0 / rl, yrr = 1.0 / rr;
+    const R yrl = 1.0 / rl, yrr = 1.0 / rr;
 #pragma unroll
     for (int n = 0; n < NS; ++n) {
       spl[n] = div_by(spl[n], rl, yrl);
       spr[n] = div_by(spr[n], rr, yrr);
     }
   }
-  const double cavg = 0.5 * (cRc + cLc);
-  double fl_rho, fl_un, fl_ut1, fl_ut2, fl_E, fl_ei;
-  double flY[NS];
-  const double rwl = mix_rw<NS>(m, spl), rwr = mix_rw<NS>(m, spr);
-  const double cl = EOS::cs_rp(m, spl, rwl, rl, pl);
-  const double cr = EOS::cs_rp(m, spr, rwr, rr, pr);
+  const R cavg = 0.5 * (cRc + cLc);
+  R fl_rho, fl_un, fl_ut1, fl_ut2, fl_E, fl_ei;
+  R flY[NS];
+  const R rwl = mix_rw<NS>(m, spl), rwr = mix_rw<NS>(m, spr);
+  const R cl = EOS::cs_rp(m, spl, rwl, rl, pl);
+  const R cr = EOS::cs_rp(m, spr, rwr, rr, pr);
   if (!f.laxf) {
     // riemann(), Source/Riemann.H:42-199.
     const double wsmall = 2.2250738585072014e-308;
-    const double wl = fmax(wsmall, cl * rl);
-    const double wr = fmax(wsmall, cr * rr);
-    const double ww = wl + wr, yww = 1.0 / ww;
-    const double pstar = fmax(wsmall, div_by((wr * pl + wl * pr) + wl * wr * (unl - unr), ww, yww));
-    double ustar = div_by((wl * unl + wr * unr) + (pl - pr), ww, yww);
+    const R wl = fmax(wsmall, cl * rl);
+    const R wr = fmax(wsmall, cr * rr);
+    const R ww = wl + wr, yww = 1.0 / ww;
+    const R pstar = fmax(wsmall, div_by((wr * pl + wl * pr) + wl * wr * (unl - unr), ww, yww));
+    R ustar = div_by((wl * unl + wr * unr) + (pl - pr), ww, yww);
     bool mask = ustar > 0.0;
-    double rspo[NS];
-    double uo = mask ? unl : unr;
-    double po = mask ? pl : pr;
+    R rspo[NS];
+    R uo = mask ? unl : unr;
+    R po = mask ? pl : pr;
     const bool m0 = fabs(ustar) < kSmallU * 0.5 * (fabs(unl) + fabs(unr)) || ustar == 0.0;
     ustar = m0 ? 0.0 : ustar;
-    double ro = 0.0;
+    R ro = 0.0;
 #pragma unroll
     for (int n = 0; n < NS; ++n) {
-      const double a = rl * spl[n], bq = rr * spr[n];
+      const R a = rl * spl[n], bq = rr * spr[n];
       rspo[n] = m0 ? 0.5 * (a + bq) : (mask ? a : bq);
       ro += rspo[n];
     }
     uo = m0 ? 0.5 * (unl + unr) : uo;
     po = m0 ? 0.5 * (pl + pr) : po;
-    double Yt[NS];
+    R Yt[NS];
     {
-      const double y = 1.0 / ro;
+      const R y = 1.0 / ro;
 #pragma unroll
       for (int n = 0; n < NS; ++n) Yt[n] = div_by(rspo[n], ro, y);
     }
-    const double co = EOS::cs_rp(m, Yt, mix_rw<NS>(m, Yt), ro, po);
-    const double drho = (pstar - po) / (co * co);
-    double rspstar[NS];
-    double rstar = 0.0;
+    const R co = EOS::cs_rp(m, Yt, mix_rw<NS>(m, Yt), ro, po);
+    const R drho = (pstar - po) / (co * co);
+    R rspstar[NS];
+    R rstar = 0.0;
 #pragma unroll
     for (int n = 0; n < NS; ++n) {
       rspstar[n] = fmax(0.0, rspo[n] + drho * Yt[n]);
       rstar += rspstar[n];
     }
     {
-      const double y = 1.0 / rstar;
+      const R y = 1.0 / rstar;
 #pragma unroll
       for (int n = 0; n < NS; ++n) Yt[n] = div_by(rspstar[n], rstar, y);
     }
-    const double cstar = EOS::cs_rp(m, Yt, mix_rw<NS>(m, Yt), rstar, pstar);
-    const double sgnm = copysign(1.0, ustar);
-    double spout = co - sgnm * uo;
-    double spin = cstar - sgnm * ustar;
-    const double ushock = 0.5 * (spin + spout);
+    const R cstar = EOS::cs_rp(m, Yt, mix_rw<NS>(m, Yt), rstar, pstar);
+    const R sgnm = copysign(1.0, ustar);
+    R spout = co - sgnm * uo;
+    R spin = cstar - sgnm * ustar;
+    const R ushock = 0.5 * (spin + spout);
     mask = pstar < po;
     spout = mask ? spout : ushock;
     spin = mask ? spin : ushock;
-    const double scr = (fabs(spout - spin) < PCG_VERY_SMALL_NUM) ? kSmallNum * cavg : spout - spin;
-    const double frac = fmax(0.0, fmin(1.0, (1.0 + (spout + spin) / scr) * 0.5));
+    const R scr = (fabs(spout - spin) < PCG_VERY_SMALL_NUM) ? kSmallNum * cavg : spout - spin;
+    const R frac = fmax(0.0, fmin(1.0, (1.0 + (spout + spin) / scr) * 0.5));
     mask = ustar > 0.0;
-    double iv1 = mask ? ut1l : ut1r;
-    double iv2 = mask ? ut2l : ut2r;
+    R iv1 = mask ? ut1l : ut1r;
+    R iv2 = mask ? ut2l : ut2r;
     mask = (ustar == 0.0);
     iv1 = mask ? 0.5 * (ut1l + ut1r) : iv1;
     iv2 = mask ? 0.5 * (ut2l + ut2r) : iv2;
     const bool mout = spout < 0.0, min_ = spin >= 0.0;
-    double iu = frac * ustar + (1.0 - frac) * uo;
-    double gdp = frac * pstar + (1.0 - frac) * po;
+    R iu = frac * ustar + (1.0 - frac) * uo;
+    R gdp = frac * pstar + (1.0 - frac) * po;
     iu = mout ? uo : iu;
     gdp = mout ? po : gdp;
     iu = min_ ? ustar : iu;
     gdp = min_ ? pstar : gdp;
-    double rgd = 0.0;
+    R rgd = 0.0;
 #pragma unroll
     for (int n = 0; n < NS; ++n) {
-      double g = frac * rspstar[n] + (1.0 - frac) * rspo[n];
+      R g = frac * rspstar[n] + (1.0 - frac) * rspo[n];
       g = mout ? rspo[n] : g;
       g = min_ ? rspstar[n] : g;
       flY[n] = g;
       rgd += g;
     }
     {
-      const double y = 1.0 / rgd;
+      const R y = 1.0 / rgd;
 #pragma unroll
       for (int n = 0; n < NS; ++n) Yt[n] = div_by(flY[n], rgd, y);
     }
-    const double regd = rgd * EOS::e_rp(m, Yt, mix_rw<NS>(m, Yt), rgd, gdp);
+    const R regd = rgd * EOS::e_rp(m, Yt, mix_rw<NS>(m, Yt), rgd, gdp);
     fl_rho = rgd * iu;
 #pragma unroll
     for (int n = 0; n < NS; ++n) flY[n] *= iu;
     fl_un = fl_rho * iu + gdp;
     fl_ut1 = fl_rho * iv1;
     fl_ut2 = fl_rho * iv2;
-    const double rhoetot = regd + 0.5 * rgd * (iu * iu + iv1 * iv1 + iv2 * iv2);
+    const R rhoetot = regd + 0.5 * rgd * (iu * iu + iv1 * iv1 + iv2 * iv2);
     fl_E = iu * (rhoetot + gdp);
     fl_ei = iu * regd;
   } else {
     // laxfriedrich_flux(), Source/Riemann.H:202-307.
-    const double el = EOS::e_rp(m, spl, rwl, rl, pl);
-    const double er = EOS::e_rp(m, spr, rwr, rr, pr);
-    const double r_elt = rl * (el + 0.5 * (unl * unl + ut1l * ut1l + ut2l * ut2l));
-    const double r_ert = rr * (er + 0.5 * (unr * unr + ut1r * ut1r + ut2r * ut2r));
+    const R el = EOS::e_rp(m, spl, rwl, rl, pl);
+    const R er = EOS::e_rp(m, spr, rwr, rr, pr);
+    const R r_elt = rl * (el + 0.5 * (unl * unl + ut1l * ut1l + ut2l * ut2l));
+    const R r_ert = rr * (er + 0.5 * (unr * unr + ut1r * ut1r + ut2r * ut2r));
     const double wsmall = 2.2250738585072014e-308;
-    const double wl = fmax(wsmall, cl * rl);
-    const double wr = fmax(wsmall, cr * rr);
-    double ustar = ((wl * unl + wr * unr) + (pl - pr)) / (wl + wr);
+    const R wl = fmax(wsmall, cl * rl);
+    const R wr = fmax(wsmall, cr * rr);
+    R ustar = ((wl * unl + wr * unr) + (pl - pr)) / (wl + wr);
     const bool m0 = fabs(ustar) < kSmallU * 0.5 * (fabs(unl) + fabs(unr)) || ustar == 0.0;
     ustar = m0 ? 0.0 : ustar;
-    const double mw = fabs(ustar) + 0.5 * (cr + cl);
+    const R mw = fabs(ustar) + 0.5 * (cr + cl);
     fl_rho = 0.0;
 #pragma unroll
     for (int n = 0; n < NS; ++n) {
@@ -363,22 +418,20 @@ __device__ __forceinline__ void hydro_face(const DevBox& b, const DevMech<NS>& m
 // the diffusion flux and adds the hyperbolic one, MOL.cpp:199-201; the sum of
 // two rounded terms does not depend on their order).  Components switched off
 // by the diffuse_* flags get no diffusion term (Diffusion.cpp:321-341).
-template <int NS, class EOS, int d>
-__device__ __forceinline__ void diffusion_face(const DevBox& b, const DevFlags& f, const Geo& g, long long cR,
-                                               const long long stv[3], double* F) {
+template <int NS, class EOS, int d, class R>
+__device__ __forceinline__ void diffusion_face(const RecAcc<R>& ra, const DevFlags& f, const Geo& g, long long cR,
+                                               const long long stv[3], R* F) {
   using RC = Rec<NS>;
-  const double* rec = b.rec;
-  const long long N = b.ncell;
-  auto ld = [&](int fld, long long c) { return __ldg(rec + (long long)fld * N + c); };
+  auto ld = [&](int fld, long long c) { return ra.ld(fld, c); };
   const long long cL = cR - stv[d];
   const bool harm = f.harmonic != 0;
-  const double mu = face_coef(ld(RC::MU, cR), ld(RC::MU, cL), harm);
-  const double xi = face_coef(ld(RC::XI, cR), ld(RC::XI, cL), harm);
-  const double lam = face_coef(ld(RC::LAM, cR), ld(RC::LAM, cL), harm);
+  const R mu = face_coef(ld(RC::MU, cR), ld(RC::MU, cL), harm);
+  const R xi = face_coef(ld(RC::XI, cR), ld(RC::XI, cL), harm);
+  const R lam = face_coef(ld(RC::LAM, cR), ld(RC::LAM, cL), harm);
   // Velocity gradients at the face.
-  double grad[3][3];  // grad[c][a] = d u_c / d x_a (only the entries used)
-  const double uR[3] = {ld(RC::U, cR), ld(RC::V, cR), ld(RC::W, cR)};
-  const double uL[3] = {ld(RC::U, cL), ld(RC::V, cL), ld(RC::W, cL)};
+  R grad[3][3];  // grad[c][a] = d u_c / d x_a (only the entries used)
+  const R uR[3] = {ld(RC::U, cR), ld(RC::V, cR), ld(RC::W, cR)};
+  const R uL[3] = {ld(RC::U, cL), ld(RC::V, cL), ld(RC::W, cL)};
 #pragma unroll
   for (int c = 0; c < 3; ++c) grad[c][d] = g.dxinv[d] * (uR[c] - uL[c]);
 #pragma unroll
@@ -391,8 +444,8 @@ __device__ __forceinline__ void diffusion_face(const DevBox& b, const DevFlags& 
     grad[a][a] = (ld(ca, cR + sa) + ld(ca, cL + sa) - ld(ca, cR - sa) - ld(ca, cL - sa)) * q4;
     grad[d][a] = (ld(cd, cR + sa) + ld(cd, cL + sa) - ld(cd, cR - sa) - ld(cd, cL - sa)) * q4;
   }
-  const double divu = grad[0][0] + grad[1][1] + grad[2][2];
-  double tau[3];
+  const R divu = grad[0][0] + grad[1][1] + grad[2][2];
+  R tau[3];
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
     if (a == d)
@@ -400,34 +453,34 @@ __device__ __forceinline__ void diffusion_face(const DevBox& b, const DevFlags& 
     else
       tau[a] = mu * (grad[d][a] + grad[a][d]);
   }
-  const double TR = ld(RC::T, cR), TL = ld(RC::T, cL);
-  const double dTdd = g.dxinv[d] * (TR - TL);
-  double fE = 0.5 * (-tau[0] * (uR[0] + uL[0]) - tau[1] * (uR[1] + uL[1]) - tau[2] * (uR[2] + uL[2])) - lam * dTdd;
+  const R TR = ld(RC::T, cR), TL = ld(RC::T, cL);
+  const R dTdd = g.dxinv[d] * (TR - TL);
+  R fE = 0.5 * (-tau[0] * (uR[0] + uL[0]) - tau[1] * (uR[1] + uL[1]) - tau[2] * (uR[2] + uL[2])) - lam * dTdd;
   const double A = g.area[d];
   const bool spec = f.diffuse_spec != 0;
   const bool ener = (f.diffuse_temp != 0) || (f.diffuse_enth != 0);
   if (NS > 1 || spec || ener) {
-    const double pR = ld(RC::P, cR), pL = ld(RC::P, cL);
-    const double dpdx = g.dxinv[d] * (pR - pL);
-    const double dlnp = dpdx / (0.5 * (pR + pL));
-    double Vd[NS], Yf[NS], hf[NS];
-    double Vc = 0.0;
+    const R pR = ld(RC::P, cR), pL = ld(RC::P, cL);
+    const R dpdx = g.dxinv[d] * (pR - pL);
+    const R dlnp = dpdx / (0.5 * (pR + pL));
+    R Vd[NS], Yf[NS], hf[NS];
+    R Vc = 0.0;
 #pragma unroll
     for (int n = 0; n < NS; ++n) {
-      const double x1 = ld(RC::X + n, cR), x2 = ld(RC::X + n, cL);
-      const double y1 = ld(RC::Y + n, cR), y2 = ld(RC::Y + n, cL);
-      const double Xface = 0.5 * (x1 + x2);
+      const R x1 = ld(RC::X + n, cR), x2 = ld(RC::X + n, cL);
+      const R y1 = ld(RC::Y + n, cR), y2 = ld(RC::Y + n, cL);
+      const R Xface = 0.5 * (x1 + x2);
       Yf[n] = 0.5 * (y1 + y2);
       hf[n] = 0.5 * (ld(RC::H + n, cR) + ld(RC::H + n, cL));
-      const double dXdx = g.dxinv[d] * (x1 - x2);
-      const double D = face_coef(ld(RC::D + n, cR), ld(RC::D + n, cL), harm);
+      const R dXdx = g.dxinv[d] * (x1 - x2);
+      const R D = face_coef(ld(RC::D + n, cR), ld(RC::D + n, cL), harm);
       Vd[n] = -D * (dXdx + (Xface - Yf[n]) * dlnp);
       Vc += Vd[n];
       fE += Vd[n] * hf[n];
     }
 #pragma unroll
     for (int n = 0; n < NS; ++n) {
-      const double v = Vd[n] - Yf[n] * Vc;
+      const R v = Vd[n] - Yf[n] * Vc;
       fE -= Yf[n] * hf[n] * Vc;
       if (spec) F[UFS + n] += v * A;
     }
@@ -481,12 +534,12 @@ __device__ __forceinline__ void dir_pass(const DevBox& b, const DevMech<NS>& m, 
     const long long cR = (i - b.g2lo[0]) + (j - b.g2lo[1]) * stv[1] + (k - b.g2lo[2]) * stv[2];
     double F[NVAR];
     if (f.do_hydro) {
-      hydro_face<NS, EOS, d>(b, m, f, cR, stv[d], g.area[d], F);
+      hydro_face<NS, EOS, d>(RecAcc<double>{b.rec, b.ncell}, m, f, cR, stv[d], g.area[d], F);
     } else {
 #pragma unroll
       for (int n = 0; n < NVAR; ++n) F[n] = 0.0;
     }
-    if (diff) diffusion_face<NS, EOS, d>(b, f, g, cR, stv, F);
+    if (diff) diffusion_face<NS, EOS, d>(RecAcc<double>{b.rec, b.ncell}, f, g, cR, stv, F);
 #pragma unroll
     for (int n = 0; n < NVAR; ++n) fbuf[n * TL::MAXF + fi] = F[n];
   }

@@ -15,6 +15,7 @@
 #include <new>
 #include <vector>
 
+#include "pc_adjoint.cuh"
 #include "pc_kernels.cuh"
 #include "pc_level.cuh"
 #include "pelec_mol.h"
@@ -26,6 +27,13 @@ int launch_mixed(int variant, int tile, const DevBox* boxes, const int2* items, 
 cudaError_t launch_flux_fp64_tile(int tile, int variant, const DevBox* boxes, const int4* tiles, int ntiles,
                                   const DevMech<1>& m1, const DevMech<9>& m9, const DevFlags& f, const Geo& g,
                                   unsigned long long* counters, cudaStream_t s);
+cudaError_t launch_vjp_passes(int variant, const DevBox* boxes, const AdjBox* adj, const int2* items, int nitems,
+                              const int4* fitems, int nfitems, double* recbar, const long long* recbar_off,
+                              const DevMech<1>& m1, const DevMech<9>& m9, const DevFlags& f, const Geo& g,
+                              cudaStream_t s);
+cudaError_t launch_jvp_passes(int variant, const DevBox* boxes, const TanBox* tans, const int2* items, int nitems,
+                              const int4* tiles, int ntiles, const DevMech<1>& m1, const DevMech<9>& m9,
+                              const DevFlags& f, const Geo& g, unsigned long long* counters, cudaStream_t s);
 }  // namespace pcg
 
 namespace {
@@ -79,8 +87,11 @@ struct pc_mol_handle {
     void* dev = nullptr;
     size_t cap = 0;
   };
-  Upload up[8];
+  Upload up[12];
   unsigned long long* d_dt = nullptr;  // 4 time-step minima
+  // adjoint: record cotangents, same layout as the records
+  double* recbar = nullptr;
+  size_t recbar_cap = 0;  // doubles
 };
 
 namespace {
@@ -256,7 +267,10 @@ int prepare(pc_mol_handle* h, const pc_box_desc* boxes, int nboxes, const double
   const bool same_boxes = (int)h->last_boxes.size() == nboxes &&
                           std::memcmp(h->last_boxes.data(), boxes, sizeof(pc_box_desc) * nboxes) == 0 &&
                           h->last_dx[0] == dx[0] && h->last_dx[1] == dx[1] && h->last_dx[2] == dx[2];
-  if (!same_boxes) h->tile = choose_tile(h, boxes, nboxes);
+  if (h->tile_forced >= 0)
+    h->tile = h->tile_forced;
+  else if (!same_boxes)
+    h->tile = choose_tile(h, boxes, nboxes);
   if (same_boxes && h->lay_tile == h->tile) return PC_OK;
   h->lay_tile = -1;
   build_layout(boxes, nboxes, h->nrec, h->tile, h->lay);
@@ -452,6 +466,7 @@ void pc_mol_destroy(pc_mol_handle* h) {
     if (e) cudaEventDestroy(e);
   for (auto& u : h->up) cudaFree(u.dev);
   cudaFree(h->d_dt);
+  cudaFree(h->recbar);
   delete h;
 }
 
@@ -733,7 +748,19 @@ extern "C" int pc_mol_rhs_box_static(const pc_mol_config* cfg, const pc_box_desc
 // ---------------------------------------------------------------------------
 namespace {
 
-enum { kUpFillBoxes = 0, kUpFillItems, kUpOwner, kUpLcDst, kUpLcX, kUpLcY, kUpItems, kUpBoxes };
+enum {
+  kUpFillBoxes = 0,
+  kUpFillItems,
+  kUpOwner,
+  kUpLcDst,
+  kUpLcX,
+  kUpLcY,
+  kUpItems,
+  kUpBoxes,
+  kUpAdjBoxes,
+  kUpAdjFaces,
+  kUpAdjOff
+};
 
 // Copies bytes to the handle's device slot unless they equal the last upload
 // of that slot (repeated calls on the same layout launch kernels only).
@@ -986,6 +1013,138 @@ extern "C" int pc_mol_est_dt(pc_mol_handle* h, const pc_box_desc* boxes, int nbo
   eh *= cfl;
   *dt = std::min(max_dt, eh);
   return h->last_error = PC_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Vector-Jacobian product of the RHS (pc_adjoint.cuh).
+// ---------------------------------------------------------------------------
+extern "C" int pc_mol_rhs_vjp(pc_mol_handle* h, const pc_box_desc* boxes, int nboxes, const double dx[3],
+                              const pc_array4* rhs_bar, pc_array4* state_bar, void* stream) {
+  if (!h) return PC_ERR_INVALID_ARGUMENT;
+  if (nboxes < 0 || (nboxes > 0 && (!boxes || !rhs_bar || !state_bar)) || !dx)
+    return h->last_error = PC_ERR_INVALID_ARGUMENT;
+  for (int d = 0; d < 3; ++d)
+    if (!(dx[d] > 0.0) || !std::isfinite(dx[d])) return h->last_error = PC_ERR_INVALID_ARGUMENT;
+  if (h->cfg.precision != PC_PRECISION_FP64 || h->flags.laxf) return h->last_error = PC_ERR_UNSUPPORTED;
+  const int nvar = 7 + h->cfg.nspec;
+  for (int b = 0; b < nboxes; ++b)
+    if (!array_ok(rhs_bar[b], boxes[b].lo, boxes[b].hi, 0, nvar) ||
+        !array_ok(state_bar[b], boxes[b].lo, boxes[b].hi, 2, nvar))
+      return h->last_error = PC_ERR_INVALID_ARGUMENT;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  int rc = cuda_fail(h, cudaSetDevice(h->device));
+  if (rc != PC_OK) return rc;
+  h->last_stream = s;
+  rc = cuda_fail(h, cudaMemsetAsync(h->d_counters, 0, sizeof(unsigned long long) * kNumCounters, s));
+  if (rc != PC_OK) return rc;
+  if (nboxes == 0) return h->last_error = PC_OK;
+  if ((rc = prepare(h, boxes, nboxes, dx, s)) != PC_OK) return h->last_error = rc;
+  const Layout& L = h->lay;
+  // per-box cotangent arrays, face chunks, record offsets
+  std::vector<AdjBox> adj(nboxes);
+  std::vector<int4> fitems;
+  std::vector<long long> off(nboxes);
+  for (int b = 0; b < nboxes; ++b) {
+    AdjBox& a = adj[b];
+    const pc_array4 &r = rhs_bar[b], &u = state_bar[b];
+    a.rbar = r.p;
+    a.rj = r.jstride;
+    a.rk = r.kstride;
+    a.rn = r.nstride;
+    a.ubar = u.p;
+    a.uj = u.jstride;
+    a.uk = u.kstride;
+    a.un = u.nstride;
+    for (int d = 0; d < 3; ++d) {
+      a.rb[d] = r.begin[d];
+      a.ub[d] = u.begin[d];
+    }
+    off[b] = (long long)(L.boxes[b].rec - h->scratch);
+    const int n0 = boxes[b].hi[0] - boxes[b].lo[0] + 1, n1 = boxes[b].hi[1] - boxes[b].lo[1] + 1,
+              n2 = boxes[b].hi[2] - boxes[b].lo[2] + 1;
+    for (int d = 0; d < 3; ++d) {
+      const long long nf = (long long)(n0 + (d == 0)) * (n1 + (d == 1)) * (n2 + (d == 2));
+      for (long long c = 0; c * kAdjThreads < nf; ++c) fitems.push_back(make_int4(b, d, (int)c, 0));
+    }
+  }
+  if ((rc = ensure(h, h->recbar, h->recbar_cap, L.scratch_doubles)) != PC_OK) return h->last_error = rc;
+  void *dadj = nullptr, *dfit = nullptr, *doff = nullptr;
+  if ((rc = upload(h, kUpAdjBoxes, adj.data(), adj.size() * sizeof(AdjBox), s, &dadj)) != PC_OK) return rc;
+  if ((rc = upload(h, kUpAdjFaces, fitems.data(), fitems.size() * sizeof(int4), s, &dfit)) != PC_OK) return rc;
+  if ((rc = upload(h, kUpAdjOff, off.data(), off.size() * sizeof(long long), s, &doff)) != PC_OK) return rc;
+  // pass 1: records of the forward state
+  const int nitems = (int)L.items.size();
+  if (h->variant == 1)
+    cell_kernel<1, GammaLawEos<1>, ConstantTransport<1>>
+        <<<nitems, kCellThreads, 0, s>>>(h->d_boxes, h->d_items, h->mech1, h->flags, h->d_counters);
+  else
+    cell_kernel<9, IdealMixEos<9>, SimpleTransport<9>>
+        <<<nitems, kCellThreads, 0, s>>>(h->d_boxes, h->d_items, h->mech9, h->flags, h->d_counters);
+  if ((rc = cuda_fail(h, cudaGetLastError())) != PC_OK) return rc;
+  if ((rc = cuda_fail(h, cudaMemsetAsync(h->recbar, 0, sizeof(double) * L.scratch_doubles, s))) != PC_OK) return rc;
+  const cudaError_t e = launch_vjp_passes(h->variant, h->d_boxes, static_cast<const AdjBox*>(dadj), h->d_items, nitems,
+                                          static_cast<const int4*>(dfit), (int)fitems.size(), h->recbar,
+                                          static_cast<const long long*>(doff), h->mech1, h->mech9, h->flags,
+                                          make_geo(dx), s);
+  return h->last_error = cuda_fail(h, e);
+}
+
+// ---------------------------------------------------------------------------
+// Jacobian-vector product of the RHS (pc_tangent.cuh).
+// ---------------------------------------------------------------------------
+extern "C" int pc_mol_rhs_jvp(pc_mol_handle* h, const pc_box_desc* boxes, int nboxes, const double dx[3],
+                              const pc_array4* state_dot, pc_array4* rhs_dot, void* stream) {
+  if (!h) return PC_ERR_INVALID_ARGUMENT;
+  if (nboxes < 0 || (nboxes > 0 && (!boxes || !state_dot || !rhs_dot)) || !dx)
+    return h->last_error = PC_ERR_INVALID_ARGUMENT;
+  for (int d = 0; d < 3; ++d)
+    if (!(dx[d] > 0.0) || !std::isfinite(dx[d])) return h->last_error = PC_ERR_INVALID_ARGUMENT;
+  if (h->cfg.precision != PC_PRECISION_FP64) return h->last_error = PC_ERR_UNSUPPORTED;
+  const int nvar = 7 + h->cfg.nspec;
+  for (int b = 0; b < nboxes; ++b)
+    if (!array_ok(state_dot[b], boxes[b].lo, boxes[b].hi, 2, nvar) ||
+        !array_ok(rhs_dot[b], boxes[b].lo, boxes[b].hi, 0, nvar))
+      return h->last_error = PC_ERR_INVALID_ARGUMENT;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  int rc = cuda_fail(h, cudaSetDevice(h->device));
+  if (rc != PC_OK) return rc;
+  h->last_stream = s;
+  rc = cuda_fail(h, cudaMemsetAsync(h->d_counters, 0, sizeof(unsigned long long) * kNumCounters, s));
+  if (rc != PC_OK) return rc;
+  if (nboxes == 0) return h->last_error = PC_OK;
+  // The tangent flux pass runs on 8x4x4 tiles.
+  const int saved_forced = h->tile_forced, saved_tile = h->tile;
+  h->tile_forced = 3;
+  rc = prepare(h, boxes, nboxes, dx, s);
+  h->tile_forced = saved_forced;
+  h->tile = (saved_forced >= 0 || rc != PC_OK) ? saved_tile : choose_tile(h, boxes, nboxes);
+  if (rc != PC_OK) return h->last_error = rc;
+  const Layout& L = h->lay;
+  if ((rc = ensure(h, h->recbar, h->recbar_cap, L.scratch_doubles)) != PC_OK) return h->last_error = rc;
+  std::vector<TanBox> tan(nboxes);
+  for (int b = 0; b < nboxes; ++b) {
+    TanBox& t = tan[b];
+    const pc_array4 &sd = state_dot[b], &rd = rhs_dot[b];
+    t.Sd = sd.p;
+    t.sj = sd.jstride;
+    t.sk = sd.kstride;
+    t.sn = sd.nstride;
+    t.Rd = rd.p;
+    t.rj = rd.jstride;
+    t.rk = rd.kstride;
+    t.rn = rd.nstride;
+    for (int d = 0; d < 3; ++d) {
+      t.sb[d] = sd.begin[d];
+      t.rb[d] = rd.begin[d];
+    }
+    t.trec = h->recbar + (L.boxes[b].rec - h->scratch);
+  }
+  void* dtan = nullptr;
+  if ((rc = upload(h, kUpAdjBoxes, tan.data(), tan.size() * sizeof(TanBox), s, &dtan)) != PC_OK) return rc;
+  const cudaError_t e = launch_jvp_passes(h->variant, h->d_boxes, static_cast<const TanBox*>(dtan), h->d_items,
+                                          (int)L.items.size(), h->d_tiles, (int)L.tiles.size(), h->mech1, h->mech9,
+                                          h->flags, make_geo(dx), h->d_counters, s);
+  return h->last_error = cuda_fail(h, e);
 }
 
 // ---------------------------------------------------------------------------

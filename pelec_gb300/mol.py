@@ -81,6 +81,12 @@ def library() -> ctypes.CDLL:
         lib.pc_mol_autotune.argtypes = [c_void_p, POINTER(abi.PcBoxDesc), c_int, POINTER(c_double), c_int,
                                         POINTER(c_int), POINTER(c_double), c_int, c_void_p]
         lib.pc_mol_autotune.restype = c_int
+        lib.pc_mol_rhs_vjp.argtypes = [c_void_p, POINTER(abi.PcBoxDesc), c_int, POINTER(c_double),
+                                       POINTER(abi.PcArray4), POINTER(abi.PcArray4), c_void_p]
+        lib.pc_mol_rhs_vjp.restype = c_int
+        lib.pc_mol_rhs_jvp.argtypes = [c_void_p, POINTER(abi.PcBoxDesc), c_int, POINTER(c_double),
+                                       POINTER(abi.PcArray4), POINTER(abi.PcArray4), c_void_p]
+        lib.pc_mol_rhs_jvp.restype = c_int
         if lib.pc_mol_abi_version() != abi.PC_MOL_ABI_VERSION:
             raise RuntimeError("libpelec_mol.so ABI version does not match pelec_gb300.abi")
         _lib = lib
@@ -243,6 +249,27 @@ class MOLOperator:
               ngrow: int | None = None) -> "LevelGraph":
         """CUDA graph of (ghost fill +) RHS on fixed arrays; replay with .launch()."""
         return LevelGraph(self, S, R, dx, geom, S.ngrow if ngrow is None else ngrow)
+
+    # ---- derivatives ----
+    def rhs_vjp(self, S: MultiFab, rhs_bar: MultiFab, state_bar: MultiFab, dx, stream=None) -> None:
+        """state_bar = (d RHS / d S)^T rhs_bar on grow(valid, 2) (pc_mol_rhs_vjp).
+        rhs_bar has S's BoxArray (valid region); state_bar needs >= 2 ghosts."""
+        if state_bar.ngrow < 2:
+            raise ValueError("state_bar needs at least 2 ghost cells")
+        descs = self._box_descs(S, rhs_bar)
+        dxa = (c_double * 3)(*[float(v) for v in dx])
+        _check(library().pc_mol_rhs_vjp(self._h, descs, len(S), dxa, self._arrays(rhs_bar), self._arrays(state_bar),
+                                        self._stream(stream)), "pc_mol_rhs_vjp")
+
+    def rhs_jvp(self, S: MultiFab, state_dot: MultiFab, R: MultiFab, rhs_dot: MultiFab, dx, stream=None) -> None:
+        """R = RHS(S) and rhs_dot = (d RHS / d S) state_dot (pc_mol_rhs_jvp).
+        state_dot needs >= 2 ghosts; R and rhs_dot have S's BoxArray."""
+        if state_dot.ngrow < 2:
+            raise ValueError("state_dot needs at least 2 ghost cells")
+        descs = self._box_descs(S, R)
+        dxa = (c_double * 3)(*[float(v) for v in dx])
+        _check(library().pc_mol_rhs_jvp(self._h, descs, len(S), dxa, self._arrays(state_dot), self._arrays(rhs_dot),
+                                        self._stream(stream)), "pc_mol_rhs_jvp")
 
     # ---- flux-pass tile shape ----
     @staticmethod

@@ -182,8 +182,9 @@ def wrinkle(fp: FlameParams, x, y):
     return a
 
 
-def flame_primitives(mech: Mechanism, fp: FlameParams, X, Yc, Z, rng):
-    """Primitive flame fields at cell centres (X, Yc, Z), with seeded noise."""
+def flame_primitives(mech: Mechanism, fp: FlameParams, X, Yc, Z, rng, w_noise: float = 0.0):
+    """Primitive flame fields at cell centres (X, Yc, Z), with seeded noise.
+    w_noise > 0 adds seeded Gaussian noise of that std (cm/s) to w as well."""
     s = 0.5 * (1.0 + np.tanh((Z - fp.z0 - wrinkle(fp, X, Yc)) / fp.delta))
     T = 300.0 + 1700.0 * s
     yu, yb = _h2air_endpoints(mech, fp.phi)
@@ -197,12 +198,19 @@ def flame_primitives(mech: Mechanism, fp: FlameParams, X, Yc, Z, rng):
     u = rng.normal(0.0, 1.0, T.shape)
     v = rng.normal(0.0, 1.0, T.shape)
     w = np.full(T.shape, 100.0)
+    if w_noise > 0.0:
+        w = w + rng.normal(0.0, w_noise, T.shape)
     return rho, u, v, w, T, Y
 
 
 def flame(shape=(128, 128, 128), dx: float = 1e-3, seed: int = 1, mech: Mechanism | None = None,
-          params: FlameParams | None = None) -> tuple:
-    """Flame box with periodic x/y ghosts and first-order-extrapolated z ghosts."""
+          params: FlameParams | None = None, w_noise: float = 0.0) -> tuple:
+    """Flame box with periodic x/y ghosts and first-order-extrapolated z ghosts.
+
+    With the default w_noise = 0 the pressure and w are exactly uniform, so
+    the MOL limiter's acoustic slopes and the slopes of w sit exactly at the
+    limiter's non-differentiable point mc(0, 0); derivative checks against
+    finite differences use w_noise > 0."""
     mech = mech or h2_air_synthetic()
     nx, ny, nz = shape
     Lx, Ly, Lz = nx * dx, ny * dx, nz * dx
@@ -212,7 +220,7 @@ def flame(shape=(128, 128, 128), dx: float = 1e-3, seed: int = 1, mech: Mechanis
     y = (np.arange(ny) + 0.5) * dx
     z = (np.arange(nz) + 0.5) * dx
     Z, Yc, X = np.meshgrid(z, y, x, indexing="ij")
-    prims = flame_primitives(mech, fp, X, Yc, Z, rng)
+    prims = flame_primitives(mech, fp, X, Yc, Z, rng, w_noise)
     Sv = conserved(mech, *prims)
     S = np.zeros((Sv.shape[0], nz + 2 * NG, ny + 2 * NG, nx + 2 * NG))
     S[:, NG:-NG, NG:-NG, NG:-NG] = Sv

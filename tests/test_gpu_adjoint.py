@@ -1,0 +1,189 @@
+"""GPU tests of the hand-written adjoint of the RHS (pc_mol_rhs_vjp) against
+central finite differences of the oracle's RHS: for a seeded cotangent mu and
+direction v, <VJP(mu), v> must equal d/dh <mu, RHS(U + h v)>."""
+import numpy as np
+import pytest
+
+from gpu_util import to_multifab
+from pelec_gb300 import abi, problems
+
+pytestmark = pytest.mark.gpu
+
+# relative agreement of the adjoint with central differences of the oracle
+FD_REL = 2e-6
+
+
+def _case(kind):
+    # w noise keeps the limiter away from its kink at mc(0, 0) (uniform p and
+    # w), where no linear derivative matches finite differences.
+    if kind == "flame":
+        mech, st, _ = problems.flame((12, 10, 8), seed=61, w_noise=1.0)
+    elif kind == "flame_noslope":
+        mech, st, _ = problems.flame((10, 8, 12), seed=63, w_noise=1.0)
+    else:
+        mech, st = problems.tgv(12, seed=62)
+    cfg = problems.make_config(mech, plm_iorder=1 if kind == "flame_noslope" else 4)
+    return mech, st, cfg
+
+
+def _vjp(mol, cfg, st, mu):
+    import torch
+
+    op = mol.MOLOperator(cfg)
+    S = to_multifab(mol, [st], st.ng)
+    Rb = mol.MultiFab(S.boxes, S.ncomp, 0, fabs=[torch.from_numpy(np.ascontiguousarray(mu)).cuda()])
+    Ub = mol.MultiFab(S.boxes, S.ncomp, 2)
+    for t in Ub.fabs:
+        t.fill_(np.nan)  # every entry of grow(valid, 2) must be written
+    op.rhs_vjp(S, Rb, Ub, st.dx)
+    torch.cuda.synchronize()
+    return Ub.fabs[0].cpu().numpy()
+
+
+def _direction(st, rng):
+    """Seeded direction on grow(valid, 2), scaled per component by its RMS."""
+    g = st.S[:, 2:-2, 2:-2, 2:-2]
+    v = rng.normal(size=g.shape)
+    scale = np.sqrt((g ** 2).mean(axis=(1, 2, 3)))
+    v *= scale[:, None, None, None]
+    v[abi.UEINT] = 0.0
+    v[abi.UTEMP] = 0.0
+    return v
+
+
+def _scale_direction(st, rng):
+    """Seeded direction that keeps the forward away from its kinks: each
+    conserved component is scaled by its own random factor, v_n = s_n U_n.
+    The MOL limiter is positively homogeneous, so a componentwise scaling
+    moves its arguments almost proportionally and crosses a min/max switch
+    only where two arguments agree to within the step; exact zeros stay zero
+    and extrapolated ghost layers stay copies of their boundary cell.
+    Returned on grow(valid, 2)."""
+    s = rng.normal(size=st.S.shape[0])
+    s[abi.UEINT] = 0.0
+    s[abi.UTEMP] = 0.0
+    return np.ascontiguousarray(s[:, None, None, None] * st.S[:, 2:-2, 2:-2, 2:-2])
+
+
+def _fd(oracle_lib, cfg, st, mu, v, h):
+    def J(sign):
+        S = st.S.copy()
+        S[:, 2:-2, 2:-2, 2:-2] += sign * h * v
+        R, = oracle_lib.mol_rhs(cfg, [problems.BoxState(st.lo, st.hi, S, st.dx)])
+        return float((mu * R).sum())
+
+    return (J(1.0) - J(-1.0)) / (2.0 * h)
+
+
+@pytest.mark.parametrize("kind", ["tgv", "flame", "flame_noslope"])
+def test_vjp_matches_oracle_finite_differences(cuda_lib, oracle_lib, kind):
+    """<VJP(mu), v> against central differences of <mu, RHS(U + h v)>
+    computed by the oracle, along smooth relative directions."""
+    mech, st, cfg = _case(kind)
+    rng = np.random.default_rng(7)
+    nx, ny, nz = st.shape
+    mu = rng.normal(size=(st.S.shape[0], nz, ny, nx))
+    Ub = _vjp(cuda_lib, cfg, st, mu)
+    assert np.all(np.isfinite(Ub))
+    assert not Ub[abi.UEINT].any() and not Ub[abi.UTEMP].any()
+    for trial in range(3):
+        v = _scale_direction(st, rng)
+        ad = float((Ub * v).sum())
+        errs = {h: abs(_fd(oracle_lib, cfg, st, mu, v, h) - ad) / abs(ad) for h in (1e-5, 1e-6, 1e-7)}
+        print(kind, "trial", trial, "adjoint", ad, "rel err vs FD by h:", errs)
+        assert min(errs.values()) <= FD_REL, errs
+
+
+def test_vjp_component_groups(cuda_lib, oracle_lib):
+    """Directions confined to one group of conserved components at a time:
+    each link of the chain rule (density, momentum, energy through the EOS
+    solve, species through the mixture rules) is checked on its own."""
+    mech, st, cfg = _case("flame")
+    rng = np.random.default_rng(9)
+    nx, ny, nz = st.shape
+    mu = rng.normal(size=(st.S.shape[0], nz, ny, nx))
+    Ub = _vjp(cuda_lib, cfg, st, mu)
+    groups = {"rho": [abi.URHO], "mom": [abi.UMX, abi.UMY, abi.UMZ], "E": [abi.UEDEN],
+              "spec": [abi.UFS + k for k in range(9)]}
+    for name, comps in groups.items():
+        v = _scale_direction(st, rng)
+        keep = np.zeros(v.shape[0], bool)
+        keep[comps] = True
+        v[~keep] = 0.0
+        ad = float((Ub * v).sum())
+        err = min(abs(_fd(oracle_lib, cfg, st, mu, v, h) - ad) / abs(ad) for h in (1e-5, 1e-6, 1e-7))
+        print("group", name, "adjoint", ad, "rel err", err)
+        assert err <= FD_REL, (name, err)
+
+
+def _jvp(mol, cfg, st, v):
+    """(RHS, J v) on the GPU; v covers grow(valid, 2)."""
+    import torch
+
+    op = mol.MOLOperator(cfg)
+    S = to_multifab(mol, [st], st.ng)
+    Sd = mol.MultiFab(S.boxes, S.ncomp, 2, fabs=[torch.from_numpy(np.ascontiguousarray(v)).cuda()])
+    R = mol.MultiFab(S.boxes, S.ncomp, 0)
+    Rd = mol.MultiFab(S.boxes, S.ncomp, 0)
+    op.rhs_jvp(S, Sd, R, Rd, st.dx)
+    torch.cuda.synchronize()
+    return R.fabs[0].cpu().numpy(), Rd.fabs[0].cpu().numpy()
+
+
+@pytest.mark.parametrize("kind", ["tgv", "flame", "flame_noslope"])
+def test_jvp_primal_is_the_rhs(cuda_lib, kind):
+    from gpu_util import gpu_rhs
+
+    mech, st, cfg = _case(kind)
+    v = _direction(st, np.random.default_rng(3))
+    R, _ = _jvp(cuda_lib, cfg, st, v)
+    (want,), _ = gpu_rhs(cuda_lib, cfg, [st])
+    np.testing.assert_array_equal(R, want)
+
+
+@pytest.mark.parametrize("kind", ["tgv", "flame", "flame_noslope"])
+def test_dot_product_adjoint_vs_tangent(cuda_lib, kind):
+    """<mu, J v> from the dual-number tangent equals <J^T mu, v> from the
+    hand-written adjoint to round-off, for seeded mu and v."""
+    mech, st, cfg = _case(kind)
+    rng = np.random.default_rng(11)
+    nx, ny, nz = st.shape
+    for trial in range(3):
+        mu = rng.normal(size=(st.S.shape[0], nz, ny, nx))
+        v = _direction(st, rng)
+        _, Jv = _jvp(cuda_lib, cfg, st, v)
+        Ub = _vjp(cuda_lib, cfg, st, mu)
+        a = float((mu * Jv).sum())
+        b = float((Ub * v).sum())
+        scale = float(np.abs(mu * Jv).sum())
+        print(kind, "trial", trial, "<mu,Jv> =", a, "<J^T mu, v> =", b, "rel", abs(a - b) / abs(a),
+              "vs sum|terms|", abs(a - b) / scale)
+        assert abs(a - b) <= 1e-10 * scale, (a, b)
+
+
+@pytest.mark.parametrize("kind", ["tgv", "flame"])
+def test_jvp_matches_oracle_finite_differences(cuda_lib, oracle_lib, kind):
+    """The dual-number tangent against central differences of the oracle RHS,
+    cell by cell.  A step that crosses a limiter switch at some face spoils
+    the difference quotient of the cells next to it, so the check is that
+    99% of the cells agree to 1e-5 of the component's RMS tangent."""
+    mech, st, cfg = _case(kind)
+    rng = np.random.default_rng(5)
+    v = _scale_direction(st, rng)
+    _, Jv = _jvp(cuda_lib, cfg, st, v)
+    comps = [abi.URHO, abi.UMX, abi.UMY, abi.UMZ, abi.UEDEN] + [abi.UFS + k for k in range(mech.nspec)]
+    best = 1.0
+    for h in (1e-6, 1e-7, 1e-8):
+        Sp, Sm = st.S.copy(), st.S.copy()
+        Sp[:, 2:-2, 2:-2, 2:-2] += h * v
+        Sm[:, 2:-2, 2:-2, 2:-2] -= h * v
+        Rp, = oracle_lib.mol_rhs(cfg, [problems.BoxState(st.lo, st.hi, Sp, st.dx)])
+        Rm, = oracle_lib.mol_rhs(cfg, [problems.BoxState(st.lo, st.hi, Sm, st.dx)])
+        fd = (Rp - Rm) / (2 * h)
+        bad = 0.0
+        for n in comps:
+            rms = np.sqrt((Jv[n] ** 2).mean())
+            bad = max(bad, float((np.abs(fd[n] - Jv[n]) > 1e-5 * rms).mean()))
+        print(kind, "h", h, "largest fraction of cells off by more than 1e-5 RMS:", bad)
+        best = min(best, bad)
+    assert best <= 0.01, best
