@@ -268,6 +268,21 @@ int pc_mol_lincomb(pc_mol_handle* h, int nboxes, const int* lohi, const pc_array
  * and pc_cmpTemp solves the EOS for T from U(UTEMP) (Utilities.H:67-84). */
 int pc_mol_compute_temp(pc_mol_handle* h, int nboxes, const int* lohi, const pc_array4* state, void* stream);
 
+/* Transposes of the two level operations above, for the adjoint of a
+ * trajectory (no counterpart in the reference).
+ * pc_mol_fill_ghosts_adjoint: boxes[b].state holds cotangents; the cotangent
+ * of every ghost cell of grow(valid, ngrow) is added (with the fill's sign
+ * flips) to the valid cell the fill copies it from, and the ghost is set to
+ * 0.  FP64 atomics: the sum order, and so the last bit, may vary between
+ * runs.
+ * pc_mol_compute_temp_adjoint: state[b] is the state after computeTemp,
+ * state_bar[b] its cotangent (valid cells), overwritten with the cotangent
+ * of the state before computeTemp (UEINT and UTEMP entries become 0). */
+int pc_mol_fill_ghosts_adjoint(pc_mol_handle* h, const pc_box_desc* boxes, int nboxes, const pc_geometry* geom,
+                               int ngrow, void* stream);
+int pc_mol_compute_temp_adjoint(pc_mol_handle* h, int nboxes, const int* lohi, const pc_array4* state,
+                                pc_array4* state_bar, void* stream);
+
 /* A CUDA graph of one level's RHS, optionally preceded by its ghost fill
  * (FillPatcherFill + getMOLSrcTerm of Advance.cpp:98-100), captured once and
  * replayed with one launch.  The layout (boxes, array pointers, dx, fill

@@ -6,6 +6,7 @@
 // the time step reproduce the CPU restatement's values.
 #pragma once
 
+#include "pc_adjoint.cuh"
 #include "pc_kernels.cuh"
 #include "pelec_mol.h"
 
@@ -34,7 +35,11 @@ struct FillGeom {
 
 // One thread per cell of grow(valid, ng) of a box; valid cells return.  The
 // ghost cell takes the value of the valid cell its index maps to.  items[b]
-// = (box, first cell of the 256-cell chunk in the grown box).
+// = (box, first cell of the 256-cell chunk in the grown box).  ADJ: the
+// transpose — the ghost cell's value (a cotangent) is added, with the same
+// sign flips, to the valid cell it maps to, and the ghost is zeroed (FP64
+// atomics: several ghosts map to one cell).
+template <bool ADJ>
 __global__ void __launch_bounds__(256) fill_ghosts_kernel(const LevelBox* __restrict__ boxes,
                                                           const int2* __restrict__ items,
                                                           const int* __restrict__ owner, const FillGeom g) {
@@ -81,12 +86,19 @@ __global__ void __launch_bounds__(256) fill_ghosts_kernel(const LevelBox* __rest
     ob = owner[o];
   }
   const LevelBox& sb = boxes[ob];
-  const double* s = at(sb, src[0], src[1], src[2]);
+  double* s = at(sb, src[0], src[1], src[2]);
   double* dst = at(b, idx[0], idx[1], idx[2]);
   for (int n = 0; n < g.nvar; ++n) {
-    double v = s[n * sb.sn];
-    if (n >= UMX && n <= UMZ) v = v * sign[n - UMX];
-    dst[n * b.sn] = v;
+    if constexpr (ADJ) {
+      double v = dst[n * b.sn];
+      dst[n * b.sn] = 0.0;
+      if (n >= UMX && n <= UMZ) v = v * sign[n - UMX];
+      if (v != 0.0) atomicAdd(s + n * sb.sn, v);
+    } else {
+      double v = s[n * sb.sn];
+      if (n >= UMX && n <= UMZ) v = v * sign[n - UMX];
+      dst[n * b.sn] = v;
+    }
   }
 }
 
@@ -153,6 +165,66 @@ __global__ void __launch_bounds__(256) compute_temp_kernel(const LevelBox* __res
     s[UTEMP * sn] = T;
   }
   warp_count(&counters[kCounterNewton], fail);
+}
+
+// Transpose of computeTemp on the valid cells.  state holds the state after
+// computeTemp (its UTEMP is the converged T); bar holds the cotangent of that
+// state and is overwritten with the cotangent of the state before it:
+// UEINT and UTEMP were overwritten (cotangent 0), their cotangents flow to
+// rho, momentum, rho E and rho Y through rho e = rho E - |m|^2 / (2 rho) and
+// the implicit-function theorem on e(T, Y) = e.
+template <int NS, class EOS>
+__global__ void __launch_bounds__(256) compute_temp_adjoint_kernel(const LevelBox* __restrict__ boxes,
+                                                                   const LevelBox* __restrict__ bars,
+                                                                   const int2* __restrict__ items,
+                                                                   const __grid_constant__ DevMech<NS> m) {
+  const int2 it = items[blockIdx.x];
+  const LevelBox& b = boxes[it.x];
+  const LevelBox& q = bars[it.x];
+  int i, j, k;
+  if (!valid_cell(b, (long long)it.y + threadIdx.x, i, j, k)) return;
+  const double* s = at(b, i, j, k);
+  double* o = at(q, i, j, k);
+  const long long sn = b.sn, qn = q.sn;
+  const double rho = s[URHO * sn];
+  const double rhoInv = 1.0 / rho;
+  const double mm[3] = {s[UMX * sn], s[UMY * sn], s[UMZ * sn]};
+  const double u[3] = {mm[0] * rhoInv, mm[1] * rhoInv, mm[2] * rhoInv};
+  const double ke = 0.5 * (u[0] * u[0] + u[1] * u[1] + u[2] * u[2]);
+  const double rhoe = s[UEDEN * sn] - rho * ke;
+  double Y[NS];
+#pragma unroll
+  for (int n = 0; n < NS; ++n) Y[n] = s[(UFS + n) * sn] * rhoInv;
+  const double rw = mix_rw<NS>(m, Y);
+  const double T = s[UTEMP * sn];
+  // reverse
+  double Yb[NS];
+#pragma unroll
+  for (int n = 0; n < NS; ++n) Yb[n] = 0.0;
+  double eb = 0.0, rwb = 0.0;
+  EosAdj<NS, EOS>::rey2t(m, Y, rw, T, o[UTEMP * qn], eb, Yb, rwb);
+#pragma unroll
+  for (int n = 0; n < NS; ++n) Yb[n] += rwb * m.rW[n];
+  const double rhoeb = o[UEINT * qn] + eb * rhoInv;  // e = rho e / rho
+  double rinvb = eb * rhoe;
+#pragma unroll
+  for (int n = 0; n < NS; ++n) {
+    o[(UFS + n) * qn] += Yb[n] * rhoInv;
+    rinvb += Yb[n] * s[(UFS + n) * sn];
+  }
+  o[UEDEN * qn] += rhoeb;  // rho e = rho E - rho ke
+  double rhob = -rhoeb * ke;
+  const double keb = -rhoeb * rho;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const double ub = keb * u[c];
+    o[(UMX + c) * qn] += ub * rhoInv;
+    rinvb += ub * mm[c];
+  }
+  rhob -= rinvb * rhoInv * rhoInv;
+  o[URHO * qn] += rhob;
+  o[UEINT * qn] = 0.0;
+  o[UTEMP * qn] = 0.0;
 }
 
 // Positive doubles order as their bit patterns: atomic minimum on the bits.

@@ -830,8 +830,8 @@ long long nvalid(const int lo[3], const int hi[3], int ng) {
 
 }  // namespace
 
-extern "C" int pc_mol_fill_ghosts(pc_mol_handle* h, const pc_box_desc* boxes, int nboxes, const pc_geometry* geom,
-                                  int ngrow, void* stream) {
+static int fill_ghosts_impl(pc_mol_handle* h, const pc_box_desc* boxes, int nboxes, const pc_geometry* geom,
+                            int ngrow, void* stream, bool adjoint) {
   if (!h || !geom || nboxes < 0 || (nboxes > 0 && !boxes) || ngrow < 0) return PC_ERR_INVALID_ARGUMENT;
   if (nboxes == 0 || ngrow == 0) return PC_OK;
   const int nvar = 7 + h->cfg.nspec;
@@ -889,10 +889,25 @@ extern "C" int pc_mol_fill_ghosts(pc_mol_handle* h, const pc_box_desc* boxes, in
   }
   if ((rc = upload(h, kUpFillBoxes, lb.data(), lb.size() * sizeof(LevelBox), s, &dbox)) != PC_OK) return rc;
   if ((rc = upload(h, kUpFillItems, items.data(), items.size() * sizeof(int2), s, &ditems)) != PC_OK) return rc;
-  fill_ghosts_kernel<<<(unsigned)items.size(), 256, 0, s>>>(static_cast<const LevelBox*>(dbox),
+  if (adjoint)
+    fill_ghosts_kernel<true><<<(unsigned)items.size(), 256, 0, s>>>(static_cast<const LevelBox*>(dbox),
+                                                            static_cast<const int2*>(ditems),
+                                                            nboxes > 1 ? static_cast<const int*>(downer) : nullptr, g);
+  else
+    fill_ghosts_kernel<false><<<(unsigned)items.size(), 256, 0, s>>>(static_cast<const LevelBox*>(dbox),
                                                             static_cast<const int2*>(ditems),
                                                             nboxes > 1 ? static_cast<const int*>(downer) : nullptr, g);
   return h->last_error = cuda_fail(h, cudaGetLastError());
+}
+
+extern "C" int pc_mol_fill_ghosts(pc_mol_handle* h, const pc_box_desc* boxes, int nboxes, const pc_geometry* geom,
+                                  int ngrow, void* stream) {
+  return fill_ghosts_impl(h, boxes, nboxes, geom, ngrow, stream, false);
+}
+
+extern "C" int pc_mol_fill_ghosts_adjoint(pc_mol_handle* h, const pc_box_desc* boxes, int nboxes,
+                                          const pc_geometry* geom, int ngrow, void* stream) {
+  return fill_ghosts_impl(h, boxes, nboxes, geom, ngrow, stream, true);
 }
 
 extern "C" int pc_mol_lincomb(pc_mol_handle* h, int nboxes, const int* lohi, const pc_array4* dst, double a,
@@ -959,6 +974,41 @@ extern "C" int pc_mol_compute_temp(pc_mol_handle* h, int nboxes, const int* lohi
   else
     compute_temp_kernel<9, IdealMixEos<9>><<<(unsigned)items.size(), 256, 0, s>>>(
         static_cast<const LevelBox*>(db), static_cast<const int2*>(di), h->mech9, maxit, h->d_counters);
+  return h->last_error = cuda_fail(h, cudaGetLastError());
+}
+
+extern "C" int pc_mol_compute_temp_adjoint(pc_mol_handle* h, int nboxes, const int* lohi, const pc_array4* state,
+                                           pc_array4* state_bar, void* stream) {
+  if (!h || nboxes < 0 || (nboxes > 0 && (!lohi || !state || !state_bar))) return PC_ERR_INVALID_ARGUMENT;
+  if (nboxes == 0) return PC_OK;
+  const int nvar = 7 + h->cfg.nspec;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  int rc = cuda_fail(h, cudaSetDevice(h->device));
+  if (rc != PC_OK) return rc;
+  std::vector<LevelBox> lb, lq;
+  std::vector<long long> nc;
+  for (int i = 0; i < nboxes; ++i) {
+    const int* lo = lohi + 6 * i;
+    const int* hi = lohi + 6 * i + 3;
+    if (!array_ok(state[i], lo, hi, 0, nvar) || !array_ok(state_bar[i], lo, hi, 0, nvar))
+      return h->last_error = PC_ERR_INVALID_ARGUMENT;
+    lb.push_back(level_box(lo, hi, state[i]));
+    lq.push_back(level_box(lo, hi, state_bar[i]));
+    nc.push_back(nvalid(lo, hi, 0));
+  }
+  std::vector<int2> items;
+  chunk_items(nc, items);
+  void *db, *dq, *di;
+  if ((rc = upload(h, kUpBoxes, lb.data(), lb.size() * sizeof(LevelBox), s, &db)) != PC_OK) return rc;
+  if ((rc = upload(h, kUpLcDst, lq.data(), lq.size() * sizeof(LevelBox), s, &dq)) != PC_OK) return rc;
+  if ((rc = upload(h, kUpItems, items.data(), items.size() * sizeof(int2), s, &di)) != PC_OK) return rc;
+  h->last_stream = s;
+  if (h->variant == 1)
+    compute_temp_adjoint_kernel<1, GammaLawEos<1>><<<(unsigned)items.size(), 256, 0, s>>>(
+        static_cast<const LevelBox*>(db), static_cast<const LevelBox*>(dq), static_cast<const int2*>(di), h->mech1);
+  else
+    compute_temp_adjoint_kernel<9, IdealMixEos<9>><<<(unsigned)items.size(), 256, 0, s>>>(
+        static_cast<const LevelBox*>(db), static_cast<const LevelBox*>(dq), static_cast<const int2*>(di), h->mech9);
   return h->last_error = cuda_fail(h, cudaGetLastError());
 }
 

@@ -87,6 +87,11 @@ def library() -> ctypes.CDLL:
         lib.pc_mol_rhs_jvp.argtypes = [c_void_p, POINTER(abi.PcBoxDesc), c_int, POINTER(c_double),
                                        POINTER(abi.PcArray4), POINTER(abi.PcArray4), c_void_p]
         lib.pc_mol_rhs_jvp.restype = c_int
+        lib.pc_mol_fill_ghosts_adjoint.argtypes = lib.pc_mol_fill_ghosts.argtypes
+        lib.pc_mol_fill_ghosts_adjoint.restype = c_int
+        lib.pc_mol_compute_temp_adjoint.argtypes = [c_void_p, c_int, POINTER(c_int), POINTER(abi.PcArray4),
+                                                    POINTER(abi.PcArray4), c_void_p]
+        lib.pc_mol_compute_temp_adjoint.restype = c_int
         if lib.pc_mol_abi_version() != abi.PC_MOL_ABI_VERSION:
             raise RuntimeError("libpelec_mol.so ABI version does not match pelec_gb300.abi")
         _lib = lib
@@ -270,6 +275,23 @@ class MOLOperator:
         dxa = (c_double * 3)(*[float(v) for v in dx])
         _check(library().pc_mol_rhs_jvp(self._h, descs, len(S), dxa, self._arrays(state_dot), self._arrays(rhs_dot),
                                         self._stream(stream)), "pc_mol_rhs_jvp")
+
+    def fill_ghosts_adjoint(self, Sbar: MultiFab, geom: abi.PcGeometry, ngrow: int | None = None,
+                            stream=None) -> None:
+        """Transpose of fill_ghosts on a cotangent MultiFab (ghosts folded
+        into the valid cells they were copied from, then zeroed)."""
+        descs = abi.box_array([abi.box_desc(lo, hi, Sbar.array4(b), Sbar.array4(b))
+                               for b, (lo, hi) in enumerate(Sbar.boxes)])
+        ng = Sbar.ngrow if ngrow is None else ngrow
+        _check(library().pc_mol_fill_ghosts_adjoint(self._h, descs, len(Sbar), ctypes.byref(geom), ng,
+                                                    self._stream(stream)), "pc_mol_fill_ghosts_adjoint")
+
+    def compute_temp_adjoint(self, S: MultiFab, Sbar: MultiFab, stream=None) -> None:
+        """Transpose of compute_temp at the post-computeTemp state S, in
+        place on the cotangent Sbar."""
+        _check(library().pc_mol_compute_temp_adjoint(self._h, len(S), self._lohi(S), self._arrays(S),
+                                                     self._arrays(Sbar), self._stream(stream)),
+               "pc_mol_compute_temp_adjoint")
 
     # ---- flux-pass tile shape ----
     @staticmethod
