@@ -43,6 +43,7 @@ def parse():
     ap.add_argument("--precision", default="fp64", choices=["fp64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-level", action="store_true", help="skip the 400-box batched-level measurement")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint and trajectory-gradient measurement")
     return ap.parse_args()
 
 
@@ -264,6 +265,156 @@ def bench_level(args, rank: int, local: int, maxover, barrier) -> dict:
     return out
 
 
+def bench_adjoint_rhs(args, st, mech, S, maxover, barrier) -> dict:
+    """Adjoint (VJP) and tangent (JVP) of one RHS on the headline box, timed
+    like the RHS itself: ms per call with CUDA events, and the ratio to the
+    forward RHS (the metric's adjoint/forward time)."""
+    import numpy as np
+    import torch
+
+    from pelec_gb300 import mol, problems
+
+    op = mol.MOLOperator(problems.make_config(mech))
+    R = mol.MultiFab(S.boxes, S.ncomp, 0)
+    Rb = mol.MultiFab(S.boxes, S.ncomp, 0,
+                      fabs=[torch.from_numpy(np.random.default_rng(5).normal(size=R.fabs[0].shape)).cuda()])
+    Ub = mol.MultiFab(S.boxes, S.ncomp, 2)
+    Sd = mol.MultiFab(S.boxes, S.ncomp, 2)
+    Sd.fabs[0].copy_(S.fabs[0][:, 2:-2, 2:-2, 2:-2] * 1e-3)
+    Rd = mol.MultiFab(S.boxes, S.ncomp, 0)
+    stream = torch.cuda.current_stream()
+    steps = max(3, min(args.steps, 10))
+
+    def timed(fn):
+        for _ in range(max(3, args.warmup)):
+            fn()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        barrier()
+        e0.record(stream)
+        for _ in range(steps):
+            fn()
+        e1.record(stream)
+        barrier()
+        return maxover(e0.elapsed_time(e1)) / steps
+
+    t_rhs = timed(lambda: op.rhs_level(S, R, st.dx))
+    t_vjp = timed(lambda: op.rhs_vjp(S, Rb, Ub, st.dx))
+    t_jvp = timed(lambda: op.rhs_jvp(S, Sd, R, Rd, st.dx))
+    op.close()
+    return {"workload": "the headline box", "ms_rhs": t_rhs, "ms_vjp": t_vjp, "ms_jvp": t_jvp,
+            "vjp_over_rhs": t_vjp / t_rhs, "jvp_over_rhs": t_jvp / t_rhs, "steps": steps,
+            "vjp": "hand-written reverse mode: record pass + face adjoint + cell adjoint (IFT for the T solve)",
+            "jvp": "forward passes instantiated with dual numbers"}
+
+
+def bench_trajectory(args, rank: int) -> dict:
+    """C5: 64^3 flame, 9 species, FP64; J = sum(T dV) after 50 SSP-RK2 steps
+    at CFL 0.3 (time steps frozen); gradient by the checkpointed adjoint
+    (every 5 steps).  Times the forward trajectory and the gradient, records
+    the device memory, and checks the gradient against central differences
+    of the trajectory: 20 seeded directions of the initial state (each
+    conserved component scaled by a seeded factor), h = 1e-6, and the three
+    first wrinkle amplitudes, h = 1e-6 relative."""
+    import dataclasses
+    import time
+
+    import numpy as np
+    import torch
+
+    from pelec_gb300 import abi, mol, problems, trajectory
+
+    nsteps, every, shape = 50, 5, (64, 64, 64)
+    out = {"workload": "C5: 64^3 premixed flame, 9 species, FP64, 50 SSP-RK2 steps at CFL 0.3, "
+                       "J = sum(T dV) at step 50, checkpoint every 5", "nsteps": nsteps, "every": every}
+
+    def make(params=None, w_noise=0.0):
+        mech, st, fp = problems.flame(shape, seed=5, params=params, w_noise=w_noise)
+        return mech, st, fp
+
+    def case(w_noise, ndirs, with_params):
+        mech, st, fp = make(w_noise=w_noise)
+        op = mol.MOLOperator(problems.make_config(mech))
+        S0 = mol.MultiFab([(st.lo, st.hi)], st.S.shape[0], 4, fabs=[torch.from_numpy(st.S).cuda()])
+        geom = abi.geometry(st.lo, st.hi, (0, 0, abi.PC_BC_OUTFLOW), (0, 0, abi.PC_BC_OUTFLOW))
+        tr = trajectory.Trajectory(op, S0, geom, st.dx)
+        dts = tr.dt_sequence(S0, nsteps, 0.3)
+        torch.cuda.synchronize()
+        res = {}
+        tr.run(S0, dts, every)  # warm-up (layouts, uploads)
+        torch.cuda.synchronize()
+        torch.cuda.reset_peak_memory_stats()
+        free0, total = torch.cuda.mem_get_info()
+        t0 = time.perf_counter()
+        final, _ = tr.run(S0, dts, every)
+        J = tr.objective(final)
+        t_fwd = time.perf_counter() - t0
+        del final
+        t0 = time.perf_counter()
+        J2, L = tr.gradient(S0, dts, every)
+        torch.cuda.synchronize()
+        t_grad = time.perf_counter() - t0
+        free1, _ = torch.cuda.mem_get_info()
+        res.update({"J": J, "forward_s": t_fwd, "gradient_s": t_grad, "adjoint_sweep_s": t_grad - t_fwd,
+                    "gradient_over_forward": t_grad / t_fwd, "adjoint_sweep_over_forward": (t_grad - t_fwd) / t_fwd,
+                    "peak_torch_bytes": int(torch.cuda.max_memory_allocated()),
+                    "device_bytes_in_use_after_gradient": int(total - free1),
+                    "dt_first_last": [dts[0], dts[-1]]})
+        g = 4
+        rng = np.random.default_rng(2024)
+        errs = []
+        for _ in range(ndirs):
+            sc = rng.normal(size=st.S.shape[0])
+            sc[abi.UEINT] = sc[abi.UTEMP] = 0.0
+            v = torch.from_numpy(sc[:, None, None, None] * st.S).cuda()
+            for ax in (1, 2, 3):
+                v.narrow(ax, 0, g).zero_()
+                v.narrow(ax, v.shape[ax] - g, g).zero_()
+            ad = float((L.fabs[0] * v).sum())
+            h = 1e-6
+            Jp = tr.objective(tr.run(mol.MultiFab(S0.boxes, S0.ncomp, 4, fabs=[S0.fabs[0] + h * v]), dts)[0])
+            Jm = tr.objective(tr.run(mol.MultiFab(S0.boxes, S0.ncomp, 4, fabs=[S0.fabs[0] - h * v]), dts)[0])
+            errs.append(abs((Jp - Jm) / (2 * h) - ad) / abs(ad))
+        if errs:
+            res["fd_state_directions"] = {"n": len(errs), "h": 1e-6, "max_rel_err": max(errs),
+                                          "median_rel_err": float(np.median(errs)),
+                                          "direction": "each conserved component scaled by a seeded N(0,1) factor"}
+        if with_params:
+            lam = L.fabs[0].cpu().numpy()
+            perr = []
+            for m in range(3):
+                def U0(amps):
+                    return make(dataclasses.replace(fp, amps=np.asarray(amps, float)), w_noise)[1].S
+
+                ha = 1e-3 * fp.amps[m]
+                ap, am = fp.amps.copy(), fp.amps.copy()
+                ap[m] += ha
+                am[m] -= ha
+                ad = float((lam * (U0(ap) - U0(am)) / (2 * ha)).sum())
+                h = 1e-6 * fp.amps[m]
+                ap, am = fp.amps.copy(), fp.amps.copy()
+                ap[m] += h
+                am[m] -= h
+                Jp = tr.objective(tr.run(mol.MultiFab(S0.boxes, S0.ncomp, 4,
+                                                      fabs=[torch.from_numpy(U0(ap)).cuda()]), dts)[0])
+                Jm = tr.objective(tr.run(mol.MultiFab(S0.boxes, S0.ncomp, 4,
+                                                      fabs=[torch.from_numpy(U0(am)).cuda()]), dts)[0])
+                fd = (Jp - Jm) / (2 * h)
+                perr.append({"mode": m, "adjoint": ad, "fd": fd, "rel_err": abs(fd - ad) / abs(ad)})
+            res["fd_wrinkle_amplitudes"] = perr
+        op.close()
+        del S0, L
+        torch.cuda.empty_cache()
+        return res
+
+    out["config_state"] = case(0.0, 20, True)
+    out["config_state"]["note"] = ("p and w exactly uniform: the limiter's acoustic slopes start at its "
+                                   "non-differentiable point mc(0,0), so state directions that make p "
+                                   "non-uniform have no linear derivative at t=0")
+    out["w_noise_state"] = case(1.0, 20, False)
+    out["w_noise_state"]["note"] = "same state with seeded N(0, 1 cm/s) noise on w, as on u and v"
+    return out
+
+
 def abi_precision(mixed: int) -> int:
     from pelec_gb300 import abi
 
@@ -407,6 +558,8 @@ def run_gpu(args):
     mx = [float(np.abs(r32[n] - r64[n]).max() / max(np.abs(r64[n]).max(), 1e-300)) for n in range(r64.shape[0])]
 
     level = None if args.no_level else bench_level(args, rank, local, maxover, barrier)
+    adj = None if args.no_adjoint else bench_adjoint_rhs(args, st, mech, S, maxover, barrier)
+    traj = None if (args.no_adjoint or rank != 0) else bench_trajectory(args, rank)
 
     if rank != 0:
         if pg is not None:
@@ -459,6 +612,10 @@ def run_gpu(args):
         line["cpu_baseline"] = cpu
     if level is not None:
         line["level_c3"] = level
+    if adj is not None:
+        line["adjoint"] = adj
+    if traj is not None:
+        line["trajectory_c5"] = traj
     print(json.dumps(line))
     if pg is not None:
         pg.destroy_process_group()

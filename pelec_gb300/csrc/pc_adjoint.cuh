@@ -144,11 +144,12 @@ struct EosAdj<NS, IdealMixEos<NS>> {
     E::template coefs<5>(m, Y, r, C);
     const double cv = E::cv_of(C, rw, T);
     const double num = (cv + rw) * p, den = cv * rho;
-    const double g = num / den;
+    const double iden = 1.0 / den;
+    const double g = num * iden;
     const double c = sqrt(g);
     if (!(c > 0.0)) return;
-    const double gb = cb / (2.0 * c);
-    const double numb = gb / den, denb = -gb * g / den;
+    const double gb = cb * 0.5 / c;
+    const double numb = gb * iden, denb = -gb * g * iden;
     double cvb = numb * p + denb * rho;
     rwb += numb * p;
     pb += numb * (cv + rw);
@@ -168,13 +169,14 @@ struct EosAdj<NS, IdealMixEos<NS>> {
   // RPY2Cs with T = p / (rho rw).
   __device__ static void cs_rp(const DevMech<NS>& m, const double* Y, double rw, double rho, double p, double cb,
                                double* Yb, double& rwb, double& rhob, double& pb) {
-    const double T = p / (rho * rw);
+    const double rr = rho * rw, T = p / rr;  // the forward's T (it selects the range)
     double Tb = 0.0;
     cs_core(m, Y, rw, rho, T, p, cb, Yb, rwb, rhob, Tb, pb);
     // T = p / (rho rw)
-    pb += Tb / (rho * rw);
-    rhob -= Tb * T / rho;
-    rwb -= Tb * T / rw;
+    const double q = Tb / rr;
+    pb += q;
+    rhob -= q * T * rw;  // dT/drho = -T/rho = -T rw / rr
+    rwb -= q * T * rho;
   }
   __device__ static void cs_T(const DevMech<NS>& m, const double* Y, double rw, double rho, double T, double p,
                               double cb, double* Yb, double& rwb, double& rhob, double& Tb, double& pb) {
@@ -205,10 +207,10 @@ struct EosAdj<NS, IdealMixEos<NS>> {
     for (int n = 0; n < 6; ++n) Cb[n] = eb * w[n];
     coefs_rev(m, r, Cb, 6, Yb);
     rwb -= eb * T;
-    const double Tb = eb * cv;
-    pb += Tb / (rho * rw);
-    rhob -= Tb * T / rho;
-    rwb -= Tb * T / rw;
+    const double q = eb * cv / (rho * rw);
+    pb += q;
+    rhob -= q * T * rw;
+    rwb -= q * T * rho;
   }
   // dh_k/dT = cp_k(T) = c0 + T (c1 + T (c2 + T (c3 + T c4))).
   __device__ static void hi_dT(const DevMech<NS>& m, double T, double* dh) {
@@ -286,13 +288,14 @@ struct TransAdj<NS, SimpleTransport<NS>> {
     for (int k = 0; k < NS; ++k) {
       sb[k] = 0.0;
       if (s[k] > 0.0) {
-        const double wrat = rw / m.rW[k];
-        const double out = rho * (1.0 - Y[k]) * wrat / s[k];
+        const double is = 1.0 / s[k], iw = 1.0 / m.rW[k];
+        const double wrat = rw * iw;
         const double db = ob[k];
-        rhob += db * (1.0 - Y[k]) * wrat / s[k];
-        Yb[k] -= db * rho * wrat / s[k];
-        rwb += db * rho * (1.0 - Y[k]) / (s[k] * m.rW[k]);
-        sb[k] = -db * out / s[k];
+        const double t = db * wrat * is;  // d out / d(rho (1 - Y_k))
+        rhob += t * (1.0 - Y[k]);
+        Yb[k] -= t * rho;
+        rwb += db * rho * (1.0 - Y[k]) * iw * is;
+        sb[k] = -t * rho * (1.0 - Y[k]) * is;
       }
     }
 #pragma unroll
@@ -317,7 +320,7 @@ struct TransAdj<NS, SimpleTransport<NS>> {
     pb += prb * m.inv_pref;
     // mu = smu^(1/6), xi = sum X bulk mk, lambda = slam^4
     const double mu = exp(log(smu) * (1.0 / 6.0));
-    const double smub = (smu > 0.0) ? ob[NS] * mu / (6.0 * smu) : 0.0;
+    const double smub = (smu > 0.0) ? ob[NS] * mu * (1.0 / 6.0) / smu : 0.0;
     const double sxib = ob[NS + 1];
     const double slamb = ob[NS + 2] * 4.0 * slam * slam * slam;
 #pragma unroll
@@ -577,9 +580,10 @@ __device__ void hydro_face_rev(const DevBox& b, const DevMech<NS>& m, const DevF
       dotp += Ygb[n] * Yg[n];
     }
     // Yg = g / rgd
+    const double irgd = 1.0 / rgd;
 #pragma unroll
-    for (int n = 0; n < NS; ++n) gb[n] += Ygb[n] / rgd;
-    rgdb -= dotp / rgd;
+    for (int n = 0; n < NS; ++n) gb[n] += Ygb[n] * irgd;
+    rgdb -= dotp * irgd;
   }
   // rgd = sum g
 #pragma unroll
@@ -669,9 +673,10 @@ __device__ void hydro_face_rev(const DevBox& b, const DevMech<NS>& m, const DevF
       Ysb[n] += rwsb * m.rW[n];
       dotp += Ysb[n] * Ys[n];
     }
-    rstarb -= dotp / rstar;
+    const double irs = 1.0 / rstar;
+    rstarb -= dotp * irs;
 #pragma unroll
-    for (int n = 0; n < NS; ++n) rspsb[n] += Ysb[n] / rstar + rstarb;
+    for (int n = 0; n < NS; ++n) rspsb[n] += Ysb[n] * irs + rstarb;
   }
   // rsps = max(0, rspo + drho Yo)
   double drhob = 0.0;
@@ -687,10 +692,10 @@ __device__ void hydro_face_rev(const DevBox& b, const DevMech<NS>& m, const DevF
   }
   // drho = (pstar - po) / (co co)
   {
-    const double ic2 = 1.0 / (co * co);
+    const double ico = 1.0 / co, ic2 = ico * ico;
     pstarb += drhob * ic2;
     pob -= drhob * ic2;
-    cob -= 2.0 * drhob * drho / co;
+    cob -= 2.0 * drhob * drho * ico;
   }
   // co = cs(Yo, rwo, ro, po)
   double rob = 0.0;
@@ -703,9 +708,10 @@ __device__ void hydro_face_rev(const DevBox& b, const DevMech<NS>& m, const DevF
       Yob[n] += rwob * m.rW[n];
       dotp += Yob[n] * Yo[n];
     }
-    rob -= dotp / ro;
+    const double iro = 1.0 / ro;
+    rob -= dotp * iro;
 #pragma unroll
-    for (int n = 0; n < NS; ++n) rspob[n] += Yob[n] / ro + rob;
+    for (int n = 0; n < NS; ++n) rspob[n] += Yob[n] * iro + rob;
   }
   // uo, po selections
   double unlb = 0.0, unrb = 0.0, plb = 0.0, prb = 0.0;
@@ -745,8 +751,8 @@ __device__ void hydro_face_rev(const DevBox& b, const DevMech<NS>& m, const DevF
   // ustar = m0 ? 0 : ustar0;  ustar0 = ((wl unl + wr unr) + (pl - pr)) / ww
   double wlb = 0.0, wrb = 0.0, wwb = 0.0;
   if (!m0) {
-    const double numb = ustarb / ww;
-    wwb -= ustarb * ustar0 / ww;
+    const double numb = ustarb * yww;
+    wwb -= ustarb * ustar0 * yww;
     wlb += numb * unl;
     unlb += numb * wl;
     wrb += numb * unr;
@@ -756,8 +762,8 @@ __device__ void hydro_face_rev(const DevBox& b, const DevMech<NS>& m, const DevF
   }
   // pstar = max(wsmall, pnum / ww)
   if (pq >= wsmall) {
-    const double Pb = pstarb / ww;
-    wwb -= pstarb * pq / ww;
+    const double Pb = pstarb * yww;
+    wwb -= pstarb * pq * yww;
     wrb += Pb * pl;
     plb += Pb * wr;
     wlb += Pb * pr;
@@ -800,12 +806,13 @@ __device__ void hydro_face_rev(const DevBox& b, const DevMech<NS>& m, const DevF
       dl += Ylb[n] * Yl[n];
       dr += Yrb[n] * Yr[n];
     }
-    rlb -= dl / rl;
-    rrb -= dr / rr;
+    const double irl = 1.0 / rl, irr = 1.0 / rr;
+    rlb -= dl * irl;
+    rrb -= dr * irr;
 #pragma unroll
     for (int n = 0; n < NS; ++n) {
-      splb[n] = Ylb[n] / rl + rlb;
-      sprb[n] = Yrb[n] / rr + rrb;
+      splb[n] = Ylb[n] * irl + rlb;
+      sprb[n] = Yrb[n] * irr + rrb;
     }
   }
   // face states and slopes
@@ -818,18 +825,18 @@ __device__ void hydro_face_rev(const DevBox& b, const DevMech<NS>& m, const DevF
     double yLb = 0.0, yRb = 0.0;
     // spl = yL rL + 0.5 (dsL + yL sL / cLc)
     const double sb = splb[n];
-    yLb += sb * rL + 0.5 * sb * sL / cLc;
+    yLb += sb * rL + 0.5 * sb * sL * ycL;
     rLb += sb * yL;
     const double dsLb = 0.5 * sb;
-    sLb += 0.5 * sb * yL / cLc;
-    cLcb -= 0.5 * sb * yL * sL / (cLc * cLc);
+    sLb += 0.5 * sb * yL * ycL;
+    cLcb -= 0.5 * sb * yL * sL * ycL2;
     // spr = yR rR - 0.5 (dsR + yR sR / cRc)
     const double sr = sprb[n];
-    yRb += sr * rR - 0.5 * sr * sR / cRc;
+    yRb += sr * rR - 0.5 * sr * sR * ycR;
     rRb += sr * yR;
     const double dsRb = -0.5 * sr;
-    sRb -= 0.5 * sr * yR / cRc;
-    cRcb += 0.5 * sr * yR * sR / (cRc * cRc);
+    sRb -= 0.5 * sr * yR * ycR;
+    cRcb += 0.5 * sr * yR * sR * ycR2;
     if (slopes) {
       const double yLL = ld(RC::Y + n, cLL), yRR = ld(RC::Y + n, cRR);
       const double ryL = rL * yL, ryR = rR * yR;
@@ -843,10 +850,10 @@ __device__ void hydro_face_rev(const DevBox& b, const DevMech<NS>& m, const DevF
         ryRb += bb;
         rLLb -= ab * yLL;
         yLLb -= ab * rLL;
-        yLb -= (ab * dpl + bb * dpc) / cL2;
-        dplb -= ab * yL / cL2;
-        dpcb -= bb * yL / cL2;
-        cL2b += (ab * yL * dpl + bb * yL * dpc) / (cL2 * cL2);
+        yLb -= (ab * dpl + bb * dpc) * ycL2;
+        dplb -= ab * yL * ycL2;
+        dpcb -= bb * yL * ycL2;
+        cL2b += (ab * yL * dpl + bb * yL * dpc) * ycL2 * ycL2;
       }
       {
         const double a = ryR - ryL - div_by(yR * dpc, cR2, ycR2);
@@ -855,10 +862,10 @@ __device__ void hydro_face_rev(const DevBox& b, const DevMech<NS>& m, const DevF
         mc_limit_rev(a, bq, dsRb, ab, bb);
         ryRb += ab - bb;
         ryLb -= ab;
-        yRb -= (ab * dpc + bb * dpr) / cR2;
-        dpcb -= ab * yR / cR2;
-        dprb -= bb * yR / cR2;
-        cR2b += (ab * yR * dpc + bb * yR * dpr) / (cR2 * cR2);
+        yRb -= (ab * dpc + bb * dpr) * ycR2;
+        dpcb -= ab * yR * ycR2;
+        dprb -= bb * yR * ycR2;
+        cR2b += (ab * yR * dpc + bb * yR * dpr) * ycR2 * ycR2;
         rRRb += bb * yRR;
         yRRb += bb * rRR;
       }
@@ -880,10 +887,11 @@ __device__ void hydro_face_rev(const DevBox& b, const DevMech<NS>& m, const DevF
   dqRb[1] += sRb;
   double uLb = 0.0, uRb = 0.0, pLb = 0.0, pRb = 0.0, t1Lb = 0.0, t1Rb = 0.0, t2Lb = 0.0, t2Rb = 0.0;
   // unl = uL + 0.5 (dqL1 - dqL0) / rL
+  const double irL = 1.0 / rL, irR = 1.0 / rR;
   uLb += unlb;
-  dqLb[1] += 0.5 * unlb / rL;
-  dqLb[0] -= 0.5 * unlb / rL;
-  rLb -= unlb * 0.5 * (dqL[1] - dqL[0]) / (rL * rL);
+  dqLb[1] += 0.5 * unlb * irL;
+  dqLb[0] -= 0.5 * unlb * irL;
+  rLb -= unlb * 0.5 * (dqL[1] - dqL[0]) * irL * irL;
   // pl = pL + 0.5 (dqL0 + dqL1) cLc
   pLb += plb;
   dqLb[0] += 0.5 * plb * cLc;
@@ -895,9 +903,9 @@ __device__ void hydro_face_rev(const DevBox& b, const DevMech<NS>& m, const DevF
   dqLb[3] += 0.5 * ut2lb;
   // unr = uR - 0.5 (dqR1 - dqR0) / rR
   uRb += unrb;
-  dqRb[1] -= 0.5 * unrb / rR;
-  dqRb[0] += 0.5 * unrb / rR;
-  rRb += unrb * 0.5 * (dqR[1] - dqR[0]) / (rR * rR);
+  dqRb[1] -= 0.5 * unrb * irR;
+  dqRb[0] += 0.5 * unrb * irR;
+  rRb += unrb * 0.5 * (dqR[1] - dqR[0]) * irR * irR;
   pRb += prb;
   dqRb[0] -= 0.5 * prb * cRc;
   dqRb[1] -= 0.5 * prb * cRc;
@@ -957,18 +965,18 @@ __device__ void hydro_face_rev(const DevBox& b, const DevMech<NS>& m, const DevF
       t2RRb += yb;
     }
     // a = 0.5 dp / c, b = 0.5 r du
-    dplb += 0.5 * aL1b / cLc;
-    cLcb -= aL1b * aL1 / cLc;
-    dpcb += 0.5 * aL2b / cLc;
-    cLcb -= aL2b * aL2 / cLc;
+    dplb += 0.5 * aL1b * ycL;
+    cLcb -= aL1b * aL1 * ycL;
+    dpcb += 0.5 * aL2b * ycL;
+    cLcb -= aL2b * aL2 * ycL;
     rLb += 0.5 * bL1b * (uL - uLL) + 0.5 * bL2b * (uR - uL);
     uLb += 0.5 * bL1b * rL - 0.5 * bL2b * rL;
     uLLb -= 0.5 * bL1b * rL;
     uRb += 0.5 * bL2b * rL;
-    dpcb += 0.5 * aR1b / cRc;
-    cRcb -= aR1b * aR1 / cRc;
-    dprb += 0.5 * aR2b / cRc;
-    cRcb -= aR2b * aR2 / cRc;
+    dpcb += 0.5 * aR1b * ycR;
+    cRcb -= aR1b * aR1 * ycR;
+    dprb += 0.5 * aR2b * ycR;
+    cRcb -= aR2b * aR2 * ycR;
     rRb += 0.5 * bR1b * (uR - uL) + 0.5 * bR2b * (uRR - uR);
     uRb += 0.5 * bR1b * rR - 0.5 * bR2b * rR;
     uLb -= 0.5 * bR1b * rR;
@@ -1107,8 +1115,9 @@ __device__ void diffusion_face_rev(const DevBox& b, const DevFlags& f, const Geo
       rb.add(RC::H + n, cL, 0.5 * hfb[n]);
     }
     // dlnp = dpdx / pm
-    const double dpdxb = dlnpb / pm;
-    const double pmb = -dlnpb * dlnp / pm;
+    const double ipm = 1.0 / pm;
+    const double dpdxb = dlnpb * ipm;
+    const double pmb = -dlnpb * dlnp * ipm;
     rb.add(RC::P, cR, g.dxinv[d] * dpdxb + 0.5 * pmb);
     rb.add(RC::P, cL, -g.dxinv[d] * dpdxb + 0.5 * pmb);
   }
@@ -1330,13 +1339,14 @@ __global__ void __launch_bounds__(kCellThreads)
       TransAdj<NS, TR>::eval(m, T, rho, p, Y, X, ob, Tb, rhob, pb, Yb, Xb);
     }
     // X_n = Y_n rW_n / rw
+    const double irw = 1.0 / rw;
     double dotp = 0.0;
 #pragma unroll
     for (int n = 0; n < NS; ++n) {
-      Yb[n] += Xb[n] * m.rW[n] / rw;
+      Yb[n] += Xb[n] * m.rW[n] * irw;
       dotp += Xb[n] * X[n];
     }
-    rwb -= dotp / rw;
+    rwb -= dotp * irw;
   }
   // c = cs_T(Y, rw, rho, T, p)
   EA::cs_T(m, Y, rw, rho, T, p, rbr(RC::C), Yb, rwb, rhob, Tb, pb);
@@ -1356,8 +1366,8 @@ __global__ void __launch_bounds__(kCellThreads)
 #pragma unroll
   for (int n = 0; n < NS; ++n) {
     if (!clip[n]) {
-      ub[UFS + n] = Yb[n] / rho;
-      rhob -= Yb[n] * Y[n] / rho;
+      ub[UFS + n] = Yb[n] * rhoinv;
+      rhob -= Yb[n] * Y[n] * rhoinv;
     }
   }
   // e = (E - kineng) rhoinv

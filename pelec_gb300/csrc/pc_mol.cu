@@ -69,8 +69,19 @@ struct pc_mol_handle {
   int tile_forced = -1;
   int tile = 0;
   std::map<std::vector<int>, int> tune_cache;
+  // Device box tables of the current layout, one per set of array pointers
+  // (callers alternate a few state/RHS buffers; a pointer change must not
+  // cost a layout rebuild).  d_boxes is the table of the last call.
+  struct BoxTable {
+    std::vector<pc_box_desc> key;
+    std::vector<DevBox> host;
+    DevBox* dev = nullptr;
+    size_t cap = 0;
+    unsigned long long stamp = 0;
+  };
+  BoxTable tables[4];
+  unsigned long long table_clock = 0;
   DevBox* d_boxes = nullptr;
-  size_t cap_boxes = 0;
   int2* d_items = nullptr;
   size_t cap_items = 0;
   int4* d_tiles = nullptr;
@@ -258,42 +269,78 @@ int choose_tile(pc_mol_handle* h, const pc_box_desc* boxes, int nboxes) {
   return it == h->tune_cache.end() ? 0 : it->second;
 }
 
+// Everything of a box descriptor but its two array pointers.
+bool same_geometry(const pc_box_desc& a, const pc_box_desc& b) {
+  pc_box_desc x = a, y = b;
+  x.state.p = y.state.p = nullptr;
+  x.rhs.p = y.rhs.p = nullptr;
+  return std::memcmp(&x, &y, sizeof(pc_box_desc)) == 0;
+}
+
 int prepare(pc_mol_handle* h, const pc_box_desc* boxes, int nboxes, const double dx[3], cudaStream_t s) {
   const int nvar = 7 + h->cfg.nspec;
   for (int b = 0; b < nboxes; ++b) {
     int rc = validate_box(boxes[b], nvar);
     if (rc != PC_OK) return rc;
   }
-  const bool same_boxes = (int)h->last_boxes.size() == nboxes &&
-                          std::memcmp(h->last_boxes.data(), boxes, sizeof(pc_box_desc) * nboxes) == 0 &&
-                          h->last_dx[0] == dx[0] && h->last_dx[1] == dx[1] && h->last_dx[2] == dx[2];
+  bool same_geom = (int)h->last_boxes.size() == nboxes && h->last_dx[0] == dx[0] && h->last_dx[1] == dx[1] &&
+                   h->last_dx[2] == dx[2];
+  for (int b = 0; same_geom && b < nboxes; ++b) same_geom = same_geometry(h->last_boxes[b], boxes[b]);
   if (h->tile_forced >= 0)
     h->tile = h->tile_forced;
-  else if (!same_boxes)
+  else if (!same_geom)
     h->tile = choose_tile(h, boxes, nboxes);
-  if (same_boxes && h->lay_tile == h->tile) return PC_OK;
-  h->lay_tile = -1;
-  build_layout(boxes, nboxes, h->nrec, h->tile, h->lay);
-  int rc = ensure(h, h->scratch, h->scratch_cap, h->lay.scratch_doubles);
-  if (rc != PC_OK) return rc;
-  for (auto& d : h->lay.boxes) d.rec = h->scratch + reinterpret_cast<size_t>(d.rec);
-  if ((rc = ensure(h, h->d_boxes, h->cap_boxes, h->lay.boxes.size())) != PC_OK) return rc;
-  if ((rc = ensure(h, h->d_items, h->cap_items, h->lay.items.size())) != PC_OK) return rc;
-  if ((rc = ensure(h, h->d_tiles, h->cap_tiles, h->lay.tiles.size())) != PC_OK) return rc;
-  cudaError_t e = cudaMemcpyAsync(h->d_boxes, h->lay.boxes.data(), sizeof(DevBox) * h->lay.boxes.size(),
-                                  cudaMemcpyHostToDevice, s);
-  if (e == cudaSuccess)
-    e = cudaMemcpyAsync(h->d_items, h->lay.items.data(), sizeof(int2) * h->lay.items.size(), cudaMemcpyHostToDevice, s);
-  if (e == cudaSuccess)
-    e = cudaMemcpyAsync(h->d_tiles, h->lay.tiles.data(), sizeof(int4) * h->lay.tiles.size(), cudaMemcpyHostToDevice, s);
-  if (e != cudaSuccess) return cuda_fail(h, e);
-  // The uploads above read host vectors owned by the handle; a layout change
-  // waits for them before the vectors can be rebuilt.
-  e = cudaStreamSynchronize(s);
-  if (e != cudaSuccess) return cuda_fail(h, e);
+  int rc = PC_OK;
+  if (!(same_geom && h->lay_tile == h->tile)) {
+    // New geometry: launch lists and record scratch.
+    h->lay_tile = -1;
+    build_layout(boxes, nboxes, h->nrec, h->tile, h->lay);
+    rc = ensure(h, h->scratch, h->scratch_cap, h->lay.scratch_doubles);
+    if (rc != PC_OK) return rc;
+    for (auto& d : h->lay.boxes) d.rec = h->scratch + reinterpret_cast<size_t>(d.rec);
+    if ((rc = ensure(h, h->d_items, h->cap_items, h->lay.items.size())) != PC_OK) return rc;
+    if ((rc = ensure(h, h->d_tiles, h->cap_tiles, h->lay.tiles.size())) != PC_OK) return rc;
+    cudaError_t e = cudaMemcpyAsync(h->d_items, h->lay.items.data(), sizeof(int2) * h->lay.items.size(),
+                                    cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(h->d_tiles, h->lay.tiles.data(), sizeof(int4) * h->lay.tiles.size(),
+                          cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) return cuda_fail(h, e);
+    // The uploads above read host vectors owned by the handle; a layout
+    // change waits for them before the vectors can be rebuilt.
+    e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_fail(h, e);
+    for (auto& t : h->tables) t.key.clear();  // their record pointers are stale
+    h->d_boxes = nullptr;
+    h->last_boxes.assign(boxes, boxes + nboxes);
+    for (int d = 0; d < 3; ++d) h->last_dx[d] = dx[d];
+    h->lay_tile = h->tile;
+  }
+  // The device box table for these array pointers.
+  pc_mol_handle::BoxTable* tb = nullptr;
+  for (auto& t : h->tables)
+    if (t.dev && (int)t.key.size() == nboxes && std::memcmp(t.key.data(), boxes, sizeof(pc_box_desc) * nboxes) == 0)
+      tb = &t;
+  if (!tb) {
+    tb = &h->tables[0];
+    for (auto& t : h->tables)
+      if (t.stamp < tb->stamp) tb = &t;
+    tb->host = h->lay.boxes;
+    for (int b = 0; b < nboxes; ++b) {
+      tb->host[b].S = boxes[b].state.p;
+      tb->host[b].R = boxes[b].rhs.p;
+    }
+    if ((rc = ensure(h, tb->dev, tb->cap, tb->host.size())) != PC_OK) return rc;
+    // Pageable source: the call returns once the data is staged, so the
+    // host vector may change afterwards; the copy is ordered on s.
+    const cudaError_t e =
+        cudaMemcpyAsync(tb->dev, tb->host.data(), sizeof(DevBox) * tb->host.size(), cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) return cuda_fail(h, e);
+    tb->key.assign(boxes, boxes + nboxes);
+  }
+  tb->stamp = ++h->table_clock;
+  h->d_boxes = tb->dev;
   h->last_boxes.assign(boxes, boxes + nboxes);
-  for (int d = 0; d < 3; ++d) h->last_dx[d] = dx[d];
-  h->lay_tile = h->tile;
   return PC_OK;
 }
 
@@ -458,7 +505,7 @@ void pc_mol_destroy(pc_mol_handle* h) {
   cudaSetDevice(h->device);
   cudaDeviceSynchronize();
   cudaFree(h->d_counters);
-  cudaFree(h->d_boxes);
+  for (auto& t : h->tables) cudaFree(t.dev);
   cudaFree(h->d_items);
   cudaFree(h->d_tiles);
   cudaFree(h->scratch);
