@@ -93,8 +93,9 @@ __device__ __forceinline__ R mix_rw(const DevMech<NS>& m, const R* Y) {
 // Y2X: X_k = Y_k (R/W_k) / (R/Wbar).
 template <int NS, class R>
 __device__ __forceinline__ void y2x(const DevMech<NS>& m, const R* Y, R rw, R* X) {
+  const R irw = 1.0 / rw;
 #pragma unroll
-  for (int k = 0; k < NS; ++k) X[k] = Y[k] * m.rW[k] / rw;
+  for (int k = 0; k < NS; ++k) X[k] = div_by(Y[k] * m.rW[k], rw, irw);  // = Y_k (R/W_k) / rw
 }
 
 // ---------------------------------------------------------------------------

@@ -22,6 +22,8 @@
 // per face: on GB300 the FP64 pipe, not HBM, bounds this computation.
 #pragma once
 
+#include <atomic>
+
 #include "pc_device.cuh"
 
 namespace pcg {
@@ -47,6 +49,7 @@ struct Geo {
   double dxinv[3];
   double area[3];
   double vol;
+  double ivol;   // 1 / vol (IEEE), the shared divisor of the divergence
   double p_ref;  // mixed precision: pressure offset of the FP32 records
 };
 
@@ -125,7 +128,7 @@ __device__ __forceinline__ void cell_record(const DevMech<NS>& m, const DevFlags
   R Y[NS];
 #pragma unroll
   for (int n = 0; n < NS; ++n) {
-    R y = U[UFS + n] / rho;
+    R y = div_by(U[UFS + n], rho, rhoinv);  // = rho Y_n / rho, correctly rounded
     if (-1e-4 * 2.220446049250313e-16 < y && y < 1e-4 * 2.220446049250313e-16) y = 0.0;
     Y[n] = y;
   }
@@ -206,45 +209,65 @@ __global__ void __launch_bounds__(kCellThreads)
 // direction d, times the face area: F[n] = flux_n * A (Riemann.H, MOL.cpp).
 // Divisions that share a divisor use div_by (exact, see pc_device.cuh).
 // ---------------------------------------------------------------------------
-template <int NS, class EOS, int d, class R>
-__device__ __forceinline__ void hydro_face(const RecAcc<R>& ra, const DevMech<NS>& m, const DevFlags& f, long long cR,
-                                           long long st, double A, R* F) {
+// MOL slopes of the cell at record index c in direction d (mol_slope,
+// MOL.H:53-112): the characteristic slopes dq[0..3] and the species slopes
+// ds[NS].  A function of the cells c - st, c and c + st only, so one
+// evaluation serves both faces of the cell.
+template <int NS, int d, class R>
+__device__ __forceinline__ void cell_slopes(const RecAcc<R>& ra, long long c, long long st, R* dq, R* ds) {
   using RC = Rec<NS>;
-  const long long cL = cR - st, cLL = cL - st, cRR = cR + st;
+  auto ld = [&](int fld, long long cc) { return ra.ld(fld, cc); };
+  const long long cm = c - st, cp = c + st;
+  const int fun = RC::U + d;
+  const int fut1 = (d == 0) ? RC::V : RC::U;
+  const int fut2 = (d == 2) ? RC::V : RC::W;
+  const R r0 = ld(RC::RHO, c), rm = ld(RC::RHO, cm), rp = ld(RC::RHO, cp);
+  const R p0 = ld(RC::P, c), pm = ld(RC::P, cm), pp = ld(RC::P, cp);
+  const R u0 = ld(fun, c), um = ld(fun, cm), up = ld(fun, cp);
+  const R c0 = ld(RC::C, c);
+  const R yc = 1.0 / c0;
+  const R dpl = p0 - pm, dpr = pp - p0;
+  {
+    const R a = div_by(0.5 * dpl, c0, yc), bb = 0.5 * r0 * (u0 - um);
+    const R a2 = div_by(0.5 * dpr, c0, yc), b2 = 0.5 * r0 * (up - u0);
+    dq[0] = mc_limit(a - bb, a2 - b2);
+    dq[1] = mc_limit(a + bb, a2 + b2);
+  }
+  {
+    const R t0 = ld(fut1, c);
+    dq[2] = mc_limit(t0 - ld(fut1, cm), ld(fut1, cp) - t0);
+    const R w0 = ld(fut2, c);
+    dq[3] = mc_limit(w0 - ld(fut2, cm), ld(fut2, cp) - w0);
+  }
+  const R c2 = c0 * c0;
+  const R yc2 = 1.0 / c2;
+#pragma unroll
+  for (int n = 0; n < NS; ++n) {
+    const R y0 = ld(RC::Y + n, c);
+    const R ry0 = r0 * y0;
+    ds[n] = mc_limit(ry0 - rm * ld(RC::Y + n, cm) - div_by(y0 * dpl, c2, yc2),
+                     rp * ld(RC::Y + n, cp) - ry0 - div_by(y0 * dpr, c2, yc2));
+  }
+}
+
+// Hyperbolic flux on the low face of the cell at record index cR in
+// direction d, times the face area, given the slopes of its two cells.
+template <int NS, class EOS, int d, class R>
+__device__ __forceinline__ void hydro_face_sl(const RecAcc<R>& ra, const DevMech<NS>& m, const DevFlags& f,
+                                              long long cR, long long st, double A, const R* dqL, const R* dsL,
+                                              const R* dqR, const R* dsR, R* F) {
+  using RC = Rec<NS>;
+  const long long cL = cR - st;
   auto ld = [&](int fld, long long c) { return ra.ld(fld, c); };
   const int fun = RC::U + d;
   const int fut1 = (d == 0) ? RC::V : RC::U;
   const int fut2 = (d == 2) ? RC::V : RC::W;
-  const R rLL = ld(RC::RHO, cLL), rL = ld(RC::RHO, cL), rR = ld(RC::RHO, cR), rRR = ld(RC::RHO, cRR);
-  const R pLL = ld(RC::P, cLL), pL = ld(RC::P, cL), pR = ld(RC::P, cR), pRR = ld(RC::P, cRR);
-  const R uLL = ld(fun, cLL), uL = ld(fun, cL), uR = ld(fun, cR), uRR = ld(fun, cRR);
+  const R rL = ld(RC::RHO, cL), rR = ld(RC::RHO, cR);
+  const R pL = ld(RC::P, cL), pR = ld(RC::P, cR);
+  const R uL = ld(fun, cL), uR = ld(fun, cR);
   const R cLc = ld(RC::C, cL), cRc = ld(RC::C, cR);
   const R t1L = ld(fut1, cL), t1R = ld(fut1, cR), t2L = ld(fut2, cL), t2R = ld(fut2, cR);
   const R ycL = 1.0 / cLc, ycR = 1.0 / cRc;
-
-  // Characteristic slopes of cells L and R (mol_slope, MOL.H:53-112).
-  R dqL[4] = {0.0, 0.0, 0.0, 0.0}, dqR[4] = {0.0, 0.0, 0.0, 0.0};
-  const bool slopes = f.slopes != 0;
-  const R dpl = pL - pLL, dpc = pR - pL, dpr = pRR - pR;
-  if (slopes) {
-    const R t1LL = ld(fut1, cLL), t1RR = ld(fut1, cRR), t2LL = ld(fut2, cLL), t2RR = ld(fut2, cRR);
-    {
-      const R a = div_by(0.5 * dpl, cLc, ycL), bb = 0.5 * rL * (uL - uLL);
-      const R a2 = div_by(0.5 * dpc, cLc, ycL), b2 = 0.5 * rL * (uR - uL);
-      dqL[0] = mc_limit(a - bb, a2 - b2);
-      dqL[1] = mc_limit(a + bb, a2 + b2);
-      dqL[2] = mc_limit(t1L - t1LL, t1R - t1L);
-      dqL[3] = mc_limit(t2L - t2LL, t2R - t2L);
-    }
-    {
-      const R a = div_by(0.5 * dpc, cRc, ycR), bb = 0.5 * rR * (uR - uL);
-      const R a2 = div_by(0.5 * dpr, cRc, ycR), b2 = 0.5 * rR * (uRR - uR);
-      dqR[0] = mc_limit(a - bb, a2 - b2);
-      dqR[1] = mc_limit(a + bb, a2 + b2);
-      dqR[2] = mc_limit(t1R - t1L, t1RR - t1R);
-      dqR[3] = mc_limit(t2R - t2L, t2RR - t2R);
-    }
-  }
   // Face states (MOL.cpp:69-123).
   const R unl = uL + 0.5 * ((dqL[1] - dqL[0]) / rL);
   const R pl = pL + 0.5 * (dqL[0] + dqL[1]) * cLc;
@@ -258,19 +281,11 @@ __device__ __forceinline__ void hydro_face(const RecAcc<R>& ra, const DevMech<NS
   R rl = 0.0, rr = 0.0;
   {
     const R sL = dqL[0] + dqL[1], sR = dqR[0] + dqR[1];
-    const R cL2 = cLc * cLc, cR2 = cRc * cRc;
-    const R ycL2 = 1.0 / cL2, ycR2 = 1.0 / cR2;
 #pragma unroll
     for (int n = 0; n < NS; ++n) {
-      const R yLL = ld(RC::Y + n, cLL), yL = ld(RC::Y + n, cL), yR = ld(RC::Y + n, cR), yRR = ld(RC::Y + n, cRR);
-      R dsL = 0.0, dsR = 0.0;
-      if (slopes) {
-        const R ryL = rL * yL, ryR = rR * yR;
-        dsL = mc_limit(ryL - rLL * yLL - div_by(yL * dpl, cL2, ycL2), ryR - ryL - div_by(yL * dpc, cL2, ycL2));
-        dsR = mc_limit(ryR - ryL - div_by(yR * dpc, cR2, ycR2), rRR * yRR - ryR - div_by(yR * dpr, cR2, ycR2));
-      }
-      spl[n] = yL * rL + 0.5 * (dsL + div_by(yL * sL, cLc, ycL));
-      spr[n] = yR * rR - 0.5 * (dsR + div_by(yR * sR, cRc, ycR));
+      const R yL = ld(RC::Y + n, cL), yR = ld(RC::Y + n, cR);
+      spl[n] = yL * rL + 0.5 * (dsL[n] + div_by(yL * sL, cLc, ycL));
+      spr[n] = yR * rR - 0.5 * (dsR[n] + div_by(yR * sR, cRc, ycR));
       rl += spl[n];
       rr += spr[n];
     }
@@ -413,6 +428,23 @@ __device__ __forceinline__ void hydro_face(const RecAcc<R>& ra, const DevMech<NS
   for (int n = 0; n < NS; ++n) F[UFS + n] = flY[n] * A;
 }
 
+// Hyperbolic flux on the low face of the cell at record index cR in
+// direction d, times the face area: F[n] = flux_n * A (Riemann.H, MOL.cpp),
+// with the slopes of both cells evaluated here.
+template <int NS, class EOS, int d, class R>
+__device__ __forceinline__ void hydro_face(const RecAcc<R>& ra, const DevMech<NS>& m, const DevFlags& f, long long cR,
+                                           long long st, double A, R* F) {
+  R dqL[4] = {0.0, 0.0, 0.0, 0.0}, dqR[4] = {0.0, 0.0, 0.0, 0.0};
+  R dsL[NS], dsR[NS];
+#pragma unroll
+  for (int n = 0; n < NS; ++n) dsL[n] = dsR[n] = 0.0;
+  if (f.slopes) {
+    cell_slopes<NS, d>(ra, cR - st, st, dqL, dsL);
+    cell_slopes<NS, d>(ra, cR, st, dqR, dsR);
+  }
+  hydro_face_sl<NS, EOS, d>(ra, m, f, cR, st, A, dqL, dsL, dqR, dsR, F);
+}
+
 // pc_diffusion_flux + SpeciesEnergyFlux (Diffterm.H:20-75, 344-461), times
 // the area, added to the hyperbolic flux already in F (the reference stores
 // the diffusion flux and adds the hyperbolic one, MOL.cpp:199-201; the sum of
@@ -504,6 +536,10 @@ struct Tile {
   static constexpr int TX = TX_, TY = TY_, TZ = TZ_, MINB = MINB_, NT = TX_ * TY_ * TZ_;
   static constexpr int F0 = (TX_ + 1) * TY_ * TZ_, F1 = TX_ * (TY_ + 1) * TZ_, F2 = TX_ * TY_ * (TZ_ + 1);
   static constexpr int MAXF = F0 > F1 ? (F0 > F2 ? F0 : F2) : (F1 > F2 ? F1 : F2);
+  // cells whose slopes a direction pass needs: the tile plus one layer on
+  // each side in that direction
+  static constexpr int C0 = (TX_ + 2) * TY_ * TZ_, C1 = TX_ * (TY_ + 2) * TZ_, C2 = TX_ * TY_ * (TZ_ + 2);
+  static constexpr int MAXC = C0 > C1 ? (C0 > C2 ? C0 : C2) : (C1 > C2 ? C1 : C2);
   static constexpr bool DYN = TX_ * TY_ * TZ_ > 256;
 };
 // The tile shapes the level autotuner chooses from (index = PC_TILE_* order).
@@ -525,21 +561,54 @@ __device__ __forceinline__ void dir_pass(const DevBox& b, const DevMech<NS>& m, 
                                          const int o[3], const int ext[3], const long long stv[3], bool mine, int tx,
                                          int ty, int tz, double* fbuf, double* acc) {
   constexpr int NVAR = 7 + NS;
+  constexpr int NSL = 4 + NS;  // slope fields of a cell
+  const RecAcc<double> ra{b.rec, b.ncell};
   const bool diff = f.diffuse_vel || f.diffuse_temp || f.diffuse_spec || f.diffuse_enth;
+  const bool slopes = f.do_hydro && f.slopes;
+  // Slopes of every cell of the tile and of its two neighbour layers in d,
+  // each evaluated once: field q of cell ci at sbuf[q MAXC + ci].
+  double* sbuf = fbuf + NVAR * TL::MAXF;
+  const int ne0 = ext[0] + 2 * (d == 0), ne1 = ext[1] + 2 * (d == 1), ne2 = ext[2] + 2 * (d == 2);
+  if (slopes) {
+    const int ncells = ne0 * ne1 * ne2;
+    for (int ci = threadIdx.x; ci < ncells; ci += TL::NT) {
+      const int ex = ci % ne0, ey = (ci / ne0) % ne1, ez = ci / (ne0 * ne1);
+      const int i = o[0] + ex - (d == 0), j = o[1] + ey - (d == 1), k = o[2] + ez - (d == 2);
+      const long long c = (i - b.g2lo[0]) + (j - b.g2lo[1]) * stv[1] + (k - b.g2lo[2]) * stv[2];
+      double sl[NSL];
+      cell_slopes<NS, d>(ra, c, stv[d], sl, sl + 4);
+#pragma unroll
+      for (int q = 0; q < NSL; ++q) sbuf[q * TL::MAXC + ci] = sl[q];
+    }
+    __syncthreads();
+  }
   const int nf0 = ext[0] + (d == 0), nf1 = ext[1] + (d == 1), nf2 = ext[2] + (d == 2);
   const int nfaces = nf0 * nf1 * nf2;
+  const int cstep = (d == 0) ? 1 : (d == 1) ? ne0 : ne0 * ne1;
   for (int fi = threadIdx.x; fi < nfaces; fi += TL::NT) {
     const int fx = fi % nf0, fy = (fi / nf0) % nf1, fz = fi / (nf0 * nf1);
     const int i = o[0] + fx, j = o[1] + fy, k = o[2] + fz;
     const long long cR = (i - b.g2lo[0]) + (j - b.g2lo[1]) * stv[1] + (k - b.g2lo[2]) * stv[2];
     double F[NVAR];
     if (f.do_hydro) {
-      hydro_face<NS, EOS, d>(RecAcc<double>{b.rec, b.ncell}, m, f, cR, stv[d], g.area[d], F);
+      double sL[NSL], sR[NSL];
+      if (slopes) {
+        const int ciL = fx + ne0 * (fy + ne1 * fz);  // the low cell's slot; the high cell is one step on
+#pragma unroll
+        for (int q = 0; q < NSL; ++q) {
+          sL[q] = sbuf[q * TL::MAXC + ciL];
+          sR[q] = sbuf[q * TL::MAXC + ciL + cstep];
+        }
+      } else {
+#pragma unroll
+        for (int q = 0; q < NSL; ++q) sL[q] = sR[q] = 0.0;
+      }
+      hydro_face_sl<NS, EOS, d>(ra, m, f, cR, stv[d], g.area[d], sL, sL + 4, sR, sR + 4, F);
     } else {
 #pragma unroll
       for (int n = 0; n < NVAR; ++n) F[n] = 0.0;
     }
-    if (diff) diffusion_face<NS, EOS, d>(RecAcc<double>{b.rec, b.ncell}, f, g, cR, stv, F);
+    if (diff) diffusion_face<NS, EOS, d>(ra, f, g, cR, stv, F);
 #pragma unroll
     for (int n = 0; n < NVAR; ++n) fbuf[n * TL::MAXF + fi] = F[n];
   }
@@ -553,19 +622,19 @@ __device__ __forceinline__ void dir_pass(const DevBox& b, const DevMech<NS>& m, 
   __syncthreads();
 }
 
+// Dynamic shared memory of the FP64 flux pass: face fluxes and cell slopes.
+template <int NS, class TL>
+constexpr size_t flux_smem_bytes() {
+  return sizeof(double) * ((size_t)(7 + NS) * TL::MAXF + (size_t)(4 + NS) * TL::MAXC);
+}
+
 template <int NS, class EOS, class TL = TileDefault>
 __global__ void __launch_bounds__(TL::NT, TL::MINB)
     flux_kernel(const DevBox* __restrict__ boxes, const int4* __restrict__ tiles, const __grid_constant__ DevMech<NS> m,
                 const DevFlags f, const Geo g, unsigned long long* __restrict__ counters) {
   constexpr int NVAR = 7 + NS;
-  double* fbuf;
-  if constexpr (TL::DYN) {
-    extern __shared__ double flux_dyn_smem[];
-    fbuf = flux_dyn_smem;
-  } else {
-    __shared__ double flux_static_smem[NVAR * TL::MAXF];
-    fbuf = flux_static_smem;
-  }
+  extern __shared__ double flux_dyn_smem[];
+  double* fbuf = flux_dyn_smem;
   const int4 t = tiles[blockIdx.x];
   const DevBox& b = boxes[t.x];
   const int o[3] = {t.y, t.z, t.w};
@@ -585,7 +654,7 @@ __global__ void __launch_bounds__(TL::NT, TL::MINB)
     double* r = b.R + (i - b.rb[0]) + (long long)(j - b.rb[1]) * b.rj + (long long)(k - b.rb[2]) * b.rk;
 #pragma unroll
     for (int n = 0; n < NVAR; ++n) {
-      const double v = acc[n] / g.vol;
+      const double v = div_by(acc[n], g.vol, g.ivol);  // = acc[n] / vol, correctly rounded
       bad |= !isfinite(v);
       r[n * b.rn] = v;
     }
@@ -594,6 +663,26 @@ __global__ void __launch_bounds__(TL::NT, TL::MINB)
   if (threadIdx.x == 0) {
     atomicAdd(&counters[kCounterCells], (unsigned long long)(ext[0] * ext[1] * ext[2]));
   }
+}
+
+// Host: opt the flux kernel into its dynamic shared memory (more than the
+// default 48 KB) on the current device, once per device; then launch it.
+template <int NS, class EOS, class TL = TileDefault>
+inline cudaError_t launch_flux_fp64(const DevBox* boxes, const int4* tiles, int ntiles, const DevMech<NS>& m,
+                                    const DevFlags& f, const Geo& g, unsigned long long* counters, cudaStream_t s) {
+  static std::atomic<unsigned long long> opted{0};  // bit per device
+  constexpr size_t smem = flux_smem_bytes<NS, TL>();
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  const unsigned long long bit = (dev >= 0 && dev < 64) ? (1ull << dev) : 0ull;
+  if (!bit || !(opted.load() & bit)) {
+    e = cudaFuncSetAttribute(flux_kernel<NS, EOS, TL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    opted.fetch_or(bit);
+  }
+  if (ntiles > 0) flux_kernel<NS, EOS, TL><<<ntiles, TL::NT, smem, s>>>(boxes, tiles, m, f, g, counters);
+  return cudaGetLastError();
 }
 
 }  // namespace pcg

@@ -354,6 +354,7 @@ Geo make_geo(const double dx[3]) {
   g.area[1] = dx[0] * dx[2];
   g.area[2] = dx[0] * dx[1];
   g.vol = dx[0] * dx[1] * dx[2];
+  g.ivol = 1.0 / g.vol;
   g.p_ref = 0.0;
   return g;
 }
@@ -373,11 +374,10 @@ int launch(pc_mol_handle* h, const DevMech<NS>& mech, const Geo& g, int ibeg, in
     if (e != cudaSuccess) return cuda_fail(h, e);
     return cuda_fail(h, cudaGetLastError());
   }
-  if (tend > tbeg)
-    flux_kernel<NS, EOS><<<tend - tbeg, kFluxThreads, 0, s>>>(h->d_boxes, h->d_tiles + tbeg, mech, h->flags, g,
-                                                              h->d_counters);
+  const cudaError_t e =
+      launch_flux_fp64<NS, EOS>(h->d_boxes, h->d_tiles + tbeg, tend - tbeg, mech, h->flags, g, h->d_counters, s);
   if (timed) cudaEventRecord(h->ev[2], s);
-  return cuda_fail(h, cudaGetLastError());
+  return cuda_fail(h, e);
 }
 
 int run(pc_mol_handle* h, const pc_box_desc* boxes, int nboxes, const double dx[3], void* stream, bool per_box) {
@@ -780,11 +780,13 @@ extern "C" int pc_mol_rhs_box_static(const pc_mol_config* cfg, const pc_box_desc
   if (variant == 1) {
     cell_kernel<1, GammaLawEos<1>, ConstantTransport<1>><<<(unsigned)nitems, kCellThreads, 0, s>>>(dbox, items, mech1,
                                                                                                    fl, ctr);
-    flux_kernel<1, GammaLawEos<1>><<<(unsigned)ntiles, kFluxThreads, 0, s>>>(dbox, tiles, mech1, fl, g, ctr);
+    if (launch_flux_fp64<1, GammaLawEos<1>>(dbox, tiles, (int)ntiles, mech1, fl, g, ctr, s) != cudaSuccess)
+      return PC_ERR_CUDA;
   } else {
     cell_kernel<9, IdealMixEos<9>, SimpleTransport<9>><<<(unsigned)nitems, kCellThreads, 0, s>>>(dbox, items, mech9,
                                                                                                  fl, ctr);
-    flux_kernel<9, IdealMixEos<9>><<<(unsigned)ntiles, kFluxThreads, 0, s>>>(dbox, tiles, mech9, fl, g, ctr);
+    if (launch_flux_fp64<9, IdealMixEos<9>>(dbox, tiles, (int)ntiles, mech9, fl, g, ctr, s) != cudaSuccess)
+      return PC_ERR_CUDA;
   }
   return cudaGetLastError() == cudaSuccess ? PC_OK : PC_ERR_CUDA;
 }

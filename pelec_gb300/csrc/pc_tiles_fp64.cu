@@ -12,14 +12,7 @@ namespace {
 template <int NS, class EOS, class TL>
 cudaError_t flux_at(const DevBox* boxes, const int4* tiles, int ntiles, const DevMech<NS>& m, const DevFlags& f,
                     const Geo& g, unsigned long long* counters, cudaStream_t s) {
-  constexpr size_t smem = TL::DYN ? sizeof(double) * (7 + NS) * TL::MAXF : 0;
-  if (TL::DYN) {
-    const cudaError_t e =
-        cudaFuncSetAttribute(flux_kernel<NS, EOS, TL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-  }
-  flux_kernel<NS, EOS, TL><<<ntiles, TL::NT, smem, s>>>(boxes, tiles, m, f, g, counters);
-  return cudaGetLastError();
+  return launch_flux_fp64<NS, EOS, TL>(boxes, tiles, ntiles, m, f, g, counters, s);
 }
 
 template <int NS, class EOS>
