@@ -201,6 +201,15 @@ int pc_mol_rhs_level(pc_mol_handle* h, const pc_box_desc* boxes, int nboxes,
 int pc_mol_rhs_level_per_box(pc_mol_handle* h, const pc_box_desc* boxes,
                              int nboxes, const double dx[3], void* stream);
 
+/* pc_mol_rhs_level that also writes the face fluxes — the hyperbolic plus
+ * diffusion flux times the face area, all NVAR components — that
+ * getMOLSrcTerm hands to the flux registers for refluxing on multi-level
+ * runs (Diffusion.cpp:652-670).  fluxes[3*b + d] covers
+ * surroundingNodes(valid_b, d); the RHS is the same as without the export.
+ * PC_PRECISION_FP64 only.  Asynchronous on stream. */
+int pc_mol_rhs_level_fluxes(pc_mol_handle* h, const pc_box_desc* boxes, int nboxes, const double dx[3],
+                            const pc_array4* fluxes, void* stream);
+
 /* Synchronize the handle's last stream and copy the diagnostic counters of
  * the last rhs call into *st. */
 int pc_mol_last_status(pc_mol_handle* h, pc_mol_status* st);

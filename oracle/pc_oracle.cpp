@@ -28,7 +28,7 @@ bool covers(const pc_array4& a, const Box& b) {
 
 template <int NS, class EOS, class TR>
 int run_box(const pc_mol_config& cfg, const EOS& eos, const TR& tr, const pc_box_desc& bd, const double dx[3],
-            long long& fails) {
+            long long& fails, const pc_array4* fluxes) {
   Box vbox;
   for (int d = 0; d < 3; ++d) { vbox.lo[d] = bd.lo[d]; vbox.hi[d] = bd.hi[d]; }
   // The reference computes primitives on grow(vbox, 4); the state FAB must
@@ -42,23 +42,33 @@ int run_box(const pc_mol_config& cfg, const EOS& eos, const TR& tr, const pc_box
   sc.ks = s.ks;
   sc.ns = s.ns;
   for (int d = 0; d < 3; ++d) sc.b[d] = s.b[d];
-  mol_rhs_box<NS>(cfg, eos, tr, vbox, sc, view(bd.rhs), dx, fails);
+  if (fluxes) {
+    Arr<double> fo[3];
+    for (int d = 0; d < 3; ++d) {
+      if (!covers(fluxes[d], surrounding_nodes(vbox, d)) || fluxes[d].ncomp < 7 + NS) return PC_ERR_INVALID_ARGUMENT;
+      fo[d] = view(fluxes[d]);
+    }
+    mol_rhs_box<NS>(cfg, eos, tr, vbox, sc, view(bd.rhs), dx, fails, fo);
+  } else {
+    mol_rhs_box<NS>(cfg, eos, tr, vbox, sc, view(bd.rhs), dx, fails);
+  }
   return PC_OK;
 }
 
 template <int NS>
-int dispatch(const pc_mol_config& cfg, const pc_box_desc& bd, const double dx[3], long long& fails) {
+int dispatch(const pc_mol_config& cfg, const pc_box_desc& bd, const double dx[3], long long& fails,
+             const pc_array4* fluxes = nullptr) {
   const int maxit = cfg.newton_max_iter > 0 ? cfg.newton_max_iter : 50;
   if (cfg.eos == PC_EOS_GAMMA_LAW) {
     GammaLaw<NS> eos{&cfg.mech};
     if (cfg.transport == PC_TRANSPORT_CONSTANT)
-      return run_box<NS>(cfg, eos, ConstantTransport<NS, GammaLaw<NS>>{&cfg.mech}, bd, dx, fails);
-    return run_box<NS>(cfg, eos, SimpleTransport<NS, GammaLaw<NS>>{&cfg.mech}, bd, dx, fails);
+      return run_box<NS>(cfg, eos, ConstantTransport<NS, GammaLaw<NS>>{&cfg.mech}, bd, dx, fails, fluxes);
+    return run_box<NS>(cfg, eos, SimpleTransport<NS, GammaLaw<NS>>{&cfg.mech}, bd, dx, fails, fluxes);
   }
   IdealMix<NS> eos{&cfg.mech, maxit};
   if (cfg.transport == PC_TRANSPORT_CONSTANT)
-    return run_box<NS>(cfg, eos, ConstantTransport<NS, IdealMix<NS>>{&cfg.mech}, bd, dx, fails);
-  return run_box<NS>(cfg, eos, SimpleTransport<NS, IdealMix<NS>>{&cfg.mech}, bd, dx, fails);
+    return run_box<NS>(cfg, eos, ConstantTransport<NS, IdealMix<NS>>{&cfg.mech}, bd, dx, fails, fluxes);
+  return run_box<NS>(cfg, eos, SimpleTransport<NS, IdealMix<NS>>{&cfg.mech}, bd, dx, fails, fluxes);
 }
 
 template <int NS, class EOS>
@@ -94,6 +104,26 @@ int oracle_mol_rhs(const pc_mol_config* cfg, const pc_box_desc* boxes, int nboxe
     if (rc != PC_OK) return rc;
   }
   if (newton_fail) *newton_fail = fails;
+  return PC_OK;
+}
+
+// RHS of each box plus its face fluxes (fluxes[3 b + dir] on
+// surroundingNodes(valid, dir)).
+int oracle_mol_rhs_fluxes(const pc_mol_config* cfg, const pc_box_desc* boxes, int nboxes, const double dx[3],
+                          const pc_array4* fluxes, int nthreads) {
+  if (!cfg || !boxes || nboxes < 0 || !dx || !fluxes) return PC_ERR_INVALID_ARGUMENT;
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+  long long fails = 0;
+  for (int b = 0; b < nboxes; ++b) {
+    int rc;
+    if (cfg->nspec == 1)
+      rc = dispatch<1>(*cfg, boxes[b], dx, fails, fluxes + 3 * b);
+    else if (cfg->nspec == 9)
+      rc = dispatch<9>(*cfg, boxes[b], dx, fails, fluxes + 3 * b);
+    else
+      return PC_ERR_UNSUPPORTED;
+    if (rc != PC_OK) return rc;
+  }
   return PC_OK;
 }
 

@@ -773,7 +773,7 @@ inline void hyp_mol_flux(const Box& cbox, const Arr<double>& q, const Arr<double
 template <int NS, class EOS, class TRANS>
 inline void mol_rhs_box(const pc_mol_config& cfg, const EOS& eos, const TRANS& trans, const Box& vbox,
                         const Arr<const double>& sar, const Arr<double>& rhs, const double dx[3],
-                        long long& newton_fail) {
+                        long long& newton_fail, const Arr<double>* flux_out = nullptr) {
   const int NVAR = 7 + NS, QVAR = 8 + NS, nCompTr = NS + 3;
   if (!cfg.diffuse_temp && !cfg.diffuse_enth && !cfg.diffuse_spec && !cfg.diffuse_vel && !cfg.do_hydro) {
     for_box(vbox, [&](int i, int j, int k) {
@@ -839,6 +839,13 @@ inline void mol_rhs_box(const pc_mol_config& cfg, const EOS& eos, const TRANS& t
   for_box(vbox, [&](int i, int j, int k) {
     for (int n = 0; n < NVAR; ++n) rhs(i, j, k, n) = Dterm(i, j, k, n);
   });
+  // The fluxes getMOLSrcTerm hands to the flux registers for refluxing
+  // (Diffusion.cpp:652-670), on surroundingNodes(vbox, dir).
+  if (flux_out)
+    for (int dir = 0; dir < 3; ++dir)
+      for_box(surrounding_nodes(vbox, dir), [&](int i, int j, int k) {
+        for (int n = 0; n < NVAR; ++n) flux_out[dir](i, j, k, n) = flx[dir](i, j, k, n);
+      });
 }
 
 // ---------------------------------------------------------------------------

@@ -89,6 +89,31 @@ def mol_rhs_sub(cfg: abi.PcMolConfig, S: np.ndarray, fab_begin, lo, hi, dx, nthr
     return R
 
 
+def mol_rhs_fluxes(cfg: abi.PcMolConfig, boxes, nthreads: int = 0):
+    """(RHS, [Fx, Fy, Fz]) of each BoxState: the face fluxes times the face
+    area on surroundingNodes(valid, d), each (NVAR, nz(+1), ny(+1), nx(+1))."""
+    lib = library()
+    lib.oracle_mol_rhs_fluxes.argtypes = [POINTER(abi.PcMolConfig), POINTER(abi.PcBoxDesc), c_int,
+                                          POINTER(c_double), POINTER(abi.PcArray4), c_int]
+    descs, outs, farr = [], [], []
+    for st in boxes:
+        S = np.ascontiguousarray(st.S, dtype=np.float64)
+        nx, ny, nz = st.shape
+        R = np.zeros((S.shape[0], nz, ny, nx))
+        descs.append(abi.box_desc(st.lo, st.hi, abi.array4(S.ctypes.data, S.shape, st.begin),
+                                  abi.array4(R.ctypes.data, R.shape, st.lo)))
+        F = [np.zeros((S.shape[0], nz + (d == 2), ny + (d == 1), nx + (d == 0))) for d in range(3)]
+        farr += [abi.array4(f.ctypes.data, f.shape, st.lo) for f in F]
+        outs.append((S, R, F))
+    arr = abi.box_array(descs)
+    fx = (abi.PcArray4 * len(farr))(*farr)
+    dx = (c_double * 3)(*boxes[0].dx)
+    rc = lib.oracle_mol_rhs_fluxes(ctypes.byref(cfg), arr, len(descs), dx, fx, int(nthreads))
+    if rc != 0:
+        raise RuntimeError(f"oracle_mol_rhs_fluxes failed with code {rc}")
+    return [(R, F) for _, R, F in outs]
+
+
 def ctoprim_cell(cfg: abi.PcMolConfig, U: np.ndarray):
     U = np.ascontiguousarray(U, dtype=np.float64)
     q = np.zeros(8 + cfg.nspec)

@@ -88,6 +88,16 @@ struct TanBox {
   double* trec;
 };
 
+// Face-flux outputs of one box (refluxing): direction d's fluxes, times the
+// face area, on surroundingNodes(valid, d): face (i,j,k), component n at
+// p[d][(i-b[d][0]) + (j-b[d][1]) js[d] + (k-b[d][2]) ks[d] + n ns[d]].
+struct FluxBox {
+  double* p[3];
+  long long js[3], ks[3], ns[3];
+  int b[3][3];
+  int pad;
+};
+
 enum { kCounterCells = 0, kCounterNewton = 1, kCounterNonpos = 2, kCounterNonfinite = 3, kNumCounters = 4 };
 
 __device__ __forceinline__ void warp_count(unsigned long long* ctr, bool pred) {
@@ -559,7 +569,7 @@ constexpr int kMaxFaces = TileDefault::MAXF;
 template <int NS, class EOS, int d, class TL>
 __device__ __forceinline__ void dir_pass(const DevBox& b, const DevMech<NS>& m, const DevFlags& f, const Geo& g,
                                          const int o[3], const int ext[3], const long long stv[3], bool mine, int tx,
-                                         int ty, int tz, double* fbuf, double* acc) {
+                                         int ty, int tz, double* fbuf, double* acc, const FluxBox* fxb) {
   constexpr int NVAR = 7 + NS;
   constexpr int NSL = 4 + NS;  // slope fields of a cell
   const RecAcc<double> ra{b.rec, b.ncell};
@@ -611,6 +621,12 @@ __device__ __forceinline__ void dir_pass(const DevBox& b, const DevMech<NS>& m, 
     if (diff) diffusion_face<NS, EOS, d>(ra, f, g, cR, stv, F);
 #pragma unroll
     for (int n = 0; n < NVAR; ++n) fbuf[n * TL::MAXF + fi] = F[n];
+    if (fxb) {  // export (a face shared by two tiles is written twice, with the same value)
+      double* q = fxb->p[d] + (i - fxb->b[d][0]) + (long long)(j - fxb->b[d][1]) * fxb->js[d] +
+                  (long long)(k - fxb->b[d][2]) * fxb->ks[d];
+#pragma unroll
+      for (int n = 0; n < NVAR; ++n) q[n * fxb->ns[d]] = F[n];
+    }
   }
   __syncthreads();
   if (mine) {
@@ -631,7 +647,8 @@ constexpr size_t flux_smem_bytes() {
 template <int NS, class EOS, class TL = TileDefault>
 __global__ void __launch_bounds__(TL::NT, TL::MINB)
     flux_kernel(const DevBox* __restrict__ boxes, const int4* __restrict__ tiles, const __grid_constant__ DevMech<NS> m,
-                const DevFlags f, const Geo g, unsigned long long* __restrict__ counters) {
+                const DevFlags f, const Geo g, unsigned long long* __restrict__ counters,
+                const FluxBox* __restrict__ fluxes) {
   constexpr int NVAR = 7 + NS;
   extern __shared__ double flux_dyn_smem[];
   double* fbuf = flux_dyn_smem;
@@ -645,9 +662,10 @@ __global__ void __launch_bounds__(TL::NT, TL::MINB)
   double acc[NVAR];
 #pragma unroll
   for (int n = 0; n < NVAR; ++n) acc[n] = 0.0;
-  dir_pass<NS, EOS, 0, TL>(b, m, f, g, o, ext, stv, mine, tx, ty, tz, fbuf, acc);
-  dir_pass<NS, EOS, 1, TL>(b, m, f, g, o, ext, stv, mine, tx, ty, tz, fbuf, acc);
-  dir_pass<NS, EOS, 2, TL>(b, m, f, g, o, ext, stv, mine, tx, ty, tz, fbuf, acc);
+  const FluxBox* fxb = fluxes ? fluxes + t.x : nullptr;
+  dir_pass<NS, EOS, 0, TL>(b, m, f, g, o, ext, stv, mine, tx, ty, tz, fbuf, acc, fxb);
+  dir_pass<NS, EOS, 1, TL>(b, m, f, g, o, ext, stv, mine, tx, ty, tz, fbuf, acc, fxb);
+  dir_pass<NS, EOS, 2, TL>(b, m, f, g, o, ext, stv, mine, tx, ty, tz, fbuf, acc, fxb);
   bool bad = false;
   if (mine) {
     const int i = o[0] + tx, j = o[1] + ty, k = o[2] + tz;
@@ -669,7 +687,8 @@ __global__ void __launch_bounds__(TL::NT, TL::MINB)
 // default 48 KB) on the current device, once per device; then launch it.
 template <int NS, class EOS, class TL = TileDefault>
 inline cudaError_t launch_flux_fp64(const DevBox* boxes, const int4* tiles, int ntiles, const DevMech<NS>& m,
-                                    const DevFlags& f, const Geo& g, unsigned long long* counters, cudaStream_t s) {
+                                    const DevFlags& f, const Geo& g, unsigned long long* counters, cudaStream_t s,
+                                    const FluxBox* fluxes = nullptr) {
   static std::atomic<unsigned long long> opted{0};  // bit per device
   constexpr size_t smem = flux_smem_bytes<NS, TL>();
   int dev = 0;
@@ -681,7 +700,7 @@ inline cudaError_t launch_flux_fp64(const DevBox* boxes, const int4* tiles, int 
     if (e != cudaSuccess) return e;
     opted.fetch_or(bit);
   }
-  if (ntiles > 0) flux_kernel<NS, EOS, TL><<<ntiles, TL::NT, smem, s>>>(boxes, tiles, m, f, g, counters);
+  if (ntiles > 0) flux_kernel<NS, EOS, TL><<<ntiles, TL::NT, smem, s>>>(boxes, tiles, m, f, g, counters, fluxes);
   return cudaGetLastError();
 }
 

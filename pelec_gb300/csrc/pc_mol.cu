@@ -26,7 +26,7 @@ int launch_mixed(int variant, int tile, const DevBox* boxes, const int2* items, 
                  unsigned long long* counters, cudaStream_t s, cudaEvent_t e0, cudaEvent_t e1, cudaEvent_t e2);
 cudaError_t launch_flux_fp64_tile(int tile, int variant, const DevBox* boxes, const int4* tiles, int ntiles,
                                   const DevMech<1>& m1, const DevMech<9>& m9, const DevFlags& f, const Geo& g,
-                                  unsigned long long* counters, cudaStream_t s);
+                                  unsigned long long* counters, cudaStream_t s, const FluxBox* fx);
 cudaError_t launch_vjp_passes(int variant, const DevBox* boxes, const AdjBox* adj, const int2* items, int nitems,
                               const int4* fitems, int nfitems, double* recbar, const long long* recbar_off,
                               const DevMech<1>& m1, const DevMech<9>& m9, const DevFlags& f, const Geo& g,
@@ -361,7 +361,7 @@ Geo make_geo(const double dx[3]) {
 
 template <int NS, class EOS, class TR>
 int launch(pc_mol_handle* h, const DevMech<NS>& mech, const Geo& g, int ibeg, int iend, int tbeg, int tend,
-           cudaStream_t s, bool timed) {
+           cudaStream_t s, bool timed, const FluxBox* fx) {
   if (timed) cudaEventRecord(h->ev[0], s);
   if (iend > ibeg)
     cell_kernel<NS, EOS, TR><<<iend - ibeg, kCellThreads, 0, s>>>(h->d_boxes, h->d_items + ibeg, mech, h->flags,
@@ -369,18 +369,19 @@ int launch(pc_mol_handle* h, const DevMech<NS>& mech, const Geo& g, int ibeg, in
   if (timed) cudaEventRecord(h->ev[1], s);
   if (h->lay_tile != 0) {
     const cudaError_t e = launch_flux_fp64_tile(h->lay_tile, h->variant, h->d_boxes, h->d_tiles + tbeg, tend - tbeg,
-                                                h->mech1, h->mech9, h->flags, g, h->d_counters, s);
+                                                h->mech1, h->mech9, h->flags, g, h->d_counters, s, fx);
     if (timed) cudaEventRecord(h->ev[2], s);
     if (e != cudaSuccess) return cuda_fail(h, e);
     return cuda_fail(h, cudaGetLastError());
   }
   const cudaError_t e =
-      launch_flux_fp64<NS, EOS>(h->d_boxes, h->d_tiles + tbeg, tend - tbeg, mech, h->flags, g, h->d_counters, s);
+      launch_flux_fp64<NS, EOS>(h->d_boxes, h->d_tiles + tbeg, tend - tbeg, mech, h->flags, g, h->d_counters, s, fx);
   if (timed) cudaEventRecord(h->ev[2], s);
   return cuda_fail(h, e);
 }
 
-int run(pc_mol_handle* h, const pc_box_desc* boxes, int nboxes, const double dx[3], void* stream, bool per_box) {
+int run(pc_mol_handle* h, const pc_box_desc* boxes, int nboxes, const double dx[3], void* stream, bool per_box,
+        const FluxBox* fx = nullptr) {
   if (!h) return PC_ERR_INVALID_ARGUMENT;
   if (nboxes < 0 || (nboxes > 0 && !boxes) || !dx) return h->last_error = PC_ERR_INVALID_ARGUMENT;
   for (int d = 0; d < 3; ++d)
@@ -410,8 +411,8 @@ int run(pc_mol_handle* h, const pc_box_desc* boxes, int nboxes, const double dx[
       return rc == 0 ? PC_OK : cuda_fail(h, cudaGetLastError());
     }
     if (h->variant == 1)
-      return launch<1, GammaLawEos<1>, ConstantTransport<1>>(h, h->mech1, g, ib, ie, tb, te, s, timed);
-    return launch<9, IdealMixEos<9>, SimpleTransport<9>>(h, h->mech9, g, ib, ie, tb, te, s, timed);
+      return launch<1, GammaLawEos<1>, ConstantTransport<1>>(h, h->mech1, g, ib, ie, tb, te, s, timed, fx);
+    return launch<9, IdealMixEos<9>, SimpleTransport<9>>(h, h->mech9, g, ib, ie, tb, te, s, timed, fx);
   };
   if (!per_box) {
     rc = go(0, (int)L.items.size(), 0, (int)L.tiles.size());
@@ -808,7 +809,8 @@ enum {
   kUpBoxes,
   kUpAdjBoxes,
   kUpAdjFaces,
-  kUpAdjOff
+  kUpAdjOff,
+  kUpFluxes
 };
 
 // Copies bytes to the handle's device slot unless they equal the last upload
@@ -1186,6 +1188,39 @@ extern "C" int pc_mol_rhs_vjp(pc_mol_handle* h, const pc_box_desc* boxes, int nb
                                           static_cast<const long long*>(doff), h->mech1, h->mech9, h->flags,
                                           make_geo(dx), s);
   return h->last_error = cuda_fail(h, e);
+}
+
+// ---------------------------------------------------------------------------
+// RHS with the face fluxes exported (refluxing).
+// ---------------------------------------------------------------------------
+extern "C" int pc_mol_rhs_level_fluxes(pc_mol_handle* h, const pc_box_desc* boxes, int nboxes, const double dx[3],
+                                       const pc_array4* fluxes, void* stream) {
+  if (!h) return PC_ERR_INVALID_ARGUMENT;
+  if (nboxes < 0 || (nboxes > 0 && (!boxes || !fluxes))) return h->last_error = PC_ERR_INVALID_ARGUMENT;
+  if (h->cfg.precision != PC_PRECISION_FP64) return h->last_error = PC_ERR_UNSUPPORTED;
+  const int nvar = 7 + h->cfg.nspec;
+  std::vector<FluxBox> fb(nboxes);
+  for (int b = 0; b < nboxes; ++b) {
+    for (int d = 0; d < 3; ++d) {
+      int hi[3] = {boxes[b].hi[0], boxes[b].hi[1], boxes[b].hi[2]};
+      hi[d] += 1;  // surroundingNodes(valid, d)
+      const pc_array4& a = fluxes[3 * b + d];
+      if (!array_ok(a, boxes[b].lo, hi, 0, nvar)) return h->last_error = PC_ERR_INVALID_ARGUMENT;
+      fb[b].p[d] = a.p;
+      fb[b].js[d] = a.jstride;
+      fb[b].ks[d] = a.kstride;
+      fb[b].ns[d] = a.nstride;
+      for (int e = 0; e < 3; ++e) fb[b].b[d][e] = a.begin[e];
+    }
+  }
+  if (nboxes == 0) return run(h, boxes, nboxes, dx, stream, false);
+  int rc = cuda_fail(h, cudaSetDevice(h->device));
+  if (rc != PC_OK) return rc;
+  void* dfx = nullptr;
+  if ((rc = upload(h, kUpFluxes, fb.data(), fb.size() * sizeof(FluxBox), static_cast<cudaStream_t>(stream), &dfx)) !=
+      PC_OK)
+    return rc;
+  return run(h, boxes, nboxes, dx, stream, false, static_cast<const FluxBox*>(dfx));
 }
 
 // ---------------------------------------------------------------------------

@@ -11,17 +11,18 @@ namespace {
 
 template <int NS, class EOS, class TL>
 cudaError_t flux_at(const DevBox* boxes, const int4* tiles, int ntiles, const DevMech<NS>& m, const DevFlags& f,
-                    const Geo& g, unsigned long long* counters, cudaStream_t s) {
-  return launch_flux_fp64<NS, EOS, TL>(boxes, tiles, ntiles, m, f, g, counters, s);
+                    const Geo& g, unsigned long long* counters, cudaStream_t s, const FluxBox* fx) {
+  return launch_flux_fp64<NS, EOS, TL>(boxes, tiles, ntiles, m, f, g, counters, s, fx);
 }
 
 template <int NS, class EOS>
 cudaError_t flux_tile(int tile, const DevBox* boxes, const int4* tiles, int ntiles, const DevMech<NS>& m,
-                      const DevFlags& f, const Geo& g, unsigned long long* counters, cudaStream_t s) {
+                      const DevFlags& f, const Geo& g, unsigned long long* counters, cudaStream_t s,
+                      const FluxBox* fx) {
   switch (tile) {
-    case 1: return flux_at<NS, EOS, TileCube>(boxes, tiles, ntiles, m, f, g, counters, s);
-    case 2: return flux_at<NS, EOS, TileLong>(boxes, tiles, ntiles, m, f, g, counters, s);
-    case 3: return flux_at<NS, EOS, TileSmall>(boxes, tiles, ntiles, m, f, g, counters, s);
+    case 1: return flux_at<NS, EOS, TileCube>(boxes, tiles, ntiles, m, f, g, counters, s, fx);
+    case 2: return flux_at<NS, EOS, TileLong>(boxes, tiles, ntiles, m, f, g, counters, s, fx);
+    case 3: return flux_at<NS, EOS, TileSmall>(boxes, tiles, ntiles, m, f, g, counters, s, fx);
     default: return cudaErrorInvalidValue;
   }
 }
@@ -30,10 +31,10 @@ cudaError_t flux_tile(int tile, const DevBox* boxes, const int4* tiles, int ntil
 
 cudaError_t launch_flux_fp64_tile(int tile, int variant, const DevBox* boxes, const int4* tiles, int ntiles,
                                   const DevMech<1>& m1, const DevMech<9>& m9, const DevFlags& f, const Geo& g,
-                                  unsigned long long* counters, cudaStream_t s) {
+                                  unsigned long long* counters, cudaStream_t s, const FluxBox* fx) {
   if (ntiles <= 0) return cudaSuccess;
-  if (variant == 1) return flux_tile<1, GammaLawEos<1>>(tile, boxes, tiles, ntiles, m1, f, g, counters, s);
-  return flux_tile<9, IdealMixEos<9>>(tile, boxes, tiles, ntiles, m9, f, g, counters, s);
+  if (variant == 1) return flux_tile<1, GammaLawEos<1>>(tile, boxes, tiles, ntiles, m1, f, g, counters, s, fx);
+  return flux_tile<9, IdealMixEos<9>>(tile, boxes, tiles, ntiles, m9, f, g, counters, s, fx);
 }
 
 }  // namespace pcg

@@ -81,6 +81,9 @@ def library() -> ctypes.CDLL:
         lib.pc_mol_autotune.argtypes = [c_void_p, POINTER(abi.PcBoxDesc), c_int, POINTER(c_double), c_int,
                                         POINTER(c_int), POINTER(c_double), c_int, c_void_p]
         lib.pc_mol_autotune.restype = c_int
+        lib.pc_mol_rhs_level_fluxes.argtypes = [c_void_p, POINTER(abi.PcBoxDesc), c_int, POINTER(c_double),
+                                                POINTER(abi.PcArray4), c_void_p]
+        lib.pc_mol_rhs_level_fluxes.restype = c_int
         lib.pc_mol_rhs_vjp.argtypes = [c_void_p, POINTER(abi.PcBoxDesc), c_int, POINTER(c_double),
                                        POINTER(abi.PcArray4), POINTER(abi.PcArray4), c_void_p]
         lib.pc_mol_rhs_vjp.restype = c_int
@@ -181,6 +184,26 @@ class MOLOperator:
         dxa = (c_double * 3)(*[float(v) for v in dx])
         fn = library().pc_mol_rhs_level_per_box if per_box else library().pc_mol_rhs_level
         _check(fn(self._h, descs, len(S), dxa, c_void_p(st.cuda_stream)), fn.__name__)
+
+    def rhs_level_fluxes(self, S: MultiFab, R: MultiFab, dx, stream=None):
+        """rhs_level plus the face fluxes (times the face areas) for
+        refluxing: returns, per box, [Fx, Fy, Fz] as float64 CUDA tensors of
+        shape (NVAR, nz(+1), ny(+1), nx(+1)) on surroundingNodes(valid, d)."""
+        import torch
+
+        out, arrs = [], []
+        for lo, hi in S.boxes:
+            n = [h - l + 1 for l, h in zip(lo, hi)]
+            F = [torch.empty((S.ncomp, n[2] + (d == 2), n[1] + (d == 1), n[0] + (d == 0)), dtype=torch.float64,
+                             device=S.fabs[0].device) for d in range(3)]
+            out.append(F)
+            arrs += [abi.array4(f.data_ptr(), f.shape, lo) for f in F]
+        descs = self._box_descs(S, R)
+        dxa = (c_double * 3)(*[float(v) for v in dx])
+        fx = (abi.PcArray4 * len(arrs))(*arrs)
+        _check(library().pc_mol_rhs_level_fluxes(self._h, descs, len(S), dxa, fx, self._stream(stream)),
+               "pc_mol_rhs_level_fluxes")
+        return out
 
     def getMOLSrcTerm(self, S: MultiFab, MOLSrcTerm: MultiFab, time: float, dt: float, flux_factor: float,
                       dx=None) -> None:

@@ -218,3 +218,19 @@ def test_oracle_fill_ghosts_periodic_matches_generator(oracle_lib):
     st.S[:, :, :, -4:] = -1.0
     oracle_lib.fill_ghosts([st], abi.geometry((0, 0, 0), (7, 5, 9), (0, 0, 0), (0, 0, 0)), 4)
     np.testing.assert_array_equal(st.S, want)
+
+
+def test_oracle_face_fluxes_difference_to_the_rhs(oracle_lib):
+    """The oracle's exported face fluxes (refluxing data) difference to its
+    own RHS: RHS = -div(F) / V."""
+    mech, st, _ = problems.flame((8, 6, 10), seed=93)
+    cfg = problems.make_config(mech)
+    (R, F), = oracle_lib.mol_rhs_fluxes(cfg, [st])
+    R2, = oracle_lib.mol_rhs(cfg, [st])
+    np.testing.assert_array_equal(R, R2)
+    fx, fy, fz = F
+    div = (fx[..., 1:] - fx[..., :-1]) + (fy[:, :, 1:] - fy[:, :, :-1]) + (fz[:, 1:] - fz[:, :-1])
+    vol = float(np.prod(st.dx))
+    scale = np.abs(R).max(axis=(1, 2, 3))
+    err = np.abs(-div / vol - R).max(axis=(1, 2, 3)) / np.where(scale > 0, scale, 1.0)
+    assert err.max() <= 1e-12, err
