@@ -178,6 +178,23 @@ def fp_peaks() -> dict:
         return {}
 
 
+def fp64_roofline(prof: dict, ms_rhs: float, peaks: dict) -> dict:
+    """The roofline that binds: executed FP64 work of one RHS (ncu counters,
+    profiles/dram_traffic_c2_fp64.txt) over the two passes' time, against the
+    FP64 FMA rate measured in this run."""
+    flops, inst = prof.get("fp64_flops_per_rhs"), prof.get("fp64_instructions_per_rhs")
+    peak = peaks.get("fp64_fma_tflops")
+    if not flops or not peak:
+        return {}
+    achieved = flops / (ms_rhs * 1e-3) / 1e12
+    # one FP64 instruction (DFMA, DADD or DMUL) per lane and issue: 2 flops at FMA peak
+    issue = inst / (ms_rhs * 1e-3) / (peak * 1e12 / 2.0)
+    return {"unit": "TFLOP/s", "achieved": achieved, "peak": peak, "frac": achieved / peak,
+            "issue_frac": issue, "flops_per_rhs": flops, "instructions_per_rhs": inst,
+            "peak_source": "FP64 FMA loop measured in this run (pc_peaks.cu)",
+            "counts_source": "ncu DFMA/DADD/DMUL thread-instruction counters of one RHS (a DFMA counts 2 flops)"}
+
+
 def bench_level(args, rank: int, local: int, maxover, barrier) -> dict:
     """C3: 400 uneven boxes (edges from {8,16,24,32,48,64} per axis, seeded),
     9 species.  Times one RHS of the whole level per step as (a) one launch per
@@ -636,6 +653,7 @@ def run_gpu(args):
                      "kernel": "cell_kernel + flux_kernel (one RHS)",
                      "alg_bytes_per_rhs": ab, "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)",
                      "binding_resource": "FP64 pipe",
+                     "fp64": fp64_roofline(prof, ms_rhs, peaks_fp),
                      "fp64_pipe_active_pct": {"flux_kernel": prof.get("fp64_pipe_active_pct_flux_kernel"),
                                               "cell_kernel": prof.get("fp64_pipe_active_pct_cell_kernel"),
                                               "source": "ncu --set full, profiles/flux_kernel_c2.md, cell_kernel_c2.md"},
