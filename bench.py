@@ -195,6 +195,14 @@ def fp64_roofline(prof: dict, ms_rhs: float, peaks: dict) -> dict:
             "counts_source": "ncu DFMA/DADD/DMUL thread-instruction counters of one RHS (a DFMA counts 2 flops)"}
 
 
+def launch_name(t: int) -> str:
+    """'8x8x4', or '8x8x4/persistent', for flux-pass launch configuration t."""
+    from pelec_gb300 import abi, mol
+
+    name = "x".join(map(str, mol.MOLOperator.tile_shape(t)[:3]))
+    return name + "/persistent" if t >= abi.PC_LAUNCH_PERSISTENT else name
+
+
 def bench_level(args, rank: int, local: int, maxover, barrier) -> dict:
     """C3: 400 uneven boxes (edges from {8,16,24,32,48,64} per axis, seeded),
     9 species.  Times one RHS of the whole level per step as (a) one launch per
@@ -250,9 +258,8 @@ def bench_level(args, rank: int, local: int, maxover, barrier) -> dict:
         res["batched_default_tile"] = {"value": cells / t_default, "ms_per_step": 1e3 * t_default,
                                        "tile": mol.MOLOperator.tile_shape(0), "gpu_launches_per_step": 2}
         res["batched_autotuned"] = {"value": cells / t_tuned, "ms_per_step": 1e3 * t_tuned,
-                                    "tile": mol.MOLOperator.tile_shape(best), "gpu_launches_per_step": 2,
-                                    "autotune_ms_per_shape": {"x".join(map(str, mol.MOLOperator.tile_shape(t)[:3])): v
-                                                              for t, v in enumerate(ms)}}
+                                    "launch": launch_name(best), "gpu_launches_per_step": 2,
+                                    "autotune_ms_per_launch": {launch_name(t): v for t, v in enumerate(ms)}}
         res["graph"] = {"value": cells / t_graph, "ms_per_step": 1e3 * t_graph, "gpu_launches_per_step": 2,
                         "note": "one cudaGraphLaunch of the autotuned batched RHS"}
         res["speedup_graph_vs_per_box"] = t_per_box / t_graph
@@ -557,6 +564,9 @@ def run_gpu(args):
             tf.append(b)
         return statistics.mean(tc), statistics.mean(tf)
 
+    # Launch configuration of the flux pass: the autotuner's choice for this
+    # BoxArray (setup, outside the timed region, as a user would run it).
+    best, tune_ms = op.autotune(S, R, st.dx, reps=3)
     t_dev, clk = timed_steps(op, with_clocks=True)
     ms_cell, ms_flux = pass_times(op)
     status = op.status()
@@ -610,6 +620,7 @@ def run_gpu(args):
 
     # mixed precision on the same state, error against the FP64 result
     opm = mol.MOLOperator(problems.make_config(mech, time_passes=1, precision=1))
+    best_m, tune_ms_m = opm.autotune(S, R, st.dx, reps=3)
     t_mix, _ = timed_steps(opm)
     ms_cell_m, ms_flux_m = pass_times(opm)
     opm.rhs_level(S, R, st.dx)
@@ -644,7 +655,9 @@ def run_gpu(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": desc, "boxes_per_gpu": 1, "cells_per_gpu": cells, "nspec": mech.nspec,
                    "precision": "fp64", "l2": "inputs larger than L2 (state %.0f MB, scratch records %.0f MB)" % (
-                       st.S.nbytes / 1e6, cells * (10 + 4 * mech.nspec) * 8 * 1.1 / 1e6)},
+                       st.S.nbytes / 1e6, cells * (10 + 4 * mech.nspec) * 8 * 1.1 / 1e6),
+                   "flux_launch": launch_name(best),
+                   "autotune_ms_per_launch": {launch_name(t): v for t, v in enumerate(tune_ms)}},
         "e2e": {"value": world * cells * args.steps / t_e2e, "unit": "cell-evals/s",
                 "h2d_bytes_per_step": int(S_h.numel() * 8), "d2h_bytes_per_step": int(R_h.numel() * 8)},
         "gpu_launches": 2 * args.steps,
@@ -662,6 +675,8 @@ def run_gpu(args):
         "mixed": {"value": world * cells * args.steps / t_mix, "unit": "cell-evals/s",
                   "ms_per_step": 1e3 * t_mix / args.steps, "speedup_vs_fp64": t_dev / t_mix,
                   "passes_ms": {"cell_kernel": ms_cell_m, "flux_kernel": ms_flux_m},
+                  "flux_launch": launch_name(best_m),
+                  "autotune_ms_per_launch": {launch_name(t): v for t, v in enumerate(tune_ms_m)},
                   "rel_l2_vs_fp64": {"max": max(l2), "per_component": l2},
                   "rel_max_vs_fp64": {"max": max(mx), "per_component": mx},
                   "precision": "FP32 reconstruction/Riemann/diffusion, FP64 Newton/mass fractions/divergence"},

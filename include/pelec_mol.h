@@ -220,11 +220,16 @@ int pc_mol_last_status(pc_mol_handle* h, pc_mol_status* st);
  * transport), ms[1] = flux pass (faces and divergence).  n >= 2. */
 int pc_mol_pass_times(pc_mol_handle* h, double* ms, int n);
 
-/* Tile shapes of the flux pass (one thread per cell of a tile; every shape
- * gives bit-identical FP64 results).  The reference's counterpart is the
- * MFIter tile size and the launch shape of its GPU loops (hydro_tile_size,
+/* Launch configurations of the flux pass: a tile shape (one thread per cell
+ * of a tile; every shape gives bit-identical FP64 results), launched with one
+ * CTA per tile, or the same shape + PC_LAUNCH_PERSISTENT, launched with as many
+ * CTAs as are resident on the GPU at once, each striding over the tile list
+ * (same results again).  The reference's counterpart is the MFIter tile size
+ * and the launch shape of its GPU loops (hydro_tile_size,
  * Diffusion.cpp:81-86; amrex::ParallelFor block size), which are fixed. */
 #define PC_NUM_TILES 4
+#define PC_LAUNCH_PERSISTENT PC_NUM_TILES
+#define PC_NUM_LAUNCH_CONFIGS (2 * PC_NUM_TILES)
 enum {
   PC_TILE_8x8x4 = 0,   /* 256 threads, 2 CTAs/SM (default)                   */
   PC_TILE_8x8x8 = 1,   /* 512 threads, 1 CTA/SM                               */
@@ -232,25 +237,26 @@ enum {
   PC_TILE_8x4x4 = 3    /* 128 threads, 4 CTAs/SM                              */
 };
 
-/* shape[0..3] = tile extents x, y, z and threads per CTA of tile t. */
+/* shape[0..3] = tile extents x, y, z and threads per CTA of launch
+ * configuration t (0 <= t < PC_NUM_LAUNCH_CONFIGS). */
 int pc_mol_tile_shape(int t, int shape[4]);
 
-/* Force tile shape t for the following calls, or t = -1 to return to the
- * automatic choice (the autotune cache entry of the BoxArray's box-size
- * histogram, else PC_TILE_8x8x4). */
+/* Force launch configuration t for the following calls, or t = -1 to return
+ * to the automatic choice (the autotune cache entry of the BoxArray's
+ * box-size histogram, else PC_TILE_8x8x4). */
 int pc_mol_set_tile(pc_mol_handle* h, int t);
 
-/* The tile shape that the last rhs call used. */
+/* The launch configuration that the last rhs call used. */
 int pc_mol_current_tile(pc_mol_handle* h, int* t);
 
-/* Autotuner: time pc_mol_rhs_level on this BoxArray at every tile shape
- * (one warm-up, then reps timed calls each, CUDA events on stream), keep the
- * fastest in the handle's cache under the BoxArray's box-size histogram (the
- * species count and precision are the handle's) and return it in *best.
- * ms[t] receives the mean time per call of shape t when ms is not NULL and
- * n_ms >= PC_NUM_TILES.  Writes the RHS into the boxes' rhs arrays (every
- * shape gives the same values).  Synchronous; not to be called during a
- * stream capture. */
+/* Autotuner: time pc_mol_rhs_level on this BoxArray at every launch
+ * configuration (one warm-up, then reps timed calls each, CUDA events on
+ * stream), keep the fastest in the handle's cache under the BoxArray's
+ * box-size histogram (the species count and precision are the handle's) and
+ * return it in *best.  ms[t] receives the mean time per call of
+ * configuration t when ms is not NULL and n_ms >= PC_NUM_LAUNCH_CONFIGS.
+ * Writes the RHS into the boxes' rhs arrays (every configuration gives the
+ * same values).  Synchronous; not to be called during a stream capture. */
 int pc_mol_autotune(pc_mol_handle* h, const pc_box_desc* boxes, int nboxes, const double dx[3], int reps,
                     int* best, double* ms, int n_ms, void* stream);
 

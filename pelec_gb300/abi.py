@@ -108,8 +108,11 @@ PC_BC_SYMMETRY = 2
 PC_BC_SLIPWALL = 3
 PC_BC_NOSLIPWALL = 4
 
-# flux-pass tile shapes (PC_TILE_*): 8x8x4, 8x8x8, 16x8x4, 8x4x4
+# flux-pass tile shapes (PC_TILE_*): 8x8x4, 8x8x8, 16x8x4, 8x4x4; a launch
+# configuration is a shape, + PC_LAUNCH_PERSISTENT for the persistent grid
 PC_NUM_TILES = 4
+PC_LAUNCH_PERSISTENT = PC_NUM_TILES
+PC_NUM_LAUNCH_CONFIGS = 2 * PC_NUM_TILES
 
 
 class PcGeometry(ctypes.Structure):

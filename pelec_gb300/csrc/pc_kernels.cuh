@@ -558,6 +558,9 @@ using TileCube = Tile<8, 8, 8, 1>;
 using TileLong = Tile<16, 8, 4, 1>;
 using TileSmall = Tile<8, 4, 4, 4>;
 constexpr int kNumTiles = 4;
+// Launch configurations of the flux pass: tile shape t (one CTA per tile) and
+// t + kNumTiles (the same shape, persistent grid).
+constexpr int kNumLaunchConfigs = 2 * kNumTiles;
 __host__ __device__ constexpr int tile_extent(int t, int d) {
   return t == 1 ? 8 : t == 2 ? (d == 0 ? 16 : d == 1 ? 8 : 4) : t == 3 ? (d == 0 ? 8 : 4) : (d == 2 ? 4 : 8);
 }
@@ -644,52 +647,69 @@ constexpr size_t flux_smem_bytes() {
   return sizeof(double) * ((size_t)(7 + NS) * TL::MAXF + (size_t)(4 + NS) * TL::MAXC);
 }
 
+// Pass 2 over the tile list.  CTA b takes tiles b, b + gridDim.x, ... : with
+// one CTA per tile every CTA takes one; a persistent launch (as many CTAs as
+// fit on the GPU at once) strides over the whole list.
 template <int NS, class EOS, class TL = TileDefault>
 __global__ void __launch_bounds__(TL::NT, TL::MINB)
-    flux_kernel(const DevBox* __restrict__ boxes, const int4* __restrict__ tiles, const __grid_constant__ DevMech<NS> m,
-                const DevFlags f, const Geo g, unsigned long long* __restrict__ counters,
-                const FluxBox* __restrict__ fluxes) {
+    flux_kernel(const DevBox* __restrict__ boxes, const int4* __restrict__ tiles, int ntiles,
+                const __grid_constant__ DevMech<NS> m, const DevFlags f, const Geo g,
+                unsigned long long* __restrict__ counters, const FluxBox* __restrict__ fluxes) {
   constexpr int NVAR = 7 + NS;
   extern __shared__ double flux_dyn_smem[];
   double* fbuf = flux_dyn_smem;
-  const int4 t = tiles[blockIdx.x];
-  const DevBox& b = boxes[t.x];
-  const int o[3] = {t.y, t.z, t.w};
-  const int ext[3] = {min(TL::TX, b.hi[0] - o[0] + 1), min(TL::TY, b.hi[1] - o[1] + 1), min(TL::TZ, b.hi[2] - o[2] + 1)};
   const int tx = threadIdx.x % TL::TX, ty = (threadIdx.x / TL::TX) % TL::TY, tz = threadIdx.x / (TL::TX * TL::TY);
-  const bool mine = tx < ext[0] && ty < ext[1] && tz < ext[2];
-  const long long stv[3] = {1, b.n2[0], (long long)b.n2[0] * b.n2[1]};
-  double acc[NVAR];
+  for (int tb = blockIdx.x; tb < ntiles; tb += gridDim.x) {
+    const int4 t = tiles[tb];
+    const DevBox& b = boxes[t.x];
+    const int o[3] = {t.y, t.z, t.w};
+    const int ext[3] = {min(TL::TX, b.hi[0] - o[0] + 1), min(TL::TY, b.hi[1] - o[1] + 1),
+                        min(TL::TZ, b.hi[2] - o[2] + 1)};
+    const bool mine = tx < ext[0] && ty < ext[1] && tz < ext[2];
+    const long long stv[3] = {1, b.n2[0], (long long)b.n2[0] * b.n2[1]};
+    double acc[NVAR];
 #pragma unroll
-  for (int n = 0; n < NVAR; ++n) acc[n] = 0.0;
-  const FluxBox* fxb = fluxes ? fluxes + t.x : nullptr;
-  dir_pass<NS, EOS, 0, TL>(b, m, f, g, o, ext, stv, mine, tx, ty, tz, fbuf, acc, fxb);
-  dir_pass<NS, EOS, 1, TL>(b, m, f, g, o, ext, stv, mine, tx, ty, tz, fbuf, acc, fxb);
-  dir_pass<NS, EOS, 2, TL>(b, m, f, g, o, ext, stv, mine, tx, ty, tz, fbuf, acc, fxb);
-  bool bad = false;
-  if (mine) {
-    const int i = o[0] + tx, j = o[1] + ty, k = o[2] + tz;
-    double* r = b.R + (i - b.rb[0]) + (long long)(j - b.rb[1]) * b.rj + (long long)(k - b.rb[2]) * b.rk;
+    for (int n = 0; n < NVAR; ++n) acc[n] = 0.0;
+    const FluxBox* fxb = fluxes ? fluxes + t.x : nullptr;
+    dir_pass<NS, EOS, 0, TL>(b, m, f, g, o, ext, stv, mine, tx, ty, tz, fbuf, acc, fxb);
+    dir_pass<NS, EOS, 1, TL>(b, m, f, g, o, ext, stv, mine, tx, ty, tz, fbuf, acc, fxb);
+    dir_pass<NS, EOS, 2, TL>(b, m, f, g, o, ext, stv, mine, tx, ty, tz, fbuf, acc, fxb);
+    bool bad = false;
+    if (mine) {
+      const int i = o[0] + tx, j = o[1] + ty, k = o[2] + tz;
+      double* r = b.R + (i - b.rb[0]) + (long long)(j - b.rb[1]) * b.rj + (long long)(k - b.rb[2]) * b.rk;
 #pragma unroll
-    for (int n = 0; n < NVAR; ++n) {
-      const double v = div_by(acc[n], g.vol, g.ivol);  // = acc[n] / vol, correctly rounded
-      bad |= !isfinite(v);
-      r[n * b.rn] = v;
+      for (int n = 0; n < NVAR; ++n) {
+        const double v = div_by(acc[n], g.vol, g.ivol);  // = acc[n] / vol, correctly rounded
+        bad |= !isfinite(v);
+        r[n * b.rn] = v;
+      }
     }
-  }
-  if (f.check_output) warp_count(&counters[kCounterNonfinite], bad);
-  if (threadIdx.x == 0) {
-    atomicAdd(&counters[kCounterCells], (unsigned long long)(ext[0] * ext[1] * ext[2]));
+    if (f.check_output) warp_count(&counters[kCounterNonfinite], bad);
+    if (threadIdx.x == 0) atomicAdd(&counters[kCounterCells], (unsigned long long)(ext[0] * ext[1] * ext[2]));
   }
 }
 
+// Host: CTAs of a kernel that are resident on the current device at once
+// (the grid of a persistent launch); cached per device by the caller.
+template <class K>
+inline int resident_ctas(K kernel, int threads, size_t smem) {
+  int dev = 0, nsm = 0, nb = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+  if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel, threads, smem) != cudaSuccess) return 0;
+  return nb > 0 ? nb * nsm : nsm;
+}
+
 // Host: opt the flux kernel into its dynamic shared memory (more than the
-// default 48 KB) on the current device, once per device; then launch it.
+// default 48 KB) on the current device, once per device; then launch it, one
+// CTA per tile or (persistent) as many CTAs as are resident at once.
 template <int NS, class EOS, class TL = TileDefault>
 inline cudaError_t launch_flux_fp64(const DevBox* boxes, const int4* tiles, int ntiles, const DevMech<NS>& m,
                                     const DevFlags& f, const Geo& g, unsigned long long* counters, cudaStream_t s,
-                                    const FluxBox* fluxes = nullptr) {
+                                    const FluxBox* fluxes = nullptr, bool persistent = false) {
   static std::atomic<unsigned long long> opted{0};  // bit per device
+  static std::atomic<int> resident[64];             // persistent grid per device (0: not known yet)
   constexpr size_t smem = flux_smem_bytes<NS, TL>();
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
@@ -700,7 +720,17 @@ inline cudaError_t launch_flux_fp64(const DevBox* boxes, const int4* tiles, int 
     if (e != cudaSuccess) return e;
     opted.fetch_or(bit);
   }
-  if (ntiles > 0) flux_kernel<NS, EOS, TL><<<ntiles, TL::NT, smem, s>>>(boxes, tiles, m, f, g, counters, fluxes);
+  if (ntiles <= 0) return cudaSuccess;
+  int grid = ntiles;
+  if (persistent) {
+    int r = bit ? resident[dev].load() : 0;
+    if (r <= 0) {
+      r = resident_ctas(flux_kernel<NS, EOS, TL>, TL::NT, smem);
+      if (bit && r > 0) resident[dev].store(r);
+    }
+    if (r > 0 && r < grid) grid = r;
+  }
+  flux_kernel<NS, EOS, TL><<<grid, TL::NT, smem, s>>>(boxes, tiles, ntiles, m, f, g, counters, fluxes);
   return cudaGetLastError();
 }
 

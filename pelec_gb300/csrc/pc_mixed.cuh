@@ -642,9 +642,11 @@ __device__ __forceinline__ void dir_pass_mixed(const DevBox& b, const MechF<NS>&
   __syncthreads();
 }
 
+// Pass 2 over the tile list; CTA b takes tiles b, b + gridDim.x, ... (one
+// each with one CTA per tile; a persistent launch strides over the list).
 template <int NS, bool MIX, class TL = TileDefault>
 __global__ void __launch_bounds__(TL::NT, TL::MINB)
-    flux_kernel_mixed(const DevBox* __restrict__ boxes, const int4* __restrict__ tiles,
+    flux_kernel_mixed(const DevBox* __restrict__ boxes, const int4* __restrict__ tiles, int ntiles,
                       const __grid_constant__ MechF<NS> m, const __grid_constant__ DevMech<NS> md, const DevFlags f,
                       const Geo g, unsigned long long* __restrict__ counters) {
   constexpr int NVAR = 7 + NS;
@@ -656,31 +658,66 @@ __global__ void __launch_bounds__(TL::NT, TL::MINB)
     __shared__ double flux_static_smem[NVAR * TL::MAXF];
     fbuf = flux_static_smem;
   }
-  const int4 t = tiles[blockIdx.x];
-  const DevBox& b = boxes[t.x];
-  const int o[3] = {t.y, t.z, t.w};
-  const int ext[3] = {min(TL::TX, b.hi[0] - o[0] + 1), min(TL::TY, b.hi[1] - o[1] + 1), min(TL::TZ, b.hi[2] - o[2] + 1)};
   const int tx = threadIdx.x % TL::TX, ty = (threadIdx.x / TL::TX) % TL::TY, tz = threadIdx.x / (TL::TX * TL::TY);
-  const bool mine = tx < ext[0] && ty < ext[1] && tz < ext[2];
-  const long long stv[3] = {1, b.n2[0], (long long)b.n2[0] * b.n2[1]};
-  double acc[NVAR];
+  for (int tb = blockIdx.x; tb < ntiles; tb += gridDim.x) {
+    const int4 t = tiles[tb];
+    const DevBox& b = boxes[t.x];
+    const int o[3] = {t.y, t.z, t.w};
+    const int ext[3] = {min(TL::TX, b.hi[0] - o[0] + 1), min(TL::TY, b.hi[1] - o[1] + 1),
+                        min(TL::TZ, b.hi[2] - o[2] + 1)};
+    const bool mine = tx < ext[0] && ty < ext[1] && tz < ext[2];
+    const long long stv[3] = {1, b.n2[0], (long long)b.n2[0] * b.n2[1]};
+    double acc[NVAR];
 #pragma unroll
-  for (int n = 0; n < NVAR; ++n) acc[n] = 0.0;
-  dir_pass_mixed<NS, MIX, 0, TL>(b, m, md, f, g, o, ext, stv, mine, tx, ty, tz, fbuf, acc);
-  dir_pass_mixed<NS, MIX, 1, TL>(b, m, md, f, g, o, ext, stv, mine, tx, ty, tz, fbuf, acc);
-  dir_pass_mixed<NS, MIX, 2, TL>(b, m, md, f, g, o, ext, stv, mine, tx, ty, tz, fbuf, acc);
-  bool bad = false;
-  if (mine) {
-    const int i = o[0] + tx, j = o[1] + ty, k = o[2] + tz;
-    double* r = b.R + (i - b.rb[0]) + (long long)(j - b.rb[1]) * b.rj + (long long)(k - b.rb[2]) * b.rk;
+    for (int n = 0; n < NVAR; ++n) acc[n] = 0.0;
+    dir_pass_mixed<NS, MIX, 0, TL>(b, m, md, f, g, o, ext, stv, mine, tx, ty, tz, fbuf, acc);
+    dir_pass_mixed<NS, MIX, 1, TL>(b, m, md, f, g, o, ext, stv, mine, tx, ty, tz, fbuf, acc);
+    dir_pass_mixed<NS, MIX, 2, TL>(b, m, md, f, g, o, ext, stv, mine, tx, ty, tz, fbuf, acc);
+    bool bad = false;
+    if (mine) {
+      const int i = o[0] + tx, j = o[1] + ty, k = o[2] + tz;
+      double* r = b.R + (i - b.rb[0]) + (long long)(j - b.rb[1]) * b.rj + (long long)(k - b.rb[2]) * b.rk;
 #pragma unroll
-    for (int n = 0; n < NVAR; ++n) {
-      bad |= !isfinite(acc[n]);
-      r[n * b.rn] = acc[n];
+      for (int n = 0; n < NVAR; ++n) {
+        bad |= !isfinite(acc[n]);
+        r[n * b.rn] = acc[n];
+      }
     }
+    if (f.check_output) warp_count(&counters[kCounterNonfinite], bad);
+    if (threadIdx.x == 0) atomicAdd(&counters[kCounterCells], (unsigned long long)(ext[0] * ext[1] * ext[2]));
   }
-  if (f.check_output) warp_count(&counters[kCounterNonfinite], bad);
-  if (threadIdx.x == 0) atomicAdd(&counters[kCounterCells], (unsigned long long)(ext[0] * ext[1] * ext[2]));
+}
+
+// Host: launch the mixed flux pass at tile shape TL, one CTA per tile or
+// (persistent) as many CTAs as are resident on the device at once.
+template <int NS, bool MIX, class TL>
+inline cudaError_t launch_flux_mixed_at(const DevBox* boxes, const int4* tiles, int ntiles, const MechF<NS>& mf,
+                                        const DevMech<NS>& md, const DevFlags& f, const Geo& g,
+                                        unsigned long long* counters, cudaStream_t s, bool persistent) {
+  static std::atomic<unsigned long long> opted{0};  // bit per device
+  static std::atomic<int> resident[64];             // persistent grid per device (0: not known yet)
+  constexpr size_t smem = TL::DYN ? sizeof(double) * (7 + NS) * TL::MAXF : 0;
+  if (ntiles <= 0) return cudaSuccess;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  const unsigned long long bit = (dev >= 0 && dev < 64) ? (1ull << dev) : 0ull;
+  if (TL::DYN && (!bit || !(opted.load() & bit))) {
+    e = cudaFuncSetAttribute(flux_kernel_mixed<NS, MIX, TL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    opted.fetch_or(bit);
+  }
+  int grid = ntiles;
+  if (persistent) {
+    int r = bit ? resident[dev].load() : 0;
+    if (r <= 0) {
+      r = resident_ctas(flux_kernel_mixed<NS, MIX, TL>, TL::NT, smem);
+      if (bit && r > 0) resident[dev].store(r);
+    }
+    if (r > 0 && r < grid) grid = r;
+  }
+  flux_kernel_mixed<NS, MIX, TL><<<grid, TL::NT, smem, s>>>(boxes, tiles, ntiles, mf, md, f, g, counters);
+  return cudaGetLastError();
 }
 
 }  // namespace pcg

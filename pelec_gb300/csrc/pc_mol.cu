@@ -21,12 +21,13 @@
 #include "pelec_mol.h"
 
 namespace pcg {
-int launch_mixed(int variant, int tile, const DevBox* boxes, const int2* items, int nitems, const int4* tiles,
-                 int ntiles, const DevMech<1>& m1, const DevMech<9>& m9, const DevFlags& f, const Geo& g, double p_ref,
-                 unsigned long long* counters, cudaStream_t s, cudaEvent_t e0, cudaEvent_t e1, cudaEvent_t e2);
-cudaError_t launch_flux_fp64_tile(int tile, int variant, const DevBox* boxes, const int4* tiles, int ntiles,
-                                  const DevMech<1>& m1, const DevMech<9>& m9, const DevFlags& f, const Geo& g,
-                                  unsigned long long* counters, cudaStream_t s, const FluxBox* fx);
+int launch_mixed(int variant, int tile, bool persistent, const DevBox* boxes, const int2* items, int nitems,
+                 const int4* tiles, int ntiles, const DevMech<1>& m1, const DevMech<9>& m9, const DevFlags& f,
+                 const Geo& g, double p_ref, unsigned long long* counters, cudaStream_t s, cudaEvent_t e0,
+                 cudaEvent_t e1, cudaEvent_t e2);
+cudaError_t launch_flux_fp64_tile(int tile, bool persistent, int variant, const DevBox* boxes, const int4* tiles,
+                                  int ntiles, const DevMech<1>& m1, const DevMech<9>& m9, const DevFlags& f,
+                                  const Geo& g, unsigned long long* counters, cudaStream_t s, const FluxBox* fx);
 cudaError_t launch_vjp_passes(int variant, const DevBox* boxes, const AdjBox* adj, const int2* items, int nitems,
                               const int4* fitems, int nfitems, double* recbar, const long long* recbar_off,
                               const DevMech<1>& m1, const DevMech<9>& m9, const DevFlags& f, const Geo& g,
@@ -64,8 +65,9 @@ struct pc_mol_handle {
   double last_dx[3] = {0, 0, 0};
   int lay_tile = -1;  // tile shape the cached layout was built for
   Layout lay;
-  // flux-pass tile shape: forced by pc_mol_set_tile (>= 0), else looked up in
-  // the autotune cache by the BoxArray's box-size multiset, else 0
+  // flux-pass launch configuration (tile shape + kNumTiles if persistent):
+  // forced by pc_mol_set_tile (>= 0), else looked up in the autotune cache by
+  // the BoxArray's box-size multiset, else 0
   int tile_forced = -1;
   int tile = 0;
   std::map<std::vector<int>, int> tune_cache;
@@ -291,10 +293,11 @@ int prepare(pc_mol_handle* h, const pc_box_desc* boxes, int nboxes, const double
   else if (!same_geom)
     h->tile = choose_tile(h, boxes, nboxes);
   int rc = PC_OK;
-  if (!(same_geom && h->lay_tile == h->tile)) {
+  const int shape = h->tile % kNumTiles;
+  if (!(same_geom && h->lay_tile == shape)) {
     // New geometry: launch lists and record scratch.
     h->lay_tile = -1;
-    build_layout(boxes, nboxes, h->nrec, h->tile, h->lay);
+    build_layout(boxes, nboxes, h->nrec, shape, h->lay);
     rc = ensure(h, h->scratch, h->scratch_cap, h->lay.scratch_doubles);
     if (rc != PC_OK) return rc;
     for (auto& d : h->lay.boxes) d.rec = h->scratch + reinterpret_cast<size_t>(d.rec);
@@ -314,7 +317,7 @@ int prepare(pc_mol_handle* h, const pc_box_desc* boxes, int nboxes, const double
     h->d_boxes = nullptr;
     h->last_boxes.assign(boxes, boxes + nboxes);
     for (int d = 0; d < 3; ++d) h->last_dx[d] = dx[d];
-    h->lay_tile = h->tile;
+    h->lay_tile = shape;
   }
   // The device box table for these array pointers.
   pc_mol_handle::BoxTable* tb = nullptr;
@@ -367,15 +370,17 @@ int launch(pc_mol_handle* h, const DevMech<NS>& mech, const Geo& g, int ibeg, in
     cell_kernel<NS, EOS, TR><<<iend - ibeg, kCellThreads, 0, s>>>(h->d_boxes, h->d_items + ibeg, mech, h->flags,
                                                                    h->d_counters);
   if (timed) cudaEventRecord(h->ev[1], s);
+  const bool pers = h->tile >= kNumTiles;
   if (h->lay_tile != 0) {
-    const cudaError_t e = launch_flux_fp64_tile(h->lay_tile, h->variant, h->d_boxes, h->d_tiles + tbeg, tend - tbeg,
-                                                h->mech1, h->mech9, h->flags, g, h->d_counters, s, fx);
+    const cudaError_t e = launch_flux_fp64_tile(h->lay_tile, pers, h->variant, h->d_boxes, h->d_tiles + tbeg,
+                                                tend - tbeg, h->mech1, h->mech9, h->flags, g, h->d_counters, s, fx);
     if (timed) cudaEventRecord(h->ev[2], s);
     if (e != cudaSuccess) return cuda_fail(h, e);
     return cuda_fail(h, cudaGetLastError());
   }
   const cudaError_t e =
-      launch_flux_fp64<NS, EOS>(h->d_boxes, h->d_tiles + tbeg, tend - tbeg, mech, h->flags, g, h->d_counters, s, fx);
+      launch_flux_fp64<NS, EOS>(h->d_boxes, h->d_tiles + tbeg, tend - tbeg, mech, h->flags, g, h->d_counters, s, fx,
+                                pers);
   if (timed) cudaEventRecord(h->ev[2], s);
   return cuda_fail(h, e);
 }
@@ -405,8 +410,8 @@ int run(pc_mol_handle* h, const pc_box_desc* boxes, int nboxes, const double dx[
       const double p_ref = h->cfg.mixed_p_ref > 0.0 ? h->cfg.mixed_p_ref : 1013250.0;
       Geo gm = g;
       gm.p_ref = p_ref;
-      const int rc = launch_mixed(h->variant, h->lay_tile, h->d_boxes, h->d_items + ib, ie - ib, h->d_tiles + tb, te - tb,
-                                  h->mech1, h->mech9, h->flags, gm, p_ref, h->d_counters, s,
+      const int rc = launch_mixed(h->variant, h->lay_tile, h->tile >= kNumTiles, h->d_boxes, h->d_items + ib, ie - ib,
+                                  h->d_tiles + tb, te - tb, h->mech1, h->mech9, h->flags, gm, p_ref, h->d_counters, s,
                                   timed ? h->ev[0] : nullptr, timed ? h->ev[1] : nullptr, timed ? h->ev[2] : nullptr);
       return rc == 0 ? PC_OK : cuda_fail(h, cudaGetLastError());
     }
@@ -558,16 +563,16 @@ int pc_mol_pass_times(pc_mol_handle* h, double* ms, int n) {
 }
 
 int pc_mol_tile_shape(int t, int shape[4]) {
-  if (t < 0 || t >= kNumTiles || !shape) return PC_ERR_INVALID_ARGUMENT;
-  shape[0] = tile_extent(t, 0);
-  shape[1] = tile_extent(t, 1);
-  shape[2] = tile_extent(t, 2);
+  if (t < 0 || t >= kNumLaunchConfigs || !shape) return PC_ERR_INVALID_ARGUMENT;
+  shape[0] = tile_extent(t % kNumTiles, 0);
+  shape[1] = tile_extent(t % kNumTiles, 1);
+  shape[2] = tile_extent(t % kNumTiles, 2);
   shape[3] = shape[0] * shape[1] * shape[2];
   return PC_OK;
 }
 
 int pc_mol_set_tile(pc_mol_handle* h, int t) {
-  if (!h || t < -1 || t >= kNumTiles) return PC_ERR_INVALID_ARGUMENT;
+  if (!h || t < -1 || t >= kNumLaunchConfigs) return PC_ERR_INVALID_ARGUMENT;
   h->tile_forced = t;
   h->last_boxes.clear();  // the next call chooses again
   return PC_OK;
@@ -575,14 +580,15 @@ int pc_mol_set_tile(pc_mol_handle* h, int t) {
 
 int pc_mol_current_tile(pc_mol_handle* h, int* t) {
   if (!h || !t) return PC_ERR_INVALID_ARGUMENT;
-  *t = h->lay_tile >= 0 ? h->lay_tile : h->tile;
+  // h->tile, unless a call since (the tangent) ran at another shape
+  *t = (h->lay_tile < 0 || h->lay_tile == h->tile % kNumTiles) ? h->tile : h->lay_tile;
   return PC_OK;
 }
 
 int pc_mol_autotune(pc_mol_handle* h, const pc_box_desc* boxes, int nboxes, const double dx[3], int reps, int* best,
                     double* ms, int n_ms, void* stream) {
   if (!h || !best || nboxes <= 0 || !boxes || reps <= 0) return PC_ERR_INVALID_ARGUMENT;
-  if (ms && n_ms < kNumTiles) return PC_ERR_INVALID_ARGUMENT;
+  if (ms && n_ms < kNumLaunchConfigs) return PC_ERR_INVALID_ARGUMENT;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   int rc = cuda_fail(h, cudaSetDevice(h->device));
   if (rc != PC_OK) return rc;
@@ -594,9 +600,9 @@ int pc_mol_autotune(pc_mol_handle* h, const pc_box_desc* boxes, int nboxes, cons
   const int saved = h->tile_forced;
   double tbest = 0.0;
   int ibest = 0;
-  for (int t = 0; t < kNumTiles && rc == PC_OK; ++t) {
+  for (int t = 0; t < kNumLaunchConfigs && rc == PC_OK; ++t) {
     h->tile_forced = t;
-    rc = run(h, boxes, nboxes, dx, stream, false);  // warm-up, builds the layout of shape t
+    rc = run(h, boxes, nboxes, dx, stream, false);  // warm-up, builds the layout of configuration t
     if (rc == PC_OK) rc = cuda_fail(h, cudaEventRecord(e0, s));
     for (int r = 0; r < reps && rc == PC_OK; ++r) rc = run(h, boxes, nboxes, dx, stream, false);
     if (rc == PC_OK) rc = cuda_fail(h, cudaEventRecord(e1, s));

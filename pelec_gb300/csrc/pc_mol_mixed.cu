@@ -5,47 +5,39 @@
 
 namespace pcg {
 
-cudaError_t launch_flux_mixed_tile(int tile, int variant, const DevBox* boxes, const int4* tiles, int ntiles,
-                                   const DevMech<1>& m1, const DevMech<9>& m9, const DevFlags& f, const Geo& g,
-                                   double p_ref, unsigned long long* counters, cudaStream_t s);
+cudaError_t launch_flux_mixed_tile(int tile, bool persistent, int variant, const DevBox* boxes, const int4* tiles,
+                                   int ntiles, const DevMech<1>& m1, const DevMech<9>& m9, const DevFlags& f,
+                                   const Geo& g, double p_ref, unsigned long long* counters, cudaStream_t s);
 
 // Cell pass, then the flux pass at tile shape `tile` (0 = 8x8x4, launched
-// here; the others in pc_tiles_mixed.cu).
-int launch_mixed(int variant, int tile, const DevBox* boxes, const int2* items, int nitems, const int4* tiles,
-                 int ntiles, const DevMech<1>& m1, const DevMech<9>& m9, const DevFlags& f, const Geo& g, double p_ref,
-                 unsigned long long* counters, cudaStream_t s, cudaEvent_t e0, cudaEvent_t e1, cudaEvent_t e2) {
+// here; the others in pc_tiles_mixed.cu), persistent or one CTA per tile.
+int launch_mixed(int variant, int tile, bool persistent, const DevBox* boxes, const int2* items, int nitems,
+                 const int4* tiles, int ntiles, const DevMech<1>& m1, const DevMech<9>& m9, const DevFlags& f,
+                 const Geo& g, double p_ref, unsigned long long* counters, cudaStream_t s, cudaEvent_t e0,
+                 cudaEvent_t e1, cudaEvent_t e2) {
   if (e0) cudaEventRecord(e0, s);
-  if (tile != 0) {
-    if (nitems > 0) {
-      if (variant == 1)
-        cell_kernel_mixed<1, GammaLawEos<1>, false, false><<<nitems, kCellThreads, 0, s>>>(
-            boxes, items, m1, to_float(m1, p_ref), f, counters);
-      else
-        cell_kernel_mixed<9, IdealMixEos<9>, true, true><<<nitems, kCellThreads, 0, s>>>(
-            boxes, items, m9, to_float(m9, p_ref), f, counters);
-    }
-    if (e1) cudaEventRecord(e1, s);
-    const cudaError_t e = launch_flux_mixed_tile(tile, variant, boxes, tiles, ntiles, m1, m9, f, g, p_ref, counters, s);
-    if (e2) cudaEventRecord(e2, s);
-    return e == cudaSuccess && cudaGetLastError() == cudaSuccess ? 0 : 3;
-  }
+  cudaError_t e = cudaSuccess;
   if (variant == 1) {
     const MechF<1> mf = to_float(m1, p_ref);
     if (nitems > 0)
       cell_kernel_mixed<1, GammaLawEos<1>, false, false><<<nitems, kCellThreads, 0, s>>>(boxes, items, m1, mf, f,
                                                                                          counters);
     if (e1) cudaEventRecord(e1, s);
-    if (ntiles > 0) flux_kernel_mixed<1, false><<<ntiles, kFluxThreads, 0, s>>>(boxes, tiles, mf, m1, f, g, counters);
+    if (tile == 0)
+      e = launch_flux_mixed_at<1, false, TileDefault>(boxes, tiles, ntiles, mf, m1, f, g, counters, s, persistent);
   } else {
     const MechF<9> mf = to_float(m9, p_ref);
     if (nitems > 0)
       cell_kernel_mixed<9, IdealMixEos<9>, true, true><<<nitems, kCellThreads, 0, s>>>(boxes, items, m9, mf, f,
                                                                                        counters);
     if (e1) cudaEventRecord(e1, s);
-    if (ntiles > 0) flux_kernel_mixed<9, true><<<ntiles, kFluxThreads, 0, s>>>(boxes, tiles, mf, m9, f, g, counters);
+    if (tile == 0)
+      e = launch_flux_mixed_at<9, true, TileDefault>(boxes, tiles, ntiles, mf, m9, f, g, counters, s, persistent);
   }
+  if (tile != 0)
+    e = launch_flux_mixed_tile(tile, persistent, variant, boxes, tiles, ntiles, m1, m9, f, g, p_ref, counters, s);
   if (e2) cudaEventRecord(e2, s);
-  return cudaGetLastError() == cudaSuccess ? 0 : 3;
+  return e == cudaSuccess && cudaGetLastError() == cudaSuccess ? 0 : 3;
 }
 
 }  // namespace pcg

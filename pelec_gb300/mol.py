@@ -316,16 +316,18 @@ class MOLOperator:
                                                      self._arrays(Sbar), self._stream(stream)),
                "pc_mol_compute_temp_adjoint")
 
-    # ---- flux-pass tile shape ----
+    # ---- flux-pass launch configuration (tile shape, persistent or not) ----
     @staticmethod
     def tile_shape(t: int):
-        """(tx, ty, tz, threads) of tile shape t."""
+        """(tx, ty, tz, threads) of launch configuration t."""
         out = (c_int * 4)()
         _check(library().pc_mol_tile_shape(int(t), out), "pc_mol_tile_shape")
         return tuple(out)
 
     def set_tile(self, t: int) -> None:
-        """Force tile shape t (-1: automatic, from the autotune cache)."""
+        """Force launch configuration t: tile shape t % PC_NUM_TILES, persistent
+        grid when t >= PC_LAUNCH_PERSISTENT (-1: automatic, from the autotune
+        cache)."""
         _check(library().pc_mol_set_tile(self._h, int(t)), "pc_mol_set_tile")
 
     def current_tile(self) -> int:
@@ -334,14 +336,14 @@ class MOLOperator:
         return out.value
 
     def autotune(self, S: MultiFab, R: MultiFab, dx, reps: int = 3, stream=None):
-        """Time every tile shape on this BoxArray, cache the fastest for its
-        box-size histogram; returns (best, [ms per call of each shape])."""
+        """Time every launch configuration on this BoxArray, cache the fastest
+        for its box-size histogram; returns (best, [ms per call of each])."""
         descs = self._box_descs(S, R)
         dxa = (c_double * 3)(*[float(v) for v in dx])
         best = c_int(0)
-        ms = (c_double * abi.PC_NUM_TILES)()
+        ms = (c_double * abi.PC_NUM_LAUNCH_CONFIGS)()
         _check(library().pc_mol_autotune(self._h, descs, len(S), dxa, int(reps), ctypes.byref(best), ms,
-                                         abi.PC_NUM_TILES, self._stream(stream)), "pc_mol_autotune")
+                                         abi.PC_NUM_LAUNCH_CONFIGS, self._stream(stream)), "pc_mol_autotune")
         return best.value, list(ms)
 
     def status(self) -> abi.PcMolStatus:

@@ -103,10 +103,12 @@ def test_product_does_not_import_oracle():
 def test_tile_shapes_are_reported_without_a_gpu(lib):
     from pelec_gb300 import mol
 
-    shapes = [mol.MOLOperator.tile_shape(t) for t in range(abi.PC_NUM_TILES)]
-    assert shapes == [(8, 8, 4, 256), (8, 8, 8, 512), (16, 8, 4, 512), (8, 4, 4, 128)]
+    shapes = [mol.MOLOperator.tile_shape(t) for t in range(abi.PC_NUM_LAUNCH_CONFIGS)]
+    assert shapes[: abi.PC_NUM_TILES] == [(8, 8, 4, 256), (8, 8, 8, 512), (16, 8, 4, 512), (8, 4, 4, 128)]
+    # the persistent configurations run the same shapes
+    assert shapes[abi.PC_LAUNCH_PERSISTENT:] == shapes[: abi.PC_NUM_TILES]
     out = (ctypes.c_int * 4)()
-    assert lib.pc_mol_tile_shape(abi.PC_NUM_TILES, out) == abi.PC_ERR_INVALID_ARGUMENT
+    assert lib.pc_mol_tile_shape(abi.PC_NUM_LAUNCH_CONFIGS, out) == abi.PC_ERR_INVALID_ARGUMENT
     assert lib.pc_mol_tile_shape(-1, out) == abi.PC_ERR_INVALID_ARGUMENT
     assert lib.pc_mol_set_tile(None, 0) == abi.PC_ERR_INVALID_ARGUMENT
     assert lib.pc_mol_autotune(None, None, 0, None, 1, None, None, 0, None) == abi.PC_ERR_INVALID_ARGUMENT

@@ -1,7 +1,8 @@
-"""GPU tests of the batched-level machinery: every flux-pass tile shape gives
-the same RHS bit for bit (and the oracle's to 1e-12), the autotuner caches
-its choice per box-size histogram, and a captured CUDA graph of ghost fill +
-RHS replays to the direct calls' result.
+"""GPU tests of the batched-level machinery: every flux-pass launch
+configuration (tile shape, one CTA per tile or a persistent grid) gives the
+same RHS bit for bit (and the oracle's to 1e-12), the autotuner caches its
+choice per box-size histogram, and a captured CUDA graph of ghost fill + RHS
+replays to the direct calls' result.
 """
 import numpy as np
 import pytest
@@ -45,8 +46,8 @@ def test_every_tile_shape_gives_identical_rhs(cuda_lib, oracle_lib, precision):
     mech, boxes = _ragged_level()
     cfg = problems.make_config(mech, precision=precision)
     op = mol.MOLOperator(cfg)
-    outs = [_rhs_at_tile(mol, op, boxes, t) for t in range(abi.PC_NUM_TILES)]
-    for t in range(1, abi.PC_NUM_TILES):
+    outs = [_rhs_at_tile(mol, op, boxes, t) for t in range(abi.PC_NUM_LAUNCH_CONFIGS)]
+    for t in range(1, abi.PC_NUM_LAUNCH_CONFIGS):
         for b, (g0, gt) in enumerate(zip(outs[0], outs[t])):
             np.testing.assert_array_equal(gt, g0, err_msg=f"tile {t} box {b}")
     if precision == abi.PC_PRECISION_FP64:
@@ -60,11 +61,28 @@ def test_every_tile_shape_single_species(cuda_lib, oracle_lib):
     mech, st = problems.tgv(20, seed=33)
     cfg = problems.make_config(mech)
     op = mol.MOLOperator(cfg)
-    outs = [_rhs_at_tile(mol, op, [st], t)[0] for t in range(abi.PC_NUM_TILES)]
-    for t in range(1, abi.PC_NUM_TILES):
+    outs = [_rhs_at_tile(mol, op, [st], t)[0] for t in range(abi.PC_NUM_LAUNCH_CONFIGS)]
+    for t in range(1, abi.PC_NUM_LAUNCH_CONFIGS):
         np.testing.assert_array_equal(outs[t], outs[0])
     ref, = oracle_lib.mol_rhs(cfg, [st])
     assert rel_maxnorm(outs[3], ref).max() <= 1e-12
+
+
+@pytest.mark.parametrize("precision", [abi.PC_PRECISION_FP64, abi.PC_PRECISION_MIXED])
+def test_persistent_grid_strides_over_every_tile(cuda_lib, precision):
+    """A 64^3 flame has more tiles than the GPU holds CTAs at any shape, so
+    each CTA of a persistent launch takes several tiles: same RHS bit for bit
+    as one CTA per tile, and every cell counted once."""
+    mol = cuda_lib
+    mech, st, _ = problems.flame((64, 64, 64), w_noise=1.0)
+    cfg = problems.make_config(mech, precision=precision)
+    op = mol.MOLOperator(cfg)
+    for shape in range(abi.PC_NUM_TILES):
+        one, = _rhs_at_tile(mol, op, [st], shape)
+        pers, = _rhs_at_tile(mol, op, [st], shape + abi.PC_LAUNCH_PERSISTENT)
+        np.testing.assert_array_equal(pers, one, err_msg=f"shape {shape}")
+        assert np.isfinite(pers).all()
+        assert op.status().cells == 64 ** 3
 
 
 def test_autotune_caches_choice_per_histogram(cuda_lib):
@@ -77,7 +95,7 @@ def test_autotune_caches_choice_per_histogram(cuda_lib):
     S = to_multifab(mol, boxes, boxes[0].ng)
     R = mol.MultiFab(S.boxes, S.ncomp, 0)
     best, ms = op.autotune(S, R, boxes[0].dx, reps=2)
-    assert 0 <= best < abi.PC_NUM_TILES
+    assert 0 <= best < abi.PC_NUM_LAUNCH_CONFIGS and len(ms) == abi.PC_NUM_LAUNCH_CONFIGS
     assert all(m > 0 for m in ms) and ms[best] == min(ms)
     ref = [t.clone() for t in R.fabs]
     R2 = mol.MultiFab(S.boxes, S.ncomp, 0)
