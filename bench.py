@@ -42,7 +42,10 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="c2", choices=["c2", "c1"])
-    ap.add_argument("--precision", default="fp64", choices=["fp64"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp64_rcp"],
+                    help="FP64 form of the headline: fp64 (every quotient correctly rounded, the oracle's "
+                         "arithmetic) or fp64_rcp (quotients by a shared divisor as products with its "
+                         "reciprocal); the other form is measured beside it")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-level", action="store_true", help="skip the 400-box batched-level measurement")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint and trajectory-gradient measurement")
@@ -151,9 +154,9 @@ def cpu_baseline(st, cfg, reps: int = 3) -> dict:
             "best_s": min(times), "median_s": statistics.median(times)}
 
 
-def profile_figures(workload_name: str) -> dict:
-    """Figures from the committed ncu summary of this workload (or {})."""
-    path = os.path.join(ROOT, "profiles", f"dram_traffic_{workload_name}_fp64.txt")
+def profile_figures(workload_name: str, form: str = "fp64") -> dict:
+    """Figures from the committed ncu summary of this workload and FP64 form (or {})."""
+    path = os.path.join(ROOT, "profiles", f"dram_traffic_{workload_name}_{form}.txt")
     out = {}
     if os.path.exists(path):
         for ln in open(path):
@@ -450,6 +453,13 @@ def bench_trajectory(args, rank: int) -> dict:
     return out
 
 
+FORM_NOTE = {
+    "fp64": "every operation FP64, every quotient correctly rounded: the oracle's arithmetic bit for bit",
+    "fp64_rcp": "every operation FP64; quotients by a divisor shared by several numerators taken as products "
+                "with its correctly rounded reciprocal (within one ulp of the correctly rounded quotient)",
+}
+
+
 def abi_precision(mixed: int) -> int:
     from pelec_gb300 import abi
 
@@ -509,8 +519,12 @@ def run_gpu(args):
     cb.build()
     from pelec_gb300 import mol, problems
 
+    from pelec_gb300 import abi
+
     mech, st, desc = workload(args.workload, seed=1 + rank)
-    cfg = problems.make_config(mech, time_passes=1)
+    forms = {"fp64": abi.PC_PRECISION_FP64, "fp64_rcp": abi.PC_PRECISION_FP64_RCP}
+    other = "fp64" if args.precision == "fp64_rcp" else "fp64_rcp"
+    cfg = problems.make_config(mech, time_passes=1, precision=forms[args.precision])
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         from oracle import build as ob
@@ -570,9 +584,13 @@ def run_gpu(args):
     t_dev, clk = timed_steps(op, with_clocks=True)
     ms_cell, ms_flux = pass_times(op)
     status = op.status()
-    op.rhs_level(S, R, st.dx)
+    # The headline RHS and the scale of the flux differences it is made of
+    # (max over faces of |F_n| / V per component): the measure of round-off.
+    Fx = op.rhs_level_fluxes(S, R, st.dx)[0]
     torch.cuda.synchronize()
     r64 = R.fabs[0].cpu().numpy()
+    flux_scale = np.max([f.abs().amax(dim=(1, 2, 3)).cpu().numpy() for f in Fx], axis=0) / float(np.prod(st.dx))
+    del Fx
     # End to end through the public API: every step copies its state from
     # pinned host memory, evaluates the RHS and copies the RHS back.  Two
     # device buffer pairs and separate upload/download streams let step k+1's
@@ -618,6 +636,18 @@ def run_gpu(args):
     t_e2e = maxover(e0.elapsed_time(e1) / 1e3)
     del S2, R2
 
+    # the other FP64 form on the same state, error against the headline form
+    opo = mol.MOLOperator(problems.make_config(mech, time_passes=1, precision=forms[other]))
+    best_o, tune_ms_o = opo.autotune(S, R, st.dx, reps=3)
+    t_oth, _ = timed_steps(opo)
+    ms_cell_o, ms_flux_o = pass_times(opo)
+    opo.rhs_level(S, R, st.dx)
+    torch.cuda.synchronize()
+    r_oth = R.fabs[0].cpu().numpy()
+    mx_o = [float(np.abs(r_oth[n] - r64[n]).max() / max(np.abs(r64[n]).max(), 1e-300)) for n in range(r64.shape[0])]
+    fs_o = [float(np.abs(r_oth[n] - r64[n]).max() / max(flux_scale[n], 1e-300)) for n in range(r64.shape[0])]
+    opo.close()
+
     # mixed precision on the same state, error against the FP64 result
     opm = mol.MOLOperator(problems.make_config(mech, time_passes=1, precision=1))
     best_m, tune_ms_m = opm.autotune(S, R, st.dx, reps=3)
@@ -628,6 +658,7 @@ def run_gpu(args):
     r32 = R.fabs[0].cpu().numpy()
     l2 = [float(np.sqrt(((r32[n] - r64[n]) ** 2).sum() / max((r64[n] ** 2).sum(), 1e-300))) for n in range(r64.shape[0])]
     mx = [float(np.abs(r32[n] - r64[n]).max() / max(np.abs(r64[n]).max(), 1e-300)) for n in range(r64.shape[0])]
+    fs_m = [float(np.abs(r32[n] - r64[n]).max() / max(flux_scale[n], 1e-300)) for n in range(r64.shape[0])]
 
     level = None if args.no_level else bench_level(args, rank, local, maxover, barrier)
     adj = None if args.no_adjoint else bench_adjoint_rhs(args, st, mech, S, maxover, barrier)
@@ -646,7 +677,7 @@ def run_gpu(args):
         os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
     achieved = ab / (ms_rhs * 1e-3) / 1e9
-    prof = profile_figures(args.workload)
+    prof = profile_figures(args.workload, args.precision)
     traffic = prof.get("dram_bytes_per_rhs")
     peaks_fp = fp_peaks()
     line = {
@@ -654,7 +685,8 @@ def run_gpu(args):
         "warmup": args.warmup, "ms_per_step": 1e3 * t_dev / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": desc, "boxes_per_gpu": 1, "cells_per_gpu": cells, "nspec": mech.nspec,
-                   "precision": "fp64", "l2": "inputs larger than L2 (state %.0f MB, scratch records %.0f MB)" % (
+                   "precision": args.precision, "precision_note": FORM_NOTE[args.precision],
+                   "l2": "inputs larger than L2 (state %.0f MB, scratch records %.0f MB)" % (
                        st.S.nbytes / 1e6, cells * (10 + 4 * mech.nspec) * 8 * 1.1 / 1e6),
                    "flux_launch": launch_name(best),
                    "autotune_ms_per_launch": {launch_name(t): v for t, v in enumerate(tune_ms)}},
@@ -669,9 +701,18 @@ def run_gpu(args):
                      "fp64": fp64_roofline(prof, ms_rhs, peaks_fp),
                      "fp64_pipe_active_pct": {"flux_kernel": prof.get("fp64_pipe_active_pct_flux_kernel"),
                                               "cell_kernel": prof.get("fp64_pipe_active_pct_cell_kernel"),
-                                              "source": "ncu --set full, profiles/flux_kernel_c2.md, cell_kernel_c2.md"},
+                                              "source": "ncu, profiles/dram_traffic_%s_%s.txt" % (
+                                                  args.workload, args.precision)},
                      "fp_peaks": peaks_fp},
         "passes_ms": {"cell_kernel": ms_cell, "flux_kernel": ms_flux},
+        other: {"value": world * cells * args.steps / t_oth, "unit": "cell-evals/s",
+                "ms_per_step": 1e3 * t_oth / args.steps, "passes_ms": {"cell_kernel": ms_cell_o, "flux_kernel": ms_flux_o},
+                "flux_launch": launch_name(best_o),
+                "autotune_ms_per_launch": {launch_name(t): v for t, v in enumerate(tune_ms_o)},
+                "rel_max_vs_headline": {"max": max(mx_o), "per_component": mx_o},
+                "flux_scaled_max_vs_headline": {"max": max(fs_o), "per_component": fs_o,
+                                                "scale": "max over faces of |F_n| / V per component"},
+                "precision_note": FORM_NOTE[other]},
         "mixed": {"value": world * cells * args.steps / t_mix, "unit": "cell-evals/s",
                   "ms_per_step": 1e3 * t_mix / args.steps, "speedup_vs_fp64": t_dev / t_mix,
                   "passes_ms": {"cell_kernel": ms_cell_m, "flux_kernel": ms_flux_m},
@@ -679,6 +720,7 @@ def run_gpu(args):
                   "autotune_ms_per_launch": {launch_name(t): v for t, v in enumerate(tune_ms_m)},
                   "rel_l2_vs_fp64": {"max": max(l2), "per_component": l2},
                   "rel_max_vs_fp64": {"max": max(mx), "per_component": mx},
+                  "flux_scaled_max_vs_fp64": {"max": max(fs_m), "per_component": fs_m},
                   "precision": "FP32 reconstruction/Riemann/diffusion, FP64 Newton/mass fractions/divergence"},
         "gpu_launches_mixed": 2 * args.steps,
         "status": {"cells": status.cells, "newton_nonconverged": status.newton_nonconverged,

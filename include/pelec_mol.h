@@ -61,10 +61,23 @@ typedef enum pc_transport_kind {
 
 /* Arithmetic of the right-hand side. */
 typedef enum pc_precision {
-  PC_PRECISION_FP64 = 0, /* every operation in FP64                          */
-  PC_PRECISION_MIXED = 1 /* FP32 reconstruction, Riemann and diffusion
-                            fluxes; FP64 EOS Newton solve, mass-fraction
-                            renormalisation and flux-divergence accumulation */
+  PC_PRECISION_FP64 = 0,    /* every operation in FP64, each quotient
+                               correctly rounded                           */
+  PC_PRECISION_MIXED = 1,   /* FP32 reconstruction, Riemann and diffusion
+                               fluxes; FP64 EOS Newton solve, mass-fraction
+                               renormalisation and flux-divergence
+                               accumulation                                */
+  PC_PRECISION_FP64_RCP = 2 /* every operation in FP64; a quotient by a
+                               divisor shared by several numerators (Y_k =
+                               rhoY_k / rho, the slopes' 1/c, the face-state
+                               renormalisation, the Riemann weights, 1/V) is
+                               the product with the divisor's correctly
+                               rounded reciprocal, within one ulp of the
+                               PC_PRECISION_FP64 quotient: about 1.2x faster,
+                               and different from PC_PRECISION_FP64 by
+                               rounding (as a build with multiply-add
+                               contraction would be), about 1e-15 of each
+                               component's flux scale |F|/V               */
 } pc_precision;
 
 /* Species data.  Thermodynamics is NASA-7 per species:
@@ -206,7 +219,7 @@ int pc_mol_rhs_level_per_box(pc_mol_handle* h, const pc_box_desc* boxes,
  * getMOLSrcTerm hands to the flux registers for refluxing on multi-level
  * runs (Diffusion.cpp:652-670).  fluxes[3*b + d] covers
  * surroundingNodes(valid_b, d); the RHS is the same as without the export.
- * PC_PRECISION_FP64 only.  Asynchronous on stream. */
+ * PC_PRECISION_FP64 and PC_PRECISION_FP64_RCP.  Asynchronous on stream. */
 int pc_mol_rhs_level_fluxes(pc_mol_handle* h, const pc_box_desc* boxes, int nboxes, const double dx[3],
                             const pc_array4* fluxes, void* stream);
 

@@ -29,6 +29,7 @@ PC_TRANSPORT_CONSTANT = 0
 PC_TRANSPORT_SIMPLE = 1
 PC_PRECISION_FP64 = 0
 PC_PRECISION_MIXED = 1
+PC_PRECISION_FP64_RCP = 2
 
 # Conserved-state indices, Source/IndexDefines.H:6-13,60.
 URHO, UMX, UMY, UMZ, UEDEN, UEINT, UTEMP, UFS = range(8)

@@ -1,6 +1,6 @@
 """Build recipe of the CUDA library ``pelec_gb300/_lib/libpelec_mol.so``.
 
-Six translation units compiled by nvcc for sm_103a only (in parallel) and
+Seven translation units compiled by nvcc for sm_103a only (in parallel) and
 linked into one shared library with a plain C ABI (include/pelec_mol.h), no
 torch headers:
 
@@ -16,6 +16,9 @@ torch headers:
   (their re-evaluated forward quantities must be the forward's own).
 * pc_tangent.cu — the Jacobian-vector product (the forward passes on dual
   numbers), without contraction for the same reason.
+* pc_rhs_rcp.cu — the FP64 passes a second time, with quotients by a shared
+  divisor as products with its reciprocal (PC_PRECISION_FP64_RCP), without
+  contraction like pc_mol.cu.
 
 libpc_peaks.so (pc_peaks.cu) measures the FP64/FP32 FMA rates that bench.py
 uses as roofline denominators.
@@ -35,7 +38,8 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler",
 LIBS = {
     "libpelec_mol.so": [("pc_mol.cu", ["-fmad=false"]), ("pc_mol_mixed.cu", ["-fmad=true"]),
                         ("pc_tiles_fp64.cu", ["-fmad=false"]), ("pc_tiles_mixed.cu", ["-fmad=true"]),
-                        ("pc_adjoint.cu", ["-fmad=false"]), ("pc_tangent.cu", ["-fmad=false"])],
+                        ("pc_adjoint.cu", ["-fmad=false"]), ("pc_tangent.cu", ["-fmad=false"]),
+                        ("pc_rhs_rcp.cu", ["-fmad=false"])],
     # arithmetic peak rates for bench.py's roofline (not part of the ABI)
     "libpc_peaks.so": [("pc_peaks.cu", ["-fmad=true"])],
 }

@@ -12,7 +12,15 @@
 #include <math_constants.h>
 #include <stdint.h>
 
-namespace pcg {
+// A translation unit may compile this code a second time with quotients by a
+// shared divisor taken as products with its reciprocal (PCG_RECIPROCAL_QUOTIENTS,
+// see div_by); it then names its namespace differently (PCG_NAMESPACE), so
+// that the two compilations of the same templates never meet at link time.
+#ifndef PCG_NAMESPACE
+#define PCG_NAMESPACE pcg
+#endif
+
+namespace PCG_NAMESPACE {
 
 constexpr double RU = 8.31446261815324e7;  // erg/(mol K)
 
@@ -63,6 +71,13 @@ struct DevFlags {
 // outside |a|, |b| in [2^-400, 2^401) (where a remainder could underflow) and
 // for infinities and NaNs it divides directly.
 __device__ __forceinline__ double div_by(double a, double b, double y) {
+#ifdef PCG_RECIPROCAL_QUOTIENTS
+  // The PC_PRECISION_FP64_RCP compilation: a y = a/b (1 + e) with
+  // |e| <= 2^-52 + 2^-106, within one ulp of the correctly rounded quotient,
+  // at a fifth of the FP64 operations.
+  (void)b;
+  return a * y;
+#else
   const int ha = __double2hiint(a), hb = __double2hiint(b);
   const double q0 = a * y;
   if (((ha & 0x7fffffff) | __double2loint(a)) == 0) return q0;  // +-0 numerator: the signed zero quotient
@@ -72,6 +87,7 @@ __device__ __forceinline__ double div_by(double a, double b, double y) {
   const double q = fma(r, y, q0);
   r = fma(-b, q, a);
   return fma(r, y, q);
+#endif
 }
 
 // The functions below are templates on the scalar type R: double for the
@@ -314,4 +330,4 @@ __device__ __forceinline__ R mc_limit(R dl, R dr) {
   return copysign(1.0, dcen) * fmin(dlim, fabs(dcen));
 }
 
-}  // namespace pcg
+}  // namespace PCG_NAMESPACE

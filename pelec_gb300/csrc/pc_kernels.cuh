@@ -26,7 +26,7 @@
 
 #include "pc_device.cuh"
 
-namespace pcg {
+namespace PCG_NAMESPACE {
 
 struct DevBox {
   int lo[3], hi[3];
@@ -734,4 +734,4 @@ inline cudaError_t launch_flux_fp64(const DevBox* boxes, const int4* tiles, int 
   return cudaGetLastError();
 }
 
-}  // namespace pcg
+}  // namespace PCG_NAMESPACE

@@ -18,6 +18,7 @@
 #include "pc_adjoint.cuh"
 #include "pc_kernels.cuh"
 #include "pc_level.cuh"
+#include "pc_rcp.h"
 #include "pelec_mol.h"
 
 namespace pcg {
@@ -405,7 +406,37 @@ int run(pc_mol_handle* h, const pc_box_desc* boxes, int nboxes, const double dx[
   const bool timed = h->cfg.time_passes != 0 && !per_box;
   h->timed = timed;
   const bool mixed = h->cfg.precision == PC_PRECISION_MIXED;
+  const bool rcp = h->cfg.precision == PC_PRECISION_FP64_RCP;
   auto go = [&](int ib, int ie, int tb, int te) {
+    if (rcp) {
+      RcpLaunch a{};
+      a.variant = h->variant;
+      a.tile = h->lay_tile;
+      a.persistent = h->tile >= kNumTiles;
+      a.boxes = h->d_boxes;
+      a.items = h->d_items + ib;
+      a.nitems = ie - ib;
+      a.tiles = h->d_tiles + tb;
+      a.ntiles = te - tb;
+      if (h->variant == 1) {
+        a.mech = &h->mech1;
+        a.mech_size = sizeof h->mech1;
+      } else {
+        a.mech = &h->mech9;
+        a.mech_size = sizeof h->mech9;
+      }
+      a.flags = &h->flags;
+      a.flags_size = sizeof h->flags;
+      a.geo = &g;
+      a.geo_size = sizeof g;
+      a.fluxes = fx;
+      a.fluxbox_size = sizeof(FluxBox);
+      a.devbox_size = sizeof(DevBox);
+      a.counters = h->d_counters;
+      a.stream = s;
+      for (int k = 0; k < 3; ++k) a.ev[k] = timed ? h->ev[k] : nullptr;
+      return cuda_fail(h, launch_rhs_rcp(a));
+    }
     if (mixed) {
       const double p_ref = h->cfg.mixed_p_ref > 0.0 ? h->cfg.mixed_p_ref : 1013250.0;
       Geo gm = g;
@@ -452,7 +483,8 @@ int pc_mol_create(pc_mol_handle** out, const pc_mol_config* cfg) {
   *out = nullptr;
   const pc_mol_config& c = *cfg;
   if (c.nspec != c.mech.nspec) return PC_ERR_INVALID_ARGUMENT;
-  if (c.precision != PC_PRECISION_FP64 && c.precision != PC_PRECISION_MIXED) return PC_ERR_INVALID_ARGUMENT;
+  if (c.precision != PC_PRECISION_FP64 && c.precision != PC_PRECISION_MIXED && c.precision != PC_PRECISION_FP64_RCP)
+    return PC_ERR_INVALID_ARGUMENT;
   int variant = 0;
   if (c.nspec == 1 && c.eos == PC_EOS_GAMMA_LAW && c.transport == PC_TRANSPORT_CONSTANT) variant = 1;
   if (c.nspec == 9 && c.eos == PC_EOS_IDEAL_MIX && c.transport == PC_TRANSPORT_SIMPLE) variant = 9;
@@ -1203,7 +1235,7 @@ extern "C" int pc_mol_rhs_level_fluxes(pc_mol_handle* h, const pc_box_desc* boxe
                                        const pc_array4* fluxes, void* stream) {
   if (!h) return PC_ERR_INVALID_ARGUMENT;
   if (nboxes < 0 || (nboxes > 0 && (!boxes || !fluxes))) return h->last_error = PC_ERR_INVALID_ARGUMENT;
-  if (h->cfg.precision != PC_PRECISION_FP64) return h->last_error = PC_ERR_UNSUPPORTED;
+  if (h->cfg.precision == PC_PRECISION_MIXED) return h->last_error = PC_ERR_UNSUPPORTED;
   const int nvar = 7 + h->cfg.nspec;
   std::vector<FluxBox> fb(nboxes);
   for (int b = 0; b < nboxes; ++b) {
