@@ -294,4 +294,10 @@ int oracle_est_dt(const pc_mol_config* cfg, const pc_box_desc* boxes, int nboxes
   return PC_OK;
 }
 
+// The transport's exp and log (pc_exp.h) over an array, for their accuracy
+// tests.  which = 0: exp, 1: log.
+void oracle_exp_log(int which, const double* x, double* y, long long n) {
+  for (long long i = 0; i < n; ++i) y[i] = which == 0 ? pc_math::exp(x[i]) : pc_math::log(x[i]);
+}
+
 }  // extern "C"

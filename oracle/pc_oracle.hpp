@@ -20,6 +20,11 @@
 // restated from their published physics; the species tables are the
 // caller's (pc_mechanism).  What the reference does pin (conservation,
 // symmetry, single-species zero diffusion) is checked by the tests.
+//
+// The transport's exp and log are pc_exp.h's (pelec_gb300/csrc), the
+// table-driven functions the kernels call too, instead of the host libm's:
+// within one ulp of the correctly rounded values (tests/test_oracle.py), and
+// the same bits on every host and on the GPU.
 #pragma once
 
 #include <algorithm>
@@ -29,6 +34,7 @@
 #include <limits>
 #include <vector>
 
+#include "pc_exp.h"
 #include "pelec_mol.h"
 
 namespace orc {
@@ -318,16 +324,16 @@ struct SimpleTransport {
     eos.Y2X(Y, X);
     double p;
     eos.RTY2P(rho, T, Y, p);
-    const double L = std::log(T);
+    const double L = pc_math::log(T);
     double smu = 0.0, slam = 0.0, sxi = 0.0;
     for (int k = 0; k < NS; ++k) {
-      const double mk = std::exp(fit(m->visc_fit[k], L));
+      const double mk = pc_math::exp(fit(m->visc_fit[k], L));
       const double m2 = mk * mk;
       smu = std::fma(X[k], m2 * m2 * m2, smu);
-      slam = std::fma(X[k], std::exp(0.25 * fit(m->cond_fit[k], L)), slam);
+      slam = std::fma(X[k], pc_math::exp(0.25 * fit(m->cond_fit[k], L)), slam);
       sxi = std::fma(X[k], m->bulk_ratio[k] * mk, sxi);
     }
-    mu = std::exp(std::log(smu) * (1.0 / 6.0));
+    mu = pc_math::exp(pc_math::log(smu) * (1.0 / 6.0));
     const double l2 = slam * slam;
     lam = l2 * l2;
     xi = sxi;
@@ -337,7 +343,7 @@ struct SimpleTransport {
       double s = 0.0;
       for (int j = 0; j < NS; ++j) {
         if (j == k) continue;
-        const double invD = std::exp(-fit(m->diff_fit[std::min(j, k)][std::max(j, k)], L)) * pr;
+        const double invD = pc_math::exp(-fit(m->diff_fit[std::min(j, k)][std::max(j, k)], L)) * pr;
         s = std::fma(std::max(X[j], 1e-15), invD, s);
       }
       // W_k / Wbar = (R/Wbar) / (R/W_k): rhoD_k grad X_k is then the

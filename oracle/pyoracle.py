@@ -42,6 +42,8 @@ def library() -> ctypes.CDLL:
         lib.oracle_riemann_face.argtypes = [POINTER(abi.PcMolConfig), POINTER(c_double), POINTER(c_double), c_double,
                                             POINTER(c_double), POINTER(c_double)]
         lib.oracle_max_threads.restype = c_int
+        lib.oracle_exp_log.argtypes = [c_int, POINTER(c_double), POINTER(c_double), c_longlong]
+        lib.oracle_exp_log.restype = None
         _lib = lib
     return _lib
 
@@ -241,3 +243,11 @@ def ssprk2_step(cfg: abi.PcMolConfig, boxes, geom: abi.PcGeometry, dt: float):
         v[...] = 1.0 * v + (0.5 * dt) * r
     compute_temp(cfg, new)
     return new
+
+
+def exp_log(which: int, x: np.ndarray) -> np.ndarray:
+    """pc_exp.h's exp (which=0) or log (which=1) of each entry of x."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    y = np.empty_like(x)
+    library().oracle_exp_log(int(which), _dptr(x), _dptr(y), x.size)
+    return y

@@ -255,15 +255,15 @@ template <int NS>
 struct TransAdj<NS, SimpleTransport<NS>> {
   __device__ static void eval(const DevMech<NS>& m, double T, double rho, double p, const double* Y, const double* X,
                               const double* ob, double& Tb, double& rhob, double& pb, double* Yb, double* Xb) {
-    const double L = log(T);
+    const double L = pc_log(T);
     double smu = 0.0, slam = 0.0;
     double mk[NS], lk[NS];
 #pragma unroll
     for (int k = 0; k < NS; ++k) {
-      mk[k] = exp(horner4(m.visc[k], L));
+      mk[k] = pc_exp(horner4(m.visc[k], L));
       const double m2 = mk[k] * mk[k];
       smu = fma(X[k], m2 * m2 * m2, smu);
-      lk[k] = exp(0.25 * horner4(m.cond[k], L));
+      lk[k] = pc_exp(0.25 * horner4(m.cond[k], L));
       slam = fma(X[k], lk[k], slam);
     }
     double s[NS];
@@ -276,7 +276,7 @@ struct TransAdj<NS, SimpleTransport<NS>> {
       for (int k = 0; k < NS; ++k)
 #pragma unroll
         for (int j = k + 1; j < NS; ++j, ++q) {
-          const double invD = exp(-horner4(m.diff[q], L)) * pr;
+          const double invD = pc_exp(-horner4(m.diff[q], L)) * pr;
           s[k] = fma(fmax(X[j], 1e-15), invD, s[k]);
           s[j] = fma(fmax(X[k], 1e-15), invD, s[j]);
         }
@@ -307,7 +307,7 @@ struct TransAdj<NS, SimpleTransport<NS>> {
       for (int k = 0; k < NS; ++k)
 #pragma unroll
         for (int j = k + 1; j < NS; ++j, ++q) {
-          const double e0 = exp(-horner4(m.diff[q], L));
+          const double e0 = pc_exp(-horner4(m.diff[q], L));
           const double invD = e0 * pr;
           const double xj = fmax(X[j], 1e-15), xk = fmax(X[k], 1e-15);
           const double invDb = sb[k] * xj + sb[j] * xk;
@@ -319,7 +319,7 @@ struct TransAdj<NS, SimpleTransport<NS>> {
     }
     pb += prb * m.inv_pref;
     // mu = smu^(1/6), xi = sum X bulk mk, lambda = slam^4
-    const double mu = exp(log(smu) * (1.0 / 6.0));
+    const double mu = pc_exp(pc_log(smu) * (1.0 / 6.0));
     const double smub = (smu > 0.0) ? ob[NS] * mu * (1.0 / 6.0) / smu : 0.0;
     const double sxib = ob[NS + 1];
     const double slamb = ob[NS + 2] * 4.0 * slam * slam * slam;

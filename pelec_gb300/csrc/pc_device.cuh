@@ -12,6 +12,8 @@
 #include <math_constants.h>
 #include <stdint.h>
 
+#include "pc_exp.h"
+
 // A translation unit may compile this code a second time with quotients by a
 // shared divisor taken as products with its reciprocal (PCG_RECIPROCAL_QUOTIENTS,
 // see div_by); it then names its namespace differently (PCG_NAMESPACE), so
@@ -89,6 +91,12 @@ __device__ __forceinline__ double div_by(double a, double b, double y) {
   return fma(r, y, q);
 #endif
 }
+
+// exp and log of the transport fits: pc_exp.h's table-driven functions, the
+// ones the CPU restatement evaluates too (the Dual overloads are in
+// pc_dual.cuh).
+__device__ __forceinline__ double pc_exp(double x) { return pc_math::exp(x); }
+__device__ __forceinline__ double pc_log(double x) { return pc_math::log(x); }
 
 // The functions below are templates on the scalar type R: double for the
 // RHS, Dual (pc_dual.cuh) for its forward-mode tangent.
@@ -275,14 +283,14 @@ template <int NS>
 struct SimpleTransport {
   template <class R>
   __device__ static void eval(const DevMech<NS>& m, R T, R rho, R p, const R* Y, const R* X, R* out) {
-    const R L = log(T);
+    const R L = pc_log(T);
     R smu = 0.0, slam = 0.0, sxi = 0.0;
 #pragma unroll
     for (int k = 0; k < NS; ++k) {
-      const R mk = exp(horner4(m.visc[k], L));
+      const R mk = pc_exp(horner4(m.visc[k], L));
       const R m2 = mk * mk;
       smu = fma(X[k], m2 * m2 * m2, smu);
-      slam = fma(X[k], exp(0.25 * horner4(m.cond[k], L)), slam);
+      slam = fma(X[k], pc_exp(0.25 * horner4(m.cond[k], L)), slam);
       sxi = fma(X[k], m.bulk[k] * mk, sxi);
     }
     R s[NS];
@@ -294,7 +302,7 @@ struct SimpleTransport {
     for (int k = 0; k < NS; ++k) {
 #pragma unroll
       for (int j = k + 1; j < NS; ++j, ++q) {
-        const R invD = exp(-horner4(m.diff[q], L)) * pr;
+        const R invD = pc_exp(-horner4(m.diff[q], L)) * pr;
         s[k] = fma(fmax(X[j], 1e-15), invD, s[k]);
         s[j] = fma(fmax(X[k], 1e-15), invD, s[j]);
       }
@@ -305,7 +313,7 @@ struct SimpleTransport {
       const R wrat = rw / m.rW[k];  // W_k / Wbar
       out[k] = (s[k] > 0.0) ? rho * (1.0 - Y[k]) * wrat / s[k] : 0.0;
     }
-    out[NS] = exp(log(smu) * (1.0 / 6.0));
+    out[NS] = pc_exp(pc_log(smu) * (1.0 / 6.0));
     out[NS + 1] = sxi;
     const R l2 = slam * slam;
     out[NS + 2] = l2 * l2;

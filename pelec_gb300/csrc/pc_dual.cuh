@@ -9,6 +9,8 @@
 
 #include <cuda_runtime.h>
 
+#include "pc_exp.h"
+
 namespace pcg {
 
 // The double overloads stay visible next to the Dual ones.
@@ -102,10 +104,11 @@ __device__ __forceinline__ Dual sqrt(const Dual& a) {
   const double s = ::sqrt(a.v);
   return Dual(s, (s > 0.0) ? a.d / (2.0 * s) : 0.0);
 }
-__device__ __forceinline__ Dual exp(const Dual& a) {
-  const double e = ::exp(a.v);
+// The transport's exp and log (pc_exp.h) on dual numbers.
+__device__ __forceinline__ Dual pc_exp(const Dual& a) {
+  const double e = ::pc_math::exp(a.v);
   return Dual(e, e * a.d);
 }
-__device__ __forceinline__ Dual log(const Dual& a) { return Dual(::log(a.v), a.d / a.v); }
+__device__ __forceinline__ Dual pc_log(const Dual& a) { return Dual(::pc_math::log(a.v), a.d / a.v); }
 
 }  // namespace pcg
