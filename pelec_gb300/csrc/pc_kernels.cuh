@@ -567,12 +567,27 @@ __host__ __device__ constexpr int tile_extent(int t, int d) {
 constexpr int kTX = TileDefault::TX, kTY = TileDefault::TY, kTZ = TileDefault::TZ, kFluxThreads = TileDefault::NT;
 constexpr int kMaxFaces = TileDefault::MAXF;
 
+// What a CTA hands from one tile to the next tile up the same column (z
+// pass only): the fluxes of the shared face layer and the slopes of the cell
+// layer above it, which the next tile would otherwise evaluate again.
+//   carry: this tile continues the column of the CTA's previous tile: take
+//          face layer 0 and slope layer 1 from cflux / cslope;
+//   save:  the CTA's next tile continues this one: leave the top face layer
+//          and the top slope layer there.
+struct ZCarry {
+  bool carry, save;
+  double* cflux;   // NVAR x (TX TY)
+  double* cslope;  // (4 + NS) x (TX TY)
+};
+
 // One direction of pass 2: every face of the tile with normal d, staged in
 // shared memory, then differenced into the cell accumulators.
 template <int NS, class EOS, int d, class TL>
 __device__ __forceinline__ void dir_pass(const DevBox& b, const DevMech<NS>& m, const DevFlags& f, const Geo& g,
                                          const int o[3], const int ext[3], const long long stv[3], bool mine, int tx,
-                                         int ty, int tz, double* fbuf, double* acc, const FluxBox* fxb) {
+                                         int ty, int tz, double* fbuf, double* acc, const FluxBox* fxb,
+                                         const ZCarry& zc) {
+  constexpr int LAYER = TL::TX * TL::TY;  // carry buffer stride
   constexpr int NVAR = 7 + NS;
   constexpr int NSL = 4 + NS;  // slope fields of a cell
   const RecAcc<double> ra{b.rec, b.ncell};
@@ -582,10 +597,18 @@ __device__ __forceinline__ void dir_pass(const DevBox& b, const DevMech<NS>& m, 
   // each evaluated once: field q of cell ci at sbuf[q MAXC + ci].
   double* sbuf = fbuf + NVAR * TL::MAXF;
   const int ne0 = ext[0] + 2 * (d == 0), ne1 = ext[1] + 2 * (d == 1), ne2 = ext[2] + 2 * (d == 2);
+  const bool carry = d == 2 && zc.carry;
   if (slopes) {
     const int ncells = ne0 * ne1 * ne2;
     for (int ci = threadIdx.x; ci < ncells; ci += TL::NT) {
       const int ex = ci % ne0, ey = (ci / ne0) % ne1, ez = ci / (ne0 * ne1);
+      if (carry && ez < 2) {  // layer 0 feeds only face layer 0 (carried); layer 1 is the carried top layer
+        if (ez == 1) {
+#pragma unroll
+          for (int q = 0; q < NSL; ++q) sbuf[q * TL::MAXC + ci] = zc.cslope[q * LAYER + ex + ne0 * ey];
+        }
+        continue;
+      }
       const int i = o[0] + ex - (d == 0), j = o[1] + ey - (d == 1), k = o[2] + ez - (d == 2);
       const long long c = (i - b.g2lo[0]) + (j - b.g2lo[1]) * stv[1] + (k - b.g2lo[2]) * stv[2];
       double sl[NSL];
@@ -601,6 +624,11 @@ __device__ __forceinline__ void dir_pass(const DevBox& b, const DevMech<NS>& m, 
   for (int fi = threadIdx.x; fi < nfaces; fi += TL::NT) {
     const int fx = fi % nf0, fy = (fi / nf0) % nf1, fz = fi / (nf0 * nf1);
     const int i = o[0] + fx, j = o[1] + fy, k = o[2] + fz;
+    if (carry && fz == 0) {  // the face layer the previous tile of the column evaluated (and exported)
+#pragma unroll
+      for (int n = 0; n < NVAR; ++n) fbuf[n * TL::MAXF + fi] = zc.cflux[n * LAYER + fx + nf0 * fy];
+      continue;
+    }
     const long long cR = (i - b.g2lo[0]) + (j - b.g2lo[1]) * stv[1] + (k - b.g2lo[2]) * stv[2];
     double F[NVAR];
     if (f.do_hydro) {
@@ -632,6 +660,17 @@ __device__ __forceinline__ void dir_pass(const DevBox& b, const DevMech<NS>& m, 
     }
   }
   __syncthreads();
+  if (d == 2 && zc.save) {  // top face layer and top slope layer, for the next tile of the column
+    const int nl = nf0 * nf1;
+    for (int l = threadIdx.x; l < nl; l += TL::NT) {
+#pragma unroll
+      for (int n = 0; n < NVAR; ++n) zc.cflux[n * LAYER + l] = fbuf[n * TL::MAXF + (nf2 - 1) * nl + l];
+      if (slopes) {
+#pragma unroll
+        for (int q = 0; q < NSL; ++q) zc.cslope[q * LAYER + l] = sbuf[q * TL::MAXC + (ne2 - 1) * nl + l];
+      }
+    }
+  }
   if (mine) {
     const int flo = tx + nf0 * (ty + nf1 * tz);
     const int fhi = flo + ((d == 0) ? 1 : (d == 1) ? nf0 : nf0 * nf1);
@@ -641,15 +680,22 @@ __device__ __forceinline__ void dir_pass(const DevBox& b, const DevMech<NS>& m, 
   __syncthreads();
 }
 
-// Dynamic shared memory of the FP64 flux pass: face fluxes and cell slopes.
+// Dynamic shared memory of the FP64 flux pass: face fluxes, cell slopes and
+// the z carry (one face layer, one slope layer).
 template <int NS, class TL>
 constexpr size_t flux_smem_bytes() {
-  return sizeof(double) * ((size_t)(7 + NS) * TL::MAXF + (size_t)(4 + NS) * TL::MAXC);
+  return sizeof(double) * ((size_t)(7 + NS) * TL::MAXF + (size_t)(4 + NS) * TL::MAXC +
+                           (size_t)(7 + NS + 4 + NS) * TL::TX * TL::TY);
 }
 
-// Pass 2 over the tile list.  CTA b takes tiles b, b + gridDim.x, ... : with
-// one CTA per tile every CTA takes one; a persistent launch (as many CTAs as
-// fit on the GPU at once) strides over the whole list.
+// Pass 2 over the tile list.  CTA b takes the contiguous share
+// [b n / G, (b + 1) n / G) of the n tiles (G = gridDim.x): one tile each when
+// G = n; in a persistent launch (as many CTAs as fit on the GPU at once) a
+// run of tiles.  The list holds each column of a box's tiles bottom to top,
+// so consecutive tiles of a run are mostly z neighbours, and the z pass hands
+// its top face and slope layers on (ZCarry) instead of having them evaluated
+// again: a tile of 8x8x4 cells then evaluates 4 z face layers and 4 z slope
+// layers instead of 5 and 6.
 template <int NS, class EOS, class TL = TileDefault>
 __global__ void __launch_bounds__(TL::NT, TL::MINB)
     flux_kernel(const DevBox* __restrict__ boxes, const int4* __restrict__ tiles, int ntiles,
@@ -659,7 +705,17 @@ __global__ void __launch_bounds__(TL::NT, TL::MINB)
   extern __shared__ double flux_dyn_smem[];
   double* fbuf = flux_dyn_smem;
   const int tx = threadIdx.x % TL::TX, ty = (threadIdx.x / TL::TX) % TL::TY, tz = threadIdx.x / (TL::TX * TL::TY);
-  for (int tb = blockIdx.x; tb < ntiles; tb += gridDim.x) {
+  ZCarry zc;
+  zc.cflux = fbuf + (size_t)NVAR * TL::MAXF + (size_t)(4 + NS) * TL::MAXC;
+  zc.cslope = zc.cflux + (size_t)NVAR * TL::TX * TL::TY;
+  const int t0 = (int)((long long)blockIdx.x * ntiles / gridDim.x);
+  const int t1 = (int)((long long)(blockIdx.x + 1) * ntiles / gridDim.x);
+  // the next tile continues tile a's column: same box and x/y origin, z origin one tile up
+  auto continues = [&](int a) {
+    const int4 p = tiles[a], q = tiles[a + 1];
+    return q.x == p.x && q.y == p.y && q.z == p.z && q.w == p.w + TL::TZ;
+  };
+  for (int tb = t0; tb < t1; ++tb) {
     const int4 t = tiles[tb];
     const DevBox& b = boxes[t.x];
     const int o[3] = {t.y, t.z, t.w};
@@ -671,9 +727,11 @@ __global__ void __launch_bounds__(TL::NT, TL::MINB)
 #pragma unroll
     for (int n = 0; n < NVAR; ++n) acc[n] = 0.0;
     const FluxBox* fxb = fluxes ? fluxes + t.x : nullptr;
-    dir_pass<NS, EOS, 0, TL>(b, m, f, g, o, ext, stv, mine, tx, ty, tz, fbuf, acc, fxb);
-    dir_pass<NS, EOS, 1, TL>(b, m, f, g, o, ext, stv, mine, tx, ty, tz, fbuf, acc, fxb);
-    dir_pass<NS, EOS, 2, TL>(b, m, f, g, o, ext, stv, mine, tx, ty, tz, fbuf, acc, fxb);
+    zc.carry = tb > t0 && continues(tb - 1);
+    zc.save = tb + 1 < t1 && continues(tb);
+    dir_pass<NS, EOS, 0, TL>(b, m, f, g, o, ext, stv, mine, tx, ty, tz, fbuf, acc, fxb, zc);
+    dir_pass<NS, EOS, 1, TL>(b, m, f, g, o, ext, stv, mine, tx, ty, tz, fbuf, acc, fxb, zc);
+    dir_pass<NS, EOS, 2, TL>(b, m, f, g, o, ext, stv, mine, tx, ty, tz, fbuf, acc, fxb, zc);
     bool bad = false;
     if (mine) {
       const int i = o[0] + tx, j = o[1] + ty, k = o[2] + tz;

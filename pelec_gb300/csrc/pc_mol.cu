@@ -225,9 +225,11 @@ void build_layout(const pc_box_desc* boxes, int nboxes, int nrec, int tile, Layo
     L.item_start.push_back((int)L.items.size());
     for (long long c = 0; c < d.ncell; c += kCellThreads) L.items.push_back(make_int2(bi, (int)c));
     L.tile_start.push_back((int)L.tiles.size());
-    for (int k = b.lo[2]; k <= b.hi[2]; k += TZ)
-      for (int j = b.lo[1]; j <= b.hi[1]; j += TY)
-        for (int i = b.lo[0]; i <= b.hi[0]; i += TX) L.tiles.push_back(make_int4(bi, i, j, k));
+    // each column of tiles bottom to top: a persistent CTA's run of tiles
+    // then hands its z face and slope layers from one tile to the next
+    for (int j = b.lo[1]; j <= b.hi[1]; j += TY)
+      for (int i = b.lo[0]; i <= b.hi[0]; i += TX)
+        for (int k = b.lo[2]; k <= b.hi[2]; k += TZ) L.tiles.push_back(make_int4(bi, i, j, k));
   }
   L.item_start.push_back((int)L.items.size());
   L.tile_start.push_back((int)L.tiles.size());

@@ -71,8 +71,9 @@ def test_every_tile_shape_single_species(cuda_lib, oracle_lib):
 @pytest.mark.parametrize("precision", [abi.PC_PRECISION_FP64, abi.PC_PRECISION_MIXED])
 def test_persistent_grid_strides_over_every_tile(cuda_lib, precision):
     """A 64^3 flame has more tiles than the GPU holds CTAs at any shape, so
-    each CTA of a persistent launch takes several tiles: same RHS bit for bit
-    as one CTA per tile, and every cell counted once."""
+    each CTA of a persistent launch takes a run of several tiles (handing the
+    z face and slope layers up each column): same RHS bit for bit as one CTA
+    per tile, and every cell counted once."""
     mol = cuda_lib
     mech, st, _ = problems.flame((64, 64, 64), w_noise=1.0)
     cfg = problems.make_config(mech, precision=precision)
@@ -83,6 +84,21 @@ def test_persistent_grid_strides_over_every_tile(cuda_lib, precision):
         np.testing.assert_array_equal(pers, one, err_msg=f"shape {shape}")
         assert np.isfinite(pers).all()
         assert op.status().cells == 64 ** 3
+    if precision == abi.PC_PRECISION_FP64:
+        # the exported face fluxes too: a persistent CTA hands the z face layer
+        # between consecutive tiles of a column instead of evaluating it again
+        import torch
+
+        out = []
+        for t in (0, abi.PC_LAUNCH_PERSISTENT):
+            op.set_tile(t)
+            S = to_multifab(mol, [st], st.ng)
+            R = mol.MultiFab([(st.lo, st.hi)], st.S.shape[0], 0)
+            F = op.rhs_level_fluxes(S, R, st.dx)[0]
+            torch.cuda.synchronize()
+            out.append([f.cpu().numpy() for f in F] + [R.fabs[0].cpu().numpy()])
+        for a, b in zip(*out):
+            np.testing.assert_array_equal(a, b)
 
 
 def test_autotune_caches_choice_per_histogram(cuda_lib):
