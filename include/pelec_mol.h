@@ -362,6 +362,14 @@ int pc_mol_rhs_jvp(pc_mol_handle* h, const pc_box_desc* boxes, int nboxes, const
 int pc_mol_est_dt(pc_mol_handle* h, const pc_box_desc* boxes, int nboxes, const double dx[3], double cfl,
                   double max_dt, double* dt, void* stream);
 
+/* Diagnostic: q[i] = a[i] / b[i] (device arrays of n doubles) through the
+ * exact shared-divisor quotient of the FP64 kernels (the product with the
+ * IEEE reciprocal of b, corrected to the correctly rounded quotient in
+ * integer arithmetic).  No counterpart in the reference; it lets a test
+ * compare that routine with IEEE division on arbitrary operands.
+ * Asynchronous on stream. */
+int pc_mol_check_quotients(const double* a, const double* b, double* q, long long n, void* stream);
+
 /* Right-hand side of ONE box without allocating any device memory.  This
  * entry point has no counterpart in the reference: it exists for callers
  * that cannot call cudaMalloc while they run (code recording a CUDA stream

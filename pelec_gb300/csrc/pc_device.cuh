@@ -63,33 +63,164 @@ struct DevFlags {
 // is compiled without multiply-add contraction).  The CPU restatement used
 // to check the kernels evaluates the same sequence.
 
+// Runs f() on the lanes where need holds, inside a branch that a warp takes
+// only if one of its lanes needs it, so that rare paths cost nothing in warps
+// where no lane needs them.  The empty volatile asm keeps the compiler from
+// evaluating the path's FP64 operations speculatively on every lane (code
+// without side effects may otherwise be executed ahead of its branch).
+template <class F>
+__device__ __forceinline__ void rare_for_warp(bool need, F&& f) {
+  if (__any_sync(__activemask(), need)) {
+    if (need) {
+      asm volatile("");
+      f();
+    }
+  }
+}
+
 // a / b, correctly rounded, for a divisor b shared by several quotients, given
-// y = 1.0 / b (an IEEE division).  Markstein's theorem (IBM J. Res. Dev. 34,
-// 1990): if y = RN(1/b) and q is within one ulp of a/b, the remainder
-// r = a - b q is exact in one fma and RN(q + r y) = RN(a/b).  q0 = RN(a y) can
-// be up to 1.5 ulp off, so one correction brings it within an ulp and a
-// second gives the correctly rounded quotient: 1 multiply + 4 fma instead of
-// a full division.  A zero numerator gives a*y, the correctly signed zero;
-// outside |a|, |b| in [2^-400, 2^401) (where a remainder could underflow) and
-// for infinities and NaNs it divides directly.
-__device__ __forceinline__ double div_by(double a, double b, double y) {
+// y = 1.0 / b (an IEEE division), without a branch: the result for the
+// common operands, with slow set for the rare ones that need a real division
+// (the caller then evaluates again with exact_quotient, see Quot).
+//
+// q0 = RN(a y) is within two ulps of a/b (y and the product each round by at
+// most half an ulp), so the correctly rounded quotient is q0 + s ulp(q0) for
+// some s in [-2, 2].  s is decided exactly in integer arithmetic on the
+// significands, off the FP64 pipe (the binding resource on GB300, which runs
+// integer instructions at 32-64 times its FP64 rate): with
+// a = A 2^(ea-1075), b = B 2^(eb-1075) and q0 = M 2^(eq-1075) (A, B, M the
+// 53-bit significands),
+//   R = A 2^k - B M,   k = ea - eb - eq + 1075 (51 <= k <= 54),
+// equals (a/b - q0) / ulp(q0) times B and |R| < 2B < 2^54, so it is exact
+// modulo 2^64; and as k >= 32, A 2^k mod 2^64 depends only on A's low word.
+// s counts the half-integers 1/2 and 3/2 that R/B exceeds (a quotient of two
+// doubles is never exactly halfway between two doubles, so there are no
+// ties), and s ulp is added to q0's bit pattern.  One FP64 multiply instead
+// of a division.  A zero numerator gives a*y, the correctly signed zero.
+// Slow: a nonzero numerator that is subnormal, infinite or NaN; b zero,
+// subnormal, infinite, NaN or above 2^1022 (1/b not a normal number); q0
+// outside [2^-1021, 2^1022) (the quotient or its neighbours not normal); or
+// q0's significand within 4 of either end of its binade (where s ulp could
+// cross into a binade of other spacing).  For a zero numerator only b zero or
+// subnormal (1/b infinite).
+__device__ __forceinline__ double div_fast(double a, double b, double y, bool& slow) {
 #ifdef PCG_RECIPROCAL_QUOTIENTS
   // The PC_PRECISION_FP64_RCP compilation: a y = a/b (1 + e) with
-  // |e| <= 2^-52 + 2^-106, within one ulp of the correctly rounded quotient,
-  // at a fifth of the FP64 operations.
+  // |e| <= 2^-52 + 2^-106, within one ulp of the correctly rounded quotient.
+  (void)b;
+  (void)slow;
+  return a * y;
+#else
+  const double q0 = a * y;
+  const unsigned ah = (unsigned)__double2hiint(a), al = (unsigned)__double2loint(a);
+  const unsigned bh = (unsigned)__double2hiint(b), bl = (unsigned)__double2loint(b);
+  const unsigned qh = (unsigned)__double2hiint(q0), ql = (unsigned)__double2loint(q0);
+  const unsigned ea = (ah >> 20) & 0x7ffu, eb = (bh >> 20) & 0x7ffu, eq = (qh >> 20) & 0x7ffu;
+  const unsigned sh = (ea - eb - eq + 1043u) & 31u;  // k - 32
+  const unsigned Bh = (bh & 0xfffffu) | 0x100000u, Mh = (qh & 0xfffffu) | 0x100000u;
+  const unsigned long long p = (unsigned long long)bl * ql;  // B M mod 2^64 = p + (bl Mh + Bh ql) 2^32
+  const unsigned phi = (unsigned)(p >> 32) + bl * Mh + Bh * ql;
+  const long long R = (long long)(((unsigned long long)(al << sh) << 32) - (((unsigned long long)phi << 32) | (unsigned)p));
+  const long long Bs = (long long)(((unsigned long long)Bh << 32) | bl), R2 = 2 * R, B3 = 3 * Bs;
+  const long long st = (long long)(R2 > Bs) + (long long)(R2 > B3) - (long long)(R2 < -Bs) - (long long)(R2 < -B3);
+  const bool zero = ((ah << 1) | al) == 0u;
+  const bool edge = (((qh & 0xfffffu) + 1u) & 0xfffffu) <= 1u && ql + 4u <= 8u;
+  slow |= zero ? (eb == 0u) : (ea - 1u > 2045u || eb - 1u > 2043u || eq - 2u > 2043u || edge);
+  const unsigned long long iq = ((unsigned long long)qh << 32) | ql;
+  return zero ? q0 : __longlong_as_double((long long)(iq + (unsigned long long)st));
+#endif
+}
+
+// a / b by IEEE division (a y in the PC_PRECISION_FP64_RCP compilation).
+__device__ __forceinline__ double exact_quotient(double a, double b, double y) {
+#ifdef PCG_RECIPROCAL_QUOTIENTS
   (void)b;
   return a * y;
 #else
-  const int ha = __double2hiint(a), hb = __double2hiint(b);
-  const double q0 = a * y;
-  if (((ha & 0x7fffffff) | __double2loint(a)) == 0) return q0;  // +-0 numerator: the signed zero quotient
-  const unsigned ea = (unsigned)((ha >> 20) & 0x7ff), eb = (unsigned)((hb >> 20) & 0x7ff);
-  if (ea - 623u > 800u || eb - 623u > 800u) return a / b;
-  double r = fma(-b, q0, a);
-  const double q = fma(r, y, q0);
-  r = fma(-b, q, a);
-  return fma(r, y, q);
+  (void)y;
+  return a / b;
 #endif
+}
+
+// a / b, correctly rounded, for a divisor b shared by several quotients, given
+// y = 1.0 / b: div_fast, with the rare operands divided in a branch that only
+// warps containing one take.
+__device__ __forceinline__ double div_by(double a, double b, double y) {
+  bool slow = false;
+  double q = div_fast(a, b, y, slow);
+  rare_for_warp(slow, [&] { q = exact_quotient(a, b, y); });
+  return q;
+}
+
+// Quotient policy of a pass.  Quot<false> divides with div_fast and records
+// in .slow whether any operand needed a real division; a pass evaluated that
+// way counts such lanes, and an exact twin of the pass (Quot<true>: IEEE
+// division), launched after it, evaluates everything again when the count is
+// not zero.  The fast pass thus has no branch per quotient, and the compiler
+// can interleave the integer work of neighbouring quotients.  Other scalar
+// types (the dual numbers of the tangent) divide with their own div_by.
+template <bool kExact>
+struct Quot;
+template <>
+struct Quot<false> {
+  bool slow = false;
+  template <class R>
+  __device__ __forceinline__ R operator()(const R& a, const R& b, const R& y) {
+    return div_by(a, b, y);
+  }
+  __device__ __forceinline__ double operator()(double a, double b, double y) { return div_fast(a, b, y, slow); }
+};
+template <>
+struct Quot<true> {
+  bool slow = false;
+  template <class R>
+  __device__ __forceinline__ R operator()(const R& a, const R& b, const R& y) {
+    return div_by(a, b, y);
+  }
+  __device__ __forceinline__ double operator()(double a, double b, double y) { return exact_quotient(a, b, y); }
+};
+
+// Exact binary scalings on the bit patterns (integer pipe).  Multiplying by
+// 0.5 or 2 is exact except where the result leaves the normal range, and
+// those cases are rounded here as IEEE multiplication rounds them, so the
+// results equal 0.5 * x and 2 * |x| bit for bit.
+__device__ __forceinline__ unsigned long long dbits(double x) { return (unsigned long long)__double_as_longlong(x); }
+__device__ __forceinline__ double dfrom(unsigned long long b) { return __longlong_as_double((long long)b); }
+
+// 0.5 * x (R = double: integer form; other scalar types multiply).
+template <class R>
+__device__ __forceinline__ R halve(R x) {
+  return 0.5 * x;
+}
+template <>
+__device__ __forceinline__ double halve<double>(double x) {
+  const unsigned long long b = dbits(x), sgn = b & 0x8000000000000000ULL, mag = b ^ sgn;
+  const unsigned e = (unsigned)(mag >> 52);
+  unsigned long long r;
+  if (e >= 2u)
+    r = (e == 0x7ffu) ? mag : mag - (1ULL << 52);  // normal result (infinities and NaNs unchanged)
+  else
+    r = (mag >> 1) + (mag & (mag >> 1) & 1ULL);  // subnormal result: halve the integer significand, ties to even
+  return dfrom(r | sgn);
+}
+
+// 2 * m for the bit pattern m of a non-negative double.
+__device__ __forceinline__ unsigned long long twice_mag(unsigned long long m) {
+  const unsigned e = (unsigned)(m >> 52);
+  if (e == 0u) return m << 1;                                 // zero or subnormal: exact (may become normal)
+  if (e >= 0x7feu) return e == 0x7ffu ? m : 0x7ff0000000000000ULL;  // inf/NaN unchanged; overflow to inf
+  return m + (1ULL << 52);
+}
+
+// copysign(1, s) * x (R = double: x with its sign bit flipped where s is
+// negative, which is what the multiplication by +-1 gives).
+template <class R>
+__device__ __forceinline__ R signed_by(R x, R s) {
+  return copysign(1.0, s) * x;
+}
+template <>
+__device__ __forceinline__ double signed_by<double>(double x, double s) {
+  return dfrom(dbits(x) ^ (dbits(s) & 0x8000000000000000ULL));
 }
 
 // exp and log of the transport fits: pc_exp.h's table-driven functions, the
@@ -115,11 +246,16 @@ __device__ __forceinline__ R mix_rw(const DevMech<NS>& m, const R* Y) {
 }
 
 // Y2X: X_k = Y_k (R/W_k) / (R/Wbar).
-template <int NS, class R>
-__device__ __forceinline__ void y2x(const DevMech<NS>& m, const R* Y, R rw, R* X) {
+template <int NS, class R, class Q>
+__device__ __forceinline__ void y2x(const DevMech<NS>& m, const R* Y, R rw, R* X, Q& q) {
   const R irw = 1.0 / rw;
 #pragma unroll
-  for (int k = 0; k < NS; ++k) X[k] = div_by(Y[k] * m.rW[k], rw, irw);  // = Y_k (R/W_k) / rw
+  for (int k = 0; k < NS; ++k) X[k] = q(Y[k] * m.rW[k], rw, irw);  // = Y_k (R/W_k) / rw
+}
+template <int NS, class R>
+__device__ __forceinline__ void y2x(const DevMech<NS>& m, const R* Y, R rw, R* X) {
+  Quot<true> q;
+  y2x(m, Y, rw, X, q);
 }
 
 // ---------------------------------------------------------------------------
@@ -336,6 +472,22 @@ __device__ __forceinline__ R mc_limit(R dl, R dr) {
   const R dcen = 0.5 * (dl + dr);
   const R dlim = (dl * dr >= 0.0) ? 2.0 * fmin(fabs(dl), fabs(dr)) : R(0.0);
   return copysign(1.0, dcen) * fmin(dlim, fabs(dcen));
+}
+
+// The same limiter for double, with every step that is exact in binary done
+// on the bit patterns by the integer pipe: the halving of dl + dr (halve),
+// min(|dl|, |dr|) and min(dlim, |dcen|) (non-negative doubles order like
+// their bit patterns; a NaN never wins, like fmin), the doubling (twice_mag)
+// and the sign of dcen (copysign(1, dcen) * r = r with dcen's sign bit for
+// r >= 0).  Only dl + dr and the sign test dl * dr >= 0 stay on the FP64
+// pipe: 3 FP64 operations instead of 8, bit for bit the same result.
+__device__ __forceinline__ double mc_limit(double dl, double dr) {
+  constexpr unsigned long long kSign = 0x8000000000000000ULL;
+  const unsigned long long bc = dbits(halve(dl + dr));
+  const unsigned long long sgn = bc & kSign, acen = bc ^ sgn;
+  const unsigned long long al = dbits(dl) & ~kSign, ar = dbits(dr) & ~kSign;
+  const unsigned long long dlim = (dl * dr >= 0.0) ? twice_mag(al < ar ? al : ar) : 0ULL;
+  return dfrom((dlim < acen ? dlim : acen) | sgn);
 }
 
 }  // namespace PCG_NAMESPACE

@@ -98,7 +98,18 @@ struct FluxBox {
   int pad;
 };
 
-enum { kCounterCells = 0, kCounterNewton = 1, kCounterNonpos = 2, kCounterNonfinite = 3, kNumCounters = 4 };
+// kCounterSlowCell / kCounterSlowFlux: lanes of the fast cell / flux pass
+// with an operand that div_fast leaves to a real division; nonzero makes the
+// exact twin of that pass evaluate it again.
+enum {
+  kCounterCells = 0,
+  kCounterNewton = 1,
+  kCounterNonpos = 2,
+  kCounterNonfinite = 3,
+  kCounterSlowCell = 4,
+  kCounterSlowFlux = 5,
+  kNumCounters = 6
+};
 
 __device__ __forceinline__ void warp_count(unsigned long long* ctr, bool pred) {
   const unsigned m = __ballot_sync(0xffffffffu, pred);
@@ -124,9 +135,9 @@ __device__ __forceinline__ double rey2t_of(const DevMech<NS>& m, const double* Y
 // U(UTEMP); st(field, value) writes a record field.  inner: the cell lies in
 // grow(valid, 1), where the diffusion fluxes need T, X, h and the transport
 // coefficients.
-template <int NS, class EOS, class TR, class R, class Store>
+template <int NS, class EOS, class TR, class R, class Store, class Q = Quot<true>>
 __device__ __forceinline__ void cell_record(const DevMech<NS>& m, const DevFlags& f, const R* U, double Tguess,
-                                            bool inner, Store st, bool& newton_fail, bool& nonpos) {
+                                            bool inner, Store st, bool& newton_fail, bool& nonpos, Q&& q = Q()) {
   using RC = Rec<NS>;
   const R rho = U[URHO];
   const R rhoinv = 1.0 / rho;
@@ -138,7 +149,7 @@ __device__ __forceinline__ void cell_record(const DevMech<NS>& m, const DevFlags
   R Y[NS];
 #pragma unroll
   for (int n = 0; n < NS; ++n) {
-    R y = div_by(U[UFS + n], rho, rhoinv);  // = rho Y_n / rho, correctly rounded
+    R y = q(U[UFS + n], rho, rhoinv);  // = rho Y_n / rho, correctly rounded
     if (-1e-4 * 2.220446049250313e-16 < y && y < 1e-4 * 2.220446049250313e-16) y = 0.0;
     Y[n] = y;
   }
@@ -160,7 +171,7 @@ __device__ __forceinline__ void cell_record(const DevMech<NS>& m, const DevFlags
   if (inner) {
     // Mole fractions (Y2X) and enthalpies (T2Hi) of the cell.
     R X[NS];
-    y2x(m, Y, rw, X);
+    y2x(m, Y, rw, X, q);
     R out[NS + 3];
     TR::eval(m, T, rho, p, Y, X, out);
     st(RC::T, T);
@@ -188,15 +199,21 @@ __device__ __forceinline__ bool in_grow1(const DevBox& b, int i, int j, int k) {
          k <= b.hi[2] + 1;
 }
 
-template <int NS, class EOS, class TR>
+// kExact = false: the fast pass (quotients by div_fast); kExact = true: its
+// exact twin, which returns at once unless the fast pass counted a lane that
+// needs a real division, and then writes every record again with IEEE
+// quotients (bit for bit what the fast pass gives where it needs none).
+template <int NS, class EOS, class TR, bool kExact = false>
 __global__ void __launch_bounds__(kCellThreads)
     cell_kernel(const DevBox* __restrict__ boxes, const int2* __restrict__ items, const __grid_constant__ DevMech<NS> m,
                 const DevFlags f, unsigned long long* __restrict__ counters) {
   constexpr int NVAR = 7 + NS;
+  if (kExact && __ldcg(&counters[kCounterSlowCell]) == 0ull) return;
   const int2 it = items[blockIdx.x];
   const DevBox& b = boxes[it.x];
   const long long c = (long long)it.y + threadIdx.x;
   bool newton_fail = false, nonpos = false;
+  Quot<kExact> quo;
   if (c < b.ncell) {
     int i, j, k;
     cell_index(b, c, i, j, k);
@@ -208,10 +225,28 @@ __global__ void __launch_bounds__(kCellThreads)
     double* r = b.rec + c;
     const long long N = b.ncell;
     cell_record<NS, EOS, TR>(m, f, U, __ldg(s + UTEMP * sn), in_grow1(b, i, j, k),
-                             [&](int fld, double v) { r[fld * N] = v; }, newton_fail, nonpos);
+                             [&](int fld, double v) { r[fld * N] = v; }, newton_fail, nonpos, quo);
   }
-  warp_count(&counters[kCounterNewton], newton_fail);
-  warp_count(&counters[kCounterNonpos], nonpos);
+  if (!kExact) {  // the exact twin re-evaluates cells the fast pass has counted already
+    warp_count(&counters[kCounterNewton], newton_fail);
+    warp_count(&counters[kCounterNonpos], nonpos);
+    warp_count(&counters[kCounterSlowCell], quo.slow);
+  }
+}
+
+// Host: the cell pass over nitems chunks: the fast kernel, then its exact
+// twin (which returns at once unless the fast kernel counted a lane that
+// needs a real division).  The PC_PRECISION_FP64_RCP compilation has no
+// such lanes and launches the fast kernel only.
+template <int NS, class EOS, class TR>
+inline cudaError_t launch_cell_fp64(const DevBox* boxes, const int2* items, unsigned nitems, const DevMech<NS>& m,
+                                    const DevFlags& f, unsigned long long* counters, cudaStream_t s) {
+  if (nitems == 0) return cudaSuccess;
+  cell_kernel<NS, EOS, TR, false><<<nitems, kCellThreads, 0, s>>>(boxes, items, m, f, counters);
+#ifndef PCG_RECIPROCAL_QUOTIENTS
+  cell_kernel<NS, EOS, TR, true><<<nitems, kCellThreads, 0, s>>>(boxes, items, m, f, counters);
+#endif
+  return cudaGetLastError();
 }
 
 // ---------------------------------------------------------------------------
@@ -223,8 +258,9 @@ __global__ void __launch_bounds__(kCellThreads)
 // MOL.H:53-112): the characteristic slopes dq[0..3] and the species slopes
 // ds[NS].  A function of the cells c - st, c and c + st only, so one
 // evaluation serves both faces of the cell.
-template <int NS, int d, class R>
-__device__ __forceinline__ void cell_slopes(const RecAcc<R>& ra, long long c, long long st, R* dq, R* ds) {
+template <int NS, int d, class R, class Q = Quot<true>>
+__device__ __forceinline__ void cell_slopes(const RecAcc<R>& ra, long long c, long long st, R* dq, R* ds,
+                                            Q&& q = Q()) {
   using RC = Rec<NS>;
   auto ld = [&](int fld, long long cc) { return ra.ld(fld, cc); };
   const long long cm = c - st, cp = c + st;
@@ -238,8 +274,8 @@ __device__ __forceinline__ void cell_slopes(const RecAcc<R>& ra, long long c, lo
   const R yc = 1.0 / c0;
   const R dpl = p0 - pm, dpr = pp - p0;
   {
-    const R a = div_by(0.5 * dpl, c0, yc), bb = 0.5 * r0 * (u0 - um);
-    const R a2 = div_by(0.5 * dpr, c0, yc), b2 = 0.5 * r0 * (up - u0);
+    const R a = q(halve(dpl), c0, yc), bb = halve(r0) * (u0 - um);
+    const R a2 = q(halve(dpr), c0, yc), b2 = halve(r0) * (up - u0);
     dq[0] = mc_limit(a - bb, a2 - b2);
     dq[1] = mc_limit(a + bb, a2 + b2);
   }
@@ -255,17 +291,17 @@ __device__ __forceinline__ void cell_slopes(const RecAcc<R>& ra, long long c, lo
   for (int n = 0; n < NS; ++n) {
     const R y0 = ld(RC::Y + n, c);
     const R ry0 = r0 * y0;
-    ds[n] = mc_limit(ry0 - rm * ld(RC::Y + n, cm) - div_by(y0 * dpl, c2, yc2),
-                     rp * ld(RC::Y + n, cp) - ry0 - div_by(y0 * dpr, c2, yc2));
+    ds[n] = mc_limit(ry0 - rm * ld(RC::Y + n, cm) - q(y0 * dpl, c2, yc2),
+                     rp * ld(RC::Y + n, cp) - ry0 - q(y0 * dpr, c2, yc2));
   }
 }
 
 // Hyperbolic flux on the low face of the cell at record index cR in
 // direction d, times the face area, given the slopes of its two cells.
-template <int NS, class EOS, int d, class R>
+template <int NS, class EOS, int d, class R, class Q = Quot<true>>
 __device__ __forceinline__ void hydro_face_sl(const RecAcc<R>& ra, const DevMech<NS>& m, const DevFlags& f,
                                               long long cR, long long st, double A, const R* dqL, const R* dsL,
-                                              const R* dqR, const R* dsR, R* F) {
+                                              const R* dqR, const R* dsR, R* F, Q&& q = Q()) {
   using RC = Rec<NS>;
   const long long cL = cR - st;
   auto ld = [&](int fld, long long c) { return ra.ld(fld, c); };
@@ -279,14 +315,14 @@ __device__ __forceinline__ void hydro_face_sl(const RecAcc<R>& ra, const DevMech
   const R t1L = ld(fut1, cL), t1R = ld(fut1, cR), t2L = ld(fut2, cL), t2R = ld(fut2, cR);
   const R ycL = 1.0 / cLc, ycR = 1.0 / cRc;
   // Face states (MOL.cpp:69-123).
-  const R unl = uL + 0.5 * ((dqL[1] - dqL[0]) / rL);
-  const R pl = pL + 0.5 * (dqL[0] + dqL[1]) * cLc;
-  const R ut1l = t1L + 0.5 * dqL[2];
-  const R ut2l = t2L + 0.5 * dqL[3];
-  const R unr = uR - 0.5 * ((dqR[1] - dqR[0]) / rR);
-  const R pr = pR - 0.5 * (dqR[0] + dqR[1]) * cRc;
-  const R ut1r = t1R - 0.5 * dqR[2];
-  const R ut2r = t2R - 0.5 * dqR[3];
+  const R unl = uL + halve((dqL[1] - dqL[0]) / rL);
+  const R pl = pL + halve(dqL[0] + dqL[1]) * cLc;
+  const R ut1l = t1L + halve(dqL[2]);
+  const R ut2l = t2L + halve(dqL[3]);
+  const R unr = uR - halve((dqR[1] - dqR[0]) / rR);
+  const R pr = pR - halve(dqR[0] + dqR[1]) * cRc;
+  const R ut1r = t1R - halve(dqR[2]);
+  const R ut2r = t2R - halve(dqR[3]);
   R spl[NS], spr[NS];
   R rl = 0.0, rr = 0.0;
   {
@@ -294,19 +330,19 @@ __device__ __forceinline__ void hydro_face_sl(const RecAcc<R>& ra, const DevMech
 #pragma unroll
     for (int n = 0; n < NS; ++n) {
       const R yL = ld(RC::Y + n, cL), yR = ld(RC::Y + n, cR);
-      spl[n] = yL * rL + 0.5 * (dsL[n] + div_by(yL * sL, cLc, ycL));
-      spr[n] = yR * rR - 0.5 * (dsR[n] + div_by(yR * sR, cRc, ycR));
+      spl[n] = yL * rL + halve(dsL[n] + q(yL * sL, cLc, ycL));
+      spr[n] = yR * rR - halve(dsR[n] + q(yR * sR, cRc, ycR));
       rl += spl[n];
       rr += spr[n];
     }
     const R yrl = 1.0 / rl, yrr = 1.0 / rr;
 #pragma unroll
     for (int n = 0; n < NS; ++n) {
-      spl[n] = div_by(spl[n], rl, yrl);
-      spr[n] = div_by(spr[n], rr, yrr);
+      spl[n] = q(spl[n], rl, yrl);
+      spr[n] = q(spr[n], rr, yrr);
     }
   }
-  const R cavg = 0.5 * (cRc + cLc);
+  const R cavg = halve(cRc + cLc);
   R fl_rho, fl_un, fl_ut1, fl_ut2, fl_E, fl_ei;
   R flY[NS];
   const R rwl = mix_rw<NS>(m, spl), rwr = mix_rw<NS>(m, spr);
@@ -318,28 +354,39 @@ __device__ __forceinline__ void hydro_face_sl(const RecAcc<R>& ra, const DevMech
     const R wl = fmax(wsmall, cl * rl);
     const R wr = fmax(wsmall, cr * rr);
     const R ww = wl + wr, yww = 1.0 / ww;
-    const R pstar = fmax(wsmall, div_by((wr * pl + wl * pr) + wl * wr * (unl - unr), ww, yww));
-    R ustar = div_by((wl * unl + wr * unr) + (pl - pr), ww, yww);
+    const R pstar = fmax(wsmall, q((wr * pl + wl * pr) + wl * wr * (unl - unr), ww, yww));
+    R ustar = q((wl * unl + wr * unr) + (pl - pr), ww, yww);
     bool mask = ustar > 0.0;
     R rspo[NS];
     R uo = mask ? unl : unr;
     R po = mask ? pl : pr;
     const bool m0 = fabs(ustar) < kSmallU * 0.5 * (fabs(unl) + fabs(unr)) || ustar == 0.0;
     ustar = m0 ? 0.0 : ustar;
+    {
+      const R ro_ = mask ? rl : rr;
+#pragma unroll
+      for (int n = 0; n < NS; ++n) rspo[n] = ro_ * (mask ? spl[n] : spr[n]);
+    }
+    R iv1 = mask ? ut1l : ut1r;
+    R iv2 = mask ? ut2l : ut2r;
+    // u* = 0 (Riemann.H:79-85, 131-133): the average of both sides.  Rare, so
+    // evaluated only in warps where some face needs it.
+    rare_for_warp(m0, [&] {
+#pragma unroll
+      for (int n = 0; n < NS; ++n) rspo[n] = halve(rl * spl[n] + rr * spr[n]);
+      uo = halve(unl + unr);
+      po = halve(pl + pr);
+      iv1 = halve(ut1l + ut1r);
+      iv2 = halve(ut2l + ut2r);
+    });
     R ro = 0.0;
 #pragma unroll
-    for (int n = 0; n < NS; ++n) {
-      const R a = rl * spl[n], bq = rr * spr[n];
-      rspo[n] = m0 ? 0.5 * (a + bq) : (mask ? a : bq);
-      ro += rspo[n];
-    }
-    uo = m0 ? 0.5 * (unl + unr) : uo;
-    po = m0 ? 0.5 * (pl + pr) : po;
+    for (int n = 0; n < NS; ++n) ro += rspo[n];
     R Yt[NS];
     {
       const R y = 1.0 / ro;
 #pragma unroll
-      for (int n = 0; n < NS; ++n) Yt[n] = div_by(rspo[n], ro, y);
+      for (int n = 0; n < NS; ++n) Yt[n] = q(rspo[n], ro, y);
     }
     const R co = EOS::cs_rp(m, Yt, mix_rw<NS>(m, Yt), ro, po);
     const R drho = (pstar - po) / (co * co);
@@ -353,44 +400,41 @@ __device__ __forceinline__ void hydro_face_sl(const RecAcc<R>& ra, const DevMech
     {
       const R y = 1.0 / rstar;
 #pragma unroll
-      for (int n = 0; n < NS; ++n) Yt[n] = div_by(rspstar[n], rstar, y);
+      for (int n = 0; n < NS; ++n) Yt[n] = q(rspstar[n], rstar, y);
     }
     const R cstar = EOS::cs_rp(m, Yt, mix_rw<NS>(m, Yt), rstar, pstar);
-    const R sgnm = copysign(1.0, ustar);
-    R spout = co - sgnm * uo;
-    R spin = cstar - sgnm * ustar;
-    const R ushock = 0.5 * (spin + spout);
+    R spout = co - signed_by(uo, ustar);     // co - copysign(1, u*) uo
+    R spin = cstar - signed_by(ustar, ustar);
+    const R ushock = halve(spin + spout);
     mask = pstar < po;
     spout = mask ? spout : ushock;
     spin = mask ? spin : ushock;
-    const R scr = (fabs(spout - spin) < PCG_VERY_SMALL_NUM) ? kSmallNum * cavg : spout - spin;
-    const R frac = fmax(0.0, fmin(1.0, (1.0 + (spout + spin) / scr) * 0.5));
-    mask = ustar > 0.0;
-    R iv1 = mask ? ut1l : ut1r;
-    R iv2 = mask ? ut2l : ut2r;
-    mask = (ustar == 0.0);
-    iv1 = mask ? 0.5 * (ut1l + ut1r) : iv1;
-    iv2 = mask ? 0.5 * (ut2l + ut2r) : iv2;
+    // Godunov state (Riemann.H:123-162): the star state where spin >= 0, else
+    // the upwind state where spout < 0, else the rarefaction-fan blend.  The
+    // blend and its fraction are evaluated only in warps where some face lies
+    // in a fan (transonic rarefactions; none in subsonic flow).
     const bool mout = spout < 0.0, min_ = spin >= 0.0;
-    R iu = frac * ustar + (1.0 - frac) * uo;
-    R gdp = frac * pstar + (1.0 - frac) * po;
-    iu = mout ? uo : iu;
-    gdp = mout ? po : gdp;
-    iu = min_ ? ustar : iu;
-    gdp = min_ ? pstar : gdp;
+    R iu = min_ ? ustar : uo;
+    R gdp = min_ ? pstar : po;
+#pragma unroll
+    for (int n = 0; n < NS; ++n) flY[n] = min_ ? rspstar[n] : rspo[n];
+    const bool fan = !min_ && !mout;
+    rare_for_warp(fan, [&] {
+      const R scr = (fabs(spout - spin) < PCG_VERY_SMALL_NUM) ? kSmallNum * cavg : spout - spin;
+      const R frac = fmax(0.0, fmin(1.0, (1.0 + (spout + spin) / scr) * 0.5));
+      const R omf = 1.0 - frac;
+      iu = frac * ustar + omf * uo;
+      gdp = frac * pstar + omf * po;
+#pragma unroll
+      for (int n = 0; n < NS; ++n) flY[n] = frac * rspstar[n] + omf * rspo[n];
+    });
     R rgd = 0.0;
 #pragma unroll
-    for (int n = 0; n < NS; ++n) {
-      R g = frac * rspstar[n] + (1.0 - frac) * rspo[n];
-      g = mout ? rspo[n] : g;
-      g = min_ ? rspstar[n] : g;
-      flY[n] = g;
-      rgd += g;
-    }
+    for (int n = 0; n < NS; ++n) rgd += flY[n];
     {
       const R y = 1.0 / rgd;
 #pragma unroll
-      for (int n = 0; n < NS; ++n) Yt[n] = div_by(flY[n], rgd, y);
+      for (int n = 0; n < NS; ++n) Yt[n] = q(flY[n], rgd, y);
     }
     const R regd = rgd * EOS::e_rp(m, Yt, mix_rw<NS>(m, Yt), rgd, gdp);
     fl_rho = rgd * iu;
@@ -399,7 +443,7 @@ __device__ __forceinline__ void hydro_face_sl(const RecAcc<R>& ra, const DevMech
     fl_un = fl_rho * iu + gdp;
     fl_ut1 = fl_rho * iv1;
     fl_ut2 = fl_rho * iv2;
-    const R rhoetot = regd + 0.5 * rgd * (iu * iu + iv1 * iv1 + iv2 * iv2);
+    const R rhoetot = regd + halve(rgd) * (iu * iu + iv1 * iv1 + iv2 * iv2);
     fl_E = iu * (rhoetot + gdp);
     fl_ei = iu * regd;
   } else {
@@ -497,23 +541,23 @@ __device__ __forceinline__ void diffusion_face(const RecAcc<R>& ra, const DevFla
   }
   const R TR = ld(RC::T, cR), TL = ld(RC::T, cL);
   const R dTdd = g.dxinv[d] * (TR - TL);
-  R fE = 0.5 * (-tau[0] * (uR[0] + uL[0]) - tau[1] * (uR[1] + uL[1]) - tau[2] * (uR[2] + uL[2])) - lam * dTdd;
+  R fE = halve(-tau[0] * (uR[0] + uL[0]) - tau[1] * (uR[1] + uL[1]) - tau[2] * (uR[2] + uL[2])) - lam * dTdd;
   const double A = g.area[d];
   const bool spec = f.diffuse_spec != 0;
   const bool ener = (f.diffuse_temp != 0) || (f.diffuse_enth != 0);
   if (NS > 1 || spec || ener) {
     const R pR = ld(RC::P, cR), pL = ld(RC::P, cL);
     const R dpdx = g.dxinv[d] * (pR - pL);
-    const R dlnp = dpdx / (0.5 * (pR + pL));
+    const R dlnp = dpdx / halve(pR + pL);
     R Vd[NS], Yf[NS], hf[NS];
     R Vc = 0.0;
 #pragma unroll
     for (int n = 0; n < NS; ++n) {
       const R x1 = ld(RC::X + n, cR), x2 = ld(RC::X + n, cL);
       const R y1 = ld(RC::Y + n, cR), y2 = ld(RC::Y + n, cL);
-      const R Xface = 0.5 * (x1 + x2);
-      Yf[n] = 0.5 * (y1 + y2);
-      hf[n] = 0.5 * (ld(RC::H + n, cR) + ld(RC::H + n, cL));
+      const R Xface = halve(x1 + x2);
+      Yf[n] = halve(y1 + y2);
+      hf[n] = halve(ld(RC::H + n, cR) + ld(RC::H + n, cL));
       const R dXdx = g.dxinv[d] * (x1 - x2);
       const R D = face_coef(ld(RC::D + n, cR), ld(RC::D + n, cL), harm);
       Vd[n] = -D * (dXdx + (Xface - Yf[n]) * dlnp);
@@ -582,11 +626,11 @@ struct ZCarry {
 
 // One direction of pass 2: every face of the tile with normal d, staged in
 // shared memory, then differenced into the cell accumulators.
-template <int NS, class EOS, int d, class TL>
+template <int NS, class EOS, int d, class TL, class Q>
 __device__ __forceinline__ void dir_pass(const DevBox& b, const DevMech<NS>& m, const DevFlags& f, const Geo& g,
                                          const int o[3], const int ext[3], const long long stv[3], bool mine, int tx,
                                          int ty, int tz, double* fbuf, double* acc, const FluxBox* fxb,
-                                         const ZCarry& zc) {
+                                         const ZCarry& zc, Q& quo) {
   constexpr int LAYER = TL::TX * TL::TY;  // carry buffer stride
   constexpr int NVAR = 7 + NS;
   constexpr int NSL = 4 + NS;  // slope fields of a cell
@@ -612,7 +656,7 @@ __device__ __forceinline__ void dir_pass(const DevBox& b, const DevMech<NS>& m, 
       const int i = o[0] + ex - (d == 0), j = o[1] + ey - (d == 1), k = o[2] + ez - (d == 2);
       const long long c = (i - b.g2lo[0]) + (j - b.g2lo[1]) * stv[1] + (k - b.g2lo[2]) * stv[2];
       double sl[NSL];
-      cell_slopes<NS, d>(ra, c, stv[d], sl, sl + 4);
+      cell_slopes<NS, d>(ra, c, stv[d], sl, sl + 4, quo);
 #pragma unroll
       for (int q = 0; q < NSL; ++q) sbuf[q * TL::MAXC + ci] = sl[q];
     }
@@ -644,7 +688,7 @@ __device__ __forceinline__ void dir_pass(const DevBox& b, const DevMech<NS>& m, 
 #pragma unroll
         for (int q = 0; q < NSL; ++q) sL[q] = sR[q] = 0.0;
       }
-      hydro_face_sl<NS, EOS, d>(ra, m, f, cR, stv[d], g.area[d], sL, sL + 4, sR, sR + 4, F);
+      hydro_face_sl<NS, EOS, d>(ra, m, f, cR, stv[d], g.area[d], sL, sL + 4, sR, sR + 4, F, quo);
     } else {
 #pragma unroll
       for (int n = 0; n < NVAR; ++n) F[n] = 0.0;
@@ -696,12 +740,19 @@ constexpr size_t flux_smem_bytes() {
 // its top face and slope layers on (ZCarry) instead of having them evaluated
 // again: a tile of 8x8x4 cells then evaluates 4 z face layers and 4 z slope
 // layers instead of 5 and 6.
-template <int NS, class EOS, class TL = TileDefault>
+//
+// kExact = false: the fast pass (quotients by div_fast); kExact = true: its
+// exact twin, which returns at once unless the fast pass counted a lane that
+// needs a real division, and then evaluates every tile again with IEEE
+// quotients (bit for bit what the fast pass gives where it needs none).
+template <int NS, class EOS, class TL = TileDefault, bool kExact = false>
 __global__ void __launch_bounds__(TL::NT, TL::MINB)
     flux_kernel(const DevBox* __restrict__ boxes, const int4* __restrict__ tiles, int ntiles,
                 const __grid_constant__ DevMech<NS> m, const DevFlags f, const Geo g,
                 unsigned long long* __restrict__ counters, const FluxBox* __restrict__ fluxes) {
   constexpr int NVAR = 7 + NS;
+  if (kExact && __ldcg(&counters[kCounterSlowFlux]) == 0ull) return;
+  Quot<kExact> quo;
   extern __shared__ double flux_dyn_smem[];
   double* fbuf = flux_dyn_smem;
   const int tx = threadIdx.x % TL::TX, ty = (threadIdx.x / TL::TX) % TL::TY, tz = threadIdx.x / (TL::TX * TL::TY);
@@ -729,23 +780,26 @@ __global__ void __launch_bounds__(TL::NT, TL::MINB)
     const FluxBox* fxb = fluxes ? fluxes + t.x : nullptr;
     zc.carry = tb > t0 && continues(tb - 1);
     zc.save = tb + 1 < t1 && continues(tb);
-    dir_pass<NS, EOS, 0, TL>(b, m, f, g, o, ext, stv, mine, tx, ty, tz, fbuf, acc, fxb, zc);
-    dir_pass<NS, EOS, 1, TL>(b, m, f, g, o, ext, stv, mine, tx, ty, tz, fbuf, acc, fxb, zc);
-    dir_pass<NS, EOS, 2, TL>(b, m, f, g, o, ext, stv, mine, tx, ty, tz, fbuf, acc, fxb, zc);
+    dir_pass<NS, EOS, 0, TL>(b, m, f, g, o, ext, stv, mine, tx, ty, tz, fbuf, acc, fxb, zc, quo);
+    dir_pass<NS, EOS, 1, TL>(b, m, f, g, o, ext, stv, mine, tx, ty, tz, fbuf, acc, fxb, zc, quo);
+    dir_pass<NS, EOS, 2, TL>(b, m, f, g, o, ext, stv, mine, tx, ty, tz, fbuf, acc, fxb, zc, quo);
     bool bad = false;
     if (mine) {
       const int i = o[0] + tx, j = o[1] + ty, k = o[2] + tz;
       double* r = b.R + (i - b.rb[0]) + (long long)(j - b.rb[1]) * b.rj + (long long)(k - b.rb[2]) * b.rk;
 #pragma unroll
       for (int n = 0; n < NVAR; ++n) {
-        const double v = div_by(acc[n], g.vol, g.ivol);  // = acc[n] / vol, correctly rounded
+        const double v = quo(acc[n], g.vol, g.ivol);  // = acc[n] / vol, correctly rounded
         bad |= !isfinite(v);
         r[n * b.rn] = v;
       }
     }
-    if (f.check_output) warp_count(&counters[kCounterNonfinite], bad);
-    if (threadIdx.x == 0) atomicAdd(&counters[kCounterCells], (unsigned long long)(ext[0] * ext[1] * ext[2]));
+    if (!kExact) {  // the exact twin re-evaluates tiles the fast pass has counted already
+      if (f.check_output) warp_count(&counters[kCounterNonfinite], bad);
+      if (threadIdx.x == 0) atomicAdd(&counters[kCounterCells], (unsigned long long)(ext[0] * ext[1] * ext[2]));
+    }
   }
+  if (!kExact) warp_count(&counters[kCounterSlowFlux], quo.slow);
 }
 
 // Host: CTAs of a kernel that are resident on the current device at once
@@ -790,6 +844,44 @@ inline cudaError_t launch_flux_fp64(const DevBox* boxes, const int4* tiles, int 
   }
   flux_kernel<NS, EOS, TL><<<grid, TL::NT, smem, s>>>(boxes, tiles, ntiles, m, f, g, counters, fluxes);
   return cudaGetLastError();
+}
+
+// Host: the exact twin of the flux pass (flux_kernel with kExact), launched
+// after the fast pass of any tile shape; persistent, at the default tile
+// shape (every shape gives the same result).  Its CTAs return at once unless
+// the fast pass counted a lane that needs a real division.  Not needed in the
+// PC_PRECISION_FP64_RCP compilation.
+template <int NS, class EOS>
+inline cudaError_t launch_flux_exact(const DevBox* boxes, const int4* tiles, int ntiles, const DevMech<NS>& m,
+                                     const DevFlags& f, const Geo& g, unsigned long long* counters, cudaStream_t s,
+                                     const FluxBox* fluxes = nullptr) {
+#ifdef PCG_RECIPROCAL_QUOTIENTS
+  (void)boxes, (void)tiles, (void)ntiles, (void)m, (void)f, (void)g, (void)counters, (void)s, (void)fluxes;
+  return cudaSuccess;
+#else
+  using TL = TileDefault;
+  static std::atomic<unsigned long long> opted{0};
+  static std::atomic<int> resident[64];
+  constexpr size_t smem = flux_smem_bytes<NS, TL>();
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  const unsigned long long bit = (dev >= 0 && dev < 64) ? (1ull << dev) : 0ull;
+  if (!bit || !(opted.load() & bit)) {
+    e = cudaFuncSetAttribute(flux_kernel<NS, EOS, TL, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    opted.fetch_or(bit);
+  }
+  if (ntiles <= 0) return cudaSuccess;
+  int r = bit ? resident[dev].load() : 0;
+  if (r <= 0) {
+    r = resident_ctas(flux_kernel<NS, EOS, TL, true>, TL::NT, smem);
+    if (bit && r > 0) resident[dev].store(r);
+  }
+  const int grid = (r > 0 && r < ntiles) ? r : ntiles;
+  flux_kernel<NS, EOS, TL, true><<<grid, TL::NT, smem, s>>>(boxes, tiles, ntiles, m, f, g, counters, fluxes);
+  return cudaGetLastError();
+#endif
 }
 
 }  // namespace PCG_NAMESPACE

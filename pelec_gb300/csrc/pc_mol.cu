@@ -369,21 +369,21 @@ template <int NS, class EOS, class TR>
 int launch(pc_mol_handle* h, const DevMech<NS>& mech, const Geo& g, int ibeg, int iend, int tbeg, int tend,
            cudaStream_t s, bool timed, const FluxBox* fx) {
   if (timed) cudaEventRecord(h->ev[0], s);
-  if (iend > ibeg)
-    cell_kernel<NS, EOS, TR><<<iend - ibeg, kCellThreads, 0, s>>>(h->d_boxes, h->d_items + ibeg, mech, h->flags,
-                                                                   h->d_counters);
+  if (iend > ibeg) {
+    const cudaError_t e = launch_cell_fp64<NS, EOS, TR>(h->d_boxes, h->d_items + ibeg, (unsigned)(iend - ibeg), mech,
+                                                        h->flags, h->d_counters, s);
+    if (e != cudaSuccess) return cuda_fail(h, e);
+  }
   if (timed) cudaEventRecord(h->ev[1], s);
   const bool pers = h->tile >= kNumTiles;
-  if (h->lay_tile != 0) {
-    const cudaError_t e = launch_flux_fp64_tile(h->lay_tile, pers, h->variant, h->d_boxes, h->d_tiles + tbeg,
-                                                tend - tbeg, h->mech1, h->mech9, h->flags, g, h->d_counters, s, fx);
-    if (timed) cudaEventRecord(h->ev[2], s);
-    if (e != cudaSuccess) return cuda_fail(h, e);
-    return cuda_fail(h, cudaGetLastError());
-  }
-  const cudaError_t e =
-      launch_flux_fp64<NS, EOS>(h->d_boxes, h->d_tiles + tbeg, tend - tbeg, mech, h->flags, g, h->d_counters, s, fx,
-                                pers);
+  cudaError_t e = (h->lay_tile != 0)
+                      ? launch_flux_fp64_tile(h->lay_tile, pers, h->variant, h->d_boxes, h->d_tiles + tbeg, tend - tbeg,
+                                              h->mech1, h->mech9, h->flags, g, h->d_counters, s, fx)
+                      : launch_flux_fp64<NS, EOS>(h->d_boxes, h->d_tiles + tbeg, tend - tbeg, mech, h->flags, g,
+                                                  h->d_counters, s, fx, pers);
+  if (e == cudaSuccess)
+    e = launch_flux_exact<NS, EOS>(h->d_boxes, h->d_tiles + tbeg, tend - tbeg, mech, h->flags, g, h->d_counters, s,
+                                   fx);
   if (timed) cudaEventRecord(h->ev[2], s);
   return cuda_fail(h, e);
 }
@@ -662,6 +662,24 @@ int pc_mol_autotune(pc_mol_handle* h, const pc_box_desc* boxes, int nboxes, cons
 
 }  // extern "C"
 
+namespace {
+__global__ void check_quotients_kernel(const double* __restrict__ a, const double* __restrict__ b,
+                                       double* __restrict__ q, long long n) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const double bi = b[i];
+    q[i] = div_by(a[i], bi, 1.0 / bi);
+  }
+}
+}  // namespace
+
+extern "C" int pc_mol_check_quotients(const double* a, const double* b, double* q, long long n, void* stream) {
+  if (n < 0 || (n > 0 && (!a || !b || !q))) return PC_ERR_INVALID_ARGUMENT;
+  if (n == 0) return PC_OK;
+  const long long blocks = std::min<long long>((n + 255) / 256, 152LL * 32);
+  check_quotients_kernel<<<(int)blocks, 256, 0, (cudaStream_t)stream>>>(a, b, q, n);
+  return cudaGetLastError() == cudaSuccess ? PC_OK : PC_ERR_CUDA;
+}
+
 // ---------------------------------------------------------------------------
 // Single-box right-hand side that allocates no device memory.
 //
@@ -819,14 +837,16 @@ extern "C" int pc_mol_rhs_box_static(const pc_mol_config* cfg, const pc_box_desc
                                                                        items, tiles, ctr);
   const Geo g = make_geo(dx);
   if (variant == 1) {
-    cell_kernel<1, GammaLawEos<1>, ConstantTransport<1>><<<(unsigned)nitems, kCellThreads, 0, s>>>(dbox, items, mech1,
-                                                                                                   fl, ctr);
-    if (launch_flux_fp64<1, GammaLawEos<1>>(dbox, tiles, (int)ntiles, mech1, fl, g, ctr, s) != cudaSuccess)
+    if (launch_cell_fp64<1, GammaLawEos<1>, ConstantTransport<1>>(dbox, items, (unsigned)nitems, mech1, fl, ctr, s) !=
+            cudaSuccess ||
+        launch_flux_fp64<1, GammaLawEos<1>>(dbox, tiles, (int)ntiles, mech1, fl, g, ctr, s) != cudaSuccess ||
+        launch_flux_exact<1, GammaLawEos<1>>(dbox, tiles, (int)ntiles, mech1, fl, g, ctr, s) != cudaSuccess)
       return PC_ERR_CUDA;
   } else {
-    cell_kernel<9, IdealMixEos<9>, SimpleTransport<9>><<<(unsigned)nitems, kCellThreads, 0, s>>>(dbox, items, mech9,
-                                                                                                 fl, ctr);
-    if (launch_flux_fp64<9, IdealMixEos<9>>(dbox, tiles, (int)ntiles, mech9, fl, g, ctr, s) != cudaSuccess)
+    if (launch_cell_fp64<9, IdealMixEos<9>, SimpleTransport<9>>(dbox, items, (unsigned)nitems, mech9, fl, ctr, s) !=
+            cudaSuccess ||
+        launch_flux_fp64<9, IdealMixEos<9>>(dbox, tiles, (int)ntiles, mech9, fl, g, ctr, s) != cudaSuccess ||
+        launch_flux_exact<9, IdealMixEos<9>>(dbox, tiles, (int)ntiles, mech9, fl, g, ctr, s) != cudaSuccess)
       return PC_ERR_CUDA;
   }
   return cudaGetLastError() == cudaSuccess ? PC_OK : PC_ERR_CUDA;
@@ -1215,13 +1235,13 @@ extern "C" int pc_mol_rhs_vjp(pc_mol_handle* h, const pc_box_desc* boxes, int nb
   if ((rc = upload(h, kUpAdjOff, off.data(), off.size() * sizeof(long long), s, &doff)) != PC_OK) return rc;
   // pass 1: records of the forward state
   const int nitems = (int)L.items.size();
-  if (h->variant == 1)
-    cell_kernel<1, GammaLawEos<1>, ConstantTransport<1>>
-        <<<nitems, kCellThreads, 0, s>>>(h->d_boxes, h->d_items, h->mech1, h->flags, h->d_counters);
-  else
-    cell_kernel<9, IdealMixEos<9>, SimpleTransport<9>>
-        <<<nitems, kCellThreads, 0, s>>>(h->d_boxes, h->d_items, h->mech9, h->flags, h->d_counters);
-  if ((rc = cuda_fail(h, cudaGetLastError())) != PC_OK) return rc;
+  const cudaError_t ec =
+      (h->variant == 1)
+          ? launch_cell_fp64<1, GammaLawEos<1>, ConstantTransport<1>>(h->d_boxes, h->d_items, (unsigned)nitems,
+                                                                      h->mech1, h->flags, h->d_counters, s)
+          : launch_cell_fp64<9, IdealMixEos<9>, SimpleTransport<9>>(h->d_boxes, h->d_items, (unsigned)nitems,
+                                                                    h->mech9, h->flags, h->d_counters, s);
+  if ((rc = cuda_fail(h, ec)) != PC_OK) return rc;
   if ((rc = cuda_fail(h, cudaMemsetAsync(h->recbar, 0, sizeof(double) * L.scratch_doubles, s))) != PC_OK) return rc;
   const cudaError_t e = launch_vjp_passes(h->variant, h->d_boxes, static_cast<const AdjBox*>(dadj), h->d_items, nitems,
                                           static_cast<const int4*>(dfit), (int)fitems.size(), h->recbar,
