@@ -724,7 +724,8 @@ def run_gpu(args):
                   "precision": "FP32 reconstruction/Riemann/diffusion, FP64 Newton/mass fractions/divergence"},
         "gpu_launches_mixed": 2 * args.steps,
         "status": {"cells": status.cells, "newton_nonconverged": status.newton_nonconverged,
-                   "nonpositive_state": status.nonpositive_state, "nonfinite_output": status.nonfinite_output},
+                   "nonpositive_state": status.nonpositive_state, "nonfinite_output": status.nonfinite_output,
+                   "exact_recomputes": status.exact_recomputes},
         "clocks": clk,
     }
     if cpu is not None:

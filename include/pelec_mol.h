@@ -162,6 +162,12 @@ typedef struct pc_mol_status {
   long long nonfinite_output;      /* RHS entries that are NaN or Inf        */
   int last_error;                  /* pc_status_code of the last call        */
   int pad_;
+  long long exact_recomputes;      /* lanes of the FP64 passes whose quotient
+                                      operands needed an IEEE division (the
+                                      pass was then evaluated again with
+                                      IEEE quotients): subnormal, infinite or
+                                      NaN operands, or a quotient next to a
+                                      power of two                           */
 } pc_mol_status;
 
 /* Physical boundary conditions of a domain face (PCPhysBCType, PeleC.H, and
@@ -380,8 +386,8 @@ int pc_mol_check_quotients(const double* a, const double* b, double* q, long lon
  * pc_mol_rhs_level and gets the same result.  The per-cell scratch, launch
  * lists and counters live in one fixed 48 MiB device array that each GPU
  * reserves when the library is loaded and keeps until the process exits; a
- * box that does not fit (larger than about 47^3 valid cells with 9 species,
- * 72^3 with one) returns PC_ERR_TOO_LARGE before anything is launched.  The first call
+ * box that does not fit (larger than about 46^3 valid cells with 9 species,
+ * 67^3 with one) returns PC_ERR_TOO_LARGE before anything is launched.  The first call
  * on each device looks up that array's device address, so make that first
  * call outside any stream capture.  Every call reuses the same array: calls
  * whose work overlaps on the GPU (other streams, other host threads) race

@@ -143,6 +143,7 @@ class PcMolStatus(ctypes.Structure):
         ("nonfinite_output", c_longlong),
         ("last_error", c_int),
         ("pad_", c_int),
+        ("exact_recomputes", c_longlong),
     ]
 
 

@@ -99,10 +99,8 @@ __device__ __forceinline__ void rare_for_warp(bool need, F&& f) {
 // of a division.  A zero numerator gives a*y, the correctly signed zero.
 // Slow: a nonzero numerator that is subnormal, infinite or NaN; b zero,
 // subnormal, infinite, NaN or above 2^1022 (1/b not a normal number); q0
-// outside [2^-1021, 2^1022) (the quotient or its neighbours not normal); or
-// q0's significand within 4 of either end of its binade (where s ulp could
-// cross into a binade of other spacing).  For a zero numerator only b zero or
-// subnormal (1/b infinite).
+// outside [2^-1021, 2^1022) (the quotient or its neighbours not normal).  For
+// a zero numerator only b zero or subnormal (1/b infinite).
 __device__ __forceinline__ double div_fast(double a, double b, double y, bool& slow) {
 #ifdef PCG_RECIPROCAL_QUOTIENTS
   // The PC_PRECISION_FP64_RCP compilation: a y = a/b (1 + e) with
@@ -122,10 +120,23 @@ __device__ __forceinline__ double div_fast(double a, double b, double y, bool& s
   const unsigned phi = (unsigned)(p >> 32) + bl * Mh + Bh * ql;
   const long long R = (long long)(((unsigned long long)(al << sh) << 32) - (((unsigned long long)phi << 32) | (unsigned)p));
   const long long Bs = (long long)(((unsigned long long)Bh << 32) | bl), R2 = 2 * R, B3 = 3 * Bs;
-  const long long st = (long long)(R2 > Bs) + (long long)(R2 > B3) - (long long)(R2 < -Bs) - (long long)(R2 < -B3);
+  long long st = (long long)(R2 > Bs) + (long long)(R2 > B3) - (long long)(R2 < -Bs) - (long long)(R2 < -B3);
+  // Binade ends, where the spacing of doubles changes.  q0 = (2^53 - 1) ulp
+  // with the quotient more than 1.5 ulp above it: the quotient is less than
+  // 2 ulp above q0 (the error bound), so it lies within one ulp of the power
+  // of two 2^53 ulp, whose upper neighbour is 2 ulp away: the step is 1.  q0
+  // = P or P + ulp for a power of two P, with the quotient below P (within one
+  // ulp of it, the error bound there): the doubles below P are half an ulp
+  // apart, so the step is counted from P in half ulps, T / 2B with
+  // T = 4 (R + (q0 - P) B / ulp) in (-4B(1 + 2^-52), 0).  An exact
+  // power-of-two quotient (R = 0) takes neither branch.
+  const unsigned m20 = qh & 0xfffffu;
+  st = (m20 == 0xfffffu && ql == 0xffffffffu && st == 2) ? 1 : st;
+  const long long T = 4 * (R + (ql == 1u ? Bs : 0));
+  const long long half = -((long long)(T < -Bs) + (long long)(T < -B3));
+  st = (m20 == 0u && ((ql == 0u && R < 0) || (ql == 1u && R < -Bs))) ? half - (long long)ql : st;
   const bool zero = ((ah << 1) | al) == 0u;
-  const bool edge = (((qh & 0xfffffu) + 1u) & 0xfffffu) <= 1u && ql + 4u <= 8u;
-  slow |= zero ? (eb == 0u) : (ea - 1u > 2045u || eb - 1u > 2043u || eq - 2u > 2043u || edge);
+  slow |= zero ? (eb == 0u) : (ea - 1u > 2045u || eb - 1u > 2043u || eq - 2u > 2043u);
   const unsigned long long iq = ((unsigned long long)qh << 32) | ql;
   return zero ? q0 : __longlong_as_double((long long)(iq + (unsigned long long)st));
 #endif
@@ -210,6 +221,29 @@ __device__ __forceinline__ unsigned long long twice_mag(unsigned long long m) {
   if (e == 0u) return m << 1;                                 // zero or subnormal: exact (may become normal)
   if (e >= 0x7feu) return e == 0x7ffu ? m : 0x7ff0000000000000ULL;  // inf/NaN unchanged; overflow to inf
   return m + (1ULL << 52);
+}
+
+// fmax(x, c) for a constant c > 0 (R = double: on the bit patterns; a
+// negative or NaN x gives c, as fmax does).
+template <class R>
+__device__ __forceinline__ R fmax_pos(R x, double c) {
+  return fmax(x, c);
+}
+template <>
+__device__ __forceinline__ double fmax_pos<double>(double x, double c) {
+  const long long ix = __double_as_longlong(x), ic = __double_as_longlong(c);
+  return (ix > ic && ix <= 0x7ff0000000000000LL) ? x : c;
+}
+
+// 0 where -c < x < c (c > 0), else x (R = double: |x| < c compared on the
+// bit patterns, false for a NaN like the floating-point comparison).
+template <class R>
+__device__ __forceinline__ R zero_below(R x, double c) {
+  return (-c < x && x < c) ? R(0.0) : x;
+}
+template <>
+__device__ __forceinline__ double zero_below<double>(double x, double c) {
+  return (dbits(x) & 0x7fffffffffffffffULL) < dbits(c) ? 0.0 : x;
 }
 
 // copysign(1, s) * x (R = double: x with its sign bit flipped where s is
@@ -439,8 +473,8 @@ struct SimpleTransport {
 #pragma unroll
       for (int j = k + 1; j < NS; ++j, ++q) {
         const R invD = pc_exp(-horner4(m.diff[q], L)) * pr;
-        s[k] = fma(fmax(X[j], 1e-15), invD, s[k]);
-        s[j] = fma(fmax(X[k], 1e-15), invD, s[j]);
+        s[k] = fma(fmax_pos(X[j], 1e-15), invD, s[k]);
+        s[j] = fma(fmax_pos(X[k], 1e-15), invD, s[j]);
       }
     }
     const R rw = mix_rw<NS>(m, Y);

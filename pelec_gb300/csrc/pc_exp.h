@@ -78,7 +78,7 @@ PC_MATH_HD double double_of(int64_t b) {
 #endif
 
 PC_MATH_HD double exp(double x) {
-  if (!(fabs(x) < 700.0)) return ::exp(x);
+  if (!((bits_of(x) & INT64_C(0x7fffffffffffffff)) < bits_of(700.0))) return ::exp(x);  // |x| < 700 (NaN: no)
   const double shifter = 0x1.8p52;  // adding it rounds |x 64/ln2| < 2^51 to an integer
   const double t = fma(x, PC_EXP_64_LN2, shifter);
   const int k = (int)(int32_t)(uint32_t)(uint64_t)bits_of(t);  // that integer, from the low word
@@ -99,13 +99,13 @@ PC_MATH_HD double exp(double x) {
 }
 
 PC_MATH_HD double log(double x) {
-  if (!(x >= 0x1p-1022 && x <= 0x1.fffffffffffffp1023)) return ::log(x);
   const int64_t b = bits_of(x);
+  if (!(b >= INT64_C(0x0010000000000000) && b <= INT64_C(0x7fefffffffffffff))) return ::log(x);  // positive normal x
   const int m = (int)(b >> 52) - 1023;
   const int64_t mant = b & (((int64_t)1 << 52) - 1);
   const double f = double_of(mant | ((int64_t)1023 << 52));            // in [1, 2)
   const int j = (int)((mant + ((int64_t)1 << 44)) >> 45);              // nearest j/128 to f - 1, 0..128
-  const double F = 1.0 + (double)j * (1.0 / 128.0);
+  const double F = double_of((INT64_C(1023) << 52) + ((int64_t)j << 45));  // 1 + j/128, exactly
   const double d = f - F;                                                // exact
   const double iF = PC_MATH_TAB(log_inv, j);
   const double u = d * iF;

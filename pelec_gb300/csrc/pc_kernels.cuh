@@ -53,13 +53,16 @@ struct Geo {
   double p_ref;  // mixed precision: pressure offset of the FP32 records
 };
 
-// Record fields (pass 1 -> pass 2).
+// Record fields (pass 1 -> pass 2).  IRHO, IC, IC2 are the IEEE reciprocals
+// 1/rho, 1/c and 1/(c c) of every cell, the divisors' reciprocals of the
+// slopes' and face states' quotients (div_by), evaluated once per cell.
 template <int NS>
 struct Rec {
   static constexpr int RHO = 0, U = 1, V = 2, W = 3, P = 4, C = 5, Y = 6;
   static constexpr int T = 6 + NS, X = 7 + NS, H = 7 + 2 * NS, D = 7 + 3 * NS;
   static constexpr int MU = 7 + 4 * NS, XI = 8 + 4 * NS, LAM = 9 + 4 * NS;
-  static constexpr int N = 10 + 4 * NS;
+  static constexpr int IRHO = 10 + 4 * NS, IC = 11 + 4 * NS, IC2 = 12 + 4 * NS;
+  static constexpr int N = 13 + 4 * NS;
 };
 
 // Loads of record fields in the flux pass (a Dual specialisation reads
@@ -149,9 +152,8 @@ __device__ __forceinline__ void cell_record(const DevMech<NS>& m, const DevFlags
   R Y[NS];
 #pragma unroll
   for (int n = 0; n < NS; ++n) {
-    R y = q(U[UFS + n], rho, rhoinv);  // = rho Y_n / rho, correctly rounded
-    if (-1e-4 * 2.220446049250313e-16 < y && y < 1e-4 * 2.220446049250313e-16) y = 0.0;
-    Y[n] = y;
+    const R y = q(U[UFS + n], rho, rhoinv);  // = rho Y_n / rho, correctly rounded
+    Y[n] = zero_below(y, 1e-4 * 2.220446049250313e-16);  // |Y| < 1e-4 eps -> 0 (Utilities.H:288-294)
   }
   const R rw = mix_rw<NS>(m, Y);
   bool ok = true;
@@ -166,6 +168,9 @@ __device__ __forceinline__ void cell_record(const DevMech<NS>& m, const DevFlags
   st(RC::W, vz);
   st(RC::P, p);
   st(RC::C, cs);
+  st(RC::IRHO, rhoinv);
+  st(RC::IC, 1.0 / cs);
+  st(RC::IC2, 1.0 / (cs * cs));
 #pragma unroll
   for (int n = 0; n < NS; ++n) st(RC::Y + n, Y[n]);
   if (inner) {
@@ -271,7 +276,7 @@ __device__ __forceinline__ void cell_slopes(const RecAcc<R>& ra, long long c, lo
   const R p0 = ld(RC::P, c), pm = ld(RC::P, cm), pp = ld(RC::P, cp);
   const R u0 = ld(fun, c), um = ld(fun, cm), up = ld(fun, cp);
   const R c0 = ld(RC::C, c);
-  const R yc = 1.0 / c0;
+  const R yc = ld(RC::IC, c);  // 1 / c0
   const R dpl = p0 - pm, dpr = pp - p0;
   {
     const R a = q(halve(dpl), c0, yc), bb = halve(r0) * (u0 - um);
@@ -286,7 +291,7 @@ __device__ __forceinline__ void cell_slopes(const RecAcc<R>& ra, long long c, lo
     dq[3] = mc_limit(w0 - ld(fut2, cm), ld(fut2, cp) - w0);
   }
   const R c2 = c0 * c0;
-  const R yc2 = 1.0 / c2;
+  const R yc2 = ld(RC::IC2, c);  // 1 / c2
 #pragma unroll
   for (int n = 0; n < NS; ++n) {
     const R y0 = ld(RC::Y + n, c);
@@ -313,13 +318,13 @@ __device__ __forceinline__ void hydro_face_sl(const RecAcc<R>& ra, const DevMech
   const R uL = ld(fun, cL), uR = ld(fun, cR);
   const R cLc = ld(RC::C, cL), cRc = ld(RC::C, cR);
   const R t1L = ld(fut1, cL), t1R = ld(fut1, cR), t2L = ld(fut2, cL), t2R = ld(fut2, cR);
-  const R ycL = 1.0 / cLc, ycR = 1.0 / cRc;
+  const R ycL = ld(RC::IC, cL), ycR = ld(RC::IC, cR);  // 1 / c of both cells
   // Face states (MOL.cpp:69-123).
-  const R unl = uL + halve((dqL[1] - dqL[0]) / rL);
+  const R unl = uL + halve(q(dqL[1] - dqL[0], rL, ld(RC::IRHO, cL)));
   const R pl = pL + halve(dqL[0] + dqL[1]) * cLc;
   const R ut1l = t1L + halve(dqL[2]);
   const R ut2l = t2L + halve(dqL[3]);
-  const R unr = uR - halve((dqR[1] - dqR[0]) / rR);
+  const R unr = uR - halve(q(dqR[1] - dqR[0], rR, ld(RC::IRHO, cR)));
   const R pr = pR - halve(dqR[0] + dqR[1]) * cRc;
   const R ut1r = t1R - halve(dqR[2]);
   const R ut2r = t2R - halve(dqR[3]);

@@ -74,10 +74,12 @@ __host__ MechF<NS> to_float(const DevMech<NS>& m, double p_ref) {
 // fields of a mixed record.  Both enter the diffusion fluxes only through
 // differences between neighbouring cells, which FP32 values would resolve
 // to no better than 1e-4 K / 1e-7 (the flame's second differences of T are
-// a few K per cell).
+// a few K per cell).  They start at the first 8-byte boundary after the
+// Rec<NS>::N FP32 fields of every cell (N ncell floats may be odd).
 template <int NS>
 __device__ __forceinline__ double* mixed_x(const DevBox& b) {
-  return reinterpret_cast<double*>(reinterpret_cast<float*>(b.rec) + (long long)Rec<NS>::N * b.ncell);
+  const long long nf = ((long long)Rec<NS>::N * b.ncell + 1) & ~1LL;
+  return reinterpret_cast<double*>(reinterpret_cast<float*>(b.rec) + nf);
 }
 
 template <int NS>

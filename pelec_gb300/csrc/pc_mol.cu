@@ -569,7 +569,7 @@ int pc_mol_rhs_level_per_box(pc_mol_handle* h, const pc_box_desc* boxes, int nbo
 int pc_mol_last_status(pc_mol_handle* h, pc_mol_status* st) {
   if (!h || !st) return PC_ERR_INVALID_ARGUMENT;
   std::memset(st, 0, sizeof(*st));
-  unsigned long long c[kNumCounters] = {0, 0, 0, 0};
+  unsigned long long c[kNumCounters] = {};
   cudaError_t e = cudaSetDevice(h->device);
   if (e == cudaSuccess) e = cudaStreamSynchronize(h->last_stream);
   if (e == cudaSuccess) e = cudaMemcpy(c, h->d_counters, sizeof(c), cudaMemcpyDeviceToHost);
@@ -578,6 +578,7 @@ int pc_mol_last_status(pc_mol_handle* h, pc_mol_status* st) {
   st->newton_nonconverged = (long long)c[kCounterNewton];
   st->nonpositive_state = (long long)c[kCounterNonpos];
   st->nonfinite_output = (long long)c[kCounterNonfinite];
+  st->exact_recomputes = (long long)(c[kCounterSlowCell] + c[kCounterSlowFlux]);
   st->last_error = h->last_error;
   return PC_OK;
 }

@@ -1,0 +1,64 @@
+"""GPU tests of the exact twins of the FP64 passes.
+
+The fast cell and flux passes take each quotient by a shared divisor as the
+product with the divisor's reciprocal, corrected in integer arithmetic; the
+operands that correction does not cover (subnormal, infinite or NaN values,
+quotients next to a power of two) are counted, and a twin of the pass,
+launched right after it, evaluates the whole pass again with IEEE divisions
+when that count is not zero.  These states put subnormal numbers into those
+quotients so that the twins run, and the result must still equal the
+oracle's bit for bit.
+"""
+import numpy as np
+import pytest
+
+from gpu_util import gpu_rhs
+from pelec_gb300 import problems
+
+pytestmark = pytest.mark.gpu
+
+
+def _same(gpu, ref, what):
+    assert np.all(np.isfinite(gpu)), what
+    np.testing.assert_array_equal(gpu, ref, err_msg=f"{what}: not bit-identical to the oracle")
+
+
+def test_subnormal_species_densities_run_the_exact_cell_pass(cuda_lib, oracle_lib):
+    """rho Y_k subnormal in a scatter of cells (ghosts included): the cell
+    pass's Y_k = rho Y_k / rho has a subnormal numerator there."""
+    mech, st, _ = problems.flame((12, 10, 14), seed=41)
+    rng = np.random.default_rng(41)
+    S = st.S
+    n_h2o = 7 + 2
+    mask = rng.random(S.shape[1:]) < 0.05
+    S[n_h2o][mask] = rng.integers(1, 1 << 40, mask.sum()) * 5e-324
+    cfg = problems.make_config(mech)
+    ref, = oracle_lib.mol_rhs(cfg, [st])
+    for per_box in (False, True):
+        (gpu,), status = gpu_rhs(cuda_lib, cfg, [st], per_box=per_box)
+        _same(gpu, ref, f"subnormal rho Y, per_box={per_box}")
+        assert status.exact_recomputes > 0
+        assert status.cells == 12 * 10 * 14
+
+
+def test_subnormal_velocities_run_the_exact_flux_pass(cuda_lib, oracle_lib):
+    """Momenta scaled into the subnormal range on a uniform-pressure
+    Taylor-Green box: the Riemann solver's u* numerator and the face-state
+    quotients are subnormal, so the flux pass's twin runs."""
+    mech, st = problems.tgv(16, seed=42)
+    for n in (1, 2, 3):
+        st.S[n] *= 1e-318
+    cfg = problems.make_config(mech)
+    ref, = oracle_lib.mol_rhs(cfg, [st])
+    (gpu,), status = gpu_rhs(cuda_lib, cfg, [st])
+    _same(gpu, ref, "subnormal momenta")
+    assert status.exact_recomputes > 0
+
+
+def test_ordinary_states_need_no_exact_pass(cuda_lib, oracle_lib):
+    mech, st, _ = problems.flame((16, 16, 16), seed=43)
+    cfg = problems.make_config(mech)
+    ref, = oracle_lib.mol_rhs(cfg, [st])
+    (gpu,), status = gpu_rhs(cuda_lib, cfg, [st])
+    _same(gpu, ref, "flame 16^3")
+    assert status.exact_recomputes == 0

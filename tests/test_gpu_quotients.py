@@ -62,13 +62,17 @@ def test_quotients_equal_ieee_division(cuda_lib, kinds):
 
 
 def test_quotients_of_workload_like_operands(cuda_lib):
-    """Mass fractions over densities, pressure differences over sound speeds,
-    exact quotients (a = b t for small integers t) and powers of two."""
+    """Quotients within a few ulp of a power of two (either side, where the
+    spacing of doubles changes), mass fractions over densities, pressure
+    differences over sound speeds, exact quotients (a = b t for small
+    integers t) and powers of two."""
     rng = np.random.default_rng(7)
     n = 1 << 22
     b = rng.uniform(1e-5, 1e-2, n)
     t = rng.integers(1, 1 << 20, n).astype(np.float64) * np.ldexp(1.0, rng.integers(-30, 30, n))
-    cases = [(rng.uniform(0, 1e-2, n) * rng.uniform(0, 1, n), b),
+    near = b * (1.0 + rng.integers(-3, 4, n) * 2.0 ** -52)  # quotients within a few ulp of 1, both sides
+    cases = [(np.ldexp(near, rng.integers(-40, 40, n)), b),
+             (rng.uniform(0, 1e-2, n) * rng.uniform(0, 1, n), b),
              (rng.normal(0, 1e3, n), rng.uniform(3e4, 1e5, n)),
              (b * t, b), (b, b), (np.ldexp(1.0, rng.integers(-300, 300, n)), b),
              (b, np.ldexp(1.0, rng.integers(-300, 300, n)))]
