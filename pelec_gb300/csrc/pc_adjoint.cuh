@@ -351,9 +351,9 @@ struct RecBar {
 // Hyperbolic face flux reverse (two-shock Riemann solver, slopes on or off).
 // Fb: cotangent of the face flux times the area (the F of hydro_face).
 // ---------------------------------------------------------------------------
-template <int NS, class EOS, int d>
+template <int NS, class EOS, int d, class Q>
 __device__ void hydro_face_rev(const DevBox& b, const DevMech<NS>& m, const DevFlags& f, long long cR, long long st,
-                               double A, const double* Fb, const RecBar& rb) {
+                               double A, const double* Fb, const RecBar& rb, Q& q) {
   using RC = Rec<NS>;
   using EA = EosAdj<NS, EOS>;
   const double* rec = b.rec;
@@ -369,7 +369,7 @@ __device__ void hydro_face_rev(const DevBox& b, const DevMech<NS>& m, const DevF
   const double uLL = ld(fun, cLL), uL = ld(fun, cL), uR = ld(fun, cR), uRR = ld(fun, cRR);
   const double cLc = ld(RC::C, cL), cRc = ld(RC::C, cR);
   const double t1L = ld(fut1, cL), t1R = ld(fut1, cR), t2L = ld(fut2, cL), t2R = ld(fut2, cR);
-  const double ycL = 1.0 / cLc, ycR = 1.0 / cRc;
+  const double ycL = ld(RC::IC, cL), ycR = ld(RC::IC, cR);  // 1 / c (records)
   const bool slopes = f.slopes != 0;
   double t1LL = 0.0, t1RR = 0.0, t2LL = 0.0, t2RR = 0.0;
   const double dpl = pL - pLL, dpc = pR - pL, dpr = pRR - pR;
@@ -380,17 +380,17 @@ __device__ void hydro_face_rev(const DevBox& b, const DevMech<NS>& m, const DevF
     t1RR = ld(fut1, cRR);
     t2LL = ld(fut2, cLL);
     t2RR = ld(fut2, cRR);
-    aL1 = div_by(0.5 * dpl, cLc, ycL);
+    aL1 = q(0.5 * dpl, cLc, ycL);
     bL1 = 0.5 * rL * (uL - uLL);
-    aL2 = div_by(0.5 * dpc, cLc, ycL);
+    aL2 = q(0.5 * dpc, cLc, ycL);
     bL2 = 0.5 * rL * (uR - uL);
     dqL[0] = mc_limit(aL1 - bL1, aL2 - bL2);
     dqL[1] = mc_limit(aL1 + bL1, aL2 + bL2);
     dqL[2] = mc_limit(t1L - t1LL, t1R - t1L);
     dqL[3] = mc_limit(t2L - t2LL, t2R - t2L);
-    aR1 = div_by(0.5 * dpc, cRc, ycR);
+    aR1 = q(0.5 * dpc, cRc, ycR);
     bR1 = 0.5 * rR * (uR - uL);
-    aR2 = div_by(0.5 * dpr, cRc, ycR);
+    aR2 = q(0.5 * dpr, cRc, ycR);
     bR2 = 0.5 * rR * (uRR - uR);
     dqR[0] = mc_limit(aR1 - bR1, aR2 - bR2);
     dqR[1] = mc_limit(aR1 + bR1, aR2 + bR2);
@@ -407,7 +407,7 @@ __device__ void hydro_face_rev(const DevBox& b, const DevMech<NS>& m, const DevF
   const double ut2r = t2R - 0.5 * dqR[3];
   const double sL = dqL[0] + dqL[1], sR = dqR[0] + dqR[1];
   const double cL2 = cLc * cLc, cR2 = cRc * cRc;
-  const double ycL2 = 1.0 / cL2, ycR2 = 1.0 / cR2;
+  const double ycL2 = ld(RC::IC2, cL), ycR2 = ld(RC::IC2, cR);  // 1 / c^2 (records)
   double Yl[NS], Yr[NS];
   double rl = 0.0, rr = 0.0;
 #pragma unroll
@@ -417,11 +417,11 @@ __device__ void hydro_face_rev(const DevBox& b, const DevMech<NS>& m, const DevF
     if (slopes) {
       const double yLL = ld(RC::Y + n, cLL), yRR = ld(RC::Y + n, cRR);
       const double ryL = rL * yL, ryR = rR * yR;
-      dsL = mc_limit(ryL - rLL * yLL - div_by(yL * dpl, cL2, ycL2), ryR - ryL - div_by(yL * dpc, cL2, ycL2));
-      dsR = mc_limit(ryR - ryL - div_by(yR * dpc, cR2, ycR2), rRR * yRR - ryR - div_by(yR * dpr, cR2, ycR2));
+      dsL = mc_limit(ryL - rLL * yLL - q(yL * dpl, cL2, ycL2), ryR - ryL - q(yL * dpc, cL2, ycL2));
+      dsR = mc_limit(ryR - ryL - q(yR * dpc, cR2, ycR2), rRR * yRR - ryR - q(yR * dpr, cR2, ycR2));
     }
-    Yl[n] = yL * rL + 0.5 * (dsL + div_by(yL * sL, cLc, ycL));
-    Yr[n] = yR * rR - 0.5 * (dsR + div_by(yR * sR, cRc, ycR));
+    Yl[n] = yL * rL + 0.5 * (dsL + q(yL * sL, cLc, ycL));
+    Yr[n] = yR * rR - 0.5 * (dsR + q(yR * sR, cRc, ycR));
     rl += Yl[n];
     rr += Yr[n];
   }
@@ -429,8 +429,8 @@ __device__ void hydro_face_rev(const DevBox& b, const DevMech<NS>& m, const DevF
     const double yrl = 1.0 / rl, yrr = 1.0 / rr;
 #pragma unroll
     for (int n = 0; n < NS; ++n) {
-      Yl[n] = div_by(Yl[n], rl, yrl);
-      Yr[n] = div_by(Yr[n], rr, yrr);
+      Yl[n] = q(Yl[n], rl, yrl);
+      Yr[n] = q(Yr[n], rr, yrr);
     }
   }
   const double cavg = 0.5 * (cRc + cLc);
@@ -442,9 +442,9 @@ __device__ void hydro_face_rev(const DevBox& b, const DevMech<NS>& m, const DevF
   const double wr = fmax(wsmall, cr * rr);
   const double ww = wl + wr, yww = 1.0 / ww;
   const double pnum = (wr * pl + wl * pr) + wl * wr * (unl - unr);
-  const double pq = div_by(pnum, ww, yww);
+  const double pq = q(pnum, ww, yww);
   const double pstar = fmax(wsmall, pq);
-  const double ustar0 = div_by((wl * unl + wr * unr) + (pl - pr), ww, yww);
+  const double ustar0 = q((wl * unl + wr * unr) + (pl - pr), ww, yww);
   const bool mask = ustar0 > 0.0;
   const bool m0 = fabs(ustar0) < kSmallU * 0.5 * (fabs(unl) + fabs(unr)) || ustar0 == 0.0;
   const double ustar = m0 ? 0.0 : ustar0;
@@ -464,7 +464,7 @@ __device__ void hydro_face_rev(const DevBox& b, const DevMech<NS>& m, const DevF
   {
     const double y = 1.0 / ro;
 #pragma unroll
-    for (int n = 0; n < NS; ++n) Yo[n] = div_by(rspo[n], ro, y);
+    for (int n = 0; n < NS; ++n) Yo[n] = q(rspo[n], ro, y);
   }
   const double rwo = mix_rw<NS>(m, Yo);
   const double co = EOS::cs_rp(m, Yo, rwo, ro, po);
@@ -480,7 +480,7 @@ __device__ void hydro_face_rev(const DevBox& b, const DevMech<NS>& m, const DevF
   {
     const double y = 1.0 / rstar;
 #pragma unroll
-    for (int n = 0; n < NS; ++n) Ys[n] = div_by(rsps[n], rstar, y);
+    for (int n = 0; n < NS; ++n) Ys[n] = q(rsps[n], rstar, y);
   }
   const double rws = mix_rw<NS>(m, Ys);
   const double cstar = EOS::cs_rp(m, Ys, rws, rstar, pstar);
@@ -521,7 +521,7 @@ __device__ void hydro_face_rev(const DevBox& b, const DevMech<NS>& m, const DevF
   {
     const double y = 1.0 / rgd;
 #pragma unroll
-    for (int n = 0; n < NS; ++n) Yg[n] = div_by(gq[n], rgd, y);
+    for (int n = 0; n < NS; ++n) Yg[n] = q(gq[n], rgd, y);
   }
   const double rwg = mix_rw<NS>(m, Yg);
   const double eg = EOS::e_rp(m, Yg, rwg, rgd, gdp);
@@ -842,8 +842,8 @@ __device__ void hydro_face_rev(const DevBox& b, const DevMech<NS>& m, const DevF
       const double ryL = rL * yL, ryR = rR * yR;
       double ryLb = 0.0, ryRb = 0.0, yLLb = 0.0, yRRb = 0.0;
       {
-        const double a = ryL - rLL * yLL - div_by(yL * dpl, cL2, ycL2);
-        const double bq = ryR - ryL - div_by(yL * dpc, cL2, ycL2);
+        const double a = ryL - rLL * yLL - q(yL * dpl, cL2, ycL2);
+        const double bq = ryR - ryL - q(yL * dpc, cL2, ycL2);
         double ab = 0.0, bb = 0.0;
         mc_limit_rev(a, bq, dsLb, ab, bb);
         ryLb += ab - bb;
@@ -856,8 +856,8 @@ __device__ void hydro_face_rev(const DevBox& b, const DevMech<NS>& m, const DevF
         cL2b += (ab * yL * dpl + bb * yL * dpc) * ycL2 * ycL2;
       }
       {
-        const double a = ryR - ryL - div_by(yR * dpc, cR2, ycR2);
-        const double bq = rRR * yRR - ryR - div_by(yR * dpr, cR2, ycR2);
+        const double a = ryR - ryL - q(yR * dpc, cR2, ycR2);
+        const double bq = rRR * yRR - ryR - q(yR * dpr, cR2, ycR2);
         double ab = 0.0, bb = 0.0;
         mc_limit_rev(a, bq, dsRb, ab, bb);
         ryRb += ab - bb;
@@ -1212,9 +1212,10 @@ struct AdjBox {
 // ---------------------------------------------------------------------------
 constexpr int kAdjThreads = 128;
 
-template <int NS, class EOS, int d>
+template <int NS, class EOS, int d, class Q>
 __device__ __forceinline__ void face_adjoint_dir(const DevBox& b, const AdjBox& a, const DevMech<NS>& m,
-                                                 const DevFlags& f, const Geo& g, long long fi, const RecBar& rb) {
+                                                 const DevFlags& f, const Geo& g, long long fi, const RecBar& rb,
+                                                 Q& q) {
   constexpr int NVAR = 7 + NS;
   const int nf0 = b.hi[0] - b.lo[0] + 1 + (d == 0), nf1 = b.hi[1] - b.lo[1] + 1 + (d == 1);
   const int nf2 = b.hi[2] - b.lo[2] + 1 + (d == 2);
@@ -1239,27 +1240,44 @@ __device__ __forceinline__ void face_adjoint_dir(const DevBox& b, const AdjBox& 
   if (!any) return;
   const long long stv[3] = {1, b.n2[0], (long long)b.n2[0] * b.n2[1]};
   const long long cR = (i - b.g2lo[0]) + (j - b.g2lo[1]) * stv[1] + (k - b.g2lo[2]) * stv[2];
-  if (f.do_hydro) hydro_face_rev<NS, EOS, d>(b, m, f, cR, stv[d], g.area[d], Fb, rb);
+  if (f.do_hydro) hydro_face_rev<NS, EOS, d>(b, m, f, cR, stv[d], g.area[d], Fb, rb, q);
   const bool diff = f.diffuse_vel || f.diffuse_temp || f.diffuse_spec || f.diffuse_enth;
   if (diff) diffusion_face_rev<NS, d>(b, f, g, cR, stv, Fb, rb);
 }
 
-template <int NS, class EOS>
+// kExact = false: quotients by div_fast, lanes that need a real division
+// counted in counters[kCounterSlowAdj]; kExact = true: the exact twin, which
+// returns at once unless that count is nonzero and then (after the record
+// cotangents have been cleared again, zero_recbar_if_slow) accumulates them
+// anew with IEEE quotients.
+template <int NS, class EOS, bool kExact = false>
 __global__ void __launch_bounds__(kAdjThreads)
     face_adjoint_kernel(const DevBox* __restrict__ boxes, const AdjBox* __restrict__ adj,
                         const int4* __restrict__ items, double* __restrict__ recbar_base,
                         const long long* __restrict__ recbar_off, const __grid_constant__ DevMech<NS> m,
-                        const DevFlags f, const Geo g) {
+                        const DevFlags f, const Geo g, unsigned long long* __restrict__ counters) {
+  if (kExact && __ldcg(&counters[kCounterSlowAdj]) == 0ull) return;
   const int4 it = items[blockIdx.x];
   const DevBox& b = boxes[it.x];
   const RecBar rb{recbar_base + recbar_off[it.x], b.ncell};
   const long long fi = (long long)it.z * kAdjThreads + threadIdx.x;
+  Quot<kExact> quo;
   if (it.y == 0)
-    face_adjoint_dir<NS, EOS, 0>(b, adj[it.x], m, f, g, fi, rb);
+    face_adjoint_dir<NS, EOS, 0>(b, adj[it.x], m, f, g, fi, rb, quo);
   else if (it.y == 1)
-    face_adjoint_dir<NS, EOS, 1>(b, adj[it.x], m, f, g, fi, rb);
+    face_adjoint_dir<NS, EOS, 1>(b, adj[it.x], m, f, g, fi, rb, quo);
   else
-    face_adjoint_dir<NS, EOS, 2>(b, adj[it.x], m, f, g, fi, rb);
+    face_adjoint_dir<NS, EOS, 2>(b, adj[it.x], m, f, g, fi, rb, quo);
+  if (!kExact) warp_count(&counters[kCounterSlowAdj], quo.slow);
+}
+
+// Clears the record cotangents before the exact twin of the face adjoint,
+// when the fast pass counted a lane that needs a real division.
+static __global__ void zero_recbar_if_slow(double* __restrict__ recbar, long long n,
+                                    const unsigned long long* __restrict__ counters) {
+  if (__ldcg(&counters[kCounterSlowAdj]) == 0ull) return;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    recbar[i] = 0.0;
 }
 
 // ---------------------------------------------------------------------------

@@ -111,7 +111,8 @@ enum {
   kCounterNonfinite = 3,
   kCounterSlowCell = 4,
   kCounterSlowFlux = 5,
-  kNumCounters = 6
+  kCounterSlowAdj = 6,  // the same for the face adjoint of the VJP
+  kNumCounters = 7
 };
 
 __device__ __forceinline__ void warp_count(unsigned long long* ctr, bool pred) {

@@ -30,9 +30,9 @@ cudaError_t launch_flux_fp64_tile(int tile, bool persistent, int variant, const 
                                   int ntiles, const DevMech<1>& m1, const DevMech<9>& m9, const DevFlags& f,
                                   const Geo& g, unsigned long long* counters, cudaStream_t s, const FluxBox* fx);
 cudaError_t launch_vjp_passes(int variant, const DevBox* boxes, const AdjBox* adj, const int2* items, int nitems,
-                              const int4* fitems, int nfitems, double* recbar, const long long* recbar_off,
-                              const DevMech<1>& m1, const DevMech<9>& m9, const DevFlags& f, const Geo& g,
-                              cudaStream_t s);
+                              const int4* fitems, int nfitems, double* recbar, long long nrecbar,
+                              const long long* recbar_off, const DevMech<1>& m1, const DevMech<9>& m9,
+                              const DevFlags& f, const Geo& g, unsigned long long* counters, cudaStream_t s);
 cudaError_t launch_jvp_passes(int variant, const DevBox* boxes, const TanBox* tans, const int2* items, int nitems,
                               const int4* tiles, int ntiles, const DevMech<1>& m1, const DevMech<9>& m9,
                               const DevFlags& f, const Geo& g, unsigned long long* counters, cudaStream_t s);
@@ -578,7 +578,7 @@ int pc_mol_last_status(pc_mol_handle* h, pc_mol_status* st) {
   st->newton_nonconverged = (long long)c[kCounterNewton];
   st->nonpositive_state = (long long)c[kCounterNonpos];
   st->nonfinite_output = (long long)c[kCounterNonfinite];
-  st->exact_recomputes = (long long)(c[kCounterSlowCell] + c[kCounterSlowFlux]);
+  st->exact_recomputes = (long long)(c[kCounterSlowCell] + c[kCounterSlowFlux] + c[kCounterSlowAdj]);
   st->last_error = h->last_error;
   return PC_OK;
 }
@@ -1246,8 +1246,8 @@ extern "C" int pc_mol_rhs_vjp(pc_mol_handle* h, const pc_box_desc* boxes, int nb
   if ((rc = cuda_fail(h, cudaMemsetAsync(h->recbar, 0, sizeof(double) * L.scratch_doubles, s))) != PC_OK) return rc;
   const cudaError_t e = launch_vjp_passes(h->variant, h->d_boxes, static_cast<const AdjBox*>(dadj), h->d_items, nitems,
                                           static_cast<const int4*>(dfit), (int)fitems.size(), h->recbar,
-                                          static_cast<const long long*>(doff), h->mech1, h->mech9, h->flags,
-                                          make_geo(dx), s);
+                                          (long long)L.scratch_doubles, static_cast<const long long*>(doff),
+                                          h->mech1, h->mech9, h->flags, make_geo(dx), h->d_counters, s);
   return h->last_error = cuda_fail(h, e);
 }
 

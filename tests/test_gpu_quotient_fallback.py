@@ -62,3 +62,42 @@ def test_ordinary_states_need_no_exact_pass(cuda_lib, oracle_lib):
     (gpu,), status = gpu_rhs(cuda_lib, cfg, [st])
     _same(gpu, ref, "flame 16^3")
     assert status.exact_recomputes == 0
+
+
+def test_subnormal_velocities_run_the_exact_face_adjoint(cuda_lib):
+    """The vector-Jacobian product on the same state: its face adjoint meets
+    the same subnormal quotients, so its exact twin clears the record
+    cotangents and accumulates them again.  <mu, J v> from the dual-number
+    tangent (IEEE quotients throughout) must equal <J^T mu, v>."""
+    import torch
+
+    from gpu_util import to_multifab
+
+    mol = cuda_lib
+    mech, st = problems.tgv(12, seed=44)
+    for n in (1, 2, 3):
+        st.S[n] *= 1e-318
+    cfg = problems.make_config(mech)
+    rng = np.random.default_rng(44)
+    nx, ny, nz = st.shape
+    mu = rng.normal(size=(st.S.shape[0], nz, ny, nx))
+    g = st.S[:, 2:-2, 2:-2, 2:-2]
+    v = rng.normal(size=g.shape) * np.sqrt((g ** 2).mean(axis=(1, 2, 3)))[:, None, None, None]
+    v[5] = 0.0
+    v[6] = 0.0
+    op = mol.MOLOperator(cfg)
+    S = to_multifab(mol, [st], st.ng)
+    Rb = mol.MultiFab(S.boxes, S.ncomp, 0, fabs=[torch.from_numpy(np.ascontiguousarray(mu)).cuda()])
+    Ub = mol.MultiFab(S.boxes, S.ncomp, 2)
+    op.rhs_vjp(S, Rb, Ub, st.dx)
+    torch.cuda.synchronize()
+    assert op.status().exact_recomputes > 0
+    Sd = mol.MultiFab(S.boxes, S.ncomp, 2, fabs=[torch.from_numpy(np.ascontiguousarray(v)).cuda()])
+    R = mol.MultiFab(S.boxes, S.ncomp, 0)
+    Rd = mol.MultiFab(S.boxes, S.ncomp, 0)
+    op.rhs_jvp(S, Sd, R, Rd, st.dx)
+    torch.cuda.synchronize()
+    Jv = Rd.fabs[0].cpu().numpy()
+    a = float((mu * Jv).sum())
+    b = float((Ub.fabs[0].cpu().numpy() * v).sum())
+    assert abs(a - b) <= 1e-10 * float(np.abs(mu * Jv).sum()), (a, b)
