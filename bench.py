@@ -181,6 +181,13 @@ def fp_peaks() -> dict:
         return {}
 
 
+def launches_per_rhs(form: str) -> int:
+    """Kernel launches of one RHS: the cell and flux passes, and for the
+    exact FP64 form each pass's exact twin (which returns at once unless a
+    lane of the fast pass needs an IEEE division)."""
+    return 4 if form == "fp64" else 2
+
+
 def fp64_roofline(prof: dict, ms_rhs: float, peaks: dict) -> dict:
     """The roofline that binds: executed FP64 work of one RHS (ncu counters,
     profiles/dram_traffic_c2_fp64.txt) over the two passes' time, against the
@@ -256,14 +263,15 @@ def bench_level(args, rank: int, local: int, maxover, barrier) -> dict:
         g = op.graph(S, R, dx)
         t_graph = timed(g.launch)
         g.close()
+        nl = launches_per_rhs(name)
         res["per_box"] = {"value": cells / t_per_box, "ms_per_step": 1e3 * t_per_box,
-                          "gpu_launches_per_step": 2 * len(boxes)}
+                          "gpu_launches_per_step": nl * len(boxes)}
         res["batched_default_tile"] = {"value": cells / t_default, "ms_per_step": 1e3 * t_default,
-                                       "tile": mol.MOLOperator.tile_shape(0), "gpu_launches_per_step": 2}
+                                       "tile": mol.MOLOperator.tile_shape(0), "gpu_launches_per_step": nl}
         res["batched_autotuned"] = {"value": cells / t_tuned, "ms_per_step": 1e3 * t_tuned,
-                                    "launch": launch_name(best), "gpu_launches_per_step": 2,
+                                    "launch": launch_name(best), "gpu_launches_per_step": nl,
                                     "autotune_ms_per_launch": {launch_name(t): v for t, v in enumerate(ms)}}
-        res["graph"] = {"value": cells / t_graph, "ms_per_step": 1e3 * t_graph, "gpu_launches_per_step": 2,
+        res["graph"] = {"value": cells / t_graph, "ms_per_step": 1e3 * t_graph, "gpu_launches_per_step": nl,
                         "note": "one cudaGraphLaunch of the autotuned batched RHS"}
         res["speedup_graph_vs_per_box"] = t_per_box / t_graph
         if prec == 0:
@@ -687,12 +695,12 @@ def run_gpu(args):
         "config": {"workload": desc, "boxes_per_gpu": 1, "cells_per_gpu": cells, "nspec": mech.nspec,
                    "precision": args.precision, "precision_note": FORM_NOTE[args.precision],
                    "l2": "inputs larger than L2 (state %.0f MB, scratch records %.0f MB)" % (
-                       st.S.nbytes / 1e6, cells * (10 + 4 * mech.nspec) * 8 * 1.1 / 1e6),
+                       st.S.nbytes / 1e6, cells * (13 + 4 * mech.nspec) * 8 * 1.1 / 1e6),
                    "flux_launch": launch_name(best),
                    "autotune_ms_per_launch": {launch_name(t): v for t, v in enumerate(tune_ms)}},
         "e2e": {"value": world * cells * args.steps / t_e2e, "unit": "cell-evals/s",
                 "h2d_bytes_per_step": int(S_h.numel() * 8), "d2h_bytes_per_step": int(R_h.numel() * 8)},
-        "gpu_launches": 2 * args.steps,
+        "gpu_launches": launches_per_rhs(args.precision) * args.steps,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved / hbm_peak, "traffic": traffic,
                      "kernel": "cell_kernel + flux_kernel (one RHS)",
@@ -722,7 +730,7 @@ def run_gpu(args):
                   "rel_max_vs_fp64": {"max": max(mx), "per_component": mx},
                   "flux_scaled_max_vs_fp64": {"max": max(fs_m), "per_component": fs_m},
                   "precision": "FP32 reconstruction/Riemann/diffusion, FP64 Newton/mass fractions/divergence"},
-        "gpu_launches_mixed": 2 * args.steps,
+        "gpu_launches_mixed": launches_per_rhs("mixed") * args.steps,
         "status": {"cells": status.cells, "newton_nonconverged": status.newton_nonconverged,
                    "nonpositive_state": status.nonpositive_state, "nonfinite_output": status.nonfinite_output,
                    "exact_recomputes": status.exact_recomputes},
