@@ -82,6 +82,26 @@ __device__ __forceinline__ double* mixed_x(const DevBox& b) {
   return reinterpret_cast<double*>(reinterpret_cast<float*>(b.rec) + nf);
 }
 
+// Reference velocity of a box: the velocity of its first valid cell (lo
+// corner), in FP64 (0 where that is not finite).  The FP32 records hold the
+// velocity minus it, so that FP32 resolves the velocity's variations within
+// the box rather than its mean: a face flux u * (rho e) whose divergence is
+// a small difference (rho e nearly uniform across a low-Mach flame) is then
+// formed in FP64 as (U + u') rho e, with the FP32 rounding on u' only.  The
+// Riemann solver is Galilean covariant in u (u* of shifted states is u* + U),
+// so the face states and u* are computed on the offsets; its switches and
+// wave speeds use U + u' in FP32.
+__device__ __forceinline__ void box_uref(const DevBox& b, double U[3]) {
+  const double* s = b.S + (b.lo[0] - b.sb[0]) + (long long)(b.lo[1] - b.sb[1]) * b.sj +
+                    (long long)(b.lo[2] - b.sb[2]) * b.sk;
+  const double ir = 1.0 / __ldg(s + URHO * b.sn);
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const double u = __ldg(s + (UMX + a) * b.sn) * ir;
+    U[a] = isfinite(u) ? u : 0.0;
+  }
+}
+
 template <int NS>
 __device__ __forceinline__ float mix_rwf(const MechF<NS>& m, const float* Y) {
   float s = 0.f;
@@ -225,6 +245,9 @@ __global__ void __launch_bounds__(kCellThreads)
   const int2 it = items[blockIdx.x];
   const DevBox& b = boxes[it.x];
   const long long c = (long long)it.y + threadIdx.x;
+  __shared__ double Us[3];  // the box's reference velocity
+  if (threadIdx.x == 0) box_uref(b, Us);
+  __syncthreads();
   bool newton_fail = false, nonpos = false;
   if (c < b.ncell) {
     const int nx = b.n2[0], ny = b.n2[1];
@@ -259,9 +282,9 @@ __global__ void __launch_bounds__(kCellThreads)
     float* r = reinterpret_cast<float*>(b.rec) + c;
     const long long N = b.ncell;
     r[RC::RHO * N] = rhof;
-    r[RC::U * N] = (float)vx;
-    r[RC::V * N] = (float)vy;
-    r[RC::W * N] = (float)vz;
+    r[RC::U * N] = (float)(vx - Us[0]);  // velocity offsets from the box's reference velocity
+    r[RC::V * N] = (float)(vy - Us[1]);
+    r[RC::W * N] = (float)(vz - Us[2]);
     r[RC::P * N] = (float)(p - (double)mf.p_ref);
     r[RC::C * N] = cs;
 #pragma unroll
@@ -326,8 +349,8 @@ __device__ __forceinline__ double e_rpY_fp64(const DevMech<NS>& md, const float*
 // divergence is ~1e-3 of their size, below what an FP32 flux can resolve.
 template <int NS, bool MIX, int d>
 __device__ __forceinline__ void hydro_face_f(const DevBox& b, const MechF<NS>& m, const DevMech<NS>& md,
-                                             const DevFlags& f, long long cR, long long st, float* F, double& FE,
-                                             double& FEI) {
+                                             const DevFlags& f, long long cR, long long st, const double* U,
+                                             float* F, double& FE, double& FEI) {
   using RC = Rec<NS>;
   using E = EosF<NS, MIX>;
   const float* rec = reinterpret_cast<const float*>(b.rec);
@@ -337,6 +360,10 @@ __device__ __forceinline__ void hydro_face_f(const DevBox& b, const MechF<NS>& m
   const int fun = RC::U + d;
   const int fut1 = (d == 0) ? RC::V : RC::U;
   const int fut2 = (d == 2) ? RC::V : RC::W;
+  // reference velocity of the normal and the two transverse components (the
+  // velocities below are offsets from them)
+  const double Un = U[d], Ut1 = U[(d == 0) ? 1 : 0], Ut2 = U[(d == 2) ? 1 : 2];
+  const float Unf = (float)Un, Ut1f = (float)Ut1, Ut2f = (float)Ut2;
   const float rLL = ld(RC::RHO, cLL), rL = ld(RC::RHO, cL), rR = ld(RC::RHO, cR), rRR = ld(RC::RHO, cRR);
   const float pLL = ld(RC::P, cLL), pL = ld(RC::P, cL), pR = ld(RC::P, cR), pRR = ld(RC::P, cRR);
   const float uLL = ld(fun, cLL), uL = ld(fun, cL), uR = ld(fun, cR), uRR = ld(fun, cRR);
@@ -413,12 +440,13 @@ __device__ __forceinline__ void hydro_face_f(const DevBox& b, const MechF<NS>& m
     const float wr = fmaxf(wsmall, cr * rr);
     const float iw = 1.f / (wl + wr);
     const float pstar = fmaxf(wsmall - pref, ((wr * pl + wl * pr) + wl * wr * (unl - unr)) * iw);
-    float ustar = ((wl * unl + wr * unr) + (pl - pr)) * iw;
-    bool mask = ustar > 0.f;
+    float ustar = ((wl * unl + wr * unr) + (pl - pr)) * iw;  // offset from Un
+    bool mask = ustar + Unf > 0.f;
     float uo = mask ? unl : unr;
     float po = mask ? pl : pr;
-    const bool m0 = fabsf(ustar) < 1e-12f * 0.5f * (fabsf(unl) + fabsf(unr)) || ustar == 0.f;
-    ustar = m0 ? 0.f : ustar;
+    const float usa = ustar + Unf;
+    const bool m0 = fabsf(usa) < 1e-12f * 0.5f * (fabsf(unl + Unf) + fabsf(unr + Unf)) || usa == 0.f;
+    ustar = m0 ? -Unf : ustar;
     float rspo[NS];
     float ro = 0.f;
 #pragma unroll
@@ -450,21 +478,20 @@ __device__ __forceinline__ void hydro_face_f(const DevBox& b, const MechF<NS>& m
       for (int n = 0; n < NS; ++n) Yt[n] = rspstar[n] * y;
     }
     const float cstar = E::cs_rp(m, Yt, mix_rwf<NS>(m, Yt), rstar, pstar + pref);
-    const float sgnm = copysignf(1.f, ustar);
-    float spout = co - sgnm * uo;
-    float spin = cstar - sgnm * ustar;
+    const float sgnm = copysignf(1.f, m0 ? 0.f : ustar + Unf);
+    float spout = co - sgnm * (uo + Unf);
+    float spin = cstar - sgnm * (m0 ? 0.f : ustar + Unf);
     const float ushock = 0.5f * (spin + spout);
     mask = pstar < po;
     spout = mask ? spout : ushock;
     spin = mask ? spin : ushock;
     const float scr = (fabsf(spout - spin) < 1e-30f) ? 1e-8f * cavg : spout - spin;
     const float frac = fmaxf(0.f, fminf(1.f, (1.f + (spout + spin) / scr) * 0.5f));
-    mask = ustar > 0.f;
+    mask = !m0 && ustar + Unf > 0.f;
     float iv1 = mask ? ut1l : ut1r;
     float iv2 = mask ? ut2l : ut2r;
-    mask = (ustar == 0.f);
-    iv1 = mask ? 0.5f * (ut1l + ut1r) : iv1;
-    iv2 = mask ? 0.5f * (ut2l + ut2r) : iv2;
+    iv1 = m0 ? 0.5f * (ut1l + ut1r) : iv1;
+    iv2 = m0 ? 0.5f * (ut2l + ut2r) : iv2;
     const bool mout = spout < 0.f, min_ = spin >= 0.f;
     float iu = frac * ustar + (1.f - frac) * uo;
     float gdp = frac * pstar + (1.f - frac) * po;
@@ -483,39 +510,43 @@ __device__ __forceinline__ void hydro_face_f(const DevBox& b, const MechF<NS>& m
     }
     const double gdpa = (double)gdp + (double)pref;
     const double regd = (double)rgd * e_rp_fp64<NS, MIX>(md, flY, rgd, gdpa);
-    fl_rho = rgd * iu;
+    const float iua = iu + Unf, iv1a = iv1 + Ut1f, iv2a = iv2 + Ut2f;  // absolute velocities
+    fl_rho = rgd * iua;
 #pragma unroll
-    for (int n = 0; n < NS; ++n) flY[n] *= iu;
-    fl_un = fl_rho * iu + gdp;  // p_ref dropped: zero divergence
-    fl_ut1 = fl_rho * iv1;
-    fl_ut2 = fl_rho * iv2;
-    const double iud = (double)iu;
-    fl_E = iud * (regd + (double)(0.5f * rgd * (iu * iu + iv1 * iv1 + iv2 * iv2)) + gdpa);
+    for (int n = 0; n < NS; ++n) flY[n] *= iua;
+    fl_un = fl_rho * iua + gdp;  // p_ref dropped: zero divergence
+    fl_ut1 = fl_rho * iv1a;
+    fl_ut2 = fl_rho * iv2a;
+    const double iud = Un + (double)iu;  // FP64: U + u'
+    fl_E = iud * (regd + (double)(0.5f * rgd * (iua * iua + iv1a * iv1a + iv2a * iv2a)) + gdpa);
     fl_ei = iud * regd;
   } else {
+    // Lax-Friedrichs on absolute velocities (U + u')
+    const float unlA = unl + Unf, unrA = unr + Unf, ut1lA = ut1l + Ut1f, ut1rA = ut1r + Ut1f;
+    const float ut2lA = ut2l + Ut2f, ut2rA = ut2r + Ut2f;
     const double pla = (double)pl + (double)pref, pra = (double)pr + (double)pref;
     const double el = e_rpY_fp64<NS, MIX>(md, spl, rl, pla);
     const double er = e_rpY_fp64<NS, MIX>(md, spr, rr, pra);
-    const double r_elt = (double)rl * (el + (double)(0.5f * (unl * unl + ut1l * ut1l + ut2l * ut2l)));
-    const double r_ert = (double)rr * (er + (double)(0.5f * (unr * unr + ut1r * ut1r + ut2r * ut2r)));
+    const double r_elt = (double)rl * (el + (double)(0.5f * (unlA * unlA + ut1lA * ut1lA + ut2lA * ut2lA)));
+    const double r_ert = (double)rr * (er + (double)(0.5f * (unrA * unrA + ut1rA * ut1rA + ut2rA * ut2rA)));
     const float wl = fmaxf(1.17549435e-38f, cl * rl);
     const float wr = fmaxf(1.17549435e-38f, cr * rr);
-    float ustar = ((wl * unl + wr * unr) + (pl - pr)) / (wl + wr);
-    const bool m0 = fabsf(ustar) < 1e-12f * 0.5f * (fabsf(unl) + fabsf(unr)) || ustar == 0.f;
+    float ustar = ((wl * unlA + wr * unrA) + (pl - pr)) / (wl + wr);
+    const bool m0 = fabsf(ustar) < 1e-12f * 0.5f * (fabsf(unlA) + fabsf(unrA)) || ustar == 0.f;
     ustar = m0 ? 0.f : ustar;
     const float mw = fabsf(ustar) + 0.5f * (cr + cl);
     fl_rho = 0.f;
 #pragma unroll
     for (int n = 0; n < NS; ++n) {
-      flY[n] = 0.5f * ((rl * unl * spl[n] + rr * unr * spr[n]) - mw * (rr * spr[n] - rl * spl[n]));
+      flY[n] = 0.5f * ((rl * unlA * spl[n] + rr * unrA * spr[n]) - mw * (rr * spr[n] - rl * spl[n]));
       fl_rho += flY[n];
     }
-    fl_un = 0.5f * ((rl * unl * unl + pl + rr * unr * unr + pr) - mw * (rr * unr - rl * unl));
-    fl_ut1 = 0.5f * ((rl * ut1l * unl + rr * ut1r * unr) - mw * (rr * ut1r - rl * ut1l));
-    fl_ut2 = 0.5f * ((rl * ut2l * unl + rr * ut2r * unr) - mw * (rr * ut2r - rl * ut2l));
+    fl_un = 0.5f * ((rl * unlA * unlA + pl + rr * unrA * unrA + pr) - mw * (rr * unrA - rl * unlA));
+    fl_ut1 = 0.5f * ((rl * ut1lA * unlA + rr * ut1rA * unrA) - mw * (rr * ut1rA - rl * ut1lA));
+    fl_ut2 = 0.5f * ((rl * ut2lA * unlA + rr * ut2rA * unrA) - mw * (rr * ut2rA - rl * ut2lA));
     const double mwd = (double)mw;
-    fl_E = 0.5 * (((r_elt + pla) * (double)unl + (r_ert + pra) * (double)unr) - mwd * (r_ert - r_elt));
-    fl_ei = 0.5 * (((double)rl * el * (double)unl + (double)rr * er * (double)unr) -
+    fl_E = 0.5 * (((r_elt + pla) * (Un + (double)unl) + (r_ert + pra) * (Un + (double)unr)) - mwd * (r_ert - r_elt));
+    fl_ei = 0.5 * (((double)rl * el * (Un + (double)unl) + (double)rr * er * (Un + (double)unr)) -
                    mwd * ((double)rr * er - (double)rl * el));
   }
   F[URHO] = fl_rho;
@@ -534,7 +565,7 @@ __device__ __forceinline__ void hydro_face_f(const DevBox& b, const MechF<NS>& m
 // FP32 diffusion flux (not area-scaled), added to F.
 template <int NS, int d>
 __device__ __forceinline__ void diffusion_face_f(const DevBox& b, const DevFlags& f, const Geo& g, long long cR,
-                                                 const long long stv[3], float* F) {
+                                                 const long long stv[3], const double* U, float* F) {
   using RC = Rec<NS>;
   const float* rec = reinterpret_cast<const float*>(b.rec);
   const long long N = b.ncell;
@@ -570,7 +601,10 @@ __device__ __forceinline__ void diffusion_face_f(const DevBox& b, const DevFlags
       tau[a] = mu * (grad[d][a] + grad[a][d]);
   }
   const float dT = (float)(__ldg(xrec + NS * N + cR) - __ldg(xrec + NS * N + cL));
-  float fE = 0.5f * (-tau[0] * (uR[0] + uL[0]) - tau[1] * (uR[1] + uL[1]) - tau[2] * (uR[2] + uL[2])) -
+  // the work term needs absolute velocities: the offsets plus the box's reference
+  const float Uf[3] = {(float)U[0], (float)U[1], (float)U[2]};
+  float fE = 0.5f * (-tau[0] * (uR[0] + uL[0] + 2.f * Uf[0]) - tau[1] * (uR[1] + uL[1] + 2.f * Uf[1]) -
+                     tau[2] * (uR[2] + uL[2] + 2.f * Uf[2])) -
              lam * dxi * dT;
   const bool spec = f.diffuse_spec != 0;
   const bool ener = (f.diffuse_temp != 0) || (f.diffuse_enth != 0);
@@ -610,7 +644,7 @@ template <int NS, bool MIX, int d, class TL>
 __device__ __forceinline__ void dir_pass_mixed(const DevBox& b, const MechF<NS>& m, const DevMech<NS>& md,
                                                const DevFlags& f, const Geo& g,
                                                const int o[3], const int ext[3], const long long stv[3], bool mine,
-                                               int tx, int ty, int tz, double* fbuf, double* acc) {
+                                               int tx, int ty, int tz, double* fbuf, double* acc, const double* U) {
   constexpr int NVAR = 7 + NS;
   const bool diff = f.diffuse_vel || f.diffuse_temp || f.diffuse_spec || f.diffuse_enth;
   const int nf0 = ext[0] + (d == 0), nf1 = ext[1] + (d == 1), nf2 = ext[2] + (d == 2);
@@ -622,12 +656,12 @@ __device__ __forceinline__ void dir_pass_mixed(const DevBox& b, const MechF<NS>&
     float F[NVAR];
     double FE = 0.0, FEI = 0.0;
     if (f.do_hydro) {
-      hydro_face_f<NS, MIX, d>(b, m, md, f, cR, stv[d], F, FE, FEI);
+      hydro_face_f<NS, MIX, d>(b, m, md, f, cR, stv[d], U, F, FE, FEI);
     } else {
 #pragma unroll
       for (int n = 0; n < NVAR; ++n) F[n] = 0.f;
     }
-    if (diff) diffusion_face_f<NS, d>(b, f, g, cR, stv, F);
+    if (diff) diffusion_face_f<NS, d>(b, f, g, cR, stv, U, F);
 #pragma unroll
     for (int n = 0; n < NVAR; ++n) fbuf[n * TL::MAXF + fi] = (double)F[n];  // exact widening
     fbuf[UEDEN * TL::MAXF + fi] = FE + (double)F[UEDEN];
@@ -669,12 +703,15 @@ __global__ void __launch_bounds__(TL::NT, TL::MINB)
                         min(TL::TZ, b.hi[2] - o[2] + 1)};
     const bool mine = tx < ext[0] && ty < ext[1] && tz < ext[2];
     const long long stv[3] = {1, b.n2[0], (long long)b.n2[0] * b.n2[1]};
+    __shared__ double Us[3];  // the box's reference velocity (read before the first direction pass's barrier)
+    if (threadIdx.x == 0) box_uref(b, Us);
+    __syncthreads();
     double acc[NVAR];
 #pragma unroll
     for (int n = 0; n < NVAR; ++n) acc[n] = 0.0;
-    dir_pass_mixed<NS, MIX, 0, TL>(b, m, md, f, g, o, ext, stv, mine, tx, ty, tz, fbuf, acc);
-    dir_pass_mixed<NS, MIX, 1, TL>(b, m, md, f, g, o, ext, stv, mine, tx, ty, tz, fbuf, acc);
-    dir_pass_mixed<NS, MIX, 2, TL>(b, m, md, f, g, o, ext, stv, mine, tx, ty, tz, fbuf, acc);
+    dir_pass_mixed<NS, MIX, 0, TL>(b, m, md, f, g, o, ext, stv, mine, tx, ty, tz, fbuf, acc, Us);
+    dir_pass_mixed<NS, MIX, 1, TL>(b, m, md, f, g, o, ext, stv, mine, tx, ty, tz, fbuf, acc, Us);
+    dir_pass_mixed<NS, MIX, 2, TL>(b, m, md, f, g, o, ext, stv, mine, tx, ty, tz, fbuf, acc, Us);
     bool bad = false;
     if (mine) {
       const int i = o[0] + tx, j = o[1] + ty, k = o[2] + tz;
