@@ -163,13 +163,15 @@ __device__ __forceinline__ double div_by(double a, double b, double y) {
   return q;
 }
 
-// Quotient policy of a pass.  Quot<false> divides with div_fast and records
-// in .slow whether any operand needed a real division; a pass evaluated that
+// Quotient policies.  Quot<false> divides with div_fast and records in
+// .slow whether any operand needed a real division; a pass evaluated that
 // way counts such lanes, and an exact twin of the pass (Quot<true>: IEEE
 // division), launched after it, evaluates everything again when the count is
 // not zero.  The fast pass thus has no branch per quotient, and the compiler
-// can interleave the integer work of neighbouring quotients.  Other scalar
-// types (the dual numbers of the tangent) divide with their own div_by.
+// can interleave the integer work of neighbouring quotients.  QuotSelf
+// (div_by: rare operands divided in a per-warp branch) serves passes without
+// an exact twin.  The dual numbers of the tangent have their own div_fast,
+// exact_quotient and div_by (pc_tangent.cuh), found by argument lookup.
 template <bool kExact>
 struct Quot;
 template <>
@@ -177,7 +179,7 @@ struct Quot<false> {
   bool slow = false;
   template <class R>
   __device__ __forceinline__ R operator()(const R& a, const R& b, const R& y) {
-    return div_by(a, b, y);
+    return div_fast(a, b, y, slow);
   }
   __device__ __forceinline__ double operator()(double a, double b, double y) { return div_fast(a, b, y, slow); }
 };
@@ -186,9 +188,16 @@ struct Quot<true> {
   bool slow = false;
   template <class R>
   __device__ __forceinline__ R operator()(const R& a, const R& b, const R& y) {
-    return div_by(a, b, y);
+    return exact_quotient(a, b, y);
   }
   __device__ __forceinline__ double operator()(double a, double b, double y) { return exact_quotient(a, b, y); }
+};
+struct QuotSelf {
+  bool slow = false;
+  template <class R>
+  __device__ __forceinline__ R operator()(const R& a, const R& b, const R& y) {
+    return div_by(a, b, y);
+  }
 };
 
 // Exact binary scalings on the bit patterns (integer pipe).  Multiplying by
@@ -288,7 +297,7 @@ __device__ __forceinline__ void y2x(const DevMech<NS>& m, const R* Y, R rw, R* X
 }
 template <int NS, class R>
 __device__ __forceinline__ void y2x(const DevMech<NS>& m, const R* Y, R rw, R* X) {
-  Quot<true> q;
+  QuotSelf q;
   y2x(m, Y, rw, X, q);
 }
 

@@ -139,7 +139,7 @@ __device__ __forceinline__ double rey2t_of(const DevMech<NS>& m, const double* Y
 // U(UTEMP); st(field, value) writes a record field.  inner: the cell lies in
 // grow(valid, 1), where the diffusion fluxes need T, X, h and the transport
 // coefficients.
-template <int NS, class EOS, class TR, class R, class Store, class Q = Quot<true>>
+template <int NS, class EOS, class TR, class R, class Store, class Q = QuotSelf>
 __device__ __forceinline__ void cell_record(const DevMech<NS>& m, const DevFlags& f, const R* U, double Tguess,
                                             bool inner, Store st, bool& newton_fail, bool& nonpos, Q&& q = Q()) {
   using RC = Rec<NS>;
@@ -264,7 +264,7 @@ inline cudaError_t launch_cell_fp64(const DevBox* boxes, const int2* items, unsi
 // MOL.H:53-112): the characteristic slopes dq[0..3] and the species slopes
 // ds[NS].  A function of the cells c - st, c and c + st only, so one
 // evaluation serves both faces of the cell.
-template <int NS, int d, class R, class Q = Quot<true>>
+template <int NS, int d, class R, class Q = QuotSelf>
 __device__ __forceinline__ void cell_slopes(const RecAcc<R>& ra, long long c, long long st, R* dq, R* ds,
                                             Q&& q = Q()) {
   using RC = Rec<NS>;
@@ -304,7 +304,7 @@ __device__ __forceinline__ void cell_slopes(const RecAcc<R>& ra, long long c, lo
 
 // Hyperbolic flux on the low face of the cell at record index cR in
 // direction d, times the face area, given the slopes of its two cells.
-template <int NS, class EOS, int d, class R, class Q = Quot<true>>
+template <int NS, class EOS, int d, class R, class Q = QuotSelf>
 __device__ __forceinline__ void hydro_face_sl(const RecAcc<R>& ra, const DevMech<NS>& m, const DevFlags& f,
                                               long long cR, long long st, double A, const R* dqL, const R* dsL,
                                               const R* dqR, const R* dsR, R* F, Q&& q = Q()) {
@@ -491,18 +491,18 @@ __device__ __forceinline__ void hydro_face_sl(const RecAcc<R>& ra, const DevMech
 // Hyperbolic flux on the low face of the cell at record index cR in
 // direction d, times the face area: F[n] = flux_n * A (Riemann.H, MOL.cpp),
 // with the slopes of both cells evaluated here.
-template <int NS, class EOS, int d, class R>
+template <int NS, class EOS, int d, class R, class Q = QuotSelf>
 __device__ __forceinline__ void hydro_face(const RecAcc<R>& ra, const DevMech<NS>& m, const DevFlags& f, long long cR,
-                                           long long st, double A, R* F) {
+                                           long long st, double A, R* F, Q&& q = Q()) {
   R dqL[4] = {0.0, 0.0, 0.0, 0.0}, dqR[4] = {0.0, 0.0, 0.0, 0.0};
   R dsL[NS], dsR[NS];
 #pragma unroll
   for (int n = 0; n < NS; ++n) dsL[n] = dsR[n] = 0.0;
   if (f.slopes) {
-    cell_slopes<NS, d>(ra, cR - st, st, dqL, dsL);
-    cell_slopes<NS, d>(ra, cR, st, dqR, dsR);
+    cell_slopes<NS, d>(ra, cR - st, st, dqL, dsL, q);
+    cell_slopes<NS, d>(ra, cR, st, dqR, dsR, q);
   }
-  hydro_face_sl<NS, EOS, d>(ra, m, f, cR, st, A, dqL, dsL, dqR, dsR, F);
+  hydro_face_sl<NS, EOS, d>(ra, m, f, cR, st, A, dqL, dsL, dqR, dsR, F, q);
 }
 
 // pc_diffusion_flux + SpeciesEnergyFlux (Diffterm.H:20-75, 344-461), times

@@ -5,22 +5,31 @@
 
 namespace pcg {
 
+// Each pass fast, then its exact twin (which returns at once unless the fast
+// pass counted a lane whose quotients need an IEEE division).
+template <int NS, class EOS, class TR>
+static void jvp_passes(const DevBox* boxes, const TanBox* tans, const int2* items, int nitems, const int4* tiles,
+                       int ntiles, const DevMech<NS>& m, const DevFlags& f, const Geo& g,
+                       unsigned long long* counters, cudaStream_t s) {
+  if (nitems > 0) {
+    cell_tangent_kernel<NS, EOS, TR, false><<<nitems, kCellThreads, 0, s>>>(boxes, tans, items, m, f, counters);
+    cell_tangent_kernel<NS, EOS, TR, true><<<nitems, kCellThreads, 0, s>>>(boxes, tans, items, m, f, counters);
+  }
+  if (ntiles > 0) {
+    flux_tangent_kernel<NS, EOS, false><<<ntiles, TileTangent::NT, 0, s>>>(boxes, tans, tiles, m, f, g, counters);
+    flux_tangent_kernel<NS, EOS, true><<<ntiles, TileTangent::NT, 0, s>>>(boxes, tans, tiles, m, f, g, counters);
+  }
+}
+
 cudaError_t launch_jvp_passes(int variant, const DevBox* boxes, const TanBox* tans, const int2* items, int nitems,
                               const int4* tiles, int ntiles, const DevMech<1>& m1, const DevMech<9>& m9,
                               const DevFlags& f, const Geo& g, unsigned long long* counters, cudaStream_t s) {
-  if (variant == 1) {
-    if (nitems > 0)
-      cell_tangent_kernel<1, GammaLawEos<1>, ConstantTransport<1>>
-          <<<nitems, kCellThreads, 0, s>>>(boxes, tans, items, m1, f, counters);
-    if (ntiles > 0)
-      flux_tangent_kernel<1, GammaLawEos<1>><<<ntiles, TileTangent::NT, 0, s>>>(boxes, tans, tiles, m1, f, g);
-  } else {
-    if (nitems > 0)
-      cell_tangent_kernel<9, IdealMixEos<9>, SimpleTransport<9>>
-          <<<nitems, kCellThreads, 0, s>>>(boxes, tans, items, m9, f, counters);
-    if (ntiles > 0)
-      flux_tangent_kernel<9, IdealMixEos<9>><<<ntiles, TileTangent::NT, 0, s>>>(boxes, tans, tiles, m9, f, g);
-  }
+  if (variant == 1)
+    jvp_passes<1, GammaLawEos<1>, ConstantTransport<1>>(boxes, tans, items, nitems, tiles, ntiles, m1, f, g,
+                                                        counters, s);
+  else
+    jvp_passes<9, IdealMixEos<9>, SimpleTransport<9>>(boxes, tans, items, nitems, tiles, ntiles, m9, f, g,
+                                                      counters, s);
   return cudaGetLastError();
 }
 

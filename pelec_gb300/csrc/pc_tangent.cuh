@@ -24,9 +24,19 @@ struct RecAcc<Dual> {
   }
 };
 
-// a / b for a shared divisor (div_by of the forward for the value).
+// a / b for a shared divisor: the forward's quotient for the value (div_by,
+// div_fast or exact_quotient, as the policy of the pass chooses), and
+// (a' - q b') / b for the tangent.
 __device__ __forceinline__ Dual div_by(const Dual& a, const Dual& b, const Dual& y) {
   const double q = div_by(a.v, b.v, y.v);
+  return Dual(q, (a.d - q * b.d) * y.v);
+}
+__device__ __forceinline__ Dual div_fast(const Dual& a, const Dual& b, const Dual& y, bool& slow) {
+  const double q = div_fast(a.v, b.v, y.v, slow);
+  return Dual(q, (a.d - q * b.d) * y.v);
+}
+__device__ __forceinline__ Dual exact_quotient(const Dual& a, const Dual& b, const Dual& y) {
+  const double q = exact_quotient(a.v, b.v, y.v);
   return Dual(q, (a.d - q * b.d) * y.v);
 }
 
@@ -60,12 +70,16 @@ __device__ __forceinline__ Dual rey2t_of(const DevMech<NS>& m, const Dual* Y, Du
   }
 }
 
-template <int NS, class EOS, class TR>
+// kExact as for cell_kernel: the fast pass counts lanes whose quotients need
+// an IEEE division; the exact twin returns at once unless there were some.
+template <int NS, class EOS, class TR, bool kExact = false>
 __global__ void __launch_bounds__(kCellThreads)
     cell_tangent_kernel(const DevBox* __restrict__ boxes, const TanBox* __restrict__ tans,
                         const int2* __restrict__ items, const __grid_constant__ DevMech<NS> m, const DevFlags f,
                         unsigned long long* __restrict__ counters) {
   constexpr int NVAR = 7 + NS;
+  if (kExact && __ldcg(&counters[kCounterSlowCell]) == 0ull) return;
+  Quot<kExact> quo;
   const int2 it = items[blockIdx.x];
   const DevBox& b = boxes[it.x];
   const TanBox& tb = tans[it.x];
@@ -88,10 +102,13 @@ __global__ void __launch_bounds__(kCellThreads)
                                r[fld * N] = v.v;
                                rt[fld * N] = v.d;
                              },
-                             newton_fail, nonpos);
+                             newton_fail, nonpos, quo);
   }
-  warp_count(&counters[kCounterNewton], newton_fail);
-  warp_count(&counters[kCounterNonpos], nonpos);
+  if (!kExact) {
+    warp_count(&counters[kCounterNewton], newton_fail);
+    warp_count(&counters[kCounterNonpos], nonpos);
+    warp_count(&counters[kCounterSlowCell], quo.slow);
+  }
 }
 
 // Flux pass of the tangent on 8x4x4 tiles (the layout's tile list must use
@@ -99,11 +116,11 @@ __global__ void __launch_bounds__(kCellThreads)
 // into the cell accumulators.
 using TileTangent = TileSmall;
 
-template <int NS, class EOS, int d>
+template <int NS, class EOS, int d, class Q>
 __device__ __forceinline__ void dir_pass_tangent(const DevBox& b, const RecAcc<Dual>& ra, const DevMech<NS>& m,
                                                  const DevFlags& f, const Geo& g, const int o[3], const int ext[3],
                                                  const long long stv[3], bool mine, int tx, int ty, int tz,
-                                                 Dual* fbuf, Dual* acc) {
+                                                 Dual* fbuf, Dual* acc, Q& quo) {
   using TL = TileTangent;
   constexpr int NVAR = 7 + NS;
   const bool diff = f.diffuse_vel || f.diffuse_temp || f.diffuse_spec || f.diffuse_enth;
@@ -115,7 +132,7 @@ __device__ __forceinline__ void dir_pass_tangent(const DevBox& b, const RecAcc<D
     const long long cR = (i - b.g2lo[0]) + (j - b.g2lo[1]) * stv[1] + (k - b.g2lo[2]) * stv[2];
     Dual F[NVAR];
     if (f.do_hydro) {
-      hydro_face<NS, EOS, d>(ra, m, f, cR, stv[d], g.area[d], F);
+      hydro_face<NS, EOS, d>(ra, m, f, cR, stv[d], g.area[d], F, quo);
     } else {
 #pragma unroll
       for (int n = 0; n < NVAR; ++n) F[n] = Dual(0.0);
@@ -134,13 +151,15 @@ __device__ __forceinline__ void dir_pass_tangent(const DevBox& b, const RecAcc<D
   __syncthreads();
 }
 
-template <int NS, class EOS>
+template <int NS, class EOS, bool kExact = false>
 __global__ void __launch_bounds__(TileTangent::NT)
     flux_tangent_kernel(const DevBox* __restrict__ boxes, const TanBox* __restrict__ tans,
                         const int4* __restrict__ tiles, const __grid_constant__ DevMech<NS> m, const DevFlags f,
-                        const Geo g) {
+                        const Geo g, unsigned long long* __restrict__ counters) {
   using TL = TileTangent;
   constexpr int NVAR = 7 + NS;
+  if (kExact && __ldcg(&counters[kCounterSlowFlux]) == 0ull) return;
+  Quot<kExact> quo;
   __shared__ double2 fbuf_raw[NVAR * TL::MAXF];  // Dual has a constructor: raw storage
   Dual* fbuf = reinterpret_cast<Dual*>(fbuf_raw);
   const int4 t = tiles[blockIdx.x];
@@ -155,9 +174,9 @@ __global__ void __launch_bounds__(TileTangent::NT)
   Dual acc[NVAR];
 #pragma unroll
   for (int n = 0; n < NVAR; ++n) acc[n] = Dual(0.0);
-  dir_pass_tangent<NS, EOS, 0>(b, ra, m, f, g, o, ext, stv, mine, tx, ty, tz, fbuf, acc);
-  dir_pass_tangent<NS, EOS, 1>(b, ra, m, f, g, o, ext, stv, mine, tx, ty, tz, fbuf, acc);
-  dir_pass_tangent<NS, EOS, 2>(b, ra, m, f, g, o, ext, stv, mine, tx, ty, tz, fbuf, acc);
+  dir_pass_tangent<NS, EOS, 0>(b, ra, m, f, g, o, ext, stv, mine, tx, ty, tz, fbuf, acc, quo);
+  dir_pass_tangent<NS, EOS, 1>(b, ra, m, f, g, o, ext, stv, mine, tx, ty, tz, fbuf, acc, quo);
+  dir_pass_tangent<NS, EOS, 2>(b, ra, m, f, g, o, ext, stv, mine, tx, ty, tz, fbuf, acc, quo);
   if (mine) {
     const int i = o[0] + tx, j = o[1] + ty, k = o[2] + tz;
     double* r = b.R + (i - b.rb[0]) + (long long)(j - b.rb[1]) * b.rj + (long long)(k - b.rb[2]) * b.rk;
@@ -169,6 +188,7 @@ __global__ void __launch_bounds__(TileTangent::NT)
       rd[n * tb.rn] = v.d;
     }
   }
+  if (!kExact) warp_count(&counters[kCounterSlowFlux], quo.slow);
 }
 
 }  // namespace pcg
