@@ -40,6 +40,7 @@ constexpr double kSmallNum = 1.0e-8;
 template <int NS>
 struct DevMech {
   double rW[NS];     // R / W_k
+  double irW[NS];    // 1 / (R / W_k), IEEE: the shared divisor's reciprocal of W_k / Wbar
   double gamma, gm1; // GammaLaw
   double cpk[NS];    // GammaLaw cp_k = gamma/(gamma-1) R/W_k
   double tmid;
@@ -443,8 +444,8 @@ struct IdealMixEos {
 // ---------------------------------------------------------------------------
 template <int NS>
 struct ConstantTransport {
-  template <class R>
-  __device__ static void eval(const DevMech<NS>& m, R, R, R, const R*, const R*, R* out) {
+  template <class R, class Q = QuotSelf>
+  __device__ static void eval(const DevMech<NS>& m, R, R, R, const R*, const R*, R* out, Q&& = Q()) {
 #pragma unroll
     for (int k = 0; k < NS; ++k) out[k] = m.const_rhoD;
     out[NS] = m.const_mu;
@@ -460,8 +461,9 @@ struct ConstantTransport {
 // rhoD_k grad X_k), 1/D_kj(T,p) = exp(-fit_kj(ln T)) p / p_ref.
 template <int NS>
 struct SimpleTransport {
-  template <class R>
-  __device__ static void eval(const DevMech<NS>& m, R T, R rho, R p, const R* Y, const R* X, R* out) {
+  template <class R, class Q = QuotSelf>
+  __device__ static void eval(const DevMech<NS>& m, R T, R rho, R p, const R* Y, const R* X, R* out,
+                              Q&& q = Q()) {
     const R L = pc_log(T);
     R smu = 0.0, slam = 0.0, sxi = 0.0;
 #pragma unroll
@@ -476,12 +478,12 @@ struct SimpleTransport {
 #pragma unroll
     for (int k = 0; k < NS; ++k) s[k] = 0.0;
     const R pr = p * m.inv_pref;
-    int q = 0;
+    int pq = 0;
 #pragma unroll
     for (int k = 0; k < NS; ++k) {
 #pragma unroll
-      for (int j = k + 1; j < NS; ++j, ++q) {
-        const R invD = pc_exp(-horner4(m.diff[q], L)) * pr;
+      for (int j = k + 1; j < NS; ++j, ++pq) {
+        const R invD = pc_exp(-horner4(m.diff[pq], L)) * pr;
         s[k] = fma(fmax_pos(X[j], 1e-15), invD, s[k]);
         s[j] = fma(fmax_pos(X[k], 1e-15), invD, s[j]);
       }
@@ -489,7 +491,7 @@ struct SimpleTransport {
     const R rw = mix_rw<NS>(m, Y);
 #pragma unroll
     for (int k = 0; k < NS; ++k) {
-      const R wrat = rw / m.rW[k];  // W_k / Wbar
+      const R wrat = q(rw, R(m.rW[k]), R(m.irW[k]));  // W_k / Wbar, correctly rounded
       out[k] = (s[k] > 0.0) ? rho * (1.0 - Y[k]) * wrat / s[k] : 0.0;
     }
     out[NS] = pc_exp(pc_log(smu) * (1.0 / 6.0));

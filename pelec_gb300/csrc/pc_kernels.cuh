@@ -179,7 +179,7 @@ __device__ __forceinline__ void cell_record(const DevMech<NS>& m, const DevFlags
     R X[NS];
     y2x(m, Y, rw, X, q);
     R out[NS + 3];
-    TR::eval(m, T, rho, p, Y, X, out);
+    TR::eval(m, T, rho, p, Y, X, out, q);
     st(RC::T, T);
 #pragma unroll
     for (int n = 0; n < NS; ++n) st(RC::X + n, X[n]);

@@ -118,7 +118,10 @@ int cuda_fail(pc_mol_handle* h, cudaError_t e) {
 
 template <int NS>
 void fill_common(DevMech<NS>& d, const pc_mechanism& m) {
-  for (int k = 0; k < NS; ++k) d.rW[k] = RU / m.mw[k];
+  for (int k = 0; k < NS; ++k) {
+    d.rW[k] = RU / m.mw[k];
+    d.irW[k] = 1.0 / d.rW[k];
+  }
   d.gamma = m.gamma;
   d.gm1 = m.gamma - 1.0;
   for (int k = 0; k < NS; ++k) d.cpk[k] = m.gamma / (m.gamma - 1.0) * RU / m.mw[k];
