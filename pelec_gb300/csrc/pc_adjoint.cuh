@@ -426,7 +426,7 @@ __device__ void hydro_face_rev(const DevBox& b, const DevMech<NS>& m, const DevF
     rr += Yr[n];
   }
   {
-    const double yrl = 1.0 / rl, yrr = 1.0 / rr;
+    const double yrl = rcp_q(rl), yrr = rcp_q(rr);
 #pragma unroll
     for (int n = 0; n < NS; ++n) {
       Yl[n] = q(Yl[n], rl, yrl);
@@ -440,7 +440,7 @@ __device__ void hydro_face_rev(const DevBox& b, const DevMech<NS>& m, const DevF
   const double wsmall = 2.2250738585072014e-308;
   const double wl = fmax(wsmall, cl * rl);
   const double wr = fmax(wsmall, cr * rr);
-  const double ww = wl + wr, yww = 1.0 / ww;
+  const double ww = wl + wr, yww = rcp_q(ww);
   const double pnum = (wr * pl + wl * pr) + wl * wr * (unl - unr);
   const double pq = q(pnum, ww, yww);
   const double pstar = fmax(wsmall, pq);
@@ -462,7 +462,7 @@ __device__ void hydro_face_rev(const DevBox& b, const DevMech<NS>& m, const DevF
   po = m0 ? 0.5 * (pl + pr) : po;
   double Yo[NS];
   {
-    const double y = 1.0 / ro;
+    const double y = rcp_q(ro);
 #pragma unroll
     for (int n = 0; n < NS; ++n) Yo[n] = q(rspo[n], ro, y);
   }
@@ -478,7 +478,7 @@ __device__ void hydro_face_rev(const DevBox& b, const DevMech<NS>& m, const DevF
   }
   double Ys[NS];
   {
-    const double y = 1.0 / rstar;
+    const double y = rcp_q(rstar);
 #pragma unroll
     for (int n = 0; n < NS; ++n) Ys[n] = q(rsps[n], rstar, y);
   }
@@ -519,7 +519,7 @@ __device__ void hydro_face_rev(const DevBox& b, const DevMech<NS>& m, const DevF
   }
   double Yg[NS];
   {
-    const double y = 1.0 / rgd;
+    const double y = rcp_q(rgd);
 #pragma unroll
     for (int n = 0; n < NS; ++n) Yg[n] = q(gq[n], rgd, y);
   }

@@ -40,7 +40,7 @@ constexpr double kSmallNum = 1.0e-8;
 template <int NS>
 struct DevMech {
   double rW[NS];     // R / W_k
-  double irW[NS];    // 1 / (R / W_k), IEEE: the shared divisor's reciprocal of W_k / Wbar
+  double irW[NS];    // rcp_q(R / W_k): the shared divisor's reciprocal of W_k / Wbar
   double gamma, gm1; // GammaLaw
   double cpk[NS];    // GammaLaw cp_k = gamma/(gamma-1) R/W_k
   double tmid;
@@ -79,29 +79,45 @@ __device__ __forceinline__ void rare_for_warp(bool need, F&& f) {
   }
 }
 
+// The reciprocal y of a shared divisor b that div_fast and div_by expect:
+// 1/b rounded toward zero (in the PC_PRECISION_FP64_RCP compilation, 1/b
+// rounded to nearest, whose product with a is the quotient of that form).
+__device__ __forceinline__ double rcp_q(double b) {
+#ifdef PCG_RECIPROCAL_QUOTIENTS
+  return 1.0 / b;
+#else
+  return __drcp_rz(b);
+#endif
+}
+
 // a / b, correctly rounded, for a divisor b shared by several quotients, given
-// y = 1.0 / b (an IEEE division), without a branch: the result for the
-// common operands, with slow set for the rare ones that need a real division
-// (the caller then evaluates again with exact_quotient, see Quot).
+// y = rcp_q(b) (1/b rounded toward zero), without a branch: the result for
+// the common operands, with slow set for the rare ones that need a real
+// division (the caller then evaluates again with exact_quotient, see Quot).
 //
-// q0 = RN(a y) is within two ulps of a/b (y and the product each round by at
-// most half an ulp), so the correctly rounded quotient is q0 + s ulp(q0) for
-// some s in [-2, 2].  s is decided exactly in integer arithmetic on the
-// significands, off the FP64 pipe (the binding resource on GB300, which runs
-// integer instructions at 32-64 times its FP64 rate): with
-// a = A 2^(ea-1075), b = B 2^(eb-1075) and q0 = M 2^(eq-1075) (A, B, M the
-// 53-bit significands),
-//   R = A 2^k - B M,   k = ea - eb - eq + 1075 (51 <= k <= 54),
-// equals (a/b - q0) / ulp(q0) times B and |R| < 2B < 2^54, so it is exact
+// q0 = a y rounded toward zero is at most the quotient in magnitude and
+// within four ulps of it (y and the product each lose less than an ulp), so
+// the correctly rounded quotient is q0 + s ulp(q0) for some s in [0, 4].
+// s is decided exactly in integer arithmetic on the significands, off the
+// FP64 pipe (the binding resource on GB300, which runs integer instructions
+// at 32-64 times its FP64 rate): with a = A 2^(ea-1075), b = B 2^(eb-1075)
+// and q0 = M 2^(eq-1075) (A, B, M the 53-bit significands),
+//   R = A 2^k - B M,   k = ea - eb - eq + 1075 (51 <= k <= 55),
+// equals (|a/b| - |q0|) / ulp(q0) times B, 0 <= R < 4B < 2^55, so it is exact
 // modulo 2^64; and as k >= 32, A 2^k mod 2^64 depends only on A's low word.
-// s counts the half-integers 1/2 and 3/2 that R/B exceeds (a quotient of two
+// s counts the half-integers 1/2 .. 7/2 that R/B exceeds (a quotient of two
 // doubles is never exactly halfway between two doubles, so there are no
 // ties), and s ulp is added to q0's bit pattern.  One FP64 multiply instead
-// of a division.  A zero numerator gives a*y, the correctly signed zero.
+// of a division.  Rounding toward zero keeps the quotient on q0's side of
+// any power of two below it; above it (q0 within 4 ulp of the next power of
+// two P = q0 + d ulp and s > d) the doubles are 2 ulp apart, and the
+// quotient, less than 3 ulp above P, rounds to P or to P + 2 ulp.  A zero
+// numerator gives a*y, the correctly signed zero.
 // Slow: a nonzero numerator that is subnormal, infinite or NaN; b zero,
 // subnormal, infinite, NaN or above 2^1022 (1/b not a normal number); q0
-// outside [2^-1021, 2^1022) (the quotient or its neighbours not normal).  For
-// a zero numerator only b zero or subnormal (1/b infinite).
+// outside [2^-1021, 2^1022) (the quotient or its neighbours not normal); or
+// R < 0 (y not rounded toward zero).  For a zero numerator only b zero or
+// subnormal (1/b infinite).
 __device__ __forceinline__ double div_fast(double a, double b, double y, bool& slow) {
 #ifdef PCG_RECIPROCAL_QUOTIENTS
   // The PC_PRECISION_FP64_RCP compilation: a y = a/b (1 + e) with
@@ -110,7 +126,7 @@ __device__ __forceinline__ double div_fast(double a, double b, double y, bool& s
   (void)slow;
   return a * y;
 #else
-  const double q0 = a * y;
+  const double q0 = __dmul_rz(a, y);
   const unsigned ah = (unsigned)__double2hiint(a), al = (unsigned)__double2loint(a);
   const unsigned bh = (unsigned)__double2hiint(b), bl = (unsigned)__double2loint(b);
   const unsigned qh = (unsigned)__double2hiint(q0), ql = (unsigned)__double2loint(q0);
@@ -120,26 +136,16 @@ __device__ __forceinline__ double div_fast(double a, double b, double y, bool& s
   const unsigned long long p = (unsigned long long)bl * ql;  // B M mod 2^64 = p + (bl Mh + Bh ql) 2^32
   const unsigned phi = (unsigned)(p >> 32) + bl * Mh + Bh * ql;
   const long long R = (long long)(((unsigned long long)(al << sh) << 32) - (((unsigned long long)phi << 32) | (unsigned)p));
-  const long long Bs = (long long)(((unsigned long long)Bh << 32) | bl), R2 = 2 * R, B3 = 3 * Bs;
-  long long st = (long long)(R2 > Bs) + (long long)(R2 > B3) - (long long)(R2 < -Bs) - (long long)(R2 < -B3);
-  // Binade ends, where the spacing of doubles changes.  q0 = (2^53 - 1) ulp
-  // with the quotient more than 1.5 ulp above it: the quotient is less than
-  // 2 ulp above q0 (the error bound), so it lies within one ulp of the power
-  // of two 2^53 ulp, whose upper neighbour is 2 ulp away: the step is 1.  q0
-  // = P or P + ulp for a power of two P, with the quotient below P (within one
-  // ulp of it, the error bound there): the doubles below P are half an ulp
-  // apart, so the step is counted from P in half ulps, T / 2B with
-  // T = 4 (R + (q0 - P) B / ulp) in (-4B(1 + 2^-52), 0).  An exact
-  // power-of-two quotient (R = 0) takes neither branch.
-  const unsigned m20 = qh & 0xfffffu;
-  st = (m20 == 0xfffffu && ql == 0xffffffffu && st == 2) ? 1 : st;
-  const long long T = 4 * (R + (ql == 1u ? Bs : 0));
-  const long long half = -((long long)(T < -Bs) + (long long)(T < -B3));
-  st = (m20 == 0u && ((ql == 0u && R < 0) || (ql == 1u && R < -Bs))) ? half - (long long)ql : st;
+  const long long Bs = (long long)(((unsigned long long)Bh << 32) | bl), R2 = 2 * R;
+  int st = (int)(R2 > Bs) + (int)(R2 > 3 * Bs) + (int)(R2 > 5 * Bs) + (int)(R2 > 7 * Bs);
+  // q0 = P - d ulp below a power of two P (d = 1..4) and s > d: P, or P + 2 ulp
+  // (the next double up) if the quotient is an ulp or more above P.
+  const int d = (int)(0xffffffffu - ql) + 1;
+  if ((qh & 0xfffffu) == 0xfffffu && ql >= 0xfffffffcu && st > d) st = d + (int)(R >= (long long)(d + 1) * Bs);
   const bool zero = ((ah << 1) | al) == 0u;
-  slow |= zero ? (eb == 0u) : (ea - 1u > 2045u || eb - 1u > 2043u || eq - 2u > 2043u);
+  slow |= zero ? (eb == 0u) : (ea - 1u > 2045u || eb - 1u > 2043u || eq - 2u > 2043u || R < 0);
   const unsigned long long iq = ((unsigned long long)qh << 32) | ql;
-  return zero ? q0 : __longlong_as_double((long long)(iq + (unsigned long long)st));
+  return zero ? q0 : __longlong_as_double((long long)(iq + (unsigned long long)(long long)st));
 #endif
 }
 
@@ -155,7 +161,7 @@ __device__ __forceinline__ double exact_quotient(double a, double b, double y) {
 }
 
 // a / b, correctly rounded, for a divisor b shared by several quotients, given
-// y = 1.0 / b: div_fast, with the rare operands divided in a branch that only
+// y = rcp_q(b): div_fast, with the rare operands divided in a branch that only
 // warps containing one take.
 __device__ __forceinline__ double div_by(double a, double b, double y) {
   bool slow = false;
@@ -292,7 +298,7 @@ __device__ __forceinline__ R mix_rw(const DevMech<NS>& m, const R* Y) {
 // Y2X: X_k = Y_k (R/W_k) / (R/Wbar).
 template <int NS, class R, class Q>
 __device__ __forceinline__ void y2x(const DevMech<NS>& m, const R* Y, R rw, R* X, Q& q) {
-  const R irw = 1.0 / rw;
+  const R irw = rcp_q(rw);
 #pragma unroll
   for (int k = 0; k < NS; ++k) X[k] = q(Y[k] * m.rW[k], rw, irw);  // = Y_k (R/W_k) / rw
 }

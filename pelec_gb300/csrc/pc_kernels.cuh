@@ -53,9 +53,9 @@ struct Geo {
   double p_ref;  // mixed precision: pressure offset of the FP32 records
 };
 
-// Record fields (pass 1 -> pass 2).  IRHO, IC, IC2 are the IEEE reciprocals
-// 1/rho, 1/c and 1/(c c) of every cell, the divisors' reciprocals of the
-// slopes' and face states' quotients (div_by), evaluated once per cell.
+// Record fields (pass 1 -> pass 2).  IRHO, IC, IC2 are the reciprocals
+// rcp_q of rho, c and c c of every cell, the divisors' reciprocals of the
+// slopes' and face states' quotients (div_fast), evaluated once per cell.
 template <int NS>
 struct Rec {
   static constexpr int RHO = 0, U = 1, V = 2, W = 3, P = 4, C = 5, Y = 6;
@@ -150,10 +150,11 @@ __device__ __forceinline__ void cell_record(const DevMech<NS>& m, const DevFlags
   const R vz = U[UMZ] * rhoinv;
   const R kineng = 0.5 * rho * (vx * vx + vy * vy + vz * vz);
   const R e = (U[UEDEN] - kineng) * rhoinv;
+  const R rhoinv_q = rcp_q(rho);  // the quotients' reciprocal (rounded toward zero)
   R Y[NS];
 #pragma unroll
   for (int n = 0; n < NS; ++n) {
-    const R y = q(U[UFS + n], rho, rhoinv);  // = rho Y_n / rho, correctly rounded
+    const R y = q(U[UFS + n], rho, rhoinv_q);  // = rho Y_n / rho, correctly rounded
     Y[n] = zero_below(y, 1e-4 * 2.220446049250313e-16);  // |Y| < 1e-4 eps -> 0 (Utilities.H:288-294)
   }
   const R rw = mix_rw<NS>(m, Y);
@@ -169,9 +170,9 @@ __device__ __forceinline__ void cell_record(const DevMech<NS>& m, const DevFlags
   st(RC::W, vz);
   st(RC::P, p);
   st(RC::C, cs);
-  st(RC::IRHO, rhoinv);
-  st(RC::IC, 1.0 / cs);
-  st(RC::IC2, 1.0 / (cs * cs));
+  st(RC::IRHO, rhoinv_q);
+  st(RC::IC, rcp_q(cs));
+  st(RC::IC2, rcp_q(cs * cs));
 #pragma unroll
   for (int n = 0; n < NS; ++n) st(RC::Y + n, Y[n]);
   if (inner) {
@@ -341,7 +342,7 @@ __device__ __forceinline__ void hydro_face_sl(const RecAcc<R>& ra, const DevMech
       rl += spl[n];
       rr += spr[n];
     }
-    const R yrl = 1.0 / rl, yrr = 1.0 / rr;
+    const R yrl = rcp_q(rl), yrr = rcp_q(rr);
 #pragma unroll
     for (int n = 0; n < NS; ++n) {
       spl[n] = q(spl[n], rl, yrl);
@@ -359,7 +360,7 @@ __device__ __forceinline__ void hydro_face_sl(const RecAcc<R>& ra, const DevMech
     const double wsmall = 2.2250738585072014e-308;
     const R wl = fmax(wsmall, cl * rl);
     const R wr = fmax(wsmall, cr * rr);
-    const R ww = wl + wr, yww = 1.0 / ww;
+    const R ww = wl + wr, yww = rcp_q(ww);
     const R pstar = fmax(wsmall, q((wr * pl + wl * pr) + wl * wr * (unl - unr), ww, yww));
     R ustar = q((wl * unl + wr * unr) + (pl - pr), ww, yww);
     bool mask = ustar > 0.0;
@@ -390,7 +391,7 @@ __device__ __forceinline__ void hydro_face_sl(const RecAcc<R>& ra, const DevMech
     for (int n = 0; n < NS; ++n) ro += rspo[n];
     R Yt[NS];
     {
-      const R y = 1.0 / ro;
+      const R y = rcp_q(ro);
 #pragma unroll
       for (int n = 0; n < NS; ++n) Yt[n] = q(rspo[n], ro, y);
     }
@@ -404,7 +405,7 @@ __device__ __forceinline__ void hydro_face_sl(const RecAcc<R>& ra, const DevMech
       rstar += rspstar[n];
     }
     {
-      const R y = 1.0 / rstar;
+      const R y = rcp_q(rstar);
 #pragma unroll
       for (int n = 0; n < NS; ++n) Yt[n] = q(rspstar[n], rstar, y);
     }
@@ -438,7 +439,7 @@ __device__ __forceinline__ void hydro_face_sl(const RecAcc<R>& ra, const DevMech
 #pragma unroll
     for (int n = 0; n < NS; ++n) rgd += flY[n];
     {
-      const R y = 1.0 / rgd;
+      const R y = rcp_q(rgd);
 #pragma unroll
       for (int n = 0; n < NS; ++n) Yt[n] = q(flY[n], rgd, y);
     }

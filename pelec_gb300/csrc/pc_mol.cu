@@ -116,11 +116,20 @@ int cuda_fail(pc_mol_handle* h, cudaError_t e) {
   return (e == cudaErrorMemoryAllocation) ? PC_ERR_OUT_OF_MEMORY : PC_ERR_CUDA;
 }
 
+// 1/x rounded toward zero, on the host (the device's rcp_q): the nearest
+// reciprocal, stepped one ulp toward zero where it exceeds 1/x in magnitude
+// (r x > 1, decided exactly by the fused remainder).
+double rcp_rz_host(double x) {
+  double r = 1.0 / x;
+  if (std::isfinite(r) && r != 0.0 && std::fma(r, x, -1.0) > 0.0) r = std::nextafter(r, 0.0);
+  return r;
+}
+
 template <int NS>
 void fill_common(DevMech<NS>& d, const pc_mechanism& m) {
   for (int k = 0; k < NS; ++k) {
     d.rW[k] = RU / m.mw[k];
-    d.irW[k] = 1.0 / d.rW[k];
+    d.irW[k] = rcp_rz_host(d.rW[k]);
   }
   d.gamma = m.gamma;
   d.gm1 = m.gamma - 1.0;
@@ -363,7 +372,7 @@ Geo make_geo(const double dx[3]) {
   g.area[1] = dx[0] * dx[2];
   g.area[2] = dx[0] * dx[1];
   g.vol = dx[0] * dx[1] * dx[2];
-  g.ivol = 1.0 / g.vol;
+  g.ivol = rcp_rz_host(g.vol);
   g.p_ref = 0.0;
   return g;
 }
@@ -671,7 +680,7 @@ __global__ void check_quotients_kernel(const double* __restrict__ a, const doubl
                                        double* __restrict__ q, long long n) {
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
     const double bi = b[i];
-    q[i] = div_by(a[i], bi, 1.0 / bi);
+    q[i] = div_by(a[i], bi, rcp_q(bi));
   }
 }
 }  // namespace

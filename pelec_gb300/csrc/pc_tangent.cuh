@@ -31,6 +31,12 @@ __device__ __forceinline__ Dual div_by(const Dual& a, const Dual& b, const Dual&
   const double q = div_by(a.v, b.v, y.v);
   return Dual(q, (a.d - q * b.d) * y.v);
 }
+// rcp_q of a dual number: the value rounded as div_fast expects, the
+// tangent -b' / b^2.
+__device__ __forceinline__ Dual rcp_q(const Dual& b) {
+  const double y = rcp_q(b.v);
+  return Dual(y, -b.d * y * y);
+}
 __device__ __forceinline__ Dual div_fast(const Dual& a, const Dual& b, const Dual& y, bool& slow) {
   const double q = div_fast(a.v, b.v, y.v, slow);
   return Dual(q, (a.d - q * b.d) * y.v);
