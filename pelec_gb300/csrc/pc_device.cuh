@@ -90,6 +90,20 @@ __device__ __forceinline__ double rcp_q(double b) {
 #endif
 }
 
+// rcp_q(b) from r = 1.0 / b (rounded to nearest) where that is at hand: r
+// stepped one ulp toward zero (its bit pattern decremented) where r b > 1,
+// decided by one fused multiply-add.  Operands that make r infinite, zero or
+// NaN are the ones div_fast sends to a real division anyway.
+__device__ __forceinline__ double rcp_q_from_rn(double b, double r) {
+#ifdef PCG_RECIPROCAL_QUOTIENTS
+  (void)b;
+  return r;
+#else
+  const long long e = __double_as_longlong(fma(r, b, -1.0));
+  return (e > 0) ? __longlong_as_double(__double_as_longlong(r) - 1) : r;
+#endif
+}
+
 // a / b, correctly rounded, for a divisor b shared by several quotients, given
 // y = rcp_q(b) (1/b rounded toward zero), without a branch: the result for
 // the common operands, with slow set for the rare ones that need a real

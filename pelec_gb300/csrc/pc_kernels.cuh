@@ -150,7 +150,7 @@ __device__ __forceinline__ void cell_record(const DevMech<NS>& m, const DevFlags
   const R vz = U[UMZ] * rhoinv;
   const R kineng = 0.5 * rho * (vx * vx + vy * vy + vz * vz);
   const R e = (U[UEDEN] - kineng) * rhoinv;
-  const R rhoinv_q = rcp_q(rho);  // the quotients' reciprocal (rounded toward zero)
+  const R rhoinv_q = rcp_q_from_rn(rho, rhoinv);  // the quotients' reciprocal (rounded toward zero)
   R Y[NS];
 #pragma unroll
   for (int n = 0; n < NS; ++n) {

@@ -37,6 +37,9 @@ __device__ __forceinline__ Dual rcp_q(const Dual& b) {
   const double y = rcp_q(b.v);
   return Dual(y, -b.d * y * y);
 }
+__device__ __forceinline__ Dual rcp_q_from_rn(const Dual& b, const Dual& r) {
+  return Dual(rcp_q_from_rn(b.v, r.v), r.d);
+}
 __device__ __forceinline__ Dual div_fast(const Dual& a, const Dual& b, const Dual& y, bool& slow) {
   const double q = div_fast(a.v, b.v, y.v, slow);
   return Dual(q, (a.d - q * b.d) * y.v);
