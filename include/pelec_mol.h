@@ -73,7 +73,7 @@ typedef enum pc_precision {
                                renormalisation, the Riemann weights, 1/V) is
                                the product with the divisor's correctly
                                rounded reciprocal, within one ulp of the
-                               PC_PRECISION_FP64 quotient: about 1.2x faster,
+                               PC_PRECISION_FP64 quotient: about 1.1x faster,
                                and different from PC_PRECISION_FP64 by
                                rounding (as a build with multiply-add
                                contraction would be), about 1e-15 of each
