@@ -40,7 +40,7 @@ def _rz(fr: Fraction) -> float:
 def div_fast(a: float, b: float):
     """(quotient, slow) as the kernel computes them (finite a, nonzero finite b)."""
     y = _rz(Fraction(1) / Fraction(b))
-    q0 = _rz(Fraction(a) * Fraction(y))
+    q0 = _rz(Fraction(a) * Fraction(y)) if a != 0.0 else math.copysign(0.0, a) * math.copysign(1.0, y)
     ia, ib, iq = _bits(a), _bits(b), _bits(q0)
     ah, al, bh, bl, qh, ql = ia >> 32, ia & M32, ib >> 32, ib & M32, iq >> 32, iq & M32
     ea, eb, eq = (ah >> 20) & 0x7FF, (bh >> 20) & 0x7FF, (qh >> 20) & 0x7FF
