@@ -206,10 +206,15 @@ __device__ __forceinline__ bool in_grow1(const DevBox& b, int i, int j, int k) {
          k <= b.hi[2] + 1;
 }
 
+// Bit pattern the fast cell pass leaves in the RHO field of a record whose
+// quotients need an IEEE division (a NaN no arithmetic produces), so that
+// the exact twin evaluates only those cells again.
+constexpr long long kSlowRecord = 0x7ff8dead5107beefLL;
+
 // kExact = false: the fast pass (quotients by div_fast); kExact = true: its
 // exact twin, which returns at once unless the fast pass counted a lane that
-// needs a real division, and then writes every record again with IEEE
-// quotients (bit for bit what the fast pass gives where it needs none).
+// needs a real division, and then writes again, with IEEE quotients, the
+// records the fast pass marked (kSlowRecord).
 template <int NS, class EOS, class TR, bool kExact = false>
 __global__ void __launch_bounds__(kCellThreads)
     cell_kernel(const DevBox* __restrict__ boxes, const int2* __restrict__ items, const __grid_constant__ DevMech<NS> m,
@@ -231,8 +236,12 @@ __global__ void __launch_bounds__(kCellThreads)
     for (int n = 0; n < NVAR; ++n) U[n] = (n == UEINT || n == UTEMP) ? 0.0 : __ldg(s + n * sn);
     double* r = b.rec + c;
     const long long N = b.ncell;
-    cell_record<NS, EOS, TR>(m, f, U, __ldg(s + UTEMP * sn), in_grow1(b, i, j, k),
-                             [&](int fld, double v) { r[fld * N] = v; }, newton_fail, nonpos, quo);
+    const bool todo = !kExact || __double_as_longlong(r[Rec<NS>::RHO * N]) == kSlowRecord;
+    if (todo) {
+      cell_record<NS, EOS, TR>(m, f, U, __ldg(s + UTEMP * sn), in_grow1(b, i, j, k),
+                               [&](int fld, double v) { r[fld * N] = v; }, newton_fail, nonpos, quo);
+      if (!kExact && quo.slow) r[Rec<NS>::RHO * N] = __longlong_as_double(kSlowRecord);
+    }
   }
   if (!kExact) {  // the exact twin re-evaluates cells the fast pass has counted already
     warp_count(&counters[kCounterNewton], newton_fail);
@@ -750,8 +759,9 @@ constexpr size_t flux_smem_bytes() {
 //
 // kExact = false: the fast pass (quotients by div_fast); kExact = true: its
 // exact twin, which returns at once unless the fast pass counted a lane that
-// needs a real division, and then evaluates every tile again with IEEE
-// quotients (bit for bit what the fast pass gives where it needs none).
+// needs a real division, and then evaluates again, with IEEE quotients, the
+// tiles the fast pass marked (bit for bit what the fast pass gives where it
+// needs none).
 template <int NS, class EOS, class TL = TileDefault, bool kExact = false>
 __global__ void __launch_bounds__(TL::NT, TL::MINB)
     flux_kernel(const DevBox* __restrict__ boxes, const int4* __restrict__ tiles, int ntiles,
@@ -773,10 +783,17 @@ __global__ void __launch_bounds__(TL::NT, TL::MINB)
     const int4 p = tiles[a], q = tiles[a + 1];
     return q.x == p.x && q.y == p.y && q.z == p.z && q.w == p.w + TL::TZ;
   };
+  bool any_slow = false;     // a lane of this CTA met operands div_fast does not cover
+  bool carried_slow = false;  // ... in the tile whose z face and slope layers this one takes over
   for (int tb = t0; tb < t1; ++tb) {
     const int4 t = tiles[tb];
     const DevBox& b = boxes[t.x];
     const int o[3] = {t.y, t.z, t.w};
+    // The RHS of the tile's first cell, component 0: the fast pass leaves
+    // kSlowRecord there in a tile whose quotients need an IEEE division, and
+    // the exact twin evaluates only those tiles again (without the z carry).
+    double* r0 = b.R + (o[0] - b.rb[0]) + (long long)(o[1] - b.rb[1]) * b.rj + (long long)(o[2] - b.rb[2]) * b.rk;
+    if (kExact && __double_as_longlong(*(volatile double*)r0) != kSlowRecord) continue;
     const int ext[3] = {min(TL::TX, b.hi[0] - o[0] + 1), min(TL::TY, b.hi[1] - o[1] + 1),
                         min(TL::TZ, b.hi[2] - o[2] + 1)};
     const bool mine = tx < ext[0] && ty < ext[1] && tz < ext[2];
@@ -785,8 +802,9 @@ __global__ void __launch_bounds__(TL::NT, TL::MINB)
 #pragma unroll
     for (int n = 0; n < NVAR; ++n) acc[n] = 0.0;
     const FluxBox* fxb = fluxes ? fluxes + t.x : nullptr;
-    zc.carry = tb > t0 && continues(tb - 1);
-    zc.save = tb + 1 < t1 && continues(tb);
+    zc.carry = !kExact && tb > t0 && continues(tb - 1);
+    zc.save = !kExact && tb + 1 < t1 && continues(tb);
+    quo.slow = false;
     dir_pass<NS, EOS, 0, TL>(b, m, f, g, o, ext, stv, mine, tx, ty, tz, fbuf, acc, fxb, zc, quo);
     dir_pass<NS, EOS, 1, TL>(b, m, f, g, o, ext, stv, mine, tx, ty, tz, fbuf, acc, fxb, zc, quo);
     dir_pass<NS, EOS, 2, TL>(b, m, f, g, o, ext, stv, mine, tx, ty, tz, fbuf, acc, fxb, zc, quo);
@@ -802,11 +820,17 @@ __global__ void __launch_bounds__(TL::NT, TL::MINB)
       }
     }
     if (!kExact) {  // the exact twin re-evaluates tiles the fast pass has counted already
+      // a tile is marked when one of its own lanes, or the tile it carried
+      // from, met an operand that needs an IEEE division
+      const bool tile_slow = __syncthreads_or(quo.slow) != 0 || carried_slow;
+      if (tile_slow && threadIdx.x == 0) *r0 = __longlong_as_double(kSlowRecord);  // after the cell's own write
+      any_slow |= quo.slow;
+      carried_slow = tile_slow && zc.save;
       if (f.check_output) warp_count(&counters[kCounterNonfinite], bad);
       if (threadIdx.x == 0) atomicAdd(&counters[kCounterCells], (unsigned long long)(ext[0] * ext[1] * ext[2]));
     }
   }
-  if (!kExact) warp_count(&counters[kCounterSlowFlux], quo.slow);
+  if (!kExact) warp_count(&counters[kCounterSlowFlux], any_slow);
 }
 
 // Host: CTAs of a kernel that are resident on the current device at once

@@ -106,12 +106,17 @@ __global__ void __launch_bounds__(kCellThreads)
     double* r = b.rec + c;
     double* rt = tb.trec + c;
     const long long N = b.ncell;
-    cell_record<NS, EOS, TR>(m, f, U, __ldg(s + UTEMP * b.sn), in_grow1(b, i, j, k),
-                             [&](int fld, const Dual& v) {
-                               r[fld * N] = v.v;
-                               rt[fld * N] = v.d;
-                             },
-                             newton_fail, nonpos, quo);
+    // the twin writes again only the records the fast pass marked (kSlowRecord)
+    const bool todo = !kExact || __double_as_longlong(r[Rec<NS>::RHO * N]) == kSlowRecord;
+    if (todo) {
+      cell_record<NS, EOS, TR>(m, f, U, __ldg(s + UTEMP * b.sn), in_grow1(b, i, j, k),
+                               [&](int fld, const Dual& v) {
+                                 r[fld * N] = v.v;
+                                 rt[fld * N] = v.d;
+                               },
+                               newton_fail, nonpos, quo);
+      if (!kExact && quo.slow) r[Rec<NS>::RHO * N] = __longlong_as_double(kSlowRecord);
+    }
   }
   if (!kExact) {
     warp_count(&counters[kCounterNewton], newton_fail);

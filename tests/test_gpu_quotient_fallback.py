@@ -55,6 +55,50 @@ def test_subnormal_velocities_run_the_exact_flux_pass(cuda_lib, oracle_lib):
     assert status.exact_recomputes > 0
 
 
+def _uniform_gas_with_still_block(n, seed):
+    """Uniform density and temperature, seeded velocities, and an 8x8x8
+    block at z in [20, 28) whose velocities are subnormal: its kinetic
+    energy underflows, so its pressure is exactly uniform, and the Riemann
+    solver's u* numerator there is a subnormal number."""
+    mech = problems.gamma_law_single()
+    rng = np.random.default_rng(seed)
+    rho0, T0 = 1.17e-3, 300.0
+    shape = (n, n, n)
+    rho = np.full(shape, rho0)
+    T = np.full(shape, T0)
+    vel = [rng.normal(0.0, 3e3, shape) for _ in range(3)]
+    for v in vel:
+        v[20:28, 0:8, 0:8] *= 1e-318
+    Sv = problems.conserved(mech, rho, *vel, T, np.ones((1,) + shape))
+    ng = problems.NG
+    S = np.zeros((Sv.shape[0], n + 2 * ng, n + 2 * ng, n + 2 * ng))
+    S[:, ng:-ng, ng:-ng, ng:-ng] = Sv
+    problems.fill_ghosts(S, ng, ("periodic",) * 3)
+    dx = 2.0 * np.pi / n
+    return mech, problems.BoxState(lo=(0, 0, 0), hi=(n - 1,) * 3, S=S, dx=(dx, dx, dx))
+
+
+def test_exact_flux_twin_redoes_only_marked_tiles(cuda_lib, oracle_lib):
+    """Only the tiles in and around the still block need IEEE divisions.
+    With one CTA per tile and with the persistent grid (each CTA runs up z
+    columns of tiles, carrying face and slope layers from tile to tile), the
+    exact twin evaluates the marked tiles again, those that took a carried
+    layer from a marked tile included, and the whole RHS equals the oracle's
+    bit for bit."""
+    from pelec_gb300 import abi
+
+    mech, st = _uniform_gas_with_still_block(64, seed=45)
+    cfg = problems.make_config(mech)
+    ref, = oracle_lib.mol_rhs(cfg, [st])
+    op = cuda_lib.MOLOperator(cfg)
+    for t in (0, abi.PC_LAUNCH_PERSISTENT):
+        op.set_tile(t)
+        (gpu,), status = gpu_rhs(cuda_lib, cfg, [st], op=op)
+        _same(gpu, ref, f"still block, launch configuration {t}")
+        assert status.exact_recomputes > 0
+        assert status.cells == 64 ** 3
+
+
 def test_ordinary_states_need_no_exact_pass(cuda_lib, oracle_lib):
     mech, st, _ = problems.flame((16, 16, 16), seed=43)
     cfg = problems.make_config(mech)
