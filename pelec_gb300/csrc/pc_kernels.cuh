@@ -49,7 +49,7 @@ struct Geo {
   double dxinv[3];
   double area[3];
   double vol;
-  double ivol;   // 1 / vol (IEEE), the shared divisor of the divergence
+  double ivol;   // 1 / vol rounded toward zero (rcp_q), the divergence's shared divisor
   double p_ref;  // mixed precision: pressure offset of the FP32 records
 };
 
