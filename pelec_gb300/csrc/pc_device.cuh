@@ -253,8 +253,9 @@ __device__ __forceinline__ unsigned long long twice_mag(unsigned long long m) {
   return m + (1ULL << 52);
 }
 
-// fmax(x, c) for a constant c > 0 (R = double: on the bit patterns; a
-// negative or NaN x gives c, as fmax does).
+// max(c, x) for a constant c >= 0, as std::max(c, x) = (c < x) ? x : c
+// evaluates it (R = double: on the bit patterns; a negative, -0 or NaN x
+// gives c).
 template <class R>
 __device__ __forceinline__ R fmax_pos(R x, double c) {
   return fmax(x, c);
@@ -523,12 +524,20 @@ struct SimpleTransport {
 
 // pc_move_transcoefs_to_ec, Source/Utilities.H:322-342.
 template <class R>
+__device__ __forceinline__ R twice_pos(R x) {
+  return 2.0 * x;
+}
+template <>
+__device__ __forceinline__ double twice_pos<double>(double x) {  // 2 x for x > 0, on the bit pattern
+  return dfrom(twice_mag(dbits(x)));
+}
+template <class R>
 __device__ __forceinline__ R face_coef(R a, R b, bool harmonic) {
   if (harmonic) {
     const R ab = a * b;
-    return (ab > 0.0) ? 2.0 * ab / (a + b) : 0.0;
+    return (ab > 0.0) ? twice_pos(ab) / (a + b) : R(0.0);
   }
-  return 0.5 * (a + b);
+  return halve(a + b);
 }
 
 // MC-type limiter of mol_slope, Source/MOL.H:104-112.

@@ -367,10 +367,10 @@ __device__ __forceinline__ void hydro_face_sl(const RecAcc<R>& ra, const DevMech
   if (!f.laxf) {
     // riemann(), Source/Riemann.H:42-199.
     const double wsmall = 2.2250738585072014e-308;
-    const R wl = fmax(wsmall, cl * rl);
-    const R wr = fmax(wsmall, cr * rr);
+    const R wl = fmax_pos(cl * rl, wsmall);  // max(wsmall, c rho), on the bit patterns for double
+    const R wr = fmax_pos(cr * rr, wsmall);
     const R ww = wl + wr, yww = rcp_q(ww);
-    const R pstar = fmax(wsmall, q((wr * pl + wl * pr) + wl * wr * (unl - unr), ww, yww));
+    const R pstar = fmax_pos(q((wr * pl + wl * pr) + wl * wr * (unl - unr), ww, yww), wsmall);
     R ustar = q((wl * unl + wr * unr) + (pl - pr), ww, yww);
     bool mask = ustar > 0.0;
     R rspo[NS];
@@ -410,7 +410,7 @@ __device__ __forceinline__ void hydro_face_sl(const RecAcc<R>& ra, const DevMech
     R rstar = 0.0;
 #pragma unroll
     for (int n = 0; n < NS; ++n) {
-      rspstar[n] = fmax(0.0, rspo[n] + drho * Yt[n]);
+      rspstar[n] = fmax_pos(rspo[n] + drho * Yt[n], 0.0);  // max(0, .)
       rstar += rspstar[n];
     }
     {
@@ -469,8 +469,8 @@ __device__ __forceinline__ void hydro_face_sl(const RecAcc<R>& ra, const DevMech
     const R r_elt = rl * (el + 0.5 * (unl * unl + ut1l * ut1l + ut2l * ut2l));
     const R r_ert = rr * (er + 0.5 * (unr * unr + ut1r * ut1r + ut2r * ut2r));
     const double wsmall = 2.2250738585072014e-308;
-    const R wl = fmax(wsmall, cl * rl);
-    const R wr = fmax(wsmall, cr * rr);
+    const R wl = fmax_pos(cl * rl, wsmall);
+    const R wr = fmax_pos(cr * rr, wsmall);
     R ustar = ((wl * unl + wr * unr) + (pl - pr)) / (wl + wr);
     const bool m0 = fabs(ustar) < kSmallU * 0.5 * (fabs(unl) + fabs(unr)) || ustar == 0.0;
     ustar = m0 ? 0.0 : ustar;
