@@ -16,8 +16,11 @@ static void jvp_passes(const DevBox* boxes, const TanBox* tans, const int2* item
     cell_tangent_kernel<NS, EOS, TR, true><<<nitems, kCellThreads, 0, s>>>(boxes, tans, items, m, f, counters);
   }
   if (ntiles > 0) {
-    flux_tangent_kernel<NS, EOS, false><<<ntiles, TileTangent::NT, 0, s>>>(boxes, tans, tiles, m, f, g, counters);
-    flux_tangent_kernel<NS, EOS, true><<<ntiles, TileTangent::NT, 0, s>>>(boxes, tans, tiles, m, f, g, counters);
+    constexpr size_t smem = tangent_smem_bytes<NS>();
+    cudaFuncSetAttribute(flux_tangent_kernel<NS, EOS, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(flux_tangent_kernel<NS, EOS, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    flux_tangent_kernel<NS, EOS, false><<<ntiles, TileTangent::NT, smem, s>>>(boxes, tans, tiles, m, f, g, counters);
+    flux_tangent_kernel<NS, EOS, true><<<ntiles, TileTangent::NT, smem, s>>>(boxes, tans, tiles, m, f, g, counters);
   }
 }
 

@@ -126,27 +126,67 @@ __global__ void __launch_bounds__(kCellThreads)
 }
 
 // Flux pass of the tangent on 8x4x4 tiles (the layout's tile list must use
-// that shape): each face once, staged in shared memory as Dual, differenced
-// into the cell accumulators.
+// that shape): per direction, the slopes of the tile's cells and of one
+// neighbour layer on each side evaluated once each and staged in shared
+// memory, then each face once, staged as Dual, differenced into the cell
+// accumulators.
 using TileTangent = TileSmall;
+
+// Dynamic shared memory of the tangent flux pass: Dual face fluxes
+// (NVAR x MAXF) and Dual cell slopes ((4 + NS) x MAXC).
+template <int NS>
+constexpr size_t tangent_smem_bytes() {
+  return sizeof(double2) * ((size_t)(7 + NS) * TileTangent::MAXF + (size_t)(4 + NS) * TileTangent::MAXC);
+}
 
 template <int NS, class EOS, int d, class Q>
 __device__ __forceinline__ void dir_pass_tangent(const DevBox& b, const RecAcc<Dual>& ra, const DevMech<NS>& m,
                                                  const DevFlags& f, const Geo& g, const int o[3], const int ext[3],
                                                  const long long stv[3], bool mine, int tx, int ty, int tz,
-                                                 Dual* fbuf, Dual* acc, Q& quo) {
+                                                 Dual* fbuf, Dual* sbuf, Dual* acc, Q& quo) {
   using TL = TileTangent;
   constexpr int NVAR = 7 + NS;
+  constexpr int NSL = 4 + NS;
   const bool diff = f.diffuse_vel || f.diffuse_temp || f.diffuse_spec || f.diffuse_enth;
+  const bool slopes = f.do_hydro && f.slopes;
+  // field q of the slopes of cell ci (tile plus one layer each side in d)
+  // at sbuf[q MAXC + ci]
+  const int ne0 = ext[0] + 2 * (d == 0), ne1 = ext[1] + 2 * (d == 1), ne2 = ext[2] + 2 * (d == 2);
+  if (slopes) {
+    const int ncells = ne0 * ne1 * ne2;
+    for (int ci = threadIdx.x; ci < ncells; ci += TL::NT) {
+      const int ex = ci % ne0, ey = (ci / ne0) % ne1, ez = ci / (ne0 * ne1);
+      const int i = o[0] + ex - (d == 0), j = o[1] + ey - (d == 1), k = o[2] + ez - (d == 2);
+      const long long c = (i - b.g2lo[0]) + (j - b.g2lo[1]) * stv[1] + (k - b.g2lo[2]) * stv[2];
+      Dual sl[NSL];
+      cell_slopes<NS, d>(ra, c, stv[d], sl, sl + 4, quo);
+#pragma unroll
+      for (int q = 0; q < NSL; ++q) sbuf[q * TL::MAXC + ci] = sl[q];
+    }
+    __syncthreads();
+  }
   const int nf0 = ext[0] + (d == 0), nf1 = ext[1] + (d == 1), nf2 = ext[2] + (d == 2);
   const int nfaces = nf0 * nf1 * nf2;
+  const int cstep = (d == 0) ? 1 : (d == 1) ? ne0 : ne0 * ne1;
   for (int fi = threadIdx.x; fi < nfaces; fi += TL::NT) {
     const int fx = fi % nf0, fy = (fi / nf0) % nf1, fz = fi / (nf0 * nf1);
     const int i = o[0] + fx, j = o[1] + fy, k = o[2] + fz;
     const long long cR = (i - b.g2lo[0]) + (j - b.g2lo[1]) * stv[1] + (k - b.g2lo[2]) * stv[2];
     Dual F[NVAR];
     if (f.do_hydro) {
-      hydro_face<NS, EOS, d>(ra, m, f, cR, stv[d], g.area[d], F, quo);
+      Dual sL[NSL], sR[NSL];
+      if (slopes) {
+        const int ciL = fx + ne0 * (fy + ne1 * fz);  // the low cell's slot; the high cell is one step on
+#pragma unroll
+        for (int q = 0; q < NSL; ++q) {
+          sL[q] = sbuf[q * TL::MAXC + ciL];
+          sR[q] = sbuf[q * TL::MAXC + ciL + cstep];
+        }
+      } else {
+#pragma unroll
+        for (int q = 0; q < NSL; ++q) sL[q] = sR[q] = Dual(0.0);
+      }
+      hydro_face_sl<NS, EOS, d>(ra, m, f, cR, stv[d], g.area[d], sL, sL + 4, sR, sR + 4, F, quo);
     } else {
 #pragma unroll
       for (int n = 0; n < NVAR; ++n) F[n] = Dual(0.0);
@@ -174,8 +214,9 @@ __global__ void __launch_bounds__(TileTangent::NT)
   constexpr int NVAR = 7 + NS;
   if (kExact && __ldcg(&counters[kCounterSlowFlux]) == 0ull) return;
   Quot<kExact> quo;
-  __shared__ double2 fbuf_raw[NVAR * TL::MAXF];  // Dual has a constructor: raw storage
-  Dual* fbuf = reinterpret_cast<Dual*>(fbuf_raw);
+  extern __shared__ double2 tan_smem_raw[];  // Dual has a constructor: raw storage
+  Dual* fbuf = reinterpret_cast<Dual*>(tan_smem_raw);
+  Dual* sbuf = fbuf + NVAR * TL::MAXF;
   const int4 t = tiles[blockIdx.x];
   const DevBox& b = boxes[t.x];
   const TanBox& tb = tans[t.x];
@@ -188,9 +229,9 @@ __global__ void __launch_bounds__(TileTangent::NT)
   Dual acc[NVAR];
 #pragma unroll
   for (int n = 0; n < NVAR; ++n) acc[n] = Dual(0.0);
-  dir_pass_tangent<NS, EOS, 0>(b, ra, m, f, g, o, ext, stv, mine, tx, ty, tz, fbuf, acc, quo);
-  dir_pass_tangent<NS, EOS, 1>(b, ra, m, f, g, o, ext, stv, mine, tx, ty, tz, fbuf, acc, quo);
-  dir_pass_tangent<NS, EOS, 2>(b, ra, m, f, g, o, ext, stv, mine, tx, ty, tz, fbuf, acc, quo);
+  dir_pass_tangent<NS, EOS, 0>(b, ra, m, f, g, o, ext, stv, mine, tx, ty, tz, fbuf, sbuf, acc, quo);
+  dir_pass_tangent<NS, EOS, 1>(b, ra, m, f, g, o, ext, stv, mine, tx, ty, tz, fbuf, sbuf, acc, quo);
+  dir_pass_tangent<NS, EOS, 2>(b, ra, m, f, g, o, ext, stv, mine, tx, ty, tz, fbuf, sbuf, acc, quo);
   if (mine) {
     const int i = o[0] + tx, j = o[1] + ty, k = o[2] + tz;
     double* r = b.R + (i - b.rb[0]) + (long long)(j - b.rb[1]) * b.rj + (long long)(k - b.rb[2]) * b.rk;
