@@ -70,17 +70,26 @@ __host__ MechF<NS> to_float(const DevMech<NS>& m, double p_ref) {
   return f;
 }
 
-// FP64 mole fractions, then the FP64 temperature, stored after the FP32
-// fields of a mixed record.  Both enter the diffusion fluxes only through
-// differences between neighbouring cells, which FP32 values would resolve
-// to no better than 1e-4 K / 1e-7 (the flame's second differences of T are
-// a few K per cell).  They start at the first 8-byte boundary after the
-// Rec<NS>::N FP32 fields of every cell (N ncell floats may be odd).
+// FP64 fields stored after the FP32 fields of a mixed record, for the cells
+// whose faces the pass evaluates (the valid cells and one layer around
+// them): the mole fractions X_k (NS), the temperature, the density and the
+// mass fractions Y_k (NS), field n of cell c at [n N + c].  X and T enter the
+// diffusion fluxes only through differences between neighbouring cells,
+// which FP32 values would resolve to no better than 1e-4 K / 1e-7 (the
+// flame's second differences of T are a few K per cell).  rho and Y are the
+// base of the Godunov state's FP64 density and composition (energy fluxes,
+// hydro_face_f).  The fields start at the first 8-byte boundary after the
+// Rec<NS>::N FP32 fields of every cell (N ncell floats may be odd); with
+// 2 NS + 2 of them a mixed record stays within the FP64 record's size.
 template <int NS>
 __device__ __forceinline__ double* mixed_x(const DevBox& b) {
   const long long nf = ((long long)Rec<NS>::N * b.ncell + 1) & ~1LL;
   return reinterpret_cast<double*>(reinterpret_cast<float*>(b.rec) + nf);
 }
+// field index of the density in the FP64 part; Y_k follow it
+template <int NS>
+constexpr int kMixedRho = NS + 1;
+static_assert(2 * 9 + 2 <= Rec<9>::N / 2 && 2 * 1 + 2 <= Rec<1>::N / 2, "mixed record exceeds the FP64 record");
 
 // Reference velocity of a box: the velocity of its first valid cell (lo
 // corner), in FP64 (0 where that is not finite).  The FP32 records hold the
@@ -302,6 +311,9 @@ __global__ void __launch_bounds__(kCellThreads)
         X[n] = (float)x;
       }
       xr[NS * N] = T;
+      xr[kMixedRho<NS> * N] = rho;
+#pragma unroll
+      for (int n = 0; n < NS; ++n) xr[(kMixedRho<NS> + 1 + n) * N] = Y[n];
       float out[NS + 3];
       TransF<NS, SIMPLE>::eval(mf, Tf, rhof, pf, Yf, X, out);
       r[RC::T * N] = Tf;
@@ -318,18 +330,24 @@ __global__ void __launch_bounds__(kCellThreads)
 }
 
 // FP32 hyperbolic face flux (not area-scaled); normal momentum without p_ref.
-// Internal energy at (rho, Y, p) in FP64 (RYP2E), from FP32 inputs.
+// Internal energy at (rho, Y, p) in FP64 (RYP2E).
+template <int NS, bool MIX>
+__device__ __forceinline__ double e_rpY64(const DevMech<NS>& md, const double* Y, double rho, double p) {
+  const double rw = mix_rw<NS>(md, Y);
+  if constexpr (MIX)
+    return IdealMixEos<NS>::e_rp(md, Y, rw, rho, p);
+  else
+    return GammaLawEos<NS>::e_rp(md, Y, rw, rho, p);
+}
+
+// The same from FP32 species densities rho Y_k and density rho.
 template <int NS, bool MIX>
 __device__ __forceinline__ double e_rp_fp64(const DevMech<NS>& md, const float* rY, float rho, double p) {
   const double r = (double)rho, ir = 1.0 / r;
   double Y[NS];
 #pragma unroll
   for (int n = 0; n < NS; ++n) Y[n] = (double)rY[n] * ir;
-  const double rw = mix_rw<NS>(md, Y);
-  if constexpr (MIX)
-    return IdealMixEos<NS>::e_rp(md, Y, rw, r, p);
-  else
-    return GammaLawEos<NS>::e_rp(md, Y, rw, r, p);
+  return e_rpY64<NS, MIX>(md, Y, r, p);
 }
 
 // FP64 internal energy from FP32 mass fractions Y (for Lax-Friedrichs sides).
@@ -401,6 +419,9 @@ __device__ __forceinline__ void hydro_face_f(const DevBox& b, const MechF<NS>& m
   const float ut1r = t1R - 0.5f * dqR[2];
   const float ut2r = t2R - 0.5f * dqR[3];
   float spl[NS], spr[NS];
+  // increments of the face species densities over the cell's: rho Y_k + h_k
+  float hL[NS], hR[NS];
+  float HL = 0.f, HR = 0.f;
   float rl = 0.f, rr = 0.f;
   {
     const float sL = (dqL[0] + dqL[1]) * icL, sR = (dqR[0] + dqR[1]) * icR;
@@ -414,8 +435,12 @@ __device__ __forceinline__ void hydro_face_f(const DevBox& b, const MechF<NS>& m
         dsL = mc_limitf(ryL - rLL * yLL - yL * dpl * icL2, ryR - ryL - yL * dpc * icL2);
         dsR = mc_limitf(ryR - ryL - yR * dpc * icR2, rRR * yRR - ryR - yR * dpr * icR2);
       }
-      spl[n] = yL * rL + 0.5f * (dsL + yL * sL);
-      spr[n] = yR * rR - 0.5f * (dsR + yR * sR);
+      hL[n] = 0.5f * (dsL + yL * sL);
+      hR[n] = -(0.5f * (dsR + yR * sR));
+      HL += hL[n];
+      HR += hR[n];
+      spl[n] = yL * rL + hL[n];
+      spr[n] = yR * rR + hR[n];
       rl += spl[n];
       rr += spr[n];
     }
@@ -467,9 +492,12 @@ __device__ __forceinline__ void hydro_face_f(const DevBox& b, const MechF<NS>& m
     const float drho = (pstar - po) / (co * co);
     float rspstar[NS];
     float rstar = 0.f;
+    bool clamped = false;
 #pragma unroll
     for (int n = 0; n < NS; ++n) {
-      rspstar[n] = fmaxf(0.f, rspo[n] + drho * Yt[n]);
+      const float v = rspo[n] + drho * Yt[n];
+      clamped |= !(v >= 0.f);
+      rspstar[n] = fmaxf(0.f, v);
       rstar += rspstar[n];
     }
     {
@@ -509,7 +537,31 @@ __device__ __forceinline__ void hydro_face_f(const DevBox& b, const MechF<NS>& m
       rgd += g;
     }
     const double gdpa = (double)gdp + (double)pref;
-    const double regd = (double)rgd * e_rp_fp64<NS, MIX>(md, flY, rgd, gdpa);
+    double regd;
+    if (!m0 && !clamped) {
+      // The Godunov state has the upwind face's composition, and its density
+      // is the upwind face's plus w drho (w: the star state's share).  Both
+      // are formed in FP64 as the upwind cell's FP64 values plus the FP32
+      // increments (slopes, star jump), so the FP32 rounding falls on the
+      // increments only: rho e carries the formation energies, which turn a
+      // 6e-8 rounding of Y_k or of rho into far more than rho e varies by
+      // across the flame.
+      const long long cu = mask ? cL : cR;
+      const double* xr = mixed_x<NS>(b) + cu;
+      const float w = min_ ? 1.f : (mout ? 0.f : frac);
+      const float H = mask ? HL : HR, irf = mask ? 1.f / rl : 1.f / rr;
+      const double rg = __ldg(xr + kMixedRho<NS> * N) + (double)(H + w * drho);
+      double Yg[NS];
+#pragma unroll
+      for (int n = 0; n < NS; ++n) {
+        const double y = __ldg(xr + (kMixedRho<NS> + 1 + n) * N);
+        const float h = mask ? hL[n] : hR[n];
+        Yg[n] = y + (double)((h - (float)y * H) * irf);
+      }
+      regd = rg * e_rpY64<NS, MIX>(md, Yg, rg, gdpa);
+    } else {
+      regd = (double)rgd * e_rp_fp64<NS, MIX>(md, flY, rgd, gdpa);
+    }
     const float iua = iu + Unf, iv1a = iv1 + Ut1f, iv2a = iv2 + Ut2f;  // absolute velocities
     fl_rho = rgd * iua;
 #pragma unroll

@@ -15,11 +15,6 @@ from pelec_gb300 import abi, problems
 pytestmark = pytest.mark.gpu
 
 MIXED_L2 = 1e-5
-# The energy equations (rho E, rho e) carry the formation energy of the
-# mixture (~-2e6 erg/cm^3) at w = 100 cm/s through a far field whose RHS is
-# driven only by 1 cm/s transverse noise; FP32 rounding of the reconstructed
-# density and velocity (~6e-8) bounds their error near 1.5e-5.
-UEINT_L2 = 3e-5
 # Lax-Friedrichs adds |u|+c times the jump of the FP32 face states to every
 # flux, which amplifies their rounding by c/|u| ~ 1e3 in the energy equations.
 LAXF_L2 = 3e-4
@@ -27,8 +22,6 @@ LAXF_L2 = 3e-4
 
 def _tol(case=None):
     tol = np.full(16, MIXED_L2)
-    tol[abi.UEINT] = UEINT_L2
-    tol[abi.UEDEN] = UEINT_L2
     if case == "laxf":
         tol[:] = LAXF_L2
     return tol
