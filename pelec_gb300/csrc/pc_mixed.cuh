@@ -22,7 +22,8 @@
 // in FP32, and whose second differences (the conduction term of the energy
 // RHS) are ~1e-3 of T; the differences are taken in FP64 and rounded to FP32.  The internal energy of the Godunov
 // state is evaluated in FP64 (its formation-energy terms cancel to ~1e-2 of
-// their size, which FP32 cannot carry).
+// their size, which FP32 cannot carry), at an FP64 density and composition:
+// the upwind cell's FP64 values plus FP32 increments (hydro_face_f).
 #pragma once
 
 #include "pc_kernels.cuh"
