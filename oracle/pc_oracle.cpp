@@ -1,7 +1,8 @@
 // pc_oracle.cpp — ORACLE (test infrastructure): extern "C" entry points of the
 // CPU restatement in pc_oracle.hpp, loaded by oracle/pyoracle.py through
 // ctypes.  Only tests/, the smoke check and bench.py's CPU-baseline leg call
-// these.  Parity status: UNPINNED (see pc_oracle.hpp).
+// these.  Parity status: see pc_oracle.hpp (pinned to the reference's own
+// hot-path code; the PelePhysics parts unpinned).
 #include "pc_oracle.hpp"
 
 #include <omp.h>

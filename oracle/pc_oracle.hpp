@@ -13,13 +13,17 @@
 // Only tests/, the package smoke check and bench.py's CPU-baseline leg use
 // this code, as the checker and as the timed CPU baseline.
 //
-// Parity status: UNPINNED.  The reference cannot be compiled here (its
-// PelePhysics/AMReX submodules are absent) and ships no RHS-level golden
-// vectors.  The EOS (GammaLaw, NASA-7 ideal mixture) and the transport
-// (Constant, mixture-averaged "Simple") that PelePhysics supplies are
-// restated from their published physics; the species tables are the
-// caller's (pc_mechanism).  What the reference does pin (conservation,
-// symmetry, single-species zero diffusion) is checked by the tests.
+// Parity status: PINNED for everything that lives in the reference tree.
+// oracle/ref_build.py compiles the reference's own hot-path sources where
+// they lie (MOL.cpp, Riemann.H, Diffterm.H, Utilities.H, TransCoeff.H,
+// Timestep.H) against stand-ins for the absent AMReX and PelePhysics
+// headers, and tests/test_ref_pinned.py checks that this restatement gives
+// the same bits on every output (full C1 and C2 boxes, the flag matrix,
+// face fluxes, single faces and cells, computeTemp, estTimeStep).
+// UNPINNED: what PelePhysics supplies — the EOS (GammaLaw, NASA-7 ideal
+// mixture) and the transport (Constant, mixture-averaged "Simple") are
+// restated from their published physics, and the species tables are the
+// caller's (pc_mechanism); the reference build runs these same restatements.
 //
 // The transport's exp and log are pc_exp.h's (pelec_gb300/csrc), the
 // table-driven functions the kernels call too, instead of the host libm's:
@@ -836,10 +840,13 @@ inline void mol_rhs_box(const pc_mol_config& cfg, const EOS& eos, const TRANS& t
     });
   }
   if (cfg.do_hydro) hyp_mol_flux<NS>(cbox, qar, qauxar, flx, area, cfg.plm_iorder, cfg.use_laxf_flux != 0, eos);
+  // pc_flux_div (Diffterm.H:463-484): AMREX_D_TERM pastes the three
+  // differences into one expression, -(fx1 - fx0 + fy1 - fy0 + fz1 - fz0) / V,
+  // which C++ evaluates left to right.
   for_box(cbox, [&](int i, int j, int k) {
     for (int n = 0; n < NVAR; ++n)
-      Dterm(i, j, k, n) = -((flx[0](i + 1, j, k, n) - flx[0](i, j, k, n)) + (flx[1](i, j + 1, k, n) - flx[1](i, j, k, n)) +
-                            (flx[2](i, j, k + 1, n) - flx[2](i, j, k, n))) /
+      Dterm(i, j, k, n) = -(flx[0](i + 1, j, k, n) - flx[0](i, j, k, n) + flx[1](i, j + 1, k, n) - flx[1](i, j, k, n) +
+                            flx[2](i, j, k + 1, n) - flx[2](i, j, k, n)) /
                           vol;
   });
   for_box(vbox, [&](int i, int j, int k) {

@@ -5,8 +5,9 @@ ctypes front end of the CPU restatement in ``pc_oracle.hpp`` (compiled to
 tests/, by ``__graft_entry__.smoke()`` and by bench.py's CPU-baseline leg, as
 the checker and as the timed CPU baseline; the product never imports it.
 
-Parity status: UNPINNED (the reference cannot be built in this environment
-and ships no RHS-level golden vectors; see pc_oracle.hpp).
+Parity status: pinned bit for bit to the reference's own hot-path code
+(oracle/refharness.py, tests/test_ref_pinned.py); the EOS, transport and
+mechanism data PelePhysics would supply stay unpinned (see pc_oracle.hpp).
 """
 from __future__ import annotations
 

@@ -732,10 +732,15 @@ __device__ __forceinline__ void dir_pass(const DevBox& b, const DevMech<NS>& m, 
     }
   }
   if (mine) {
+    // pc_flux_div (Diffterm.H:475-481) sums fx1 - fx0 + fy1 - fy0 + fz1 - fz0
+    // left to right (AMREX_D_TERM pastes the three differences into one
+    // expression); acc holds that running sum, negated and divided at the end.
     const int flo = tx + nf0 * (ty + nf1 * tz);
     const int fhi = flo + ((d == 0) ? 1 : (d == 1) ? nf0 : nf0 * nf1);
 #pragma unroll
-    for (int n = 0; n < NVAR; ++n) acc[n] += fbuf[n * TL::MAXF + flo] - fbuf[n * TL::MAXF + fhi];
+    for (int n = 0; n < NVAR; ++n)
+      acc[n] = d == 0 ? fbuf[n * TL::MAXF + fhi] - fbuf[n * TL::MAXF + flo]
+                      : acc[n] + fbuf[n * TL::MAXF + fhi] - fbuf[n * TL::MAXF + flo];
   }
   __syncthreads();
 }
@@ -814,7 +819,7 @@ __global__ void __launch_bounds__(TL::NT, TL::MINB)
       double* r = b.R + (i - b.rb[0]) + (long long)(j - b.rb[1]) * b.rj + (long long)(k - b.rb[2]) * b.rk;
 #pragma unroll
       for (int n = 0; n < NVAR; ++n) {
-        const double v = quo(acc[n], g.vol, g.ivol);  // = acc[n] / vol, correctly rounded
+        const double v = quo(-acc[n], g.vol, g.ivol);  // = -acc[n] / vol, correctly rounded
         bad |= !isfinite(v);
         r[n * b.rn] = v;
       }

@@ -200,7 +200,9 @@ __device__ __forceinline__ void dir_pass_tangent(const DevBox& b, const RecAcc<D
     const int flo = tx + nf0 * (ty + nf1 * tz);
     const int fhi = flo + ((d == 0) ? 1 : (d == 1) ? nf0 : nf0 * nf1);
 #pragma unroll
-    for (int n = 0; n < NVAR; ++n) acc[n] += fbuf[n * TL::MAXF + flo] - fbuf[n * TL::MAXF + fhi];
+    for (int n = 0; n < NVAR; ++n)  // the forward's summation order (pc_kernels.cuh dir_pass)
+      acc[n] = d == 0 ? fbuf[n * TL::MAXF + fhi] - fbuf[n * TL::MAXF + flo]
+                      : acc[n] + fbuf[n * TL::MAXF + fhi] - fbuf[n * TL::MAXF + flo];
   }
   __syncthreads();
 }
@@ -238,7 +240,7 @@ __global__ void __launch_bounds__(TileTangent::NT)
     double* rd = tb.Rd + (i - tb.rb[0]) + (long long)(j - tb.rb[1]) * tb.rj + (long long)(k - tb.rb[2]) * tb.rk;
 #pragma unroll
     for (int n = 0; n < NVAR; ++n) {
-      const Dual v = acc[n] / g.vol;
+      const Dual v = -acc[n] / g.vol;
       r[n * b.rn] = v.v;
       rd[n * tb.rn] = v.d;
     }

@@ -43,3 +43,16 @@ def rel_maxnorm(a, b):
         num = np.abs(a[n] - b[n]).max()
         out.append(0.0 if num == 0 else (num / den if den > 0 else float("inf")))
     return np.array(out)
+
+
+def divergence_scale(F, vol):
+    """Per component, the sum over cells of |each face-flux term| / V that
+    enters the divergence (each face feeds two cells): the scale against
+    which the round-off of a domain total of the RHS is measured.  The
+    reference sums the six face terms left to right (Diffterm.H:475-481),
+    so the total of a periodic RHS is exact only to round-off of the large
+    uniform terms (the pressure in the momentum fluxes), not of the RHS."""
+    import numpy as np
+
+    return np.array([2.0 * sum(np.abs(np.asarray(F[d][n])).sum() for d in range(3)) / vol
+                     for n in range(np.asarray(F[0]).shape[0])])

@@ -21,6 +21,7 @@ results across launch configurations.
 import numpy as np
 import pytest
 
+from conftest import divergence_scale
 from gpu_util import gpu_rhs, to_multifab
 from pelec_gb300 import abi, problems
 
@@ -141,9 +142,13 @@ def test_every_launch_configuration_identical(cuda_lib):
 def test_periodic_flame_conservation(cuda_lib):
     mech, st, _ = problems.flame((32, 32, 32), seed=9)
     problems.fill_ghosts(st.S, 4, ("periodic",) * 3)
-    (gpu,), _ = gpu_rhs(cuda_lib, problems.make_config(mech, precision=RCP), [st])
+    op = cuda_lib.MOLOperator(problems.make_config(mech, precision=RCP))
+    R = cuda_lib.MultiFab([(st.lo, st.hi)], st.S.shape[0], 0)
+    F, = op.rhs_level_fluxes(to_multifab(cuda_lib, [st], st.ng), R, st.dx)
+    gpu = R.fabs[0].cpu().numpy()
+    scale = divergence_scale([f.cpu().numpy() for f in F], st.dx[0] * st.dx[1] * st.dx[2])
     for n in [abi.URHO, abi.UMX, abi.UMY, abi.UMZ, abi.UEDEN] + [abi.UFS + k for k in range(9)]:
-        assert abs(gpu[n].sum()) <= 1e-12 * np.abs(gpu[n]).sum(), n
+        assert abs(gpu[n].sum()) <= 1e-15 * scale[n], n
 
 
 def test_face_flux_export(cuda_lib, oracle_lib):

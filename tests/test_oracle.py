@@ -1,19 +1,21 @@
 """CPU tests of the oracle (the CPU restatement of getMOLSrcTerm).
 
-The reference ships no RHS-level golden vectors (parity unpinned), so the
-oracle is pinned by what the reference's own tests and physics do pin:
-conservation of mass/momentum/energy on periodic domains (the intent of
-Tests/test_masscons.py:20-28, rtol 1e-13), a uniform state giving a zero RHS,
-axis-permutation symmetry, zero species diffusion for one species,
-second-order convergence (Tests/CMakeLists.txt:134-173), the Riemann solver's
-exact Euler flux for equal states, and committed golden fixtures that freeze
-the oracle against regressions.
+The oracle is pinned bit for bit to PeleC's own hot-path code compiled from
+the reference tree (tests/test_ref_pinned.py) and to golden fixtures that
+code computed (tests/golden/).  The tests here add what the reference's own
+tests and physics pin: conservation of mass/momentum/energy on periodic
+domains (the intent of Tests/test_masscons.py:20-28, rtol 1e-13), a uniform
+state giving a zero RHS, axis-permutation symmetry, zero species diffusion
+for one species, second-order convergence (Tests/CMakeLists.txt:134-173),
+the Riemann solver's exact Euler flux for equal states, and Newton recovery
+of T.
 """
 import os
 
 import numpy as np
 import pytest
 
+from conftest import divergence_scale
 from pelec_gb300 import abi, mechanism, problems
 
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
@@ -47,10 +49,10 @@ def test_uniform_state_gives_zero_rhs(oracle_lib, which):
 
 def test_tgv_periodic_conservation(oracle_lib):
     mech, st = problems.tgv(16, seed=3)
-    R, = oracle_lib.mol_rhs(problems.make_config(mech), [st])
+    (R, F), = oracle_lib.mol_rhs_fluxes(problems.make_config(mech), [st])
+    scale = divergence_scale(F, st.dx[0] * st.dx[1] * st.dx[2])
     for n in (abi.URHO, abi.UMX, abi.UMY, abi.UMZ, abi.UEDEN):
-        tot = np.abs(R[n]).sum()
-        assert abs(R[n].sum()) <= 1e-13 * tot, n
+        assert abs(R[n].sum()) <= 1e-15 * scale[n], n
     # Single species: rho*Y equation equals the continuity equation.
     assert np.array_equal(R[abi.UFS], R[abi.URHO])
     assert np.all(R[abi.UTEMP] == 0.0)
@@ -60,10 +62,10 @@ def test_flame_periodic_xy_conservation(oracle_lib):
     mech, st, _ = problems.flame((8, 8, 8), seed=2)
     # make z periodic too so every conserved total must vanish
     problems.fill_ghosts(st.S, 4, ("periodic",) * 3)
-    R, = oracle_lib.mol_rhs(problems.make_config(mech), [st])
+    (R, F), = oracle_lib.mol_rhs_fluxes(problems.make_config(mech), [st])
+    scale = divergence_scale(F, st.dx[0] * st.dx[1] * st.dx[2])
     for n in [abi.URHO, abi.UMX, abi.UMY, abi.UMZ, abi.UEDEN] + [abi.UFS + k for k in range(9)]:
-        tot = np.abs(R[n]).sum()
-        assert abs(R[n].sum()) <= 1e-12 * tot, n
+        assert abs(R[n].sum()) <= 1e-15 * scale[n], n
     # Species equations sum to the continuity equation (Sum rhoY_k = rho).
     assert np.allclose(R[abi.UFS:].sum(axis=0), R[abi.URHO], rtol=0, atol=1e-10 * np.abs(R[abi.URHO]).max())
 
@@ -146,19 +148,34 @@ def test_ctoprim_recovers_temperature(oracle_lib):
         assert np.isclose(q[5], rho * mechanism.RU / mech.wbar(Y) * T, rtol=1e-13)
 
 
-def test_golden_fixtures(oracle_lib):
-    """The oracle reproduces the committed fixtures bit for bit (its exp and
-    log are pc_exp.h's, not the host's libm, so no host changes a bit)."""
-    path = os.path.join(GOLDEN, "mol_rhs_golden.npz")
-    g = np.load(path)
-    for case in ("tgv8", "flame6"):
-        S = g[f"{case}_S"]
-        n = S.shape[-1] - 8
+def _golden_cases(g):
+    """(name, BoxState, config, expected RHS) of every RHS in the fixtures."""
+    from golden.make_golden import FLAME_FLAGS
+
+    out = []
+    for case, flag_sets in (("tgv8", {"": {}}), ("flame6", {"": {}, **FLAME_FLAGS}), ("flame576", {"": {}})):
+        S = np.ascontiguousarray(g[f"{case}_S"])
+        n = [S.shape[3] - 8, S.shape[2] - 8, S.shape[1] - 8]
         mech = mechanism.gamma_law_single() if case.startswith("tgv") else mechanism.h2_air_synthetic()
-        st = problems.BoxState(lo=(0, 0, 0), hi=(n - 1,) * 3, S=np.ascontiguousarray(S), dx=tuple(g[f"{case}_dx"]))
-        R, = oracle_lib.mol_rhs(problems.make_config(mech), [st])
-        ref = g[f"{case}_R"]
-        np.testing.assert_array_equal(R, ref, err_msg=case)
+        st = problems.BoxState(lo=(0, 0, 0), hi=tuple(v - 1 for v in n), S=S, dx=tuple(g[f"{case}_dx"]))
+        for name, flags in flag_sets.items():
+            key = f"{case}_{name}_R" if name else f"{case}_R"
+            out.append((key, st, problems.make_config(mech, **flags), g[key]))
+    return out
+
+
+def test_golden_fixtures(oracle_lib):
+    """The oracle reproduces, bit for bit, the fixtures that PeleC's own
+    hot-path code computed (tests/golden/make_golden.py): every flag case and
+    the exported face fluxes."""
+    g = np.load(os.path.join(GOLDEN, "mol_rhs_golden.npz"))
+    for key, st, cfg, ref in _golden_cases(g):
+        R, = oracle_lib.mol_rhs(cfg, [st])
+        np.testing.assert_array_equal(R, ref, err_msg=key)
+    key, st, cfg, _ = _golden_cases(g)[1]
+    (R, F), = oracle_lib.mol_rhs_fluxes(cfg, [st])
+    for d in range(3):
+        np.testing.assert_array_equal(F[d], g[f"flame6_F{d}"], err_msg=f"flux {d}")
 
 
 def test_generators_are_deterministic():
@@ -168,6 +185,8 @@ def test_generators_are_deterministic():
     np.testing.assert_allclose(st.S, g["tgv8_S"], rtol=1e-14, atol=0)
     _, st, _ = problems.flame((6, 6, 6), seed=12)
     np.testing.assert_allclose(st.S, g["flame6_S"], rtol=1e-14, atol=0)
+    _, st, _ = problems.flame((5, 7, 6), seed=13)
+    np.testing.assert_allclose(st.S, g["flame576_S"], rtol=1e-14, atol=0)
 
 
 def test_rhs_conditioning(oracle_lib):
@@ -221,18 +240,17 @@ def test_oracle_fill_ghosts_periodic_matches_generator(oracle_lib):
 
 def test_oracle_face_fluxes_difference_to_the_rhs(oracle_lib):
     """The oracle's exported face fluxes (refluxing data) difference to its
-    own RHS: RHS = -div(F) / V."""
+    own RHS: RHS = -div(F) / V, bit for bit."""
     mech, st, _ = problems.flame((8, 6, 10), seed=93)
     cfg = problems.make_config(mech)
     (R, F), = oracle_lib.mol_rhs_fluxes(cfg, [st])
     R2, = oracle_lib.mol_rhs(cfg, [st])
     np.testing.assert_array_equal(R, R2)
     fx, fy, fz = F
-    div = (fx[..., 1:] - fx[..., :-1]) + (fy[:, :, 1:] - fy[:, :, :-1]) + (fz[:, 1:] - fz[:, :-1])
-    vol = float(np.prod(st.dx))
-    scale = np.abs(R).max(axis=(1, 2, 3))
-    err = np.abs(-div / vol - R).max(axis=(1, 2, 3)) / np.where(scale > 0, scale, 1.0)
-    assert err.max() <= 1e-12, err
+    # pc_flux_div's order (Diffterm.H:475-481), elementwise in numpy: the same bits
+    div = fx[..., 1:] - fx[..., :-1] + fy[:, :, 1:] - fy[:, :, :-1] + fz[:, 1:] - fz[:, :-1]
+    vol = st.dx[0] * st.dx[1] * st.dx[2]
+    np.testing.assert_array_equal(-div / vol, R)
 
 
 def _ulp_err(got, x, fn):
