@@ -1,22 +1,26 @@
 """Benchmark of the MOL right-hand side (PeleC getMOLSrcTerm path) on GB300.
 
     python bench.py [--gpus N --steps K --warmup W] [--impl gb300|reference]
-                    [--workload c2|c1] [--precision fp64] [--no-level] [--no-adjoint]
-                    [--no-trajectory] [--no-cpu-baseline]
+                    [--workload c4|c2|c1] [--precision fp64] [--no-level] [--no-adjoint]
+                    [--no-trajectory] [--no-cpu-baseline] [--no-c2]
 
-One step = one full-level RHS evaluation of the workload (default C2: one
-128^3 box of the 9-species premixed flame, FP64).  The value is cell-RHS
+One step = one full-level RHS evaluation of the workload (default C4: one
+256^3 box of the 9-species premixed flame, FP64).  The value is cell-RHS
 evaluations per second over the K timed steps (device-resident inputs, CUDA
 events on the launch stream, barrier + synchronize on both sides, max over
 ranks).  ``e2e`` repeats the measurement through the public API with the
 state copied from pinned host memory and the RHS copied back every step
 (double-buffered: the copies of neighbouring steps overlap the kernels).
-Under torchrun each rank evaluates its own box (weak scaling, no data-path
-collective).  ``level_c3`` adds the batched-level measurement (400 uneven
-boxes: per-box launches vs one batched launch vs the autotuned tile shape vs
-a CUDA-graph replay, FP64 and mixed), outside the headline's timed region.
-``--impl reference`` times the CPU restatement of the reference path (the
-oracle) on the host cores with all threads.
+The mixed-precision form runs on the same box beside it, with its error
+against the FP64 result per component.  Under torchrun each rank evaluates
+its own box (weak scaling, no data-path collective).  ``c2`` repeats the
+FP64 and mixed measurements on the 128^3 box; ``level_c3`` adds the
+batched-level measurement (400 uneven boxes: per-box launches vs one batched
+launch vs the autotuned tile shape vs a CUDA-graph replay, FP64 and mixed);
+both run outside the headline's timed region.  ``--impl reference`` times
+the CPU restatement of the reference path (the oracle, pinned bit for bit to
+the reference's own code) on the host cores with all threads, each step one
+RHS of the same full box.
 """
 from __future__ import annotations
 
@@ -41,7 +45,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="c2", choices=["c2", "c1"])
+    ap.add_argument("--workload", default="c4", choices=["c4", "c2", "c1"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp64_rcp"],
                     help="FP64 form of the headline: fp64 (every quotient correctly rounded, the oracle's "
                          "arithmetic) or fp64_rcp (quotients by a shared divisor as products with its "
@@ -50,6 +54,7 @@ def parse():
     ap.add_argument("--no-level", action="store_true", help="skip the 400-box batched-level measurement")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint and trajectory-gradient measurement")
     ap.add_argument("--no-trajectory", action="store_true", help="skip the trajectory-gradient measurement only")
+    ap.add_argument("--no-c2", action="store_true", help="skip the 128^3 sub-line")
     return ap.parse_args()
 
 
@@ -67,9 +72,10 @@ def workload(name: str, seed: int = 1):
         mech, st = problems.tgv(64, seed=0)
         desc = "C1: Taylor-Green vortex 64^3 periodic, 1 species, GammaLaw, constant transport"
     else:
-        mech, st, _ = problems.flame((128, 128, 128), seed=seed)
-        desc = ("C2: premixed H2/air flame 128^3, dx=1e-3 cm, 9 species (synthetic NASA-7/transport table), "
-                "ideal-mixture EOS, mixture-averaged transport, periodic x/y, foextrap z")
+        n = 256 if name == "c4" else 128
+        mech, st, _ = problems.flame((n, n, n), seed=seed)
+        desc = ("%s: premixed H2/air flame %d^3, dx=1e-3 cm, 9 species (synthetic NASA-7/transport table), "
+                "ideal-mixture EOS, mixture-averaged transport, periodic x/y, foextrap z" % (name.upper(), n))
     return mech, st, desc
 
 
@@ -134,35 +140,71 @@ class ClockSampler:
         return {"sm_mhz": statistics.median(mhz), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(mhz)}
 
 
-def cpu_baseline(st, cfg, reps: int = 3) -> dict:
-    """The oracle (CPU restatement) on a z-slab of the same state, all threads."""
+def cpu_baseline(st, cfg, reps: int = 2) -> dict:
+    """The oracle (CPU restatement, pinned bit for bit to the reference's own
+    code) on the full box of the workload, all threads."""
     from oracle import pyoracle
 
-    nx, ny, nz = st.shape
-    kz = min(nz, 32)
-    k0 = st.lo[2] + (nz - kz) // 2
-    lo, hi = (st.lo[0], st.lo[1], k0), (st.hi[0], st.hi[1], k0 + kz - 1)
     threads = pyoracle.max_threads()
     times = []
     for _ in range(reps):
         t0 = time.perf_counter()
-        pyoracle.mol_rhs_sub(cfg, st.S, st.begin, lo, hi, st.dx, nthreads=threads)
+        pyoracle.mol_rhs_sub(cfg, st.S, st.begin, st.lo, st.hi, st.dx, nthreads=threads)
         times.append(time.perf_counter() - t0)
-    cells = nx * ny * kz
-    return {"value": cells / statistics.median(times), "unit": "cell-evals/s", "cores": threads, "kind": "port",
-            "sample": f"{nx}x{ny}x{kz} z-slab of the same state, median of {reps}, OpenMP {threads} threads",
+    nx, ny, nz = st.shape
+    return {"value": st.ncells / statistics.median(times), "unit": "cell-evals/s", "cores": threads, "kind": "port",
+            "sample": f"the full {nx}x{ny}x{nz} box of the workload, median of {reps}, OpenMP {threads} threads",
             "best_s": min(times), "median_s": statistics.median(times)}
 
 
-def profile_figures(workload_name: str, form: str = "fp64") -> dict:
-    """Figures from the committed ncu summary of this workload and FP64 form (or {})."""
-    path = os.path.join(ROOT, "profiles", f"dram_traffic_{workload_name}_{form}.txt")
+# Sources whose compiled code the FP64 traffic and instruction counts of a
+# profile describe; a profile records their hash, and a figure whose hash no
+# longer matches is reported as stale (null), not used.
+PROFILED_SOURCES = ("pelec_gb300/csrc/pc_kernels.cuh", "pelec_gb300/csrc/pc_device.cuh", "pelec_gb300/csrc/pc_exp.h",
+                    "pelec_gb300/csrc/pc_exp_tables.h", "pelec_gb300/csrc/pc_mol.cu", "pelec_gb300/csrc/pc_rhs_rcp.cu",
+                    "pelec_gb300/build.py", "include/pelec_mol.h")
+
+
+def kernel_source_hash() -> str:
+    import hashlib
+
+    h = hashlib.sha256()
+    for f in PROFILED_SOURCES:
+        h.update(f.encode())
+        h.update(open(os.path.join(ROOT, f), "rb").read())
+    return h.hexdigest()[:16]
+
+
+def profile_figures(workload_name: str, form: str, st) -> dict:
+    """Per-RHS figures of the committed ncu summary for this FP64 form:
+    profiles/dram_traffic_<workload>_<form>.txt when the workload itself was
+    captured, else the 128^3 (C2) capture scaled to this box by its count of
+    grow(valid, 2) cells, the cells whose records the passes write and read.
+    Returns {} when there is none, and the figures with stale=True when the
+    kernel sources changed after the capture."""
     out = {}
-    if os.path.exists(path):
-        for ln in open(path):
-            if ":" in ln and not ln.startswith("#"):
-                k, v = ln.split(":", 1)
-                out[k.strip()] = float(v)
+    for name in (workload_name, "c2"):
+        path = os.path.join(ROOT, "profiles", f"dram_traffic_{name}_{form}.txt")
+        if os.path.exists(path):
+            break
+    else:
+        return out
+    meta = {}
+    for ln in open(path):
+        if ":" in ln and not ln.startswith("#"):
+            k, v = (x.strip() for x in ln.split(":", 1))
+            try:
+                out[k] = float(v)
+            except ValueError:
+                meta[k] = v
+    nx, ny, nz = st.shape
+    cells2 = (nx + 4) * (ny + 4) * (nz + 4)
+    scale = cells2 / out.get("captured_grow2_cells", cells2)
+    for k in ("dram_bytes_per_rhs", "fp64_flops_per_rhs", "fp64_instructions_per_rhs"):
+        if k in out:
+            out[k] *= scale
+    out["source"] = os.path.relpath(path, ROOT) + ("" if scale == 1 else ", scaled by grow(valid,2) cells x%.4f" % scale)
+    out["stale"] = meta.get("source_sha256") != kernel_source_hash()
     return out
 
 
@@ -189,20 +231,21 @@ def launches_per_rhs(form: str) -> int:
 
 
 def fp64_roofline(prof: dict, ms_rhs: float, peaks: dict) -> dict:
-    """The roofline that binds: executed FP64 work of one RHS (ncu counters,
-    profiles/dram_traffic_c2_fp64.txt) over the two passes' time, against the
-    FP64 FMA rate measured in this run."""
+    """The roofline that binds: executed FP64 work of one RHS (ncu counters of
+    the committed profile, profile_figures) over the two passes' time, against
+    the FP64 FMA rate measured in this run."""
     flops, inst = prof.get("fp64_flops_per_rhs"), prof.get("fp64_instructions_per_rhs")
     peak = peaks.get("fp64_fma_tflops")
-    if not flops or not peak:
-        return {}
+    if not flops or not peak or prof.get("stale"):
+        return {"frac": None, "note": "no current FP64 counts for these kernel sources" if flops else "no profile"}
     achieved = flops / (ms_rhs * 1e-3) / 1e12
     # one FP64 instruction (DFMA, DADD or DMUL) per lane and issue: 2 flops at FMA peak
     issue = inst / (ms_rhs * 1e-3) / (peak * 1e12 / 2.0)
     return {"unit": "TFLOP/s", "achieved": achieved, "peak": peak, "frac": achieved / peak,
             "issue_frac": issue, "flops_per_rhs": flops, "instructions_per_rhs": inst,
             "peak_source": "FP64 FMA loop measured in this run (pc_peaks.cu)",
-            "counts_source": "ncu DFMA/DADD/DMUL thread-instruction counters of one RHS (a DFMA counts 2 flops)"}
+            "counts_source": "ncu DFMA/DADD/DMUL thread-instruction counters of one RHS (a DFMA counts 2 flops), "
+                             + prof.get("source", "")}
 
 
 def launch_name(t: int) -> str:
@@ -298,6 +341,48 @@ def bench_level(args, rank: int, local: int, maxover, barrier) -> dict:
         dt = time.perf_counter() - t0
         out["cpu_baseline"] = {"value": ncs / dt, "unit": "cell-evals/s", "cores": pyoracle.max_threads(),
                                "kind": "port", "sample": f"first 40 of the 400 boxes ({ncs} cells), one pass"}
+    del S, R
+    torch.cuda.empty_cache()
+    return out
+
+
+def bench_sub_box(args, name: str, rank: int, maxover, barrier) -> dict:
+    """FP64 and mixed RHS of another single-box workload (device-resident,
+    autotuned launch), with the mixed form's error against the FP64 result."""
+    import numpy as np
+    import torch
+
+    from pelec_gb300 import abi, mol, problems
+
+    mech, st, desc = workload(name, seed=1 + rank)
+    S = mol.MultiFab([(st.lo, st.hi)], st.S.shape[0], st.ng, fabs=[torch.from_numpy(st.S).cuda()])
+    R = mol.MultiFab(S.boxes, S.ncomp, 0)
+    stream = torch.cuda.current_stream()
+    out = {"workload": desc, "cells": st.ncells, "steps": args.steps, "unit": "cell-evals/s"}
+    res = {}
+    for prec, form in ((abi.PC_PRECISION_FP64, "fp64"), (abi.PC_PRECISION_MIXED, "mixed")):
+        op = mol.MOLOperator(problems.make_config(mech, time_passes=1, precision=prec))
+        best, _ = op.autotune(S, R, st.dx, reps=3)
+        for _ in range(max(3, args.warmup)):
+            op.rhs_level(S, R, st.dx)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        barrier()
+        e0.record(stream)
+        for _ in range(args.steps):
+            op.rhs_level(S, R, st.dx)
+        e1.record(stream)
+        barrier()
+        t = maxover(e0.elapsed_time(e1) / 1e3) / args.steps
+        op.rhs_level(S, R, st.dx)
+        torch.cuda.synchronize()
+        res[form] = R.fabs[0].cpu().numpy()
+        out[form] = {"value": st.ncells / t, "ms_per_step": 1e3 * t, "flux_launch": launch_name(best),
+                     "gpu_launches_per_step": launches_per_rhs(form)}
+        op.close()
+    a, b = res["mixed"], res["fp64"]
+    l2 = [float(np.sqrt(((a[n] - b[n]) ** 2).sum() / max((b[n] ** 2).sum(), 1e-300))) for n in range(b.shape[0])]
+    out["mixed"]["rel_l2_vs_fp64"] = {"max": max(l2), "per_component": l2}
+    out["mixed"]["speedup_vs_fp64"] = out["fp64"]["ms_per_step"] / out["mixed"]["ms_per_step"]
     del S, R
     torch.cuda.empty_cache()
     return out
@@ -501,8 +586,11 @@ def run_reference(args):
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "cell-evals/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": desc, "precision": "fp64", "implementation":
-                       "CPU restatement of getMOLSrcTerm (oracle/), the reference's own build is not compilable here"},
+            "config": {"workload": desc, "boxes_per_gpu": 1, "cells_per_gpu": st.ncells, "nspec": mech.nspec,
+                       "precision": "fp64", "implementation":
+                       "CPU restatement of getMOLSrcTerm (oracle/), pinned bit for bit to the reference's own "
+                       "hot-path code compiled from its sources (oracle/ref_build.py); the reference's full build "
+                       "(AMReX, PelePhysics, SUNDIALS) cannot be compiled here"},
             "cpu_baseline": cb,
             "e2e": {"value": value, "unit": "cell-evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
@@ -668,6 +756,10 @@ def run_gpu(args):
     mx = [float(np.abs(r32[n] - r64[n]).max() / max(np.abs(r64[n]).max(), 1e-300)) for n in range(r64.shape[0])]
     fs_m = [float(np.abs(r32[n] - r64[n]).max() / max(flux_scale[n], 1e-300)) for n in range(r64.shape[0])]
 
+    opm.close()
+    sub = None
+    if args.workload != "c2" and not args.no_c2:
+        sub = bench_sub_box(args, "c2", rank, maxover, barrier)
     level = None if args.no_level else bench_level(args, rank, local, maxover, barrier)
     adj = None if args.no_adjoint else bench_adjoint_rhs(args, st, mech, S, maxover, barrier)
     traj = None if (args.no_adjoint or args.no_trajectory or rank != 0) else bench_trajectory(args, rank)
@@ -685,8 +777,8 @@ def run_gpu(args):
         os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
     achieved = ab / (ms_rhs * 1e-3) / 1e9
-    prof = profile_figures(args.workload, args.precision)
-    traffic = prof.get("dram_bytes_per_rhs")
+    prof = profile_figures(args.workload, args.precision, st)
+    traffic = None if prof.get("stale", True) else prof.get("dram_bytes_per_rhs")
     peaks_fp = fp_peaks()
     line = {
         "metric": METRIC, "value": value, "unit": "cell-evals/s", "n_gpus": world, "steps": args.steps,
@@ -703,14 +795,16 @@ def run_gpu(args):
         "gpu_launches": launches_per_rhs(args.precision) * args.steps,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved / hbm_peak, "traffic": traffic,
+                     "traffic_source": (prof.get("source", "no profile") +
+                                        ("; STALE: the kernel sources changed after the capture"
+                                         if prof.get("stale") else "; kernel-source hash matches")),
                      "kernel": "cell_kernel + flux_kernel (one RHS)",
                      "alg_bytes_per_rhs": ab, "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)",
                      "binding_resource": "FP64 pipe",
                      "fp64": fp64_roofline(prof, ms_rhs, peaks_fp),
                      "fp64_pipe_active_pct": {"flux_kernel": prof.get("fp64_pipe_active_pct_flux_kernel"),
                                               "cell_kernel": prof.get("fp64_pipe_active_pct_cell_kernel"),
-                                              "source": "ncu, profiles/dram_traffic_%s_%s.txt" % (
-                                                  args.workload, args.precision)},
+                                              "source": "ncu, " + prof.get("source", "no profile")},
                      "fp_peaks": peaks_fp},
         "passes_ms": {"cell_kernel": ms_cell, "flux_kernel": ms_flux},
         other: {"value": world * cells * args.steps / t_oth, "unit": "cell-evals/s",
@@ -738,6 +832,8 @@ def run_gpu(args):
     }
     if cpu is not None:
         line["cpu_baseline"] = cpu
+    if sub is not None:
+        line["c2"] = sub
     if level is not None:
         line["level_c3"] = level
     if adj is not None:

@@ -378,9 +378,9 @@ int pc_mol_check_quotients(const double* a, const double* b, double* q, long lon
 
 /* Right-hand side of ONE box without allocating any device memory.  This
  * entry point has no counterpart in the reference: it exists for callers
- * that cannot call cudaMalloc while they run (code recording a CUDA stream
- * capture, code running under an external memory pool that forbids other
- * allocations, applications that reserve all device memory at start-up).
+ * that cannot call cudaMalloc while they run (code running under an external
+ * memory pool that forbids other allocations, applications that reserve all
+ * device memory at start-up).
  * There is no handle: cfg is read on every call.  The caller passes the box
  * (state with at least 2 ghost layers, output on the valid region) as for
  * pc_mol_rhs_level and gets the same result.  The per-cell scratch, launch
@@ -388,8 +388,9 @@ int pc_mol_check_quotients(const double* a, const double* b, double* q, long lon
  * reserves when the library is loaded and keeps until the process exits; a
  * box that does not fit (larger than about 46^3 valid cells with 9 species,
  * 67^3 with one) returns PC_ERR_TOO_LARGE before anything is launched.  The first call
- * on each device looks up that array's device address, so make that first
- * call outside any stream capture.  Every call reuses the same array: calls
+ * on each device does the one-time set-up — it looks up that array's device
+ * address and raises the flux kernels' shared-memory limit — so make that
+ * first call before any stream capture.  Every call reuses the same array: calls
  * whose work overlaps on the GPU (other streams, other host threads) race
  * and must be serialised by the caller.  Only PC_PRECISION_FP64 is
  * supported.  Asynchronous on stream; no diagnostic counters are returned. */

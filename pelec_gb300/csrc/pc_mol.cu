@@ -696,13 +696,15 @@ extern "C" int pc_mol_check_quotients(const double* a, const double* b, double* 
 // ---------------------------------------------------------------------------
 // Single-box right-hand side that allocates no device memory.
 //
-// For callers that cannot call cudaMalloc while they run: code inside a CUDA
-// stream capture, code driven by an external memory pool that forbids other
-// allocations, or an application that reserves all device memory up front.
-// The per-cell records, the launch lists and the diagnostic counters of one
-// box live in g_static_scratch, a fixed array that the CUDA runtime reserves
-// when this library is loaded and that every device holds until the process
-// exits.  The kernels are the ones pc_mol_rhs_level launches.
+// For callers that cannot call cudaMalloc while they run: code driven by an
+// external memory pool that forbids other allocations, or an application
+// that reserves all device memory up front.  The per-cell records, the
+// launch lists and the diagnostic counters of one box live in
+// g_static_scratch, a fixed array that the CUDA runtime reserves when this
+// library is loaded and that every device holds until the process exits.
+// The kernels are the ones pc_mol_rhs_level launches.  The first call on a
+// device does the one-time set-up (the array's device address, the flux
+// kernels' shared-memory opt-in); later calls make no such runtime call.
 // ---------------------------------------------------------------------------
 #include <mutex>
 

@@ -19,6 +19,15 @@ States are kept at every ``every``-th step (checkpoints); the reverse sweep
 recomputes each segment forward from its checkpoint, keeping that
 segment's stage states (A, B, C per step), and then runs the segment's
 adjoint steps backwards.  Memory: (N / every + 3 every) states.
+
+``tangent`` is the forward-mode counterpart: the directional derivative of
+J along an initial-state direction, carried through every step with the
+dual-number RHS (pc_mol_rhs_jvp), the fill and LinComb applied to the
+tangent, and the last computeTemp's transpose for T.  It takes the same
+derivative of every branch as the adjoint, so <dJ/dU0, v> and the tangent
+agree to round-off wherever the forward map is differentiable or not; a
+finite difference differs from both exactly where a limiter or switch is
+evaluated at its kink.
 """
 from __future__ import annotations
 
@@ -102,6 +111,53 @@ class Trajectory:
             v = t[abi.UTEMP, g:-g, g:-g, g:-g] if g else t[abi.UTEMP]
             tot += float(v.sum())
         return tot * self.vol
+
+    # ---- forward mode ----
+    def tangent(self, S0: "mol.MultiFab", dts, V0: "mol.MultiFab"):
+        """(J, dJ): the objective and its derivative along the initial-state
+        direction V0 (valid cells; its ghosts, UEINT and UTEMP entries do not
+        matter).  Per step, with the state S and its tangent V:
+            fill(S), fill(V);  R, Rd = JVP(S, V)
+            B = S + dt R,  Vb = V + dt Rd;  computeTemp(B)
+            fill(B), fill(Vb); R, Rd = JVP(B, Vb)
+            C = 0.5 B + 0.5 S + 0.5 dt R,  Vc = 0.5 Vb + 0.5 V + 0.5 dt Rd;  computeTemp(C)
+        The RHS reads UEINT not at all and UTEMP only as its Newton guess, so
+        the tangents of those two components (left as LinComb makes them) are
+        never used; the final T's tangent is the last computeTemp's transpose
+        applied to the cotangent of J, contracted with the last state's
+        tangent."""
+        op, R = self.op, self.R
+        dts = [float(v) for v in dts]
+        S_old, S_new = _clone(S0), _clone(S0)
+        V_old, V_new = _clone(V0), _zeros_like(V0)
+        Rd = _zeros_like(S0, 0)
+        for dt in dts:
+            op.fill_ghosts(S_old, self.geom)
+            op.fill_ghosts(V_old, self.geom)
+            op.rhs_jvp(S_old, V_old, R, Rd, self.dx)
+            op.lincomb(S_new, 1.0, S_old, dt, R)
+            op.lincomb(V_new, 1.0, V_old, dt, Rd)
+            op.compute_temp(S_new)
+            op.fill_ghosts(S_new, self.geom)
+            op.fill_ghosts(V_new, self.geom)
+            op.rhs_jvp(S_new, V_new, R, Rd, self.dx)
+            op.lincomb(S_new, 0.5, S_new, 0.5, S_old)
+            op.lincomb(S_new, 1.0, S_new, 0.5 * dt, R)
+            op.lincomb(V_new, 0.5, V_new, 0.5, V_old)
+            op.lincomb(V_new, 1.0, V_new, 0.5 * dt, Rd)
+            op.compute_temp(S_new)
+            S_old, S_new = S_new, S_old
+            V_old, V_new = V_new, V_old
+        J = self.objective(S_old)
+        g = self.ng
+        L = _zeros_like(S0)
+        for t in L.fabs:
+            t[abi.UTEMP, g:-g, g:-g, g:-g] = self.vol
+        op.compute_temp_adjoint(S_old, L)
+        dJ = 0.0
+        for lt, vt in zip(L.fabs, V_old.fabs):
+            dJ += float((lt[:, g:-g, g:-g, g:-g] * vt[:, g:-g, g:-g, g:-g]).sum())
+        return J, dJ
 
     # ---- reverse ----
     def _adjoint_step(self, A, B, C, dt: float, Lc: "mol.MultiFab", La: "mol.MultiFab", Lb, Tmp, Rb) -> None:

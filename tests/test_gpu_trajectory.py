@@ -1,7 +1,10 @@
 """GPU tests of the trajectory adjoint: the transposes of the ghost fill and
 of computeTemp, the checkpointed SSP-RK2 adjoint against finite differences
-of the GPU and oracle trajectories (J = sum of T dV at the last step), the
-inflow-parameter gradient, and the torch.autograd wrapper."""
+of the GPU and oracle trajectories (J = sum of T dV at the last step) and
+against the forward-mode tangent of the trajectory, the C5 configuration
+(64^3, 50 steps) against finite differences of the oracle's CPU trajectory
+(tests/golden/c5_fd.npz), the inflow-parameter gradient, and the
+torch.autograd wrapper."""
 import dataclasses
 
 import numpy as np
@@ -102,7 +105,21 @@ def _setup(mol, nsteps, every, shape=(16, 16, 16), params=None):
     return mech, st, fp, op, S0, tr
 
 
+def _direction(st, s):
+    """A state direction: component n of U0 scaled by s[n], valid cells only."""
+    import torch
+
+    v = torch.from_numpy(s[:, None, None, None] * st.S).cuda()
+    g = st.ng
+    for ax in (1, 2, 3):
+        v.narrow(ax, 0, g).zero_()
+        v.narrow(ax, v.shape[ax] - g, g).zero_()
+    return v
+
+
 def test_trajectory_gradient_matches_gpu_finite_differences(cuda_lib):
+    """<dJ/dU0, v> from the checkpointed adjoint against a central difference
+    (fixed h = 1e-6, a relative step of the state) of the GPU trajectory."""
     import torch
 
     mol = cuda_lib
@@ -111,25 +128,47 @@ def test_trajectory_gradient_matches_gpu_finite_differences(cuda_lib):
     J, L = tr.gradient(S0, dts, every=2)
     torch.cuda.synchronize()
     rng = np.random.default_rng(8)
-    g = 4
+    h = 1e-6
     for trial in range(3):
         s = rng.normal(size=st.S.shape[0])
         s[abi.UEINT] = s[abi.UTEMP] = 0.0
-        v = torch.from_numpy(s[:, None, None, None] * st.S).cuda()
-        v[:, :g] = 0
-        v[:, -g:] = 0
-        v[:, :, :g] = 0
-        v[:, :, -g:] = 0
-        v[:, :, :, :g] = 0
-        v[:, :, :, -g:] = 0
+        v = _direction(st, s)
         ad = float((L.fabs[0] * v).sum())
-        errs = {}
-        for h in (1e-6, 1e-7):
-            Jp = tr.objective(tr.run(mol.MultiFab(S0.boxes, S0.ncomp, 4, fabs=[S0.fabs[0] + h * v]), dts)[0])
-            Jm = tr.objective(tr.run(mol.MultiFab(S0.boxes, S0.ncomp, 4, fabs=[S0.fabs[0] - h * v]), dts)[0])
-            errs[h] = abs((Jp - Jm) / (2 * h) - ad) / abs(ad)
-        print("trajectory trial", trial, "dJ.v adjoint", ad, "rel err vs FD", errs)
-        assert min(errs.values()) <= GRAD_REL, errs
+        Jp = tr.objective(tr.run(mol.MultiFab(S0.boxes, S0.ncomp, 4, fabs=[S0.fabs[0] + h * v]), dts)[0])
+        Jm = tr.objective(tr.run(mol.MultiFab(S0.boxes, S0.ncomp, 4, fabs=[S0.fabs[0] - h * v]), dts)[0])
+        err = abs((Jp - Jm) / (2 * h) - ad) / abs(ad)
+        print("trajectory trial", trial, "dJ.v adjoint", ad, "rel err vs FD", err)
+        assert err <= GRAD_REL, err
+
+
+@pytest.mark.parametrize("w_noise", [1.0, 0.0])
+def test_trajectory_tangent_equals_adjoint(cuda_lib, w_noise):
+    """Forward mode through the whole trajectory (dual-number RHS, fill and
+    LinComb of the tangent, computeTemp's transpose for the final T) gives
+    the adjoint's <dJ/dU0, v> to round-off, with or without the limiter at
+    its kink (w_noise = 0: p and w uniform at t = 0)."""
+    import torch
+
+    from pelec_gb300 import trajectory
+
+    mol = cuda_lib
+    mech, st, fp = problems.flame((16, 12, 20), seed=71, w_noise=w_noise)
+    op = mol.MOLOperator(problems.make_config(mech))
+    S0 = to_multifab(mol, [st], 4)
+    tr = trajectory.Trajectory(op, S0, _geom(st), st.dx)
+    dts = tr.dt_sequence(S0, 5, 0.3)
+    J, L = tr.gradient(S0, dts, every=2)
+    rng = np.random.default_rng(81)
+    for trial in range(3):
+        s = rng.normal(size=st.S.shape[0])
+        s[abi.UEINT] = s[abi.UTEMP] = 0.0
+        v = _direction(st, s)
+        ad = float((L.fabs[0] * v).sum())
+        J2, tan = tr.tangent(S0, dts, mol.MultiFab(S0.boxes, S0.ncomp, 4, fabs=[v]))
+        torch.cuda.synchronize()
+        print("w_noise", w_noise, "trial", trial, "adjoint", ad, "tangent", tan)
+        assert J2 == J
+        assert abs(tan - ad) <= 1e-11 * abs(ad), (tan, ad)
 
 
 def test_checkpoint_interval_does_not_change_the_gradient(cuda_lib):
@@ -186,7 +225,9 @@ def test_trajectory_gradient_matches_oracle_finite_differences(cuda_lib, oracle_
 def test_inflow_parameter_gradient(cuda_lib):
     """dJ/da for the amplitudes of the first three wrinkle modes: the
     adjoint gradient contracted with dU0/da (central differences of the
-    initial-condition generator) against FD of J in a."""
+    smooth initial-condition generator) against a Richardson-extrapolated
+    central difference of J in a (steps h and 2h, h = 1e-7 cm: far above the
+    rounding of J, and with an h^4 truncation error)."""
     import torch
 
     mol = cuda_lib
@@ -199,25 +240,22 @@ def test_inflow_parameter_gradient(cuda_lib):
         p = dataclasses.replace(fp, amps=np.asarray(amps, float))
         return _flame((12, 12, 16), params=p)[1].S
 
+    def Ja(m, step):
+        amps = fp.amps.copy()
+        amps[m] += step
+        S = mol.MultiFab(S0.boxes, S0.ncomp, 4, fabs=[torch.from_numpy(U0(amps)).cuda()])
+        return tr.objective(tr.run(S, dts)[0])
+
+    h = 1e-7
     for m in range(3):
         ha = 1e-3 * max(fp.amps[m], 1e-6)
-        a_p, a_m = fp.amps.copy(), fp.amps.copy()
-        a_p[m] += ha
-        a_m[m] -= ha
-        dU = (U0(a_p) - U0(a_m)) / (2 * ha)
+        dU = (U0(fp.amps + ha * (np.arange(8) == m)) - U0(fp.amps - ha * (np.arange(8) == m))) / (2 * ha)
         ad = float((lam * dU).sum())
-
-        def Ja(amps):
-            S = mol.MultiFab(S0.boxes, S0.ncomp, 4, fabs=[torch.from_numpy(U0(amps)).cuda()])
-            return tr.objective(tr.run(S, dts)[0])
-
-        h = 1e-6 * fp.amps[m]
-        a_p, a_m = fp.amps.copy(), fp.amps.copy()
-        a_p[m] += h
-        a_m[m] -= h
-        fd = (Ja(a_p) - Ja(a_m)) / (2 * h)
-        print("mode", m, "dJ/da adjoint", ad, "FD", fd, "rel", abs(fd - ad) / abs(ad))
-        assert abs(fd - ad) <= 1e-5 * abs(ad)
+        d1 = (Ja(m, h) - Ja(m, -h)) / (2 * h)
+        d2 = (Ja(m, 2 * h) - Ja(m, -2 * h)) / (4 * h)
+        fd = (4 * d1 - d2) / 3
+        print("mode", m, "dJ/da adjoint", ad, "FD", d1, "Richardson", fd, "rel", abs(fd - ad) / abs(ad))
+        assert abs(fd - ad) <= GRAD_REL * abs(ad)
 
 
 def test_autograd_wrapper_backward_is_the_adjoint(cuda_lib):
@@ -241,3 +279,100 @@ def test_autograd_wrapper_backward_is_the_adjoint(cuda_lib):
     err = float((S.grad - ref).abs().max() / ref.abs().max())
     assert err <= 1e-13, err
     assert float(S.grad[:, :2].abs().sum()) == 0.0  # outside grow(valid, 2)
+
+
+def _c5_fixture():
+    import os
+
+    path = os.path.join(os.path.dirname(__file__), "golden", "c5_fd.npz")
+    if not os.path.exists(path):
+        pytest.skip("tests/golden/c5_fd.npz not generated (tests/golden/make_c5_fd.py)")
+    return np.load(path)
+
+
+@pytest.mark.parametrize("tag", ["wnoise", "config"])
+def test_c5_gradient_against_oracle_trajectory_fd(cuda_lib, tag):
+    """C5 (64^3 flame, 9 species, FP64, 50 SSP-RK2 steps at CFL 0.3, J = sum
+    of T dV, checkpoint every 5): the adjoint dJ/dU0 on the 20 seeded state
+    directions of tests/golden/make_c5_fd.py against central differences of
+    the ORACLE's CPU trajectory (h = 1e-6 relative), and against the
+    forward-mode tangent of the GPU trajectory.
+
+    With w noise every direction agrees with the finite difference to 1e-6.
+    In the configuration's own state p and w are uniform up to rounding, so
+    the limiter's acoustic slopes and the slopes of w are evaluated at
+    arguments of rounding size: a step of 1e-6 moves them across the
+    limiter's kink, and the difference quotient measures a different branch
+    than the derivative of the branch the trajectory takes.  There the
+    tangent, which follows the same branches as the adjoint, must agree to
+    round-off, and the finite differences only to the size of that kink."""
+    import torch
+
+    from pelec_gb300 import trajectory
+
+    fx = _c5_fixture()
+    shape = tuple(int(v) for v in fx["shape"])
+    mech, st, fp = problems.flame(shape, seed=int(fx["seed"]), w_noise=1.0 if tag == "wnoise" else 0.0)
+    op = cuda_lib.MOLOperator(problems.make_config(mech))
+    S0 = to_multifab(cuda_lib, [st], 4)
+    tr = trajectory.Trajectory(op, S0, _geom(st), st.dx)
+    dts = [float(v) for v in fx[f"{tag}_dts"]]
+    J, L = tr.gradient(S0, dts, every=5)
+    torch.cuda.synchronize()
+    assert abs(J - float(fx[f"{tag}_J0"])) <= 1e-12 * abs(J), (J, float(fx[f"{tag}_J0"]))
+    h = float(fx["h_state"])
+    fd_errs, tan_errs = [], []
+    for d, s in enumerate(fx[f"{tag}_scales"]):
+        v = _direction(st, s)
+        ad = float((L.fabs[0] * v).sum())
+        fd = (float(fx[f"{tag}_Jp"][d]) - float(fx[f"{tag}_Jm"][d])) / (2 * h)
+        fd_errs.append(abs(fd - ad) / abs(ad))
+        if tag == "config" or d < 4:
+            _, tan = tr.tangent(S0, dts, cuda_lib.MultiFab(S0.boxes, S0.ncomp, 4, fabs=[v]))
+            tan_errs.append(abs(tan - ad) / abs(ad))
+    print(tag, "FD rel errors: max %.3e median %.3e" % (max(fd_errs), float(np.median(fd_errs))),
+          "tangent rel errors: max %.3e" % max(tan_errs))
+    assert max(tan_errs) <= 1e-10, tan_errs
+    if tag == "wnoise":
+        assert max(fd_errs) <= GRAD_REL, fd_errs
+    else:
+        assert max(fd_errs) <= 1e-4, fd_errs
+
+
+def test_c5_wrinkle_amplitude_gradient_against_oracle_fd(cuda_lib):
+    """C5 (b): dJ/da for the first three wrinkle amplitudes — the adjoint
+    contracted with dU0/da, and the tangent along dU0/da — against the
+    Richardson-extrapolated central difference of the oracle's CPU
+    trajectory in a (steps 1e-7 and 2e-7 cm)."""
+    import torch
+
+    from pelec_gb300 import trajectory
+
+    fx = _c5_fixture()
+    shape = tuple(int(v) for v in fx["shape"])
+    mech, st, fp = problems.flame(shape, seed=int(fx["seed"]))
+    np.testing.assert_array_equal(fp.amps, fx["config_amps"])
+    op = cuda_lib.MOLOperator(problems.make_config(mech))
+    S0 = to_multifab(cuda_lib, [st], 4)
+    tr = trajectory.Trajectory(op, S0, _geom(st), st.dx)
+    dts = [float(v) for v in fx["config_dts"]]
+    J, L = tr.gradient(S0, dts, every=5)
+    lam = L.fabs[0].cpu().numpy()
+    h = float(fx["h_amp"])
+
+    def U0(amps):
+        return problems.flame(shape, seed=int(fx["seed"]), params=dataclasses.replace(fp, amps=amps))[1].S
+
+    for m in range(3):
+        ha = 1e-3 * max(fp.amps[m], 1e-6)
+        e = ha * (np.arange(len(fp.amps)) == m)
+        dU = (U0(fp.amps + e) - U0(fp.amps - e)) / (2 * ha)
+        ad = float((lam * dU).sum())
+        _, tan = tr.tangent(S0, dts, cuda_lib.MultiFab(S0.boxes, S0.ncomp, 4, fabs=[torch.from_numpy(dU).cuda()]))
+        Jp, Jm, J2p, J2m = (float(x) for x in fx["config_Jamp"][m])
+        d1 = (Jp - Jm) / (2 * h)
+        d2 = (J2p - J2m) / (4 * h)
+        fd = (4 * d1 - d2) / 3
+        print("mode", m, "adjoint", ad, "tangent", tan, "FD", d1, "Richardson", fd, "rel", abs(fd - ad) / abs(ad))
+        assert abs(tan - ad) <= 1e-10 * abs(ad)
+        assert abs(fd - ad) <= GRAD_REL * abs(ad)

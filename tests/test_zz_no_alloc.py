@@ -1,12 +1,13 @@
 """GPU test of pc_mol_rhs_box_static, the entry point that allocates no
 device memory (for callers that cannot call cudaMalloc while they run, for
-example code recording a stream capture or running under a memory pool that
-forbids other allocations).
+example code running under a memory pool that forbids other allocations, or
+an application that reserved all device memory at start-up).
 
-It must give the same right-hand side as pc_mol_rhs_level on the same box,
-on consecutive calls that reuse its fixed device array, and must refuse a box
-that does not fit that array.  This file is collected last so that a run
-stopping at the first failure has already run every other test.
+It must give the same right-hand side as pc_mol_rhs_level on the same box —
+bit for bit, since it launches the same FP64 kernels — on consecutive calls
+that reuse its fixed device array, and must refuse a box that does not fit
+that array.  This file is collected last so that a run stopping at the first
+failure has already run every other test.
 """
 import ctypes
 from ctypes import POINTER, c_double, c_int, c_void_p
@@ -63,6 +64,7 @@ def test_static_entry_matches_level_entry_on_consecutive_calls(cuda_lib):
         err = rel_maxnorm(R, ref)
         assert np.all(np.isfinite(R))
         assert err.max() <= RTOL, err
+        np.testing.assert_array_equal(R, ref)  # the same kernels: the same bits
     # the repeated box gives the same answer after other boxes used the array
     np.testing.assert_array_equal(outs[0], outs[3])
 
