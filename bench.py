@@ -388,6 +388,58 @@ def bench_sub_box(args, name: str, rank: int, maxover, barrier) -> dict:
     return out
 
 
+def bench_step_graph(args, rank: int, maxover, barrier) -> dict:
+    """One SSP-RK2 step of a 64^3 flame box (periodic x/y, outflow z, FP64):
+    the host-driven sequence of nine library calls (advance.ssprk2_step)
+    against one CUDA-graph replay per step (advance.Stepper), K steps each,
+    CUDA events on the launch stream (host gaps between launches included)."""
+    import numpy as np
+    import torch
+
+    from pelec_gb300 import abi, advance, mol, problems
+
+    mech, st, _ = problems.flame((64, 64, 64), seed=5 + rank)
+    geom = abi.geometry(st.lo, st.hi, (0, 0, abi.PC_BC_OUTFLOW), (0, 0, abi.PC_BC_OUTFLOW))
+    op = mol.MOLOperator(problems.make_config(mech))
+    mk = lambda: mol.MultiFab([(st.lo, st.hi)], st.S.shape[0], st.ng, fabs=[torch.from_numpy(st.S.copy()).cuda()])
+    S_old, S_new, R = mk(), mk(), mol.MultiFab([(st.lo, st.hi)], st.S.shape[0], 0)
+    op.fill_ghosts(S_old, geom)
+    dt = op.est_dt(S_old, st.dx, 0.3)
+    stepper = advance.Stepper(op, mk(), mk(), mol.MultiFab([(st.lo, st.hi)], st.S.shape[0], 0), geom, st.dx)
+    stream = torch.cuda.current_stream()
+    steps = max(5, args.steps)
+
+    def host_step():
+        nonlocal S_old, S_new
+        advance.ssprk2_step(op, S_old, S_new, R, geom, st.dx, dt)
+        S_old, S_new = S_new, S_old
+
+    def timed(fn):
+        for _ in range(max(3, args.warmup)):
+            fn()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        barrier()
+        e0.record(stream)
+        for _ in range(steps):
+            fn()
+        e1.record(stream)
+        barrier()
+        return maxover(e0.elapsed_time(e1)) / steps
+
+    t_host = timed(host_step)
+    t_graph = timed(lambda: stepper.step(dt))
+    torch.cuda.synchronize()
+    same = bool(np.isfinite(stepper.state.fabs[0].cpu().numpy()).all())
+    stepper.close()
+    op.close()
+    return {"workload": "one SSP-RK2 step (2 fills, 2 RHS, 3 LinComb, 2 computeTemp) of a 64^3 flame box, "
+                        "9 species, FP64, periodic x/y, outflow z", "steps": steps,
+            "host_driven_ms_per_step": t_host, "graph_ms_per_step": t_graph, "speedup": t_host / t_graph,
+            "finite": same, "cells": st.ncells,
+            "graph": "pc_mol_step_graph: both directions of the state pair captured once, dt written to a device "
+                     "scalar before each replay"}
+
+
 def bench_adjoint_rhs(args, st, mech, S, maxover, barrier) -> dict:
     """Adjoint (VJP) and tangent (JVP) of one RHS on the headline box, timed
     like the RHS itself: ms per call with CUDA events, and the ratio to the
@@ -760,6 +812,7 @@ def run_gpu(args):
     sub = None
     if args.workload != "c2" and not args.no_c2:
         sub = bench_sub_box(args, "c2", rank, maxover, barrier)
+    stepg = None if args.no_level else bench_step_graph(args, rank, maxover, barrier)
     level = None if args.no_level else bench_level(args, rank, local, maxover, barrier)
     adj = None if args.no_adjoint else bench_adjoint_rhs(args, st, mech, S, maxover, barrier)
     traj = None if (args.no_adjoint or args.no_trajectory or rank != 0) else bench_trajectory(args, rank)
@@ -834,6 +887,8 @@ def run_gpu(args):
         line["cpu_baseline"] = cpu
     if sub is not None:
         line["c2"] = sub
+    if stepg is not None:
+        line["step_graph"] = stepg
     if level is not None:
         line["level_c3"] = level
     if adj is not None:

@@ -334,6 +334,33 @@ int pc_mol_graph_launch(pc_mol_graph* g, void* stream);
 int pc_mol_graph_status(pc_mol_graph* g, pc_mol_status* st);
 void pc_mol_graph_destroy(pc_mol_graph* g);
 
+/* One SSP-RK2 step of a level per CUDA-graph replay: PeleC's do_mol_advance
+ * without sources (Source/Advance.cpp:98-168), i.e. the ghost fill
+ * (FillPatcherFill, :98, :132), getMOLSrcTerm (:100, :134), MultiFab::LinComb
+ * (:117), computeTemp (:125), LinComb and Saxpy (:148-151), computeTemp (:168):
+ *   fill(S_old); R = RHS(S_old); S_new = S_old + dt R; computeTemp(S_new);
+ *   fill(S_new); R = RHS(S_new); S_new = 0.5 S_new + 0.5 S_old;
+ *   S_new += 0.5 dt R; computeTemp(S_new)
+ * with each operation's arithmetic that of the separate entry points (the
+ * replayed step equals the sequence of calls bit for bit).  a[b] gives box
+ * b's valid region, its state S_a (ngrow >= 2 filled-ghost layers, the
+ * layers the fill writes) and the RHS array R; state_b[b] is the second
+ * state S_b, with the same array geometry.  Creation captures both
+ * directions, S_a -> S_b and S_b -> S_a, so a trajectory alternates them
+ * without copies; like pc_mol_graph it owns a private copy of h with its own
+ * scratch and counters, and runs the RHS of both states once, uncaptured,
+ * writing R, then synchronizes.  geom: the level's domain and face BCs, as
+ * for pc_mol_fill_ghosts.  Launch: dt is written to a device scalar ahead of
+ * the replay (reverse = 0: S_a -> S_b, 1: S_b -> S_a); asynchronous on
+ * stream.  No counterpart in the reference, which issues these as separate
+ * launches from the host. */
+typedef struct pc_mol_step_graph pc_mol_step_graph;
+int pc_mol_step_graph_create(pc_mol_handle* h, const pc_box_desc* a, const pc_array4* state_b, int nboxes,
+                             const double dx[3], const pc_geometry* geom, int ngrow, pc_mol_step_graph** out);
+int pc_mol_step_graph_launch(pc_mol_step_graph* g, double dt, int reverse, void* stream);
+int pc_mol_step_graph_status(pc_mol_step_graph* g, pc_mol_status* st);
+void pc_mol_step_graph_destroy(pc_mol_step_graph* g);
+
 /* Vector-Jacobian product of the RHS (reverse mode, hand-written):
  *   state_bar = (d rhs / d state)^T rhs_bar
  * for PC_PRECISION_FP64 with the Riemann solver of riemann() (use_laxf_flux

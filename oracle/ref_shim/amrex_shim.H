@@ -15,6 +15,7 @@
 #include <fstream>
 #include <limits>
 #include <sstream>
+#include <stdexcept>
 #include <string>
 #include <type_traits>
 #include <vector>
@@ -51,10 +52,7 @@ constexpr T pi() { return T(3.1415926535897932384626433832795029); }
 template <class T>
 using Vector = std::vector<T>;
 
-[[noreturn]] inline void Abort(const char* msg = "") {
-  std::fprintf(stderr, "amrex::Abort: %s\n", msg);
-  std::abort();
-}
+[[noreturn]] inline void Abort(const char* msg = "") { throw std::runtime_error(std::string("amrex::Abort: ") + msg); }
 [[noreturn]] inline void Error(const char* msg = "") { Abort(msg); }
 
 struct Dim3 {
@@ -225,6 +223,7 @@ struct Geometry {
   GeometryData gd;
   GeometryData data() const { return gd; }
   GpuArray<Real, 3> InvCellSizeArray() const { return {{1.0 / gd.dx[0], 1.0 / gd.dx[1], 1.0 / gd.dx[2]}}; }
+  GpuArray<Real, 3> CellSizeArray() const { return {{gd.dx[0], gd.dx[1], gd.dx[2]}}; }
 };
 
 // ParallelFor over a box (k slowest, i fastest).  Iterations write disjoint

@@ -132,6 +132,25 @@ __global__ void __launch_bounds__(256) lincomb_kernel(const int2* __restrict__ i
   for (int n = 0; n < A.nvar; ++n) dp[n * D.sn] = A.a * xp[n * X.sn] + A.b * yp[n * Y.sn];
 }
 
+// LinComb whose second coefficient is A.b times a scalar read on the device
+// (the time step of a captured SSP-RK2 step, written before each replay).
+// A.b is 1 or 0.5 there, so the product is exact: the same bits as the
+// host-side coefficient of lincomb_kernel.
+__global__ void __launch_bounds__(256) lincomb_dt_kernel(const int2* __restrict__ items, const LinCombArgs A,
+                                                         const double* __restrict__ dt) {
+  const int2 it = items[blockIdx.x];
+  int i, j, k;
+  if (!valid_cell(A.dst[it.x], (long long)it.y + threadIdx.x, i, j, k)) return;
+  const double b = A.b * __ldg(dt);
+  const LevelBox &D = A.dst[it.x], &X = A.x[it.x], &Y = A.y[it.x];
+  const double* xp = at(X, i, j, k);
+  const double* yp = at(Y, i, j, k);
+  double* dp = at(D, i, j, k);
+  for (int n = 0; n < A.nvar; ++n) dp[n * D.sn] = A.a * xp[n * X.sn] + b * yp[n * Y.sn];
+}
+
+__global__ void set_scalar_kernel(double* p, double v) { *p = v; }
+
 // computeTemp: rho e = rho E - rho |u|^2 / 2, then T from e (guess U(UTEMP)).
 template <int NS, class EOS>
 __global__ void __launch_bounds__(256) compute_temp_kernel(const LevelBox* __restrict__ boxes,

@@ -1435,3 +1435,215 @@ extern "C" void pc_mol_graph_destroy(pc_mol_graph* g) {
   pc_mol_destroy(g->h);
   delete g;
 }
+
+// ---------------------------------------------------------------------------
+// One SSP-RK2 step of a level per CUDA-graph replay: do_mol_advance without
+// sources (Source/Advance.cpp:98-168):
+//   fill(S_old); R = RHS(S_old); S_new = 1 S_old + dt R; computeTemp(S_new)
+//   fill(S_new); R = RHS(S_new); S_new = 0.5 S_new + 0.5 S_old;
+//   S_new = 1 S_new + 0.5 dt R; computeTemp(S_new)
+// Two graphs, A -> B and B -> A, share one private handle (RHS layout,
+// record scratch, counters) and device tables built once at creation; the
+// time step is a device scalar written by a one-thread kernel ahead of each
+// replay, which the LinComb kernels read.
+// ---------------------------------------------------------------------------
+struct pc_mol_step_graph {
+  pc_mol_handle* h = nullptr;
+  cudaGraph_t graph[2] = {nullptr, nullptr};
+  cudaGraphExec_t exec[2] = {nullptr, nullptr};
+  double* d_dt = nullptr;
+  std::vector<void*> bufs;  // device tables owned by the graphs
+};
+
+namespace {
+
+int dev_copy(pc_mol_step_graph* g, const void* src, size_t bytes, void** out) {
+  void* p = nullptr;
+  if (cudaMalloc(&p, bytes ? bytes : 16) != cudaSuccess) return PC_ERR_OUT_OF_MEMORY;
+  g->bufs.push_back(p);
+  if (bytes && cudaMemcpy(p, src, bytes, cudaMemcpyHostToDevice) != cudaSuccess) return PC_ERR_CUDA;
+  *out = p;
+  return PC_OK;
+}
+
+}  // namespace
+
+extern "C" void pc_mol_step_graph_destroy(pc_mol_step_graph* g) {
+  if (!g) return;
+  if (g->h) cudaSetDevice(g->h->device);
+  for (int d = 0; d < 2; ++d) {
+    if (g->exec[d]) cudaGraphExecDestroy(g->exec[d]);
+    if (g->graph[d]) cudaGraphDestroy(g->graph[d]);
+  }
+  for (void* p : g->bufs) cudaFree(p);
+  pc_mol_destroy(g->h);
+  delete g;
+}
+
+extern "C" int pc_mol_step_graph_create(pc_mol_handle* parent, const pc_box_desc* a, const pc_array4* state_b,
+                                        int nboxes, const double dx[3], const pc_geometry* geom, int ngrow,
+                                        pc_mol_step_graph** out) {
+  if (!parent || !out || nboxes <= 0 || !a || !state_b || !dx || !geom || ngrow < 2) return PC_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  const int nvar = 7 + parent->cfg.nspec;
+  for (int d = 0; d < 3; ++d)
+    if (!(dx[d] > 0.0) || !std::isfinite(dx[d])) return parent->last_error = PC_ERR_INVALID_ARGUMENT;
+  // Both states have the same array geometry (so the RHS layout is shared)
+  // and at least ngrow filled ghost layers; the RHS array is the valid box.
+  std::vector<pc_box_desc> da(a, a + nboxes), db(a, a + nboxes);
+  for (int b = 0; b < nboxes; ++b) {
+    db[b].state = state_b[b];
+    if (!same_geometry(da[b], db[b]) || a[b].state.p == state_b[b].p ||
+        !array_ok(a[b].state, a[b].lo, a[b].hi, ngrow, nvar) || !array_ok(a[b].rhs, a[b].lo, a[b].hi, 0, nvar))
+      return parent->last_error = PC_ERR_INVALID_ARGUMENT;
+  }
+  int rc = cuda_fail(parent, cudaSetDevice(parent->device));
+  if (rc != PC_OK) return rc;
+  pc_mol_config cfg = parent->cfg;
+  cfg.time_passes = 0;
+  pc_mol_step_graph* g = new (std::nothrow) pc_mol_step_graph();
+  if (!g) return parent->last_error = PC_ERR_OUT_OF_MEMORY;
+  rc = pc_mol_create(&g->h, &cfg);
+  if (rc != PC_OK) {
+    delete g;
+    return parent->last_error = rc;
+  }
+  pc_mol_handle* h = g->h;
+  h->tile_forced = parent->tile_forced;
+  h->tune_cache = parent->tune_cache;
+  auto fail = [&](int r) {
+    pc_mol_step_graph_destroy(g);
+    return parent->last_error = r;
+  };
+
+  // Host tables: each state's and the RHS's LevelBox lists, the valid-cell
+  // and grown-box chunk lists, the fill geometry and the owner map.
+  FillGeom fg{};
+  long long ndom = 1;
+  for (int d = 0; d < 3; ++d) {
+    fg.dlo[d] = geom->domain_lo[d];
+    fg.dhi[d] = geom->domain_hi[d];
+    fg.len[d] = geom->domain_hi[d] - geom->domain_lo[d] + 1;
+    fg.bclo[d] = geom->bc_lo[d];
+    fg.bchi[d] = geom->bc_hi[d];
+    if (fg.len[d] < ngrow) return fail(PC_ERR_INVALID_ARGUMENT);
+    for (int bc : {geom->bc_lo[d], geom->bc_hi[d]})
+      if (bc < PC_BC_INTERIOR || bc > PC_BC_NOSLIPWALL) return fail(PC_ERR_UNSUPPORTED);
+    if ((geom->bc_lo[d] == PC_BC_INTERIOR) != (geom->bc_hi[d] == PC_BC_INTERIOR)) return fail(PC_ERR_INVALID_ARGUMENT);
+    fg.periodic[d] = geom->bc_lo[d] == PC_BC_INTERIOR;
+    ndom *= fg.len[d];
+  }
+  fg.ng = ngrow;
+  fg.nvar = nvar;
+  std::vector<LevelBox> lbA, lbB, lbR;
+  std::vector<long long> ncv, ncg;
+  for (int b = 0; b < nboxes; ++b) {
+    for (int d = 0; d < 3; ++d)
+      if (a[b].lo[d] < fg.dlo[d] || a[b].hi[d] > fg.dhi[d]) return fail(PC_ERR_INVALID_ARGUMENT);
+    lbA.push_back(level_box(a[b].lo, a[b].hi, a[b].state));
+    lbB.push_back(level_box(a[b].lo, a[b].hi, state_b[b]));
+    lbR.push_back(level_box(a[b].lo, a[b].hi, a[b].rhs));
+    ncv.push_back(nvalid(a[b].lo, a[b].hi, 0));
+    ncg.push_back(nvalid(a[b].lo, a[b].hi, ngrow));
+  }
+  std::vector<int2> itv, itg;
+  chunk_items(ncv, itv);
+  chunk_items(ncg, itg);
+  std::vector<int> owner;
+  if (nboxes > 1) {
+    if (ndom > 400000000LL) return fail(PC_ERR_TOO_LARGE);
+    owner.assign((size_t)ndom, -1);
+    for (int b = 0; b < nboxes; ++b)
+      for (int k = a[b].lo[2]; k <= a[b].hi[2]; ++k)
+        for (int j = a[b].lo[1]; j <= a[b].hi[1]; ++j)
+          for (int i = a[b].lo[0]; i <= a[b].hi[0]; ++i) {
+            const long long o = (i - fg.dlo[0]) + (long long)(j - fg.dlo[1]) * fg.len[0] +
+                                (long long)(k - fg.dlo[2]) * fg.len[0] * fg.len[1];
+            if (owner[o] >= 0) return fail(PC_ERR_INVALID_ARGUMENT);
+            owner[o] = b;
+          }
+    for (int o : owner)
+      if (o < 0) return fail(PC_ERR_INVALID_ARGUMENT);
+  } else {
+    for (int d = 0; d < 3; ++d)
+      if (a[0].lo[d] != fg.dlo[d] || a[0].hi[d] != fg.dhi[d]) return fail(PC_ERR_INVALID_ARGUMENT);
+  }
+  void *dA, *dB, *dR, *dItv, *dItg, *dOwn = nullptr, *dDt;
+  if ((rc = dev_copy(g, lbA.data(), lbA.size() * sizeof(LevelBox), &dA)) != PC_OK ||
+      (rc = dev_copy(g, lbB.data(), lbB.size() * sizeof(LevelBox), &dB)) != PC_OK ||
+      (rc = dev_copy(g, lbR.data(), lbR.size() * sizeof(LevelBox), &dR)) != PC_OK ||
+      (rc = dev_copy(g, itv.data(), itv.size() * sizeof(int2), &dItv)) != PC_OK ||
+      (rc = dev_copy(g, itg.data(), itg.size() * sizeof(int2), &dItg)) != PC_OK ||
+      (rc = dev_copy(g, nullptr, sizeof(double), &dDt)) != PC_OK)
+    return fail(rc);
+  if (!owner.empty() && (rc = dev_copy(g, owner.data(), owner.size() * sizeof(int), &dOwn)) != PC_OK) return fail(rc);
+  g->d_dt = static_cast<double*>(dDt);
+
+  cudaStream_t s = nullptr;
+  rc = cuda_fail(h, cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+  if (rc != PC_OK) return fail(rc);
+  const LevelBox* L[2] = {static_cast<const LevelBox*>(dA), static_cast<const LevelBox*>(dB)};
+  const LevelBox* LR = static_cast<const LevelBox*>(dR);
+  const int2* ITV = static_cast<const int2*>(dItv);
+  const int2* ITG = static_cast<const int2*>(dItg);
+  const int* OWN = static_cast<const int*>(dOwn);
+  const std::vector<pc_box_desc>* D[2] = {&da, &db};
+  const unsigned nbv = (unsigned)itv.size(), nbg = (unsigned)itg.size();
+  const int maxit = h->flags.newton_maxit;
+  auto ctemp = [&](const LevelBox* lb) {
+    if (h->variant == 1)
+      compute_temp_kernel<1, GammaLawEos<1>><<<nbv, 256, 0, s>>>(lb, ITV, h->mech1, maxit, h->d_counters);
+    else
+      compute_temp_kernel<9, IdealMixEos<9>><<<nbv, 256, 0, s>>>(lb, ITV, h->mech9, maxit, h->d_counters);
+  };
+  // The step from state o to state n (o, n = 0: A, 1: B).
+  auto seq = [&](int o) -> int {
+    const int n = 1 - o;
+    fill_ghosts_kernel<false><<<nbg, 256, 0, s>>>(L[o], ITG, OWN, fg);
+    int r = run(h, D[o]->data(), nboxes, dx, s, false);
+    if (r != PC_OK) return r;
+    lincomb_dt_kernel<<<nbv, 256, 0, s>>>(ITV, LinCombArgs{L[n], L[o], LR, 1.0, 1.0, nvar}, g->d_dt);
+    ctemp(L[n]);
+    fill_ghosts_kernel<false><<<nbg, 256, 0, s>>>(L[n], ITG, OWN, fg);
+    r = run(h, D[n]->data(), nboxes, dx, s, false);
+    if (r != PC_OK) return r;
+    lincomb_kernel<<<nbv, 256, 0, s>>>(ITV, LinCombArgs{L[n], L[n], L[o], 0.5, 0.5, nvar});
+    lincomb_dt_kernel<<<nbv, 256, 0, s>>>(ITV, LinCombArgs{L[n], L[n], LR, 1.0, 0.5, nvar}, g->d_dt);
+    ctemp(L[n]);
+    return cuda_fail(h, cudaGetLastError());
+  };
+  // Uncaptured RHS evaluations of both states make every upload and
+  // allocation the captured RHS needs (the layout and the box tables of both
+  // states); they write only R, whatever the states hold.
+  for (int o = 0; o < 2 && rc == PC_OK; ++o) rc = run(h, D[o]->data(), nboxes, dx, s, false);
+  if (rc == PC_OK) rc = cuda_fail(h, cudaStreamSynchronize(s));
+  for (int o = 0; o < 2 && rc == PC_OK; ++o) {
+    rc = cuda_fail(h, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    if (rc != PC_OK) break;
+    const int r1 = seq(o);
+    const cudaError_t e = cudaStreamEndCapture(s, &g->graph[o]);
+    rc = r1 != PC_OK ? r1 : cuda_fail(h, e);
+    if (rc == PC_OK) rc = cuda_fail(h, cudaGraphInstantiate(&g->exec[o], g->graph[o], 0));
+  }
+  if (s) cudaStreamDestroy(s);
+  if (rc != PC_OK) return fail(rc);
+  *out = g;
+  return PC_OK;
+}
+
+extern "C" int pc_mol_step_graph_launch(pc_mol_step_graph* g, double dt, int reverse, void* stream) {
+  if (!g || !g->exec[0] || !g->exec[1] || !(dt >= 0.0) || !std::isfinite(dt)) return PC_ERR_INVALID_ARGUMENT;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  int rc = cuda_fail(g->h, cudaSetDevice(g->h->device));
+  if (rc != PC_OK) return rc;
+  g->h->last_stream = s;
+  set_scalar_kernel<<<1, 1, 0, s>>>(g->d_dt, dt);
+  rc = cuda_fail(g->h, cudaGetLastError());
+  if (rc != PC_OK) return g->h->last_error = rc;
+  return g->h->last_error = cuda_fail(g->h, cudaGraphLaunch(g->exec[reverse ? 1 : 0], s));
+}
+
+extern "C" int pc_mol_step_graph_status(pc_mol_step_graph* g, pc_mol_status* st) {
+  if (!g) return PC_ERR_INVALID_ARGUMENT;
+  return pc_mol_last_status(g->h, st);
+}

@@ -72,6 +72,15 @@ def library() -> ctypes.CDLL:
         lib.pc_mol_graph_destroy.restype = None
         lib.pc_mol_graph_status.argtypes = [c_void_p, POINTER(abi.PcMolStatus)]
         lib.pc_mol_graph_status.restype = c_int
+        lib.pc_mol_step_graph_create.argtypes = [c_void_p, POINTER(abi.PcBoxDesc), POINTER(abi.PcArray4), c_int,
+                                                 POINTER(c_double), POINTER(abi.PcGeometry), c_int, POINTER(c_void_p)]
+        lib.pc_mol_step_graph_create.restype = c_int
+        lib.pc_mol_step_graph_launch.argtypes = [c_void_p, c_double, c_int, c_void_p]
+        lib.pc_mol_step_graph_launch.restype = c_int
+        lib.pc_mol_step_graph_status.argtypes = [c_void_p, POINTER(abi.PcMolStatus)]
+        lib.pc_mol_step_graph_status.restype = c_int
+        lib.pc_mol_step_graph_destroy.argtypes = [c_void_p]
+        lib.pc_mol_step_graph_destroy.restype = None
         lib.pc_mol_tile_shape.argtypes = [c_int, POINTER(c_int)]
         lib.pc_mol_tile_shape.restype = c_int
         lib.pc_mol_set_tile.argtypes = [c_void_p, c_int]
@@ -278,6 +287,11 @@ class MOLOperator:
         """CUDA graph of (ghost fill +) RHS on fixed arrays; replay with .launch()."""
         return LevelGraph(self, S, R, dx, geom, S.ngrow if ngrow is None else ngrow)
 
+    def step_graph(self, A: MultiFab, B: MultiFab, R: MultiFab, dx, geom: abi.PcGeometry) -> "StepGraph":
+        """CUDA graphs of one SSP-RK2 step between the states A and B (both
+        directions) with RHS array R; replay with .launch(dt, reverse)."""
+        return StepGraph(self, A, B, R, dx, geom)
+
     # ---- derivatives ----
     def rhs_vjp(self, S: MultiFab, rhs_bar: MultiFab, state_bar: MultiFab, dx, stream=None) -> None:
         """state_bar = (d RHS / d S)^T rhs_bar on grow(valid, 2) (pc_mol_rhs_vjp).
@@ -377,6 +391,46 @@ class LevelGraph:
     def close(self) -> None:
         if getattr(self, "_g", None) and self._g.value:
             library().pc_mol_graph_destroy(self._g)
+            self._g = c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class StepGraph:
+    """pc_mol_step_graph: one launch replays a whole SSP-RK2 step of the level
+    (fill, RHS, LinComb, computeTemp, fill, RHS, LinComb, Saxpy, computeTemp),
+    from A to B (reverse=False) or from B to A (reverse=True)."""
+
+    def __init__(self, op: MOLOperator, A: MultiFab, B: MultiFab, R: MultiFab, dx, geom: abi.PcGeometry):
+        if len(A) != len(B) or len(A) != len(R) or A.ngrow != B.ngrow:
+            raise ValueError("A, B and R must share one BoxArray, A and B one ghost width")
+        self._op = op  # keeps the parent handle alive
+        self._keep = (A, B, R, geom)
+        descs = abi.box_array([abi.box_desc(lo, hi, A.array4(b), R.array4(b)) for b, (lo, hi) in enumerate(A.boxes)])
+        sb = (abi.PcArray4 * len(B))(*[B.array4(b) for b in range(len(B))])
+        dxa = (c_double * 3)(*[float(v) for v in dx])
+        g = c_void_p()
+        _check(library().pc_mol_step_graph_create(op._h, descs, sb, len(A), dxa, ctypes.byref(geom), int(A.ngrow),
+                                                  ctypes.byref(g)), "pc_mol_step_graph_create")
+        self._g = g
+
+    def launch(self, dt: float, reverse: bool = False, stream=None) -> None:
+        _check(library().pc_mol_step_graph_launch(self._g, float(dt), int(bool(reverse)), MOLOperator._stream(stream)),
+               "pc_mol_step_graph_launch")
+
+    def status(self) -> abi.PcMolStatus:
+        """Counters of the last replay (synchronizes its stream)."""
+        st = abi.PcMolStatus()
+        _check(library().pc_mol_step_graph_status(self._g, ctypes.byref(st)), "pc_mol_step_graph_status")
+        return st
+
+    def close(self) -> None:
+        if getattr(self, "_g", None) and self._g.value:
+            library().pc_mol_step_graph_destroy(self._g)
             self._g = c_void_p()
 
     def __del__(self):

@@ -51,7 +51,7 @@ class Trajectory:
     BoxArray and ghost width; geom: abi.PcGeometry for the ghost fill;
     dx: cell size."""
 
-    def __init__(self, op: "mol.MOLOperator", template: "mol.MultiFab", geom, dx):
+    def __init__(self, op: "mol.MOLOperator", template: "mol.MultiFab", geom, dx, use_graph: bool = True):
         self.op = op
         self.geom = geom
         self.dx = tuple(float(v) for v in dx)
@@ -59,6 +59,19 @@ class Trajectory:
         self.S_new = _zeros_like(template)
         self.R = _zeros_like(template, 0)
         self.ng = template.ngrow
+        self.use_graph = use_graph
+        self._stepper = None  # advance.Stepper over two persistent states, made on first use
+
+    def _graph_stepper(self, S0: "mol.MultiFab"):
+        from . import advance
+
+        if self._stepper is None:
+            A, B = _zeros_like(S0), _zeros_like(S0)
+            self._stepper = advance.Stepper(self.op, A, B, _zeros_like(S0, 0), self.geom, self.dx)
+        st = self._stepper
+        for dst, src in zip(st.state.fabs, S0.fabs):
+            dst.copy_(src)
+        return st
 
     # ---- forward ----
     def step(self, S_old: "mol.MultiFab", S_new: "mol.MultiFab", dt: float, keep: bool = False):
@@ -80,9 +93,18 @@ class Trajectory:
 
     def run(self, S0: "mol.MultiFab", dts, every: int = 0):
         """Forward trajectory from S0 (not modified).  Returns the final
-        state and the checkpoints {step: state} (every > 0)."""
-        S_old, S_new = _clone(S0), _clone(S0)
+        state and the checkpoints {step: state} (every > 0).  With use_graph
+        each step is one replay of the step graph (advance.Stepper), the same
+        arithmetic as ``step``."""
         ckpt = {}
+        if self.use_graph:
+            st = self._graph_stepper(S0)
+            for n, dt in enumerate(dts):
+                if every and n % every == 0:
+                    ckpt[n] = _clone(st.state)
+                st.step(float(dt))
+            return _clone(st.state), ckpt
+        S_old, S_new = _clone(S0), _clone(S0)
         for n, dt in enumerate(dts):
             if every and n % every == 0:
                 ckpt[n] = _clone(S_old)
