@@ -157,12 +157,12 @@ def cpu_baseline(st, cfg, reps: int = 2) -> dict:
             "best_s": min(times), "median_s": statistics.median(times)}
 
 
-# Sources whose compiled code the FP64 traffic and instruction counts of a
-# profile describe; a profile records their hash, and a figure whose hash no
-# longer matches is reported as stale (null), not used.
+# Sources that define the FP64 cell and flux kernels (and their compile
+# flags) whose traffic and instruction counts a profile describes; a profile
+# records their hash, and a figure whose hash no longer matches is reported
+# as stale (null), not used.
 PROFILED_SOURCES = ("pelec_gb300/csrc/pc_kernels.cuh", "pelec_gb300/csrc/pc_device.cuh", "pelec_gb300/csrc/pc_exp.h",
-                    "pelec_gb300/csrc/pc_exp_tables.h", "pelec_gb300/csrc/pc_mol.cu", "pelec_gb300/csrc/pc_rhs_rcp.cu",
-                    "pelec_gb300/build.py", "include/pelec_mol.h")
+                    "pelec_gb300/csrc/pc_exp_tables.h", "pelec_gb300/build.py")
 
 
 def kernel_source_hash() -> str:
@@ -484,12 +484,15 @@ def bench_adjoint_rhs(args, st, mech, S, maxover, barrier) -> dict:
 
 def bench_trajectory(args, rank: int) -> dict:
     """C5: 64^3 flame, 9 species, FP64; J = sum(T dV) after 50 SSP-RK2 steps
-    at CFL 0.3 (time steps frozen); gradient by the checkpointed adjoint
-    (every 5 steps).  Times the forward trajectory and the gradient, records
-    the device memory, and checks the gradient against central differences
-    of the trajectory: 20 seeded directions of the initial state (each
-    conserved component scaled by a seeded factor), h = 1e-6, and the three
-    first wrinkle amplitudes, h = 1e-8 cm (a state change of ~1e-6)."""
+    at CFL 0.3 (time steps frozen, those of the oracle's base trajectory);
+    gradient by the checkpointed adjoint (every 5 steps).  Times the forward
+    trajectory (one step-graph replay per step) and the gradient, records the
+    device memory, and checks the gradient against (a) central differences of
+    the ORACLE's CPU trajectory on 20 seeded state directions, h = 1e-6
+    relative, and Richardson differences in the first three wrinkle
+    amplitudes (tests/golden/c5_fd.npz, made by tests/golden/make_c5_fd.py),
+    and (b) the forward-mode tangent of the GPU trajectory along the same
+    directions."""
     import dataclasses
     import time
 
@@ -498,27 +501,32 @@ def bench_trajectory(args, rank: int) -> dict:
 
     from pelec_gb300 import abi, mol, problems, trajectory
 
-    nsteps, every, shape = 50, 5, (64, 64, 64)
+    path = os.path.join(ROOT, "tests", "golden", "c5_fd.npz")
+    fx = np.load(path)
+    nsteps, every = int(fx["nsteps"]), 5
+    shape = tuple(int(v) for v in fx["shape"])
     out = {"workload": "C5: 64^3 premixed flame, 9 species, FP64, 50 SSP-RK2 steps at CFL 0.3, "
-                       "J = sum(T dV) at step 50, checkpoint every 5", "nsteps": nsteps, "every": every}
+                       "J = sum(T dV) at step 50, checkpoint every 5", "nsteps": nsteps, "every": every,
+           "fd_reference": "central differences of the oracle's CPU trajectory (pinned bit for bit to the "
+                           "reference's own hot-path code), tests/golden/c5_fd.npz"}
 
-    def make(params=None, w_noise=0.0):
-        mech, st, fp = problems.flame(shape, seed=5, params=params, w_noise=w_noise)
-        return mech, st, fp
+    def direction(st, s):
+        v = torch.from_numpy(s[:, None, None, None] * st.S).cuda()
+        for ax in (1, 2, 3):
+            v.narrow(ax, 0, 4).zero_()
+            v.narrow(ax, v.shape[ax] - 4, 4).zero_()
+        return v
 
-    def case(w_noise, ndirs, with_params):
-        mech, st, fp = make(w_noise=w_noise)
+    def case(tag, w_noise, ntan, with_params):
+        mech, st, fp = problems.flame(shape, seed=int(fx["seed"]), w_noise=w_noise)
         op = mol.MOLOperator(problems.make_config(mech))
         S0 = mol.MultiFab([(st.lo, st.hi)], st.S.shape[0], 4, fabs=[torch.from_numpy(st.S).cuda()])
         geom = abi.geometry(st.lo, st.hi, (0, 0, abi.PC_BC_OUTFLOW), (0, 0, abi.PC_BC_OUTFLOW))
         tr = trajectory.Trajectory(op, S0, geom, st.dx)
-        dts = tr.dt_sequence(S0, nsteps, 0.3)
-        torch.cuda.synchronize()
-        res = {}
-        tr.run(S0, dts, every)  # warm-up (layouts, uploads)
+        dts = [float(v) for v in fx[f"{tag}_dts"]]
+        tr.run(S0, dts, every)  # warm-up (graphs, layouts, uploads)
         torch.cuda.synchronize()
         torch.cuda.reset_peak_memory_stats()
-        free0, total = torch.cuda.mem_get_info()
         fwd = []
         for _ in range(3):
             t0 = time.perf_counter()
@@ -531,69 +539,60 @@ def bench_trajectory(args, rank: int) -> dict:
         J2, L = tr.gradient(S0, dts, every)
         torch.cuda.synchronize()
         t_grad = time.perf_counter() - t0
-        free1, _ = torch.cuda.mem_get_info()
-        res.update({"J": J, "forward_s": t_fwd, "forward_s_runs": fwd, "gradient_s": t_grad, "adjoint_sweep_s": t_grad - t_fwd,
-                    "gradient_over_forward": t_grad / t_fwd, "adjoint_sweep_over_forward": (t_grad - t_fwd) / t_fwd,
-                    "peak_torch_bytes": int(torch.cuda.max_memory_allocated()),
-                    "device_bytes_in_use_after_gradient": int(total - free1),
-                    "dt_first_last": [dts[0], dts[-1]]})
-        g = 4
-        rng = np.random.default_rng(2024)
-        errs = []
-        for _ in range(ndirs):
-            sc = rng.normal(size=st.S.shape[0])
-            sc[abi.UEINT] = sc[abi.UTEMP] = 0.0
-            v = torch.from_numpy(sc[:, None, None, None] * st.S).cuda()
-            for ax in (1, 2, 3):
-                v.narrow(ax, 0, g).zero_()
-                v.narrow(ax, v.shape[ax] - g, g).zero_()
+        free1, total = torch.cuda.mem_get_info()
+        res = {"J": J, "J_oracle": float(fx[f"{tag}_J0"]), "forward_s": t_fwd, "forward_s_runs": fwd,
+               "gradient_s": t_grad, "adjoint_sweep_s": t_grad - t_fwd, "gradient_over_forward": t_grad / t_fwd,
+               "adjoint_sweep_over_forward": (t_grad - t_fwd) / t_fwd,
+               "peak_torch_bytes": int(torch.cuda.max_memory_allocated()),
+               "device_bytes_in_use_after_gradient": int(total - free1), "dt_first_last": [dts[0], dts[-1]]}
+        h = float(fx["h_state"])
+        fd_err, tan_err, t_tan = [], [], []
+        for d, s in enumerate(fx[f"{tag}_scales"]):
+            v = direction(st, s)
             ad = float((L.fabs[0] * v).sum())
-            h = 1e-6
-            Jp = tr.objective(tr.run(mol.MultiFab(S0.boxes, S0.ncomp, 4, fabs=[S0.fabs[0] + h * v]), dts)[0])
-            Jm = tr.objective(tr.run(mol.MultiFab(S0.boxes, S0.ncomp, 4, fabs=[S0.fabs[0] - h * v]), dts)[0])
-            errs.append(abs((Jp - Jm) / (2 * h) - ad) / abs(ad))
-        if errs:
-            res["fd_state_directions"] = {"n": len(errs), "h": 1e-6, "max_rel_err": max(errs),
-                                          "median_rel_err": float(np.median(errs)),
-                                          "direction": "each conserved component scaled by a seeded N(0,1) factor"}
+            fd = (float(fx[f"{tag}_Jp"][d]) - float(fx[f"{tag}_Jm"][d])) / (2 * h)
+            fd_err.append(abs(fd - ad) / abs(ad))
+            if d < ntan:
+                t0 = time.perf_counter()
+                _, tan = tr.tangent(S0, dts, mol.MultiFab(S0.boxes, S0.ncomp, 4, fabs=[v]))
+                t_tan.append(time.perf_counter() - t0)
+                tan_err.append(abs(tan - ad) / abs(ad))
+        res["fd_state_directions"] = {"n": len(fd_err), "h": h, "max_rel_err": max(fd_err),
+                                      "median_rel_err": float(np.median(fd_err)), "rel_err": fd_err,
+                                      "direction": "each conserved component scaled by a seeded N(0,1) factor"}
+        res["tangent_state_directions"] = {"n": len(tan_err), "max_rel_err": max(tan_err),
+                                           "tangent_s": float(np.median(t_tan)),
+                                           "note": "forward mode through the whole trajectory (dual-number RHS)"}
         if with_params:
             lam = L.fabs[0].cpu().numpy()
+            ha = float(fx["h_amp"])
             perr = []
             for m in range(3):
                 def U0(amps):
-                    return make(dataclasses.replace(fp, amps=np.asarray(amps, float)), w_noise)[1].S
-
-                # dU0/da by central differences of the generator (smooth in a)
-                ha = 1e-6
-                ap, am = fp.amps.copy(), fp.amps.copy()
-                ap[m] += ha
-                am[m] -= ha
-                ad = float((lam * (U0(ap) - U0(am)) / (2 * ha)).sum())
-                # FD step: a shift of 1e-8 cm moves T by ~1e-6 of itself across
-                # the 0.02 cm flame (a relative step on a itself, ~1e-10 cm for
-                # the smallest amplitudes, would leave J's difference in rounding)
-                h = 1e-8
-                ap, am = fp.amps.copy(), fp.amps.copy()
-                ap[m] += h
-                am[m] -= h
-                Jp = tr.objective(tr.run(mol.MultiFab(S0.boxes, S0.ncomp, 4,
-                                                      fabs=[torch.from_numpy(U0(ap)).cuda()]), dts)[0])
-                Jm = tr.objective(tr.run(mol.MultiFab(S0.boxes, S0.ncomp, 4,
-                                                      fabs=[torch.from_numpy(U0(am)).cuda()]), dts)[0])
-                fd = (Jp - Jm) / (2 * h)
-                perr.append({"mode": m, "amplitude_cm": float(fp.amps[m]), "h_cm": h, "adjoint": ad, "fd": fd,
-                             "rel_err": abs(fd - ad) / abs(ad)})
-            res["fd_wrinkle_amplitudes"] = perr
+                    return problems.flame(shape, seed=int(fx["seed"]), w_noise=w_noise,
+                                          params=dataclasses.replace(fp, amps=amps))[1].S
+                hg = 1e-3 * max(fp.amps[m], 1e-6)
+                e = hg * (np.arange(len(fp.amps)) == m)
+                dU = (U0(fp.amps + e) - U0(fp.amps - e)) / (2 * hg)
+                ad = float((lam * dU).sum())
+                _, tan = tr.tangent(S0, dts, mol.MultiFab(S0.boxes, S0.ncomp, 4, fabs=[torch.from_numpy(dU).cuda()]))
+                Jp, Jm, J2p, J2m = (float(x) for x in fx["config_Jamp"][m])
+                d1 = (Jp - Jm) / (2 * ha)
+                fd = (4 * d1 - (J2p - J2m) / (4 * ha)) / 3
+                perr.append({"mode": m, "amplitude_cm": float(fp.amps[m]), "h_cm": ha, "adjoint": ad, "tangent": tan,
+                             "fd_central": d1, "fd_richardson": fd, "rel_err_fd": abs(fd - ad) / abs(ad),
+                             "rel_err_tangent": abs(tan - ad) / abs(ad)})
+            res["wrinkle_amplitudes"] = perr
         op.close()
         del S0, L
         torch.cuda.empty_cache()
         return res
 
-    out["config_state"] = case(0.0, 20, True)
-    out["config_state"]["note"] = ("p and w exactly uniform: the limiter's acoustic slopes start at its "
-                                   "non-differentiable point mc(0,0), so state directions that make p "
-                                   "non-uniform have no linear derivative at t=0")
-    out["w_noise_state"] = case(1.0, 20, False)
+    out["config_state"] = case("config", 0.0, 20, True)
+    out["config_state"]["note"] = ("p and w uniform up to rounding: the limiter's acoustic slopes and the slopes of w "
+                                   "are evaluated at rounding-size arguments, so a finite step crosses its switches; "
+                                   "the tangent follows the adjoint's branches")
+    out["w_noise_state"] = case("wnoise", 1.0, 5, False)
     out["w_noise_state"]["note"] = "same state with seeded N(0, 1 cm/s) noise on w, as on u and v"
     return out
 

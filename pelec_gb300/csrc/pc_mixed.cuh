@@ -20,12 +20,17 @@
 // FP64 after the FP32 fields: diffusion is driven by their cell-to-cell
 // differences, which in the far field are ~1e-6 of X itself and would be lost
 // in FP32, and whose second differences (the conduction term of the energy
-// RHS) are ~1e-3 of T; the differences are taken in FP64 and rounded to FP32.  The internal energy of the Godunov
-// state is evaluated in FP64 (its formation-energy terms cancel to ~1e-2 of
-// their size, which FP32 cannot carry), at an FP64 density and composition:
-// the upwind cell's FP64 values plus FP32 increments (hydro_face_f).
+// RHS) are ~1e-3 of T.  Those FP64 values are stored as double-float pairs
+// (pc_ff.cuh: hi + lo, about 48 bits), so the flux pass forms their
+// differences on the FP32 pipe, to full FP32 accuracy of the difference.  The
+// internal energy of the Godunov state, whose formation-energy terms cancel
+// to ~1e-2 of their size, is evaluated in double-float arithmetic at a
+// double-float density and composition: the upwind cell's values plus FP32
+// increments (hydro_face_f); the energy fluxes formed from it are widened to
+// FP64 for the divergence.
 #pragma once
 
+#include "pc_ff.cuh"
 #include "pc_kernels.cuh"
 
 namespace pcg {
@@ -41,11 +46,29 @@ struct MechF {
   float gamma, gm1, cpk[NS];
   float const_mu, const_xi, const_lam, const_rhoD;
   float p_ref;
+  // double-float copies for the Godunov-state energy (e_rp_ff)
+  ff rWf[NS];
+  ff cpcf[2][6][NS];
+  ff gm1f, third, fifth;
 };
+
+// hi + lo of a double on the host (the pair ff_of gives on the device).
+inline ff ff_host(double x) {
+  const float h = (float)x;
+  return {h, (float)(x - (double)h)};
+}
 
 template <int NS>
 __host__ MechF<NS> to_float(const DevMech<NS>& m, double p_ref) {
   MechF<NS> f{};
+  for (int k = 0; k < NS; ++k) {
+    f.rWf[k] = ff_host(m.rW[k]);
+    for (int r = 0; r < 2; ++r)
+      for (int n = 0; n < 6; ++n) f.cpcf[r][n][k] = ff_host(m.cpc[r][n][k]);
+  }
+  f.gm1f = ff_host(m.gm1);
+  f.third = ff_host(1.0 / 3.0);
+  f.fifth = ff_host(0.2);
   for (int k = 0; k < NS; ++k) {
     f.rW[k] = (float)m.rW[k];
     f.cpk[k] = (float)m.cpk[k];
@@ -74,7 +97,8 @@ __host__ MechF<NS> to_float(const DevMech<NS>& m, double p_ref) {
 // FP64 fields stored after the FP32 fields of a mixed record, for the cells
 // whose faces the pass evaluates (the valid cells and one layer around
 // them): the mole fractions X_k (NS), the temperature, the density and the
-// mass fractions Y_k (NS), field n of cell c at [n N + c].  X and T enter the
+// mass fractions Y_k (NS), each a double-float pair (hi, lo) in an FP64-wide
+// slot, field n of cell c at [n N + c].  X and T enter the
 // diffusion fluxes only through differences between neighbouring cells,
 // which FP32 values would resolve to no better than 1e-4 K / 1e-7 (the
 // flame's second differences of T are a few K per cell).  rho and Y are the
@@ -83,9 +107,22 @@ __host__ MechF<NS> to_float(const DevMech<NS>& m, double p_ref) {
 // Rec<NS>::N FP32 fields of every cell (N ncell floats may be odd); with
 // 2 NS + 2 of them a mixed record stays within the FP64 record's size.
 template <int NS>
-__device__ __forceinline__ double* mixed_x(const DevBox& b) {
+__device__ __forceinline__ float2* mixed_x(const DevBox& b) {
   const long long nf = ((long long)Rec<NS>::N * b.ncell + 1) & ~1LL;
-  return reinterpret_cast<double*>(reinterpret_cast<float*>(b.rec) + nf);
+  return reinterpret_cast<float2*>(reinterpret_cast<float*>(b.rec) + nf);
+}
+__device__ __forceinline__ float2 to_pair(double x) {
+  const ff v = ff_of(x);
+  return make_float2(v.hi, v.lo);
+}
+__device__ __forceinline__ ff ld_pair(const float2* p) {
+  const float2 v = __ldg(p);
+  return {v.x, v.y};
+}
+// x1 - x2 of two stored pairs, rounded to FP32 (the hi parts of nearby
+// values subtract exactly; the lo parts carry the rest)
+__device__ __forceinline__ float pair_diff(ff a, ff b) {
+  return __fadd_rn(__fsub_rn(a.hi, b.hi), __fsub_rn(a.lo, b.lo));
 }
 // field index of the density in the FP64 part; Y_k follow it
 template <int NS>
@@ -303,18 +340,18 @@ __global__ void __launch_bounds__(kCellThreads)
                        k >= b.lo[2] - 1 && k <= b.hi[2] + 1;
     if (inner) {
       float X[NS];
-      double* xr = mixed_x<NS>(b) + c;
+      float2* xr = mixed_x<NS>(b) + c;
       const double irw = 1.0 / rw;
 #pragma unroll
       for (int n = 0; n < NS; ++n) {
         const double x = Y[n] * m.rW[n] * irw;
-        xr[n * N] = x;
+        xr[n * N] = to_pair(x);
         X[n] = (float)x;
       }
-      xr[NS * N] = T;
-      xr[kMixedRho<NS> * N] = rho;
+      xr[NS * N] = to_pair(T);
+      xr[kMixedRho<NS> * N] = to_pair(rho);
 #pragma unroll
-      for (int n = 0; n < NS; ++n) xr[(kMixedRho<NS> + 1 + n) * N] = Y[n];
+      for (int n = 0; n < NS; ++n) xr[(kMixedRho<NS> + 1 + n) * N] = to_pair(Y[n]);
       float out[NS + 3];
       TransF<NS, SIMPLE>::eval(mf, Tf, rhof, pf, Yf, X, out);
       r[RC::T * N] = Tf;
@@ -331,24 +368,43 @@ __global__ void __launch_bounds__(kCellThreads)
 }
 
 // FP32 hyperbolic face flux (not area-scaled); normal momentum without p_ref.
-// Internal energy at (rho, Y, p) in FP64 (RYP2E).
+// Internal energy at (rho, Y, p) in double-float arithmetic: the operations
+// of IdealMixEos::e_rp / GammaLawEos::e_rp (RYP2E), each a double-float one.
 template <int NS, bool MIX>
-__device__ __forceinline__ double e_rpY64(const DevMech<NS>& md, const double* Y, double rho, double p) {
-  const double rw = mix_rw<NS>(md, Y);
-  if constexpr (MIX)
-    return IdealMixEos<NS>::e_rp(md, Y, rw, rho, p);
-  else
-    return GammaLawEos<NS>::e_rp(md, Y, rw, rho, p);
+__device__ __forceinline__ ff e_rp_ff(const MechF<NS>& m, const ff* Y, ff rho, ff p) {
+  if constexpr (MIX) {
+    ff rw = ff_mul(Y[0], m.rWf[0]);
+#pragma unroll
+    for (int k = 1; k < NS; ++k) rw = ff_fma(Y[k], m.rWf[k], rw);
+    const ff T = ff_div(p, ff_mul(rho, rw));
+    const int r = T.hi < m.tmid ? 0 : 1;
+    ff C[6];
+#pragma unroll
+    for (int n = 0; n < 6; ++n) {
+      ff c = ff_mul(Y[0], m.cpcf[r][n][0]);
+#pragma unroll
+      for (int k = 1; k < NS; ++k) c = ff_fma(Y[k], m.cpcf[r][n][k], c);
+      C[n] = c;
+    }
+    // e = C5 + T ((C0 - rw) + T (C1/2 + T (C2/3 + T (C3/4 + T C4/5))))
+    ff q = ff_fma(T, ff_mul(C[4], m.fifth), ff_mul(C[3], 0.25f));
+    q = ff_fma(T, q, ff_mul(C[2], m.third));
+    q = ff_fma(T, q, ff_mul(C[1], 0.5f));
+    q = ff_fma(T, q, ff_sub(C[0], rw));
+    return ff_fma(T, q, C[5]);
+  } else {
+    return ff_div(p, ff_mul(m.gm1f, rho));
+  }
 }
 
-// The same from FP32 species densities rho Y_k and density rho.
+// The same at species densities rho Y_k (FP32) and density rho.
 template <int NS, bool MIX>
-__device__ __forceinline__ double e_rp_fp64(const DevMech<NS>& md, const float* rY, float rho, double p) {
-  const double r = (double)rho, ir = 1.0 / r;
-  double Y[NS];
+__device__ __forceinline__ ff e_rp_ff_rY(const MechF<NS>& m, const float* rY, float rho, ff p) {
+  const ff ir = ff_div(ff_of(1.f), ff_of(rho));
+  ff Y[NS];
 #pragma unroll
-  for (int n = 0; n < NS; ++n) Y[n] = (double)rY[n] * ir;
-  return e_rpY64<NS, MIX>(md, Y, r, p);
+  for (int n = 0; n < NS; ++n) Y[n] = ff_mul(ir, rY[n]);
+  return e_rp_ff<NS, MIX>(m, Y, ff_of(rho), p);
 }
 
 // FP64 internal energy from FP32 mass fractions Y (for Lax-Friedrichs sides).
@@ -537,31 +593,31 @@ __device__ __forceinline__ void hydro_face_f(const DevBox& b, const MechF<NS>& m
       flY[n] = g;
       rgd += g;
     }
-    const double gdpa = (double)gdp + (double)pref;
-    double regd;
+    const ff gdpa = ff_sum(gdp, pref);  // absolute pressure, exact
+    ff regd;
     if (!m0 && !clamped) {
       // The Godunov state has the upwind face's composition, and its density
       // is the upwind face's plus w drho (w: the star state's share).  Both
-      // are formed in FP64 as the upwind cell's FP64 values plus the FP32
-      // increments (slopes, star jump), so the FP32 rounding falls on the
-      // increments only: rho e carries the formation energies, which turn a
-      // 6e-8 rounding of Y_k or of rho into far more than rho e varies by
-      // across the flame.
+      // are formed in double-float arithmetic as the upwind cell's stored
+      // values plus the FP32 increments (slopes, star jump), so the FP32
+      // rounding falls on the increments only: rho e carries the formation
+      // energies, which turn a 6e-8 rounding of Y_k or of rho into far more
+      // than rho e varies by across the flame.
       const long long cu = mask ? cL : cR;
-      const double* xr = mixed_x<NS>(b) + cu;
+      const float2* xr = mixed_x<NS>(b) + cu;
       const float w = min_ ? 1.f : (mout ? 0.f : frac);
       const float H = mask ? HL : HR, irf = mask ? 1.f / rl : 1.f / rr;
-      const double rg = __ldg(xr + kMixedRho<NS> * N) + (double)(H + w * drho);
-      double Yg[NS];
+      const ff rg = ff_add(ld_pair(xr + kMixedRho<NS> * N), H + w * drho);
+      ff Yg[NS];
 #pragma unroll
       for (int n = 0; n < NS; ++n) {
-        const double y = __ldg(xr + (kMixedRho<NS> + 1 + n) * N);
+        const ff y = ld_pair(xr + (kMixedRho<NS> + 1 + n) * N);
         const float h = mask ? hL[n] : hR[n];
-        Yg[n] = y + (double)((h - (float)y * H) * irf);
+        Yg[n] = ff_add(y, (h - y.hi * H) * irf);
       }
-      regd = rg * e_rpY64<NS, MIX>(md, Yg, rg, gdpa);
+      regd = ff_mul(rg, e_rp_ff<NS, MIX>(m, Yg, rg, gdpa));
     } else {
-      regd = (double)rgd * e_rp_fp64<NS, MIX>(md, flY, rgd, gdpa);
+      regd = ff_mul(e_rp_ff_rY<NS, MIX>(m, flY, rgd, gdpa), rgd);
     }
     const float iua = iu + Unf, iv1a = iv1 + Ut1f, iv2a = iv2 + Ut2f;  // absolute velocities
     fl_rho = rgd * iua;
@@ -570,9 +626,10 @@ __device__ __forceinline__ void hydro_face_f(const DevBox& b, const MechF<NS>& m
     fl_un = fl_rho * iua + gdp;  // p_ref dropped: zero divergence
     fl_ut1 = fl_rho * iv1a;
     fl_ut2 = fl_rho * iv2a;
-    const double iud = Un + (double)iu;  // FP64: U + u'
-    fl_E = iud * (regd + (double)(0.5f * rgd * (iua * iua + iv1a * iv1a + iv2a * iv2a)) + gdpa);
-    fl_ei = iud * regd;
+    const ff iud = ff_add(ff_of(Un), iu);  // U + u' in double-float
+    const ff tot = ff_add(ff_add(regd, 0.5f * rgd * (iua * iua + iv1a * iv1a + iv2a * iv2a)), gdpa);
+    fl_E = ff_to_double(ff_mul(iud, tot));
+    fl_ei = ff_to_double(ff_mul(iud, regd));
   } else {
     // Lax-Friedrichs on absolute velocities (U + u')
     const float unlA = unl + Unf, unrA = unr + Unf, ut1lA = ut1l + Ut1f, ut1rA = ut1r + Ut1f;
@@ -623,7 +680,7 @@ __device__ __forceinline__ void diffusion_face_f(const DevBox& b, const DevFlags
   const float* rec = reinterpret_cast<const float*>(b.rec);
   const long long N = b.ncell;
   auto ld = [&](int fld, long long c) { return __ldg(rec + (long long)fld * N + c); };
-  const double* xrec = mixed_x<NS>(b);
+  const float2* xrec = mixed_x<NS>(b);
   const long long cL = cR - stv[d];
   const bool harm = f.harmonic != 0;
   const float mu = face_coeff(ld(RC::MU, cR), ld(RC::MU, cL), harm);
@@ -653,7 +710,7 @@ __device__ __forceinline__ void diffusion_face_f(const DevBox& b, const DevFlags
     else
       tau[a] = mu * (grad[d][a] + grad[a][d]);
   }
-  const float dT = (float)(__ldg(xrec + NS * N + cR) - __ldg(xrec + NS * N + cL));
+  const float dT = pair_diff(ld_pair(xrec + NS * N + cR), ld_pair(xrec + NS * N + cL));
   // the work term needs absolute velocities: the offsets plus the box's reference
   const float Uf[3] = {(float)U[0], (float)U[1], (float)U[2]};
   float fE = 0.5f * (-tau[0] * (uR[0] + uL[0] + 2.f * Uf[0]) - tau[1] * (uR[1] + uL[1] + 2.f * Uf[1]) -
@@ -669,9 +726,9 @@ __device__ __forceinline__ void diffusion_face_f(const DevBox& b, const DevFlags
     float Vc = 0.f;
 #pragma unroll
     for (int n = 0; n < NS; ++n) {
-      const double x1 = __ldg(xrec + n * N + cR), x2 = __ldg(xrec + n * N + cL);
-      const float dX = (float)(x1 - x2);
-      const float Xface = (float)(0.5 * (x1 + x2));
+      const ff x1 = ld_pair(xrec + n * N + cR), x2 = ld_pair(xrec + n * N + cL);
+      const float dX = pair_diff(x1, x2);
+      const float Xface = 0.5f * ((x1.hi + x2.hi) + (x1.lo + x2.lo));
       const float y1 = ld(RC::Y + n, cR), y2 = ld(RC::Y + n, cL);
       Yf[n] = 0.5f * (y1 + y2);
       hf[n] = 0.5f * (ld(RC::H + n, cR) + ld(RC::H + n, cL));

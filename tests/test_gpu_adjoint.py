@@ -66,21 +66,22 @@ def _scale_direction(st, rng):
 
 
 def _fd(oracle_lib, cfg, st, mu, v, h):
-    """Richardson-extrapolated central difference of <mu, RHS(U + t v)> at
-    t = 0 from the steps h and 2 h (truncation error O(h^4))."""
+    """Central difference of <mu, RHS(U + t v)> at t = 0."""
     def J(t):
         S = st.S.copy()
         S[:, 2:-2, 2:-2, 2:-2] += t * v
         R, = oracle_lib.mol_rhs(cfg, [problems.BoxState(st.lo, st.hi, S, st.dx)])
         return float((mu * R).sum())
 
-    d1 = (J(h) - J(-h)) / (2.0 * h)
-    d2 = (J(2 * h) - J(-2 * h)) / (4.0 * h)
-    return (4.0 * d1 - d2) / 3.0
+    return (J(h) - J(-h)) / (2.0 * h)
 
 
-# step of the difference quotients: a relative change of the state of 1e-6
-FD_H = 1e-6
+# Step of the difference quotients, a relative change of the state: one fixed
+# value for every case.  A step of 1e-6 or more moves some limiter argument of
+# the box across a min/max switch (errors of 1e-5 to 1e-2 on these flames),
+# where the quotient measures another branch than the derivative; at 1e-7 the
+# rounding of <mu, RHS> stays below the bar and no switch is crossed.
+FD_H = 1e-7
 
 
 @pytest.mark.parametrize("kind", ["tgv", "flame", "flame_noslope"])

@@ -94,3 +94,24 @@ def test_mixed_flag_variants(cuda_lib, oracle_lib, case):
     (gpu,), _ = gpu_rhs(cuda_lib, problems.make_config(mech, precision=abi.PC_PRECISION_MIXED, **kw), [st])
     l2 = rel_l2(gpu, ref)
     assert np.all(l2 <= _tol(case)), (case, l2)
+
+
+def test_c4_mixed_256_against_fp64_oracle(cuda_lib, oracle_lib):
+    """C4: the 256^3 flame.  The FP64 form equals the oracle bit for bit; the
+    mixed form's per-component relative L2 and max error against the FP64
+    oracle are printed, and L2 must be within MIXED_L2 on every component."""
+    import torch
+
+    mol = cuda_lib
+    mech, st, _ = problems.flame((256, 256, 256), seed=1)
+    ref, = oracle_lib.mol_rhs(problems.make_config(mech), [st])
+    (g64,), _ = gpu_rhs(mol, problems.make_config(mech), [st])
+    np.testing.assert_array_equal(g64, ref)
+    del g64
+    (gm,), status = gpu_rhs(mol, problems.make_config(mech, precision=abi.PC_PRECISION_MIXED), [st])
+    l2, mx = rel_l2(gm, ref), rel_max(gm, ref)
+    print("C4 256^3 mixed vs FP64 oracle, rel L2 per component:", l2)
+    print("C4 256^3 mixed vs FP64 oracle, rel max per component:", mx)
+    assert status.nonfinite_output == 0
+    assert np.all(l2 <= _tol()), l2
+    torch.cuda.empty_cache()
