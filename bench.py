@@ -346,15 +346,22 @@ def bench_level(args, rank: int, local: int, maxover, barrier) -> dict:
     return out
 
 
-def bench_sub_box(args, name: str, rank: int, maxover, barrier) -> dict:
+def bench_sub_box(args, name: str, rank: int, maxover, barrier, nspec: int = 9) -> dict:
     """FP64 and mixed RHS of another single-box workload (device-resident,
-    autotuned launch), with the mixed form's error against the FP64 result."""
+    autotuned launch), with the mixed form's error against the FP64 result.
+    nspec = 21: the same flame with the synthetic 21-species mechanism."""
     import numpy as np
     import torch
 
-    from pelec_gb300 import abi, mol, problems
+    from pelec_gb300 import abi, mechanism, mol, problems
 
-    mech, st, desc = workload(name, seed=1 + rank)
+    if nspec == 21:
+        n = 128 if name == "c2" else 256
+        mech, st, _ = problems.flame((n, n, n), seed=1 + rank, mech=mechanism.drm_synthetic())
+        desc = (f"{name.upper()} geometry ({n}^3 flame) with 21 species (synthetic table in DRM19 species order): "
+                "the kernels instantiated for NUM_SPECIES = 21")
+    else:
+        mech, st, desc = workload(name, seed=1 + rank)
     S = mol.MultiFab([(st.lo, st.hi)], st.S.shape[0], st.ng, fabs=[torch.from_numpy(st.S).cuda()])
     R = mol.MultiFab(S.boxes, S.ncomp, 0)
     stream = torch.cuda.current_stream()
@@ -362,7 +369,7 @@ def bench_sub_box(args, name: str, rank: int, maxover, barrier) -> dict:
     res = {}
     for prec, form in ((abi.PC_PRECISION_FP64, "fp64"), (abi.PC_PRECISION_MIXED, "mixed")):
         op = mol.MOLOperator(problems.make_config(mech, time_passes=1, precision=prec))
-        best, _ = op.autotune(S, R, st.dx, reps=3)
+        best, tune_ms = op.autotune(S, R, st.dx, reps=3)
         for _ in range(max(3, args.warmup)):
             op.rhs_level(S, R, st.dx)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -377,6 +384,7 @@ def bench_sub_box(args, name: str, rank: int, maxover, barrier) -> dict:
         torch.cuda.synchronize()
         res[form] = R.fabs[0].cpu().numpy()
         out[form] = {"value": st.ncells / t, "ms_per_step": 1e3 * t, "flux_launch": launch_name(best),
+                     "autotune_ms_per_launch": {launch_name(q): v for q, v in enumerate(tune_ms)},
                      "gpu_launches_per_step": launches_per_rhs(form)}
         op.close()
     a, b = res["mixed"], res["fp64"]
@@ -808,9 +816,11 @@ def run_gpu(args):
     fs_m = [float(np.abs(r32[n] - r64[n]).max() / max(flux_scale[n], 1e-300)) for n in range(r64.shape[0])]
 
     opm.close()
-    sub = None
+    sub = sub21 = None
     if args.workload != "c2" and not args.no_c2:
         sub = bench_sub_box(args, "c2", rank, maxover, barrier)
+    if not args.no_c2:
+        sub21 = bench_sub_box(args, "c2", rank, maxover, barrier, nspec=21)
     stepg = None if args.no_level else bench_step_graph(args, rank, maxover, barrier)
     level = None if args.no_level else bench_level(args, rank, local, maxover, barrier)
     adj = None if args.no_adjoint else bench_adjoint_rhs(args, st, mech, S, maxover, barrier)
@@ -886,6 +896,8 @@ def run_gpu(args):
         line["cpu_baseline"] = cpu
     if sub is not None:
         line["c2"] = sub
+    if sub21 is not None:
+        line["c2_21_species"] = sub21
     if stepg is not None:
         line["step_graph"] = stepg
     if level is not None:

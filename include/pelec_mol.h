@@ -31,8 +31,8 @@
 extern "C" {
 #endif
 
-#define PC_MOL_ABI_VERSION 1
-#define PC_MAX_SPECIES 9
+#define PC_MOL_ABI_VERSION 2
+#define PC_MAX_SPECIES 21
 
 /* Return codes. */
 typedef enum pc_status_code {
@@ -108,7 +108,9 @@ typedef struct pc_mechanism {
  * getMOLSrcTerm (Source/Params/_cpp_parameters; defaults in
  * Source/Params/param_includes/pelec_defaults.H:32-57). */
 typedef struct pc_mol_config {
-  int nspec;                   /* NUM_SPECIES: 1 or 9                        */
+  int nspec;                   /* NUM_SPECIES: 1 (GammaLaw, constant
+                                  transport), 9 or 21 (ideal mixture,
+                                  mixture-averaged transport)                */
   int eos;                     /* pc_eos_kind                                */
   int transport;               /* pc_transport_kind                          */
   int precision;               /* pc_precision                               */

@@ -100,6 +100,8 @@ int oracle_mol_rhs(const pc_mol_config* cfg, const pc_box_desc* boxes, int nboxe
       rc = dispatch<1>(*cfg, boxes[b], dx, fails);
     else if (cfg->nspec == 9)
       rc = dispatch<9>(*cfg, boxes[b], dx, fails);
+    else if (cfg->nspec == 21)
+      rc = dispatch<21>(*cfg, boxes[b], dx, fails);
     else
       return PC_ERR_UNSUPPORTED;
     if (rc != PC_OK) return rc;
@@ -121,6 +123,8 @@ int oracle_mol_rhs_fluxes(const pc_mol_config* cfg, const pc_box_desc* boxes, in
       rc = dispatch<1>(*cfg, boxes[b], dx, fails, fluxes + 3 * b);
     else if (cfg->nspec == 9)
       rc = dispatch<9>(*cfg, boxes[b], dx, fails, fluxes + 3 * b);
+    else if (cfg->nspec == 21)
+      rc = dispatch<21>(*cfg, boxes[b], dx, fails, fluxes + 3 * b);
     else
       return PC_ERR_UNSUPPORTED;
     if (rc != PC_OK) return rc;
@@ -146,6 +150,8 @@ int oracle_ctoprim_cell(const pc_mol_config* cfg, const double* U, double* q, do
     ctoprim<1>(0, 0, 0, u, qa, qx, IdealMix<1>{&cfg->mech, maxit}, fails);
   } else if (ns == 9 && cfg->eos == PC_EOS_GAMMA_LAW) {
     ctoprim<9>(0, 0, 0, u, qa, qx, GammaLaw<9>{&cfg->mech}, fails);
+  } else if (ns == 21 && cfg->eos == PC_EOS_IDEAL_MIX) {
+    ctoprim<21>(0, 0, 0, u, qa, qx, IdealMix<21>{&cfg->mech, maxit}, fails);
   } else {
     return PC_ERR_UNSUPPORTED;
   }
@@ -250,6 +256,8 @@ int oracle_compute_temp(const pc_mol_config* cfg, int nboxes, const int* lohi, c
     ct_boxes<1>(nboxes, lohi, st, GammaLaw<1>{&cfg->mech}, fails);
   else if (cfg->nspec == 9 && cfg->eos == PC_EOS_IDEAL_MIX)
     ct_boxes<9>(nboxes, lohi, st, IdealMix<9>{&cfg->mech, maxit}, fails);
+  else if (cfg->nspec == 21 && cfg->eos == PC_EOS_IDEAL_MIX)
+    ct_boxes<21>(nboxes, lohi, st, IdealMix<21>{&cfg->mech, maxit}, fails);
   else
     return PC_ERR_UNSUPPORTED;
   if (newton_fail) *newton_fail = fails;
@@ -276,6 +284,9 @@ int oracle_est_dt(const pc_mol_config* cfg, const pc_box_desc* boxes, int nboxes
     } else if (cfg->nspec == 9 && cfg->eos == PC_EOS_IDEAL_MIX) {
       IdealMix<9> eos{&cfg->mech, 50};
       est_dt<9>(v, view(boxes[b].state), eos, SimpleTransport<9, IdealMix<9>>{&cfg->mech}, dx, o);
+    } else if (cfg->nspec == 21 && cfg->eos == PC_EOS_IDEAL_MIX) {
+      IdealMix<21> eos{&cfg->mech, 50};
+      est_dt<21>(v, view(boxes[b].state), eos, SimpleTransport<21, IdealMix<21>>{&cfg->mech}, dx, o);
     } else {
       return PC_ERR_UNSUPPORTED;
     }

@@ -31,7 +31,7 @@ ROOT = os.path.dirname(HERE)
 REF_ROOT = os.environ.get("PC_REFERENCE_ROOT", "/root/reference")
 REF_SRC = os.path.join(REF_ROOT, "Source")
 OUTDIR = os.path.join(HERE, "_ref")
-SPECIES = (1, 9)
+SPECIES = (1, 9, 21)
 REF_FILES = ("MOL.cpp", "MOL.H", "Riemann.H", "Diffterm.H", "Utilities.H", "TransCoeff.H", "Timestep.H", "IndexDefines.H",
              "Constants.H", "EBStencilTypes.H")
 

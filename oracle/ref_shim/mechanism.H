@@ -1,6 +1,6 @@
 // mechanism.H — ORACLE test infrastructure: the species count of the compiled
 // mechanism (PelePhysics' generated mechanism.H), set per build by
-// oracle/ref_build.py (-DPC_REF_NS=1 or 9).
+// oracle/ref_build.py (-DPC_REF_NS=1, 9 or 21).
 #pragma once
 
 #ifndef PC_REF_NS

@@ -12,8 +12,8 @@ from __future__ import annotations
 import ctypes
 from ctypes import c_double, c_int, c_longlong, c_void_p, POINTER
 
-PC_MAX_SPECIES = 9
-PC_MOL_ABI_VERSION = 1
+PC_MAX_SPECIES = 21
+PC_MOL_ABI_VERSION = 2
 
 PC_OK = 0
 PC_ERR_INVALID_ARGUMENT = 1

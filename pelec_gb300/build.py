@@ -1,8 +1,8 @@
 """Build recipe of the CUDA library ``pelec_gb300/_lib/libpelec_mol.so``.
 
-Seven translation units compiled by nvcc for sm_103a only (in parallel) and
+Translation units compiled by nvcc for sm_103a only (in parallel) and
 linked into one shared library with a plain C ABI (include/pelec_mol.h), no
-torch headers:
+torch headers; the kernels are instantiated for 1, 9 and 21 species:
 
 * pc_mol.cu — the ABI, the host side and the FP64 kernels, compiled with
   ``-fmad=false``: the FP64 kernels evaluate a fixed sequence of IEEE
@@ -11,7 +11,8 @@ torch headers:
   too.
 * pc_mol_mixed.cu — the mixed-precision kernels, with contraction on.
 * pc_tiles_fp64.cu / pc_tiles_mixed.cu — the flux pass of each precision at
-  the tile shapes other than the default, compiled like the unit above them.
+  the tile shapes other than the default, compiled like the unit above them
+  (pc_tiles_fp64.cu once per species count, like the two below).
 * pc_adjoint.cu — the vector-Jacobian product passes, without contraction
   (their re-evaluated forward quantities must be the forward's own).
 * pc_tangent.cu — the Jacobian-vector product (the forward passes on dual
@@ -35,11 +36,13 @@ LIBDIR = os.path.join(HERE, "_lib")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off"]
 
+# The units with the heaviest kernels are compiled once per species count
+# (pc_unit_ns.h), so that the compilations run in parallel.
+_PER_NS = [(src, ["-fmad=false", f"-DPC_UNIT_NS={ns}"]) for src in ("pc_tiles_fp64.cu", "pc_adjoint.cu", "pc_tangent.cu")
+           for ns in (1, 9, 21)]
 LIBS = {
     "libpelec_mol.so": [("pc_mol.cu", ["-fmad=false"]), ("pc_mol_mixed.cu", ["-fmad=true"]),
-                        ("pc_tiles_fp64.cu", ["-fmad=false"]), ("pc_tiles_mixed.cu", ["-fmad=true"]),
-                        ("pc_adjoint.cu", ["-fmad=false"]), ("pc_tangent.cu", ["-fmad=false"]),
-                        ("pc_rhs_rcp.cu", ["-fmad=false"])],
+                        ("pc_tiles_mixed.cu", ["-fmad=true"]), ("pc_rhs_rcp.cu", ["-fmad=false"])] + _PER_NS,
     # arithmetic peak rates for bench.py's roofline (not part of the ABI)
     "libpc_peaks.so": [("pc_peaks.cu", ["-fmad=true"])],
 }
@@ -71,7 +74,8 @@ def build(force: bool = False, verbose: bool = False) -> list:
             continue
         procs, objs = [], []
         for src, flags in units:
-            obj = os.path.join(LIBDIR, os.path.splitext(src)[0] + ".o")
+            tag = "".join("_ns" + f.split("=")[1] for f in flags if f.startswith("-DPC_UNIT_NS="))
+            obj = os.path.join(LIBDIR, os.path.splitext(src)[0] + tag + ".o")
             cmd = [nvcc(), *ARCH, *COMMON, *flags, "-I", os.path.join(ROOT, "include"), "-c", "-o", obj,
                    os.path.join(CSRC, src)]
             if verbose:

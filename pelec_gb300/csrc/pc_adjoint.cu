@@ -5,6 +5,7 @@
 #include <algorithm>
 
 #include "pc_adjoint.cuh"
+#include "pc_unit_ns.h"
 
 namespace pcg {
 
@@ -12,35 +13,43 @@ namespace pcg {
 // cotangents again, both of which return at once unless the fast pass counted
 // a lane that needs a real division), then the cell adjoint.  recbar holds
 // nrecbar doubles, cleared by the caller.
-cudaError_t launch_vjp_passes(int variant, const DevBox* boxes, const AdjBox* adj, const int2* items, int nitems,
-                              const int4* fitems, int nfitems, double* recbar, long long nrecbar,
-                              const long long* recbar_off, const DevMech<1>& m1, const DevMech<9>& m9,
-                              const DevFlags& f, const Geo& g, unsigned long long* counters, cudaStream_t s) {
+template <int NS>
+cudaError_t vjp_passes_ns(const DevBox* boxes, const AdjBox* adj, const int2* items, int nitems, const int4* fitems,
+                          int nfitems, double* recbar, long long nrecbar, const long long* recbar_off,
+                          const DevMech<NS>& m, const DevFlags& f, const Geo& g, unsigned long long* counters,
+                          cudaStream_t s) {
+  using P = Physics<NS>;
   if (nfitems > 0) {
-    if (variant == 1)
-      face_adjoint_kernel<1, GammaLawEos<1>, false><<<nfitems, kAdjThreads, 0, s>>>(boxes, adj, fitems, recbar,
-                                                                                   recbar_off, m1, f, g, counters);
-    else
-      face_adjoint_kernel<9, IdealMixEos<9>, false><<<nfitems, kAdjThreads, 0, s>>>(boxes, adj, fitems, recbar,
-                                                                                   recbar_off, m9, f, g, counters);
+    face_adjoint_kernel<NS, typename P::EOS, false><<<nfitems, kAdjThreads, 0, s>>>(boxes, adj, fitems, recbar,
+                                                                                   recbar_off, m, f, g, counters);
     zero_recbar_if_slow<<<(unsigned)std::min<long long>((nrecbar + 255) / 256, 152LL * 8), 256, 0, s>>>(
         recbar, nrecbar, counters);
-    if (variant == 1)
-      face_adjoint_kernel<1, GammaLawEos<1>, true><<<nfitems, kAdjThreads, 0, s>>>(boxes, adj, fitems, recbar,
-                                                                                  recbar_off, m1, f, g, counters);
-    else
-      face_adjoint_kernel<9, IdealMixEos<9>, true><<<nfitems, kAdjThreads, 0, s>>>(boxes, adj, fitems, recbar,
-                                                                                  recbar_off, m9, f, g, counters);
+    face_adjoint_kernel<NS, typename P::EOS, true><<<nfitems, kAdjThreads, 0, s>>>(boxes, adj, fitems, recbar,
+                                                                                  recbar_off, m, f, g, counters);
   }
-  if (nitems > 0) {
-    if (variant == 1)
-      cell_adjoint_kernel<1, GammaLawEos<1>, ConstantTransport<1>>
-          <<<nitems, kCellThreads, 0, s>>>(boxes, adj, items, recbar, recbar_off, m1, f);
-    else
-      cell_adjoint_kernel<9, IdealMixEos<9>, SimpleTransport<9>>
-          <<<nitems, kCellThreads, 0, s>>>(boxes, adj, items, recbar, recbar_off, m9, f);
-  }
+  if (nitems > 0)
+    cell_adjoint_kernel<NS, typename P::EOS, typename P::TR>
+        <<<nitems, kCellThreads, 0, s>>>(boxes, adj, items, recbar, recbar_off, m, f);
   return cudaGetLastError();
 }
+
+#define PC_VJP_INST(NS)                                                                                          \
+  template cudaError_t vjp_passes_ns<NS>(const DevBox*, const AdjBox*, const int2*, int, const int4*, int,       \
+                                         double*, long long, const long long*, const DevMech<NS>&,               \
+                                         const DevFlags&, const Geo&, unsigned long long*, cudaStream_t);
+PC_UNIT_INSTANTIATE(PC_VJP_INST)
+
+#if PC_UNIT_HAS(1)  // the dispatcher lives in the one-species compilation
+cudaError_t launch_vjp_passes(int nspec, const DevBox* boxes, const AdjBox* adj, const int2* items, int nitems,
+                              const int4* fitems, int nfitems, double* recbar, long long nrecbar,
+                              const long long* recbar_off, const MechSet& ms, const DevFlags& f, const Geo& g,
+                              unsigned long long* counters, cudaStream_t s) {
+  return with_species(nspec, [&](auto ns) {
+    constexpr int NS = decltype(ns)::value;
+    return vjp_passes_ns<NS>(boxes, adj, items, nitems, fitems, nfitems, recbar, nrecbar, recbar_off, ms.get<NS>(),
+                             f, g, counters, s);
+  });
+}
+#endif
 
 }  // namespace pcg

@@ -12,6 +12,8 @@
 #include <math_constants.h>
 #include <stdint.h>
 
+#include <type_traits>
+
 #include "pc_exp.h"
 
 // A translation unit may compile this code a second time with quotients by a
@@ -562,6 +564,63 @@ __device__ __forceinline__ double mc_limit(double dl, double dr) {
   const unsigned long long al = dbits(dl) & ~kSign, ar = dbits(dr) & ~kSign;
   const unsigned long long dlim = (dl * dr >= 0.0) ? twice_mag(al < ar ? al : ar) : 0ULL;
   return dfrom((dlim < acen ? dlim : acen) | sgn);
+}
+
+// ---------------------------------------------------------------------------
+// Species counts with compiled kernels.  NUM_SPECIES is a compile-time
+// constant of the reference's mechanism (Source/IndexDefines.H:4); the
+// library instantiates its passes for these counts: 1 (GammaLaw EOS with
+// constant transport) and 9 and 21 (ideal mixture with mixture-averaged
+// transport; H2/air-sized and DRM19-sized mechanisms).
+// ---------------------------------------------------------------------------
+template <int NS>
+struct Physics {  // ideal-gas mixture, mixture-averaged transport
+  using EOS = IdealMixEos<NS>;
+  using TR = SimpleTransport<NS>;
+  static constexpr bool MIX = true;
+};
+template <>
+struct Physics<1> {  // one species: GammaLaw, constant transport
+  using EOS = GammaLawEos<1>;
+  using TR = ConstantTransport<1>;
+  static constexpr bool MIX = false;
+};
+
+// The device species tables of every compiled count (only the handle's
+// count is filled).
+struct MechSet {
+  DevMech<1> m1;
+  DevMech<9> m9;
+  DevMech<21> m21;
+  template <int NS>
+  const DevMech<NS>& get() const {
+    if constexpr (NS == 1)
+      return m1;
+    else if constexpr (NS == 9)
+      return m9;
+    else
+      return m21;
+  }
+  template <int NS>
+  DevMech<NS>& get() {
+    if constexpr (NS == 1)
+      return m1;
+    else if constexpr (NS == 9)
+      return m9;
+    else
+      return m21;
+  }
+};
+
+template <int NS>
+using SpeciesCount = std::integral_constant<int, NS>;
+
+// f(SpeciesCount<NS>{}) for the species count of a handle (1, 9 or 21).
+template <class F>
+inline auto with_species(int nspec, F&& f) {
+  if (nspec == 1) return f(SpeciesCount<1>{});
+  if (nspec == 21) return f(SpeciesCount<21>{});
+  return f(SpeciesCount<9>{});
 }
 
 }  // namespace PCG_NAMESPACE

@@ -127,7 +127,8 @@ __device__ __forceinline__ float pair_diff(ff a, ff b) {
 // field index of the density in the FP64 part; Y_k follow it
 template <int NS>
 constexpr int kMixedRho = NS + 1;
-static_assert(2 * 9 + 2 <= Rec<9>::N / 2 && 2 * 1 + 2 <= Rec<1>::N / 2, "mixed record exceeds the FP64 record");
+static_assert(2 * 21 + 2 <= Rec<21>::N / 2 && 2 * 9 + 2 <= Rec<9>::N / 2 && 2 * 1 + 2 <= Rec<1>::N / 2,
+              "mixed record exceeds the FP64 record");
 
 // Reference velocity of a box: the velocity of its first valid cell (lo
 // corner), in FP64 (0 where that is not finite).  The FP32 records hold the

@@ -22,20 +22,19 @@
 #include "pelec_mol.h"
 
 namespace pcg {
-int launch_mixed(int variant, int tile, bool persistent, const DevBox* boxes, const int2* items, int nitems,
-                 const int4* tiles, int ntiles, const DevMech<1>& m1, const DevMech<9>& m9, const DevFlags& f,
-                 const Geo& g, double p_ref, unsigned long long* counters, cudaStream_t s, cudaEvent_t e0,
-                 cudaEvent_t e1, cudaEvent_t e2);
-cudaError_t launch_flux_fp64_tile(int tile, bool persistent, int variant, const DevBox* boxes, const int4* tiles,
-                                  int ntiles, const DevMech<1>& m1, const DevMech<9>& m9, const DevFlags& f,
-                                  const Geo& g, unsigned long long* counters, cudaStream_t s, const FluxBox* fx);
-cudaError_t launch_vjp_passes(int variant, const DevBox* boxes, const AdjBox* adj, const int2* items, int nitems,
+int launch_mixed(int nspec, int tile, bool persistent, const DevBox* boxes, const int2* items, int nitems,
+                 const int4* tiles, int ntiles, const MechSet& ms, const DevFlags& f, const Geo& g, double p_ref,
+                 unsigned long long* counters, cudaStream_t s, cudaEvent_t e0, cudaEvent_t e1, cudaEvent_t e2);
+cudaError_t launch_flux_fp64_tile(int tile, bool persistent, int nspec, const DevBox* boxes, const int4* tiles,
+                                  int ntiles, const MechSet& ms, const DevFlags& f, const Geo& g,
+                                  unsigned long long* counters, cudaStream_t s, const FluxBox* fx);
+cudaError_t launch_vjp_passes(int nspec, const DevBox* boxes, const AdjBox* adj, const int2* items, int nitems,
                               const int4* fitems, int nfitems, double* recbar, long long nrecbar,
-                              const long long* recbar_off, const DevMech<1>& m1, const DevMech<9>& m9,
-                              const DevFlags& f, const Geo& g, unsigned long long* counters, cudaStream_t s);
-cudaError_t launch_jvp_passes(int variant, const DevBox* boxes, const TanBox* tans, const int2* items, int nitems,
-                              const int4* tiles, int ntiles, const DevMech<1>& m1, const DevMech<9>& m9,
-                              const DevFlags& f, const Geo& g, unsigned long long* counters, cudaStream_t s);
+                              const long long* recbar_off, const MechSet& ms, const DevFlags& f, const Geo& g,
+                              unsigned long long* counters, cudaStream_t s);
+cudaError_t launch_jvp_passes(int nspec, const DevBox* boxes, const TanBox* tans, const int2* items, int nitems,
+                              const int4* tiles, int ntiles, const MechSet& ms, const DevFlags& f, const Geo& g,
+                              unsigned long long* counters, cudaStream_t s);
 }  // namespace pcg
 
 namespace {
@@ -55,9 +54,8 @@ struct Layout {
 struct pc_mol_handle {
   pc_mol_config cfg{};
   int device = 0;
-  int variant = 0;  // 1: NS=1 GammaLaw/Constant, 9: NS=9 IdealMix/Simple
-  DevMech<1> mech1{};
-  DevMech<9> mech9{};
+  int variant = 0;  // the species count: 1 (GammaLaw/Constant), 9 or 21 (IdealMix/Simple)
+  MechSet mech{};
   DevFlags flags{};
   int nrec = 0;
   unsigned long long* d_counters = nullptr;
@@ -173,6 +171,30 @@ int fill_simple(DevMech<NS>& d, const pc_mechanism& m) {
   if (!(m.diff_pref > 0.0)) return PC_ERR_INVALID_ARGUMENT;
   d.inv_pref = 1.0 / m.diff_pref;
   return PC_OK;
+}
+
+// The species count whose kernels serve c (0: none compiled): one species
+// with the GammaLaw EOS and constant transport, or 9 or 21 species with the
+// ideal-gas mixture and mixture-averaged transport.
+int compiled_variant(const pc_mol_config& c) {
+  if (c.nspec == 1 && c.eos == PC_EOS_GAMMA_LAW && c.transport == PC_TRANSPORT_CONSTANT) return 1;
+  if ((c.nspec == 9 || c.nspec == 21) && c.eos == PC_EOS_IDEAL_MIX && c.transport == PC_TRANSPORT_SIMPLE)
+    return c.nspec;
+  return 0;
+}
+
+// The device tables of the species count nspec from m; *nrec: doubles per record.
+int fill_mechanism(MechSet& ms, int nspec, const pc_mechanism& m, int* nrec) {
+  return with_species(nspec, [&](auto ns) {
+    constexpr int NS = decltype(ns)::value;
+    DevMech<NS>& d = ms.get<NS>();
+    fill_common(d, m);
+    *nrec = Rec<NS>::N;
+    if constexpr (NS == 1) return (int)PC_OK;
+    int rc = fill_idealmix(d, m);
+    if (rc == PC_OK) rc = fill_simple(d, m);
+    return rc;
+  });
 }
 
 bool covers(const pc_array4& a, const int lo[3], const int hi[3], int ng) {
@@ -390,7 +412,7 @@ int launch(pc_mol_handle* h, const DevMech<NS>& mech, const Geo& g, int ibeg, in
   const bool pers = h->tile >= kNumTiles;
   cudaError_t e = (h->lay_tile != 0)
                       ? launch_flux_fp64_tile(h->lay_tile, pers, h->variant, h->d_boxes, h->d_tiles + tbeg, tend - tbeg,
-                                              h->mech1, h->mech9, h->flags, g, h->d_counters, s, fx)
+                                              h->mech, h->flags, g, h->d_counters, s, fx)
                       : launch_flux_fp64<NS, EOS>(h->d_boxes, h->d_tiles + tbeg, tend - tbeg, mech, h->flags, g,
                                                   h->d_counters, s, fx, pers);
   if (e == cudaSuccess)
@@ -432,13 +454,12 @@ int run(pc_mol_handle* h, const pc_box_desc* boxes, int nboxes, const double dx[
       a.nitems = ie - ib;
       a.tiles = h->d_tiles + tb;
       a.ntiles = te - tb;
-      if (h->variant == 1) {
-        a.mech = &h->mech1;
-        a.mech_size = sizeof h->mech1;
-      } else {
-        a.mech = &h->mech9;
-        a.mech_size = sizeof h->mech9;
-      }
+      with_species(h->variant, [&](auto ns) {
+        constexpr int NS = decltype(ns)::value;
+        a.mech = &h->mech.get<NS>();
+        a.mech_size = sizeof(DevMech<NS>);
+        return 0;
+      });
       a.flags = &h->flags;
       a.flags_size = sizeof h->flags;
       a.geo = &g;
@@ -456,13 +477,15 @@ int run(pc_mol_handle* h, const pc_box_desc* boxes, int nboxes, const double dx[
       Geo gm = g;
       gm.p_ref = p_ref;
       const int rc = launch_mixed(h->variant, h->lay_tile, h->tile >= kNumTiles, h->d_boxes, h->d_items + ib, ie - ib,
-                                  h->d_tiles + tb, te - tb, h->mech1, h->mech9, h->flags, gm, p_ref, h->d_counters, s,
+                                  h->d_tiles + tb, te - tb, h->mech, h->flags, gm, p_ref, h->d_counters, s,
                                   timed ? h->ev[0] : nullptr, timed ? h->ev[1] : nullptr, timed ? h->ev[2] : nullptr);
       return rc == 0 ? PC_OK : cuda_fail(h, cudaGetLastError());
     }
-    if (h->variant == 1)
-      return launch<1, GammaLawEos<1>, ConstantTransport<1>>(h, h->mech1, g, ib, ie, tb, te, s, timed, fx);
-    return launch<9, IdealMixEos<9>, SimpleTransport<9>>(h, h->mech9, g, ib, ie, tb, te, s, timed, fx);
+    return with_species(h->variant, [&](auto ns) {
+      constexpr int NS = decltype(ns)::value;
+      using P = Physics<NS>;
+      return launch<NS, typename P::EOS, typename P::TR>(h, h->mech.get<NS>(), g, ib, ie, tb, te, s, timed, fx);
+    });
   };
   if (!per_box) {
     rc = go(0, (int)L.items.size(), 0, (int)L.tiles.size());
@@ -499,9 +522,7 @@ int pc_mol_create(pc_mol_handle** out, const pc_mol_config* cfg) {
   if (c.nspec != c.mech.nspec) return PC_ERR_INVALID_ARGUMENT;
   if (c.precision != PC_PRECISION_FP64 && c.precision != PC_PRECISION_MIXED && c.precision != PC_PRECISION_FP64_RCP)
     return PC_ERR_INVALID_ARGUMENT;
-  int variant = 0;
-  if (c.nspec == 1 && c.eos == PC_EOS_GAMMA_LAW && c.transport == PC_TRANSPORT_CONSTANT) variant = 1;
-  if (c.nspec == 9 && c.eos == PC_EOS_IDEAL_MIX && c.transport == PC_TRANSPORT_SIMPLE) variant = 9;
+  const int variant = compiled_variant(c);
   if (!variant) return PC_ERR_UNSUPPORTED;
   for (int k = 0; k < c.nspec; ++k)
     if (!(c.mech.mw[k] > 0.0)) return PC_ERR_INVALID_ARGUMENT;
@@ -513,16 +534,7 @@ int pc_mol_create(pc_mol_handle** out, const pc_mol_config* cfg) {
   h->cfg = c;
   h->variant = variant;
   cudaGetDevice(&h->device);
-  int rc = PC_OK;
-  if (variant == 1) {
-    fill_common(h->mech1, c.mech);
-    h->nrec = Rec<1>::N;
-  } else {
-    fill_common(h->mech9, c.mech);
-    rc = fill_idealmix(h->mech9, c.mech);
-    if (rc == PC_OK) rc = fill_simple(h->mech9, c.mech);
-    h->nrec = Rec<9>::N;
-  }
+  const int rc = fill_mechanism(h->mech, variant, c.mech, &h->nrec);
   if (rc != PC_OK) {
     delete h;
     return rc;
@@ -762,9 +774,7 @@ extern "C" int pc_mol_rhs_box_static(const pc_mol_config* cfg, const pc_box_desc
   if (c.precision != PC_PRECISION_FP64) return PC_ERR_UNSUPPORTED;
   for (int d = 0; d < 3; ++d)
     if (!(dx[d] > 0.0) || !std::isfinite(dx[d])) return PC_ERR_INVALID_ARGUMENT;
-  int variant = 0;
-  if (c.nspec == 1 && c.eos == PC_EOS_GAMMA_LAW && c.transport == PC_TRANSPORT_CONSTANT) variant = 1;
-  if (c.nspec == 9 && c.eos == PC_EOS_IDEAL_MIX && c.transport == PC_TRANSPORT_SIMPLE) variant = 9;
+  const int variant = compiled_variant(c);
   if (!variant) return PC_ERR_UNSUPPORTED;
   for (int k = 0; k < c.nspec; ++k)
     if (!(c.mech.mw[k] > 0.0)) return PC_ERR_INVALID_ARGUMENT;
@@ -773,19 +783,10 @@ extern "C" int pc_mol_rhs_box_static(const pc_mol_config* cfg, const pc_box_desc
   int rc = validate_box(*box, nvar);
   if (rc != PC_OK) return rc;
 
-  DevMech<1> mech1{};
-  DevMech<9> mech9{};
-  int nrec;
-  if (variant == 1) {
-    fill_common(mech1, c.mech);
-    nrec = Rec<1>::N;
-  } else {
-    fill_common(mech9, c.mech);
-    rc = fill_idealmix(mech9, c.mech);
-    if (rc == PC_OK) rc = fill_simple(mech9, c.mech);
-    if (rc != PC_OK) return rc;
-    nrec = Rec<9>::N;
-  }
+  MechSet ms{};
+  int nrec = 0;
+  rc = fill_mechanism(ms, variant, c.mech, &nrec);
+  if (rc != PC_OK) return rc;
   DevFlags fl{};
   fl.do_hydro = c.do_hydro != 0;
   fl.diffuse_vel = c.diffuse_vel != 0;
@@ -851,19 +852,16 @@ extern "C" int pc_mol_rhs_box_static(const pc_mol_config* cfg, const pc_box_desc
   static_lists_kernel<<<(unsigned)((nlist + 255) / 256), 256, 0, s>>>(d, (int)nitems, (int)ntiles, nt[0], nt[1], dbox,
                                                                        items, tiles, ctr);
   const Geo g = make_geo(dx);
-  if (variant == 1) {
-    if (launch_cell_fp64<1, GammaLawEos<1>, ConstantTransport<1>>(dbox, items, (unsigned)nitems, mech1, fl, ctr, s) !=
-            cudaSuccess ||
-        launch_flux_fp64<1, GammaLawEos<1>>(dbox, tiles, (int)ntiles, mech1, fl, g, ctr, s) != cudaSuccess ||
-        launch_flux_exact<1, GammaLawEos<1>>(dbox, tiles, (int)ntiles, mech1, fl, g, ctr, s) != cudaSuccess)
-      return PC_ERR_CUDA;
-  } else {
-    if (launch_cell_fp64<9, IdealMixEos<9>, SimpleTransport<9>>(dbox, items, (unsigned)nitems, mech9, fl, ctr, s) !=
-            cudaSuccess ||
-        launch_flux_fp64<9, IdealMixEos<9>>(dbox, tiles, (int)ntiles, mech9, fl, g, ctr, s) != cudaSuccess ||
-        launch_flux_exact<9, IdealMixEos<9>>(dbox, tiles, (int)ntiles, mech9, fl, g, ctr, s) != cudaSuccess)
-      return PC_ERR_CUDA;
-  }
+  const bool ok = with_species(variant, [&](auto ns) {
+    constexpr int NS = decltype(ns)::value;
+    using P = Physics<NS>;
+    const DevMech<NS>& m = ms.get<NS>();
+    return launch_cell_fp64<NS, typename P::EOS, typename P::TR>(dbox, items, (unsigned)nitems, m, fl, ctr, s) ==
+               cudaSuccess &&
+           launch_flux_fp64<NS, typename P::EOS>(dbox, tiles, (int)ntiles, m, fl, g, ctr, s) == cudaSuccess &&
+           launch_flux_exact<NS, typename P::EOS>(dbox, tiles, (int)ntiles, m, fl, g, ctr, s) == cudaSuccess;
+  });
+  if (!ok) return PC_ERR_CUDA;
   return cudaGetLastError() == cudaSuccess ? PC_OK : PC_ERR_CUDA;
 }
 
@@ -1094,12 +1092,12 @@ extern "C" int pc_mol_compute_temp(pc_mol_handle* h, int nboxes, const int* lohi
   h->last_stream = s;
   cudaMemsetAsync(h->d_counters, 0, sizeof(unsigned long long) * kNumCounters, s);
   const int maxit = h->flags.newton_maxit;
-  if (h->variant == 1)
-    compute_temp_kernel<1, GammaLawEos<1>><<<(unsigned)items.size(), 256, 0, s>>>(
-        static_cast<const LevelBox*>(db), static_cast<const int2*>(di), h->mech1, maxit, h->d_counters);
-  else
-    compute_temp_kernel<9, IdealMixEos<9>><<<(unsigned)items.size(), 256, 0, s>>>(
-        static_cast<const LevelBox*>(db), static_cast<const int2*>(di), h->mech9, maxit, h->d_counters);
+  with_species(h->variant, [&](auto ns) {
+    constexpr int NS = decltype(ns)::value;
+    compute_temp_kernel<NS, typename Physics<NS>::EOS><<<(unsigned)items.size(), 256, 0, s>>>(
+        static_cast<const LevelBox*>(db), static_cast<const int2*>(di), h->mech.get<NS>(), maxit, h->d_counters);
+    return 0;
+  });
   return h->last_error = cuda_fail(h, cudaGetLastError());
 }
 
@@ -1129,12 +1127,13 @@ extern "C" int pc_mol_compute_temp_adjoint(pc_mol_handle* h, int nboxes, const i
   if ((rc = upload(h, kUpLcDst, lq.data(), lq.size() * sizeof(LevelBox), s, &dq)) != PC_OK) return rc;
   if ((rc = upload(h, kUpItems, items.data(), items.size() * sizeof(int2), s, &di)) != PC_OK) return rc;
   h->last_stream = s;
-  if (h->variant == 1)
-    compute_temp_adjoint_kernel<1, GammaLawEos<1>><<<(unsigned)items.size(), 256, 0, s>>>(
-        static_cast<const LevelBox*>(db), static_cast<const LevelBox*>(dq), static_cast<const int2*>(di), h->mech1);
-  else
-    compute_temp_adjoint_kernel<9, IdealMixEos<9>><<<(unsigned)items.size(), 256, 0, s>>>(
-        static_cast<const LevelBox*>(db), static_cast<const LevelBox*>(dq), static_cast<const int2*>(di), h->mech9);
+  with_species(h->variant, [&](auto ns) {
+    constexpr int NS = decltype(ns)::value;
+    compute_temp_adjoint_kernel<NS, typename Physics<NS>::EOS><<<(unsigned)items.size(), 256, 0, s>>>(
+        static_cast<const LevelBox*>(db), static_cast<const LevelBox*>(dq), static_cast<const int2*>(di),
+        h->mech.get<NS>());
+    return 0;
+  });
   return h->last_error = cuda_fail(h, cudaGetLastError());
 }
 
@@ -1166,12 +1165,13 @@ extern "C" int pc_mol_est_dt(pc_mol_handle* h, const pc_box_desc* boxes, int nbo
     if ((rc = upload(h, kUpBoxes, lb.data(), lb.size() * sizeof(LevelBox), s, &db)) != PC_OK) return rc;
     if ((rc = upload(h, kUpItems, items.data(), items.size() * sizeof(int2), s, &di)) != PC_OK) return rc;
     const Geo g = make_geo(dx);
-    if (h->variant == 1)
-      est_dt_kernel<1, GammaLawEos<1>, ConstantTransport<1>><<<(unsigned)items.size(), 256, 0, s>>>(
-          static_cast<const LevelBox*>(db), static_cast<const int2*>(di), h->mech1, g, h->d_dt);
-    else
-      est_dt_kernel<9, IdealMixEos<9>, SimpleTransport<9>><<<(unsigned)items.size(), 256, 0, s>>>(
-          static_cast<const LevelBox*>(db), static_cast<const int2*>(di), h->mech9, g, h->d_dt);
+    with_species(h->variant, [&](auto ns) {
+      constexpr int NS = decltype(ns)::value;
+      using P = Physics<NS>;
+      est_dt_kernel<NS, typename P::EOS, typename P::TR><<<(unsigned)items.size(), 256, 0, s>>>(
+          static_cast<const LevelBox*>(db), static_cast<const int2*>(di), h->mech.get<NS>(), g, h->d_dt);
+      return 0;
+    });
   }
   unsigned long long bits[4];
   e = cudaMemcpyAsync(bits, h->d_dt, sizeof(bits), cudaMemcpyDeviceToHost, s);
@@ -1250,18 +1250,18 @@ extern "C" int pc_mol_rhs_vjp(pc_mol_handle* h, const pc_box_desc* boxes, int nb
   if ((rc = upload(h, kUpAdjOff, off.data(), off.size() * sizeof(long long), s, &doff)) != PC_OK) return rc;
   // pass 1: records of the forward state
   const int nitems = (int)L.items.size();
-  const cudaError_t ec =
-      (h->variant == 1)
-          ? launch_cell_fp64<1, GammaLawEos<1>, ConstantTransport<1>>(h->d_boxes, h->d_items, (unsigned)nitems,
-                                                                      h->mech1, h->flags, h->d_counters, s)
-          : launch_cell_fp64<9, IdealMixEos<9>, SimpleTransport<9>>(h->d_boxes, h->d_items, (unsigned)nitems,
-                                                                    h->mech9, h->flags, h->d_counters, s);
+  const cudaError_t ec = with_species(h->variant, [&](auto ns) {
+    constexpr int NS = decltype(ns)::value;
+    using P = Physics<NS>;
+    return launch_cell_fp64<NS, typename P::EOS, typename P::TR>(h->d_boxes, h->d_items, (unsigned)nitems,
+                                                                 h->mech.get<NS>(), h->flags, h->d_counters, s);
+  });
   if ((rc = cuda_fail(h, ec)) != PC_OK) return rc;
   if ((rc = cuda_fail(h, cudaMemsetAsync(h->recbar, 0, sizeof(double) * L.scratch_doubles, s))) != PC_OK) return rc;
   const cudaError_t e = launch_vjp_passes(h->variant, h->d_boxes, static_cast<const AdjBox*>(dadj), h->d_items, nitems,
                                           static_cast<const int4*>(dfit), (int)fitems.size(), h->recbar,
                                           (long long)L.scratch_doubles, static_cast<const long long*>(doff),
-                                          h->mech1, h->mech9, h->flags, make_geo(dx), h->d_counters, s);
+                                          h->mech, h->flags, make_geo(dx), h->d_counters, s);
   return h->last_error = cuda_fail(h, e);
 }
 
@@ -1351,8 +1351,8 @@ extern "C" int pc_mol_rhs_jvp(pc_mol_handle* h, const pc_box_desc* boxes, int nb
   void* dtan = nullptr;
   if ((rc = upload(h, kUpAdjBoxes, tan.data(), tan.size() * sizeof(TanBox), s, &dtan)) != PC_OK) return rc;
   const cudaError_t e = launch_jvp_passes(h->variant, h->d_boxes, static_cast<const TanBox*>(dtan), h->d_items,
-                                          (int)L.items.size(), h->d_tiles, (int)L.tiles.size(), h->mech1, h->mech9,
-                                          h->flags, make_geo(dx), h->d_counters, s);
+                                          (int)L.items.size(), h->d_tiles, (int)L.tiles.size(), h->mech, h->flags,
+                                          make_geo(dx), h->d_counters, s);
   return h->last_error = cuda_fail(h, e);
 }
 
@@ -1457,11 +1457,13 @@ struct pc_mol_step_graph {
 
 namespace {
 
+// A device buffer owned by g holding bytes copied from src (src null: left
+// uninitialised).
 int dev_copy(pc_mol_step_graph* g, const void* src, size_t bytes, void** out) {
   void* p = nullptr;
   if (cudaMalloc(&p, bytes ? bytes : 16) != cudaSuccess) return PC_ERR_OUT_OF_MEMORY;
   g->bufs.push_back(p);
-  if (bytes && cudaMemcpy(p, src, bytes, cudaMemcpyHostToDevice) != cudaSuccess) return PC_ERR_CUDA;
+  if (src && bytes && cudaMemcpy(p, src, bytes, cudaMemcpyHostToDevice) != cudaSuccess) return PC_ERR_CUDA;
   *out = p;
   return PC_OK;
 }
@@ -1591,10 +1593,12 @@ extern "C" int pc_mol_step_graph_create(pc_mol_handle* parent, const pc_box_desc
   const unsigned nbv = (unsigned)itv.size(), nbg = (unsigned)itg.size();
   const int maxit = h->flags.newton_maxit;
   auto ctemp = [&](const LevelBox* lb) {
-    if (h->variant == 1)
-      compute_temp_kernel<1, GammaLawEos<1>><<<nbv, 256, 0, s>>>(lb, ITV, h->mech1, maxit, h->d_counters);
-    else
-      compute_temp_kernel<9, IdealMixEos<9>><<<nbv, 256, 0, s>>>(lb, ITV, h->mech9, maxit, h->d_counters);
+    with_species(h->variant, [&](auto ns) {
+      constexpr int NS = decltype(ns)::value;
+      compute_temp_kernel<NS, typename Physics<NS>::EOS><<<nbv, 256, 0, s>>>(lb, ITV, h->mech.get<NS>(), maxit,
+                                                                             h->d_counters);
+      return 0;
+    });
   };
   // The step from state o to state n (o, n = 0: A, 1: B).
   auto seq = [&](int o) -> int {

@@ -11,7 +11,7 @@
 namespace pcg {
 
 struct RcpLaunch {
-  int variant;      // 1: one species, GammaLaw + constant transport; 9: ideal mixture + simple transport
+  int variant;      // species count: 1 (GammaLaw + constant transport), 9 or 21 (ideal mixture + simple transport)
   int tile;         // flux-pass tile shape, 0..3
   bool persistent;  // persistent flux-pass grid
   const void* boxes;  // device DevBox[]
@@ -19,7 +19,7 @@ struct RcpLaunch {
   int nitems;
   const void* tiles;  // device int4[] flux-pass tiles
   int ntiles;
-  const void* mech;  // host DevMech<1> or DevMech<9>
+  const void* mech;  // host DevMech<variant>
   size_t mech_size;
   const void* flags;  // host DevFlags
   size_t flags_size;

@@ -59,12 +59,12 @@ cudaError_t launch_rhs_rcp(const RcpLaunch& a) {
   if (a.flags_size != sizeof(pcg_rcp::DevFlags) || a.geo_size != sizeof(pcg_rcp::Geo) ||
       a.devbox_size != sizeof(pcg_rcp::DevBox) || a.fluxbox_size != sizeof(pcg_rcp::FluxBox))
     return cudaErrorInvalidValue;
-  if (a.variant == 1) {
-    if (a.mech_size != sizeof(pcg_rcp::DevMech<1>)) return cudaErrorInvalidValue;
-    return pcg_rcp::launch_passes<1, pcg_rcp::GammaLawEos<1>, pcg_rcp::ConstantTransport<1>>(a);
-  }
-  if (a.mech_size != sizeof(pcg_rcp::DevMech<9>)) return cudaErrorInvalidValue;
-  return pcg_rcp::launch_passes<9, pcg_rcp::IdealMixEos<9>, pcg_rcp::SimpleTransport<9>>(a);
+  return pcg_rcp::with_species(a.variant, [&](auto ns) {
+    constexpr int NS = decltype(ns)::value;
+    using P = pcg_rcp::Physics<NS>;
+    if (a.mech_size != sizeof(pcg_rcp::DevMech<NS>)) return cudaErrorInvalidValue;
+    return pcg_rcp::launch_passes<NS, typename P::EOS, typename P::TR>(a);
+  });
 }
 
 }  // namespace pcg

@@ -2,6 +2,7 @@
 // without multiply-add contraction: the value part of the Dual arithmetic is
 // the FP64 forward's own operation sequence.
 #include "pc_tangent.cuh"
+#include "pc_unit_ns.h"
 
 #include <atomic>
 
@@ -41,14 +42,30 @@ static cudaError_t jvp_passes(const DevBox* boxes, const TanBox* tans, const int
   return cudaGetLastError();
 }
 
-cudaError_t launch_jvp_passes(int variant, const DevBox* boxes, const TanBox* tans, const int2* items, int nitems,
-                              const int4* tiles, int ntiles, const DevMech<1>& m1, const DevMech<9>& m9,
-                              const DevFlags& f, const Geo& g, unsigned long long* counters, cudaStream_t s) {
-  if (variant == 1)
-    return jvp_passes<1, GammaLawEos<1>, ConstantTransport<1>>(boxes, tans, items, nitems, tiles, ntiles, m1, f, g,
-                                                               counters, s);
-  return jvp_passes<9, IdealMixEos<9>, SimpleTransport<9>>(boxes, tans, items, nitems, tiles, ntiles, m9, f, g,
-                                                           counters, s);
+template <int NS>
+cudaError_t jvp_passes_ns(const DevBox* boxes, const TanBox* tans, const int2* items, int nitems, const int4* tiles,
+                          int ntiles, const DevMech<NS>& m, const DevFlags& f, const Geo& g,
+                          unsigned long long* counters, cudaStream_t s) {
+  using P = Physics<NS>;
+  return jvp_passes<NS, typename P::EOS, typename P::TR>(boxes, tans, items, nitems, tiles, ntiles, m, f, g, counters,
+                                                         s);
 }
+
+#define PC_JVP_INST(NS)                                                                                          \
+  template cudaError_t jvp_passes_ns<NS>(const DevBox*, const TanBox*, const int2*, int, const int4*, int,        \
+                                         const DevMech<NS>&, const DevFlags&, const Geo&, unsigned long long*,   \
+                                         cudaStream_t);
+PC_UNIT_INSTANTIATE(PC_JVP_INST)
+
+#if PC_UNIT_HAS(1)  // the dispatcher lives in the one-species compilation
+cudaError_t launch_jvp_passes(int nspec, const DevBox* boxes, const TanBox* tans, const int2* items, int nitems,
+                              const int4* tiles, int ntiles, const MechSet& ms, const DevFlags& f, const Geo& g,
+                              unsigned long long* counters, cudaStream_t s) {
+  return with_species(nspec, [&](auto ns) {
+    constexpr int NS = decltype(ns)::value;
+    return jvp_passes_ns<NS>(boxes, tans, items, nitems, tiles, ntiles, ms.get<NS>(), f, g, counters, s);
+  });
+}
+#endif
 
 }  // namespace pcg

@@ -4,6 +4,7 @@
 // changes which thread evaluates a face, never the operations on it, so every
 // shape gives bit-identical results.
 #include "pc_kernels.cuh"
+#include "pc_unit_ns.h"
 
 namespace pcg {
 
@@ -29,13 +30,29 @@ cudaError_t flux_tile(int tile, const DevBox* boxes, const int4* tiles, int ntil
 
 }  // namespace
 
-cudaError_t launch_flux_fp64_tile(int tile, bool persistent, int variant, const DevBox* boxes, const int4* tiles,
-                                  int ntiles, const DevMech<1>& m1, const DevMech<9>& m9, const DevFlags& f,
-                                  const Geo& g, unsigned long long* counters, cudaStream_t s, const FluxBox* fx) {
-  if (ntiles <= 0) return cudaSuccess;
-  if (variant == 1)
-    return flux_tile<1, GammaLawEos<1>>(tile, boxes, tiles, ntiles, m1, f, g, counters, s, fx, persistent);
-  return flux_tile<9, IdealMixEos<9>>(tile, boxes, tiles, ntiles, m9, f, g, counters, s, fx, persistent);
+template <int NS>
+cudaError_t fp64_tile_ns(int tile, bool persistent, const DevBox* boxes, const int4* tiles, int ntiles,
+                         const DevMech<NS>& m, const DevFlags& f, const Geo& g, unsigned long long* counters,
+                         cudaStream_t s, const FluxBox* fx) {
+  return flux_tile<NS, typename Physics<NS>::EOS>(tile, boxes, tiles, ntiles, m, f, g, counters, s, fx, persistent);
 }
+
+#define PC_TILE_INST(NS)                                                                                         \
+  template cudaError_t fp64_tile_ns<NS>(int, bool, const DevBox*, const int4*, int, const DevMech<NS>&,          \
+                                        const DevFlags&, const Geo&, unsigned long long*, cudaStream_t,          \
+                                        const FluxBox*);
+PC_UNIT_INSTANTIATE(PC_TILE_INST)
+
+#if PC_UNIT_HAS(1)  // the dispatcher lives in the one-species compilation
+cudaError_t launch_flux_fp64_tile(int tile, bool persistent, int nspec, const DevBox* boxes, const int4* tiles,
+                                  int ntiles, const MechSet& ms, const DevFlags& f, const Geo& g,
+                                  unsigned long long* counters, cudaStream_t s, const FluxBox* fx) {
+  if (ntiles <= 0) return cudaSuccess;
+  return with_species(nspec, [&](auto ns) {
+    constexpr int NS = decltype(ns)::value;
+    return fp64_tile_ns<NS>(tile, persistent, boxes, tiles, ntiles, ms.get<NS>(), f, g, counters, s, fx);
+  });
+}
+#endif
 
 }  // namespace pcg

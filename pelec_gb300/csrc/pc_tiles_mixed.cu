@@ -21,16 +21,16 @@ cudaError_t flux_tile(int tile, bool pers, const DevBox* boxes, const int4* tile
 
 }  // namespace
 
-cudaError_t launch_flux_mixed_tile(int tile, bool persistent, int variant, const DevBox* boxes, const int4* tiles,
-                                   int ntiles, const DevMech<1>& m1, const DevMech<9>& m9, const DevFlags& f,
-                                   const Geo& g, double p_ref, unsigned long long* counters, cudaStream_t s) {
+cudaError_t launch_flux_mixed_tile(int tile, bool persistent, int nspec, const DevBox* boxes, const int4* tiles,
+                                   int ntiles, const MechSet& ms, const DevFlags& f, const Geo& g, double p_ref,
+                                   unsigned long long* counters, cudaStream_t s) {
   if (ntiles <= 0) return cudaSuccess;
-  if (variant == 1) {
-    const MechF<1> mf = to_float(m1, p_ref);
-    return flux_tile<1, false>(tile, persistent, boxes, tiles, ntiles, mf, m1, f, g, counters, s);
-  }
-  const MechF<9> mf = to_float(m9, p_ref);
-  return flux_tile<9, true>(tile, persistent, boxes, tiles, ntiles, mf, m9, f, g, counters, s);
+  return with_species(nspec, [&](auto ns) {
+    constexpr int NS = decltype(ns)::value;
+    const DevMech<NS>& m = ms.get<NS>();
+    const MechF<NS> mf = to_float(m, p_ref);
+    return flux_tile<NS, Physics<NS>::MIX>(tile, persistent, boxes, tiles, ntiles, mf, m, f, g, counters, s);
+  });
 }
 
 }  // namespace pcg

@@ -19,6 +19,12 @@ reference tree, so its data cannot be used here; this module supplies:
   Molecular weights are sums of standard atomic weights.  A real mechanism
   plugs in through the same ``pc_mechanism`` structure.
 
+* ``drm_synthetic()`` — a SYNTHETIC 21-species table in the species order of
+  the DRM19 methane mechanism (the size of a common hydrocarbon mechanism),
+  with the same kind of generated data (cp/R and transport from each
+  species' atom count and molecular weight); not DRM19 data.  It exercises
+  the kernels at NUM_SPECIES = 21.
+
 Host-side thermodynamics (numpy) for building initial states lives here too.
 """
 from __future__ import annotations
@@ -33,10 +39,16 @@ RU = 8.31446261815324e7  # erg / (mol K)
 P_ATM = 1013250.0  # dyn / cm^2
 
 SPECIES_9 = ("H2", "O2", "H2O", "H", "O", "OH", "HO2", "H2O2", "N2")
-_ATOMIC = {"H": 1.008, "O": 15.999, "N": 14.007}
+SPECIES_21 = ("H2", "H", "O", "O2", "OH", "H2O", "HO2", "CH2", "CH2(S)", "CH3", "CH4", "CO", "CO2", "HCO", "CH2O",
+              "CH3O", "C2H4", "C2H5", "C2H6", "N2", "AR")
+_ATOMIC = {"H": 1.008, "O": 15.999, "N": 14.007, "C": 12.011, "AR": 39.948}
 _COMPOSITION = {
     "H2": {"H": 2}, "O2": {"O": 2}, "H2O": {"H": 2, "O": 1}, "H": {"H": 1}, "O": {"O": 1},
     "OH": {"O": 1, "H": 1}, "HO2": {"H": 1, "O": 2}, "H2O2": {"H": 2, "O": 2}, "N2": {"N": 2},
+    "CH2": {"C": 1, "H": 2}, "CH2(S)": {"C": 1, "H": 2}, "CH3": {"C": 1, "H": 3}, "CH4": {"C": 1, "H": 4},
+    "CO": {"C": 1, "O": 1}, "CO2": {"C": 1, "O": 2}, "HCO": {"H": 1, "C": 1, "O": 1},
+    "CH2O": {"C": 1, "H": 2, "O": 1}, "CH3O": {"C": 1, "H": 3, "O": 1}, "C2H4": {"C": 2, "H": 4},
+    "C2H5": {"C": 2, "H": 5}, "C2H6": {"C": 2, "H": 6}, "AR": {"AR": 1},
 }
 
 
@@ -179,9 +191,23 @@ def _power_fit(q300: float, expo: float, c2: float, c3: float) -> np.ndarray:
     return np.array([c0, expo, c2, c3])
 
 
-def h2_air_synthetic(tmid: float = 1000.0) -> Mechanism:
-    """SYNTHETIC 9-species H2/air table (see module docstring)."""
-    names = SPECIES_9
+def _generic_species(name: str):
+    """Synthetic (cp/R coefficients, h_f/R, mu300, lambda300, bulk ratio) of a
+    species not in the 9-species tables, from its atom count and weight."""
+    natoms = sum(_COMPOSITION[name].values())
+    w = _mw(name)
+    b = (2.5 + 0.9 * (natoms - 1), 0.25 * (natoms - 1) + 0.05, -0.04 * (natoms - 1), 0.004 * (natoms - 1),
+         -0.00012 * (natoms - 1))
+    hf = -4000.0 * (len(name) % 5) + 2500.0 * ((natoms * 7) % 5)
+    mu = 1.0e-4 * np.sqrt(w / 16.0)
+    lam = 2.5e3 * np.sqrt(16.0 / w) * (1.0 + 0.1 * natoms)
+    bulk = 0.0 if natoms == 1 else 0.25 + 0.05 * min(natoms, 5)
+    return b, hf, mu, lam, bulk
+
+
+def h2_air_synthetic(tmid: float = 1000.0, names=SPECIES_9) -> Mechanism:
+    """SYNTHETIC 9-species H2/air table (see module docstring); with another
+    species list, the same construction over those species."""
     ns = len(names)
     mw = np.array([_mw(n) for n in names])
     nasa_lo = np.zeros((ns, 7))
@@ -192,31 +218,43 @@ def h2_air_synthetic(tmid: float = 1000.0) -> Mechanism:
     def h_int(a, T):  # integral of cp/R dT without the constant
         return T * (a[0] + T * (a[1] / 2 + T * (a[2] / 3 + T * (a[3] / 4 + T * a[4] / 5))))
 
+    gen = {n: _generic_species(n) for n in names if n not in _CP_B}
+    cpb = {n: (_CP_B[n] if n in _CP_B else gen[n][0]) for n in names}
+    hfr = {n: (_HF_R[n] if n in _HF_R else gen[n][1]) for n in names}
+    mu300 = {n: (_MU300[n] if n in _MU300 else gen[n][2]) for n in names}
+    lam300 = {n: (_LAM300[n] if n in _LAM300 else gen[n][3]) for n in names}
+    bulkr = {n: (_BULK[n] if n in _BULK else gen[n][4]) for n in names}
     for k, n in enumerate(names):
-        b = np.array(_CP_B[n], dtype=np.float64)
+        b = np.array(cpb[n], dtype=np.float64)
         bh = b.copy()
         bh[0] += d
         bh[1] -= 2 * d
         bh[2] += d
         alo = b * scale
         ahi = bh * scale
-        a5_lo = _HF_R[n] - h_int(alo, 298.15)
+        a5_lo = hfr[n] - h_int(alo, 298.15)
         a5_hi = h_int(alo, tmid) + a5_lo - h_int(ahi, tmid)
         nasa_lo[k, :5] = alo
         nasa_lo[k, 5] = a5_lo
         nasa_hi[k, :5] = ahi
         nasa_hi[k, 5] = a5_hi
-    visc = np.stack([_power_fit(_MU300[n], 0.70, 0.004, -0.0002) for n in names])
-    cond = np.stack([_power_fit(_LAM300[n], 0.80, 0.004, -0.0002) for n in names])
+    visc = np.stack([_power_fit(mu300[n], 0.70, 0.004, -0.0002) for n in names])
+    cond = np.stack([_power_fit(lam300[n], 0.80, 0.004, -0.0002) for n in names])
     diff = np.zeros((ns, ns, 4))
     for i in range(ns):
         for j in range(ns):
             mij = 2.0 * mw[i] * mw[j] / (mw[i] + mw[j])
             diff[i, j] = _power_fit(0.3 * np.sqrt(28.0 / mij), 1.75, 0.002, -0.0001)
-    bulk = np.array([_BULK[n] for n in names])
+    bulk = np.array([bulkr[n] for n in names])
     return Mechanism(
         names=names, mw=mw, eos=abi.PC_EOS_IDEAL_MIX, transport=abi.PC_TRANSPORT_SIMPLE,
         nasa_tmid=np.full(ns, tmid), nasa_lo=nasa_lo, nasa_hi=nasa_hi, visc_fit=visc, cond_fit=cond,
         diff_fit=diff, bulk_ratio=bulk, diff_pref=P_ATM,
         notes={"synthetic": True, "order": names},
     )
+
+
+def drm_synthetic(tmid: float = 1000.0) -> Mechanism:
+    """SYNTHETIC 21-species table in the DRM19 species order (see the module
+    docstring); the H2/air species keep the 9-species table's data."""
+    return h2_air_synthetic(tmid, SPECIES_21)

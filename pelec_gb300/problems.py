@@ -191,7 +191,12 @@ def flame_primitives(mech: Mechanism, fp: FlameParams, X, Yc, Z, rng, w_noise: f
     Y = (1.0 - s)[None] * yu[:, None, None, None] + s[None] * yb[:, None, None, None]
     idx = {n: i for i, n in enumerate(mech.names)}
     for r in ("H", "O", "OH", "HO2", "H2O2"):
-        Y[idx[r]] = Y[idx[r]] + 1e-6 * rng.uniform(0.0, 1.0, T.shape)
+        if r in idx:
+            Y[idx[r]] = Y[idx[r]] + 1e-6 * rng.uniform(0.0, 1.0, T.shape)
+    # species a larger mechanism adds (hydrocarbons, argon): seeded traces
+    for n in mech.names:
+        if n not in ("H2", "O2", "H2O", "N2", "H", "O", "OH", "HO2", "H2O2"):
+            Y[idx[n]] = Y[idx[n]] + 1e-6 * rng.uniform(0.0, 1.0, T.shape)
     Y = Y / Y.sum(axis=0, keepdims=True)
     p = np.full(T.shape, P_ATM)
     rho = p * mech.wbar(Y) / (RU * T)

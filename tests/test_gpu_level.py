@@ -9,7 +9,7 @@ import pytest
 
 from conftest import rel_maxnorm
 from gpu_util import to_multifab
-from pelec_gb300 import abi, problems
+from pelec_gb300 import abi, mechanism, problems
 
 pytestmark = pytest.mark.gpu
 
@@ -205,3 +205,27 @@ def test_c3_full_level_against_oracle(cuda_lib, oracle_lib):
     print("C3 mixed rel L2 per component:", l2)
     l2[abi.UTEMP] = 0.0  # identically zero in both
     assert l2.max() <= 1e-5, l2
+
+
+def test_21_species_level_every_tile_and_autotune(cuda_lib, oracle_lib):
+    """A 21-species level: every launch configuration gives the same RHS bit
+    for bit, equal to the oracle; the autotuner times and caches a choice for
+    this species count on the handle."""
+    mol = cuda_lib
+    mech, boxes = problems.level_boxes(nboxes=4, seed=33, edges=(8, 12, 16), mech=mechanism.drm_synthetic())
+    cfg = problems.make_config(mech)
+    refs = oracle_lib.mol_rhs(cfg, boxes)
+    op = mol.MOLOperator(cfg)
+    first = None
+    for t in range(abi.PC_NUM_LAUNCH_CONFIGS):
+        out = _rhs_at_tile(mol, op, boxes, t)
+        for a, r in zip(out, refs):
+            np.testing.assert_array_equal(a, r, err_msg=f"configuration {t}")
+        first = first or out
+    op.set_tile(-1)
+    S = to_multifab(mol, boxes, boxes[0].ng)
+    R = mol.MultiFab([(st.lo, st.hi) for st in boxes], boxes[0].S.shape[0], 0)
+    best, ms = op.autotune(S, R, boxes[0].dx, reps=2)
+    assert 0 <= best < abi.PC_NUM_LAUNCH_CONFIGS and all(m > 0 for m in ms)
+    op.rhs_level(S, R, boxes[0].dx)
+    assert op.current_tile() == best

@@ -10,7 +10,7 @@ import numpy as np
 import pytest
 
 from gpu_util import gpu_rhs
-from pelec_gb300 import abi, problems
+from pelec_gb300 import abi, mechanism, problems
 
 pytestmark = pytest.mark.gpu
 
@@ -115,3 +115,13 @@ def test_c4_mixed_256_against_fp64_oracle(cuda_lib, oracle_lib):
     assert status.nonfinite_output == 0
     assert np.all(l2 <= _tol()), l2
     torch.cuda.empty_cache()
+
+
+def test_mixed_21_species_error_vs_fp64_oracle(cuda_lib, oracle_lib):
+    """NUM_SPECIES = 21: the mixed form within MIXED_L2 of the FP64 oracle."""
+    mech, st, _ = problems.flame((24, 20, 32), seed=45, mech=mechanism.drm_synthetic())
+    ref, = oracle_lib.mol_rhs(problems.make_config(mech), [st])
+    (gpu,), _ = gpu_rhs(cuda_lib, problems.make_config(mech, precision=abi.PC_PRECISION_MIXED), [st])
+    l2 = rel_l2(gpu, ref)
+    print("21 species mixed rel L2 per component:", l2)
+    assert np.all(l2 <= MIXED_L2), l2

@@ -236,3 +236,18 @@ def test_face_flux_export_matches_oracle(cuda_lib, oracle_lib):
         fx, fy, fz = (Fg[d].cpu().numpy() for d in range(3))
         div = fx[..., 1:] - fx[..., :-1] + fy[:, :, 1:] - fy[:, :, :-1] + fz[:, 1:] - fz[:, :-1]
         np.testing.assert_array_equal(-div / vol, Rg)
+
+
+@pytest.mark.parametrize("case", ["default", "laxf", "first_order", "diffusion_only"])
+def test_flame_21_species_parity(cuda_lib, oracle_lib, case):
+    """NUM_SPECIES = 21 (the synthetic DRM19-sized mechanism): bit for bit
+    equal to the oracle, which is bit for bit the reference's own code at 21
+    species too (tests/test_ref_pinned.py)."""
+    kw = {"default": {}, "laxf": dict(use_laxf_flux=1), "first_order": dict(plm_iorder=1),
+          "diffusion_only": dict(do_hydro=0)}[case]
+    mech, st, _ = problems.flame((16, 12, 20), seed=24, mech=mechanism.drm_synthetic())
+    cfg = problems.make_config(mech, **kw)
+    ref, = oracle_lib.mol_rhs(cfg, [st])
+    (gpu,), status = gpu_rhs(cuda_lib, cfg, [st])
+    _check(gpu, ref, what=f"21 species/{case}")
+    assert status.cells == 16 * 12 * 20 and status.newton_nonconverged == 0

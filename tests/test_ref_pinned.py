@@ -169,3 +169,12 @@ def test_compute_temp_and_est_dt(oracle_lib, which):
     refharness.compute_temp(cfg, [b])
     _same(a.S, b.S, "computeTemp")
     assert oracle_lib.est_dt(cfg, [st], 0.3)[1] == refharness.est_dt_parts(cfg, [st])
+
+
+@pytest.mark.parametrize("case", ["default", "laxf", "first_order", "arithmetic_mean", "spec_only"])
+def test_21_species(oracle_lib, case):
+    """NUM_SPECIES = 21 (the synthetic DRM19-sized mechanism; the reference
+    built with -DPC_REF_NS=21)."""
+    mech, st, _ = problems.flame((10, 8, 12), seed=4, mech=mechanism.drm_synthetic())
+    cfg = problems.make_config(mech, **FLAGS.get(case, {}))
+    _same(oracle_lib.mol_rhs(cfg, [st])[0], refharness.mol_rhs(cfg, [st])[0], f"21 species/{case}")
