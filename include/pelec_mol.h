@@ -264,7 +264,10 @@ int pc_mol_tile_shape(int t, int shape[4]);
 
 /* Force launch configuration t for the following calls, or t = -1 to return
  * to the automatic choice (the autotune cache entry of the BoxArray's
- * box-size histogram, else PC_TILE_8x8x4). */
+ * box-size histogram, else PC_TILE_8x8x4).  PC_ERR_UNSUPPORTED when the flux
+ * pass of configuration t needs more shared memory per CTA than the device
+ * allows at the handle's species count and precision (FP64 with 21 species:
+ * the 8x8x8 and 16x8x4 tiles). */
 int pc_mol_set_tile(pc_mol_handle* h, int t);
 
 /* The launch configuration that the last rhs call used. */
@@ -275,7 +278,9 @@ int pc_mol_current_tile(pc_mol_handle* h, int* t);
  * stream), keep the fastest in the handle's cache under the BoxArray's
  * box-size histogram (the species count and precision are the handle's) and
  * return it in *best.  ms[t] receives the mean time per call of
- * configuration t when ms is not NULL and n_ms >= PC_NUM_LAUNCH_CONFIGS.
+ * configuration t when ms is not NULL and n_ms >= PC_NUM_LAUNCH_CONFIGS, or
+ * -1 for a configuration that does not fit the device (pc_mol_set_tile) and
+ * is not timed.
  * Writes the RHS into the boxes' rhs arrays (every configuration gives the
  * same values).  Synchronous; not to be called during a stream capture. */
 int pc_mol_autotune(pc_mol_handle* h, const pc_box_desc* boxes, int nboxes, const double dx[3], int reps,

@@ -70,6 +70,7 @@ struct pc_mol_handle {
   int tile_forced = -1;
   int tile = 0;
   std::map<std::vector<int>, int> tune_cache;
+  int smem_optin = 0;  // shared memory a CTA may opt into on the device (bytes)
   // Device box tables of the current layout, one per set of array pointers
   // (callers alternate a few state/RHS buffers; a pointer change must not
   // cost a layout rebuild).  d_boxes is the table of the last call.
@@ -300,6 +301,32 @@ std::vector<int> tune_key(const pc_box_desc* boxes, int nboxes) {
   }
   return k;
 }
+
+// Dynamic shared memory of the flux pass at launch configuration t for the
+// handle's species count and precision (bytes).  The FP64 passes stage face
+// fluxes, cell slopes and the z carry; the mixed pass only the face fluxes,
+// and those in static shared memory for tiles of at most 256 cells.
+size_t flux_pass_smem(const pc_mol_handle* h, int t) {
+  return with_species(h->cfg.nspec, [&](auto sc) -> size_t {
+    constexpr int NS = decltype(sc)::value;
+    auto of = [&](auto tl) -> size_t {
+      using TL = decltype(tl);
+      if (h->cfg.precision == PC_PRECISION_MIXED) return TL::DYN ? sizeof(double) * (7 + NS) * TL::MAXF : 0;
+      return flux_smem_bytes<NS, TL>();
+    };
+    switch (t % kNumTiles) {
+      case 1: return of(TileCube{});
+      case 2: return of(TileLong{});
+      case 3: return of(TileSmall{});
+      default: return of(TileDefault{});
+    }
+  });
+}
+
+// Launch configuration t fits the device at the handle's species count: with
+// 21 species the FP64 flux pass of the 8x8x8 and 16x8x4 tiles needs 278 and
+// 343 KB of shared memory per CTA, more than the 227 KB a CTA may have.
+bool config_fits(const pc_mol_handle* h, int t) { return flux_pass_smem(h, t) <= (size_t)h->smem_optin; }
 
 int choose_tile(pc_mol_handle* h, const pc_box_desc* boxes, int nboxes) {
   if (h->tile_forced >= 0) return h->tile_forced;
@@ -534,6 +561,7 @@ int pc_mol_create(pc_mol_handle** out, const pc_mol_config* cfg) {
   h->cfg = c;
   h->variant = variant;
   cudaGetDevice(&h->device);
+  cudaDeviceGetAttribute(&h->smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device);
   const int rc = fill_mechanism(h->mech, variant, c.mech, &h->nrec);
   if (rc != PC_OK) {
     delete h;
@@ -632,6 +660,7 @@ int pc_mol_tile_shape(int t, int shape[4]) {
 
 int pc_mol_set_tile(pc_mol_handle* h, int t) {
   if (!h || t < -1 || t >= kNumLaunchConfigs) return PC_ERR_INVALID_ARGUMENT;
+  if (t >= 0 && !config_fits(h, t)) return PC_ERR_UNSUPPORTED;
   h->tile_forced = t;
   h->last_boxes.clear();  // the next call chooses again
   return PC_OK;
@@ -659,7 +688,12 @@ int pc_mol_autotune(pc_mol_handle* h, const pc_box_desc* boxes, int nboxes, cons
   const int saved = h->tile_forced;
   double tbest = 0.0;
   int ibest = 0;
+  bool any = false;
   for (int t = 0; t < kNumLaunchConfigs && rc == PC_OK; ++t) {
+    if (!config_fits(h, t)) {  // not timed
+      if (ms) ms[t] = -1.0;
+      continue;
+    }
     h->tile_forced = t;
     rc = run(h, boxes, nboxes, dx, stream, false);  // warm-up, builds the layout of configuration t
     if (rc == PC_OK) rc = cuda_fail(h, cudaEventRecord(e0, s));
@@ -670,9 +704,10 @@ int pc_mol_autotune(pc_mol_handle* h, const pc_box_desc* boxes, int nboxes, cons
     if (rc == PC_OK) rc = cuda_fail(h, cudaEventElapsedTime(&el, e0, e1));
     const double per = (double)el / reps;
     if (ms) ms[t] = per;
-    if (rc == PC_OK && (t == 0 || per < tbest)) {
+    if (rc == PC_OK && (!any || per < tbest)) {
       tbest = per;
       ibest = t;
+      any = true;
     }
   }
   cudaEventDestroy(e0);

@@ -79,22 +79,42 @@ def _fd(oracle_lib, cfg, st, mu, v, h):
     return float((mu * (R(h) - R(-h))).sum()) / (2.0 * h)
 
 
-# Step of the difference quotients, a relative change of the state, fixed.
+# Steps of the difference quotients, relative changes of the state, fixed.
 # Over a whole box a step of 1e-7 or more moves some limiter argument across
 # a min/max switch (errors up to 1e-2 on these flames), where the quotient
 # measures another branch than the derivative; the directions below are
 # therefore local (a few seeded cells), so that the few limiters they reach
-# sit far from their switches.
-FD_H = 1e-7
+# sit far from their switches.  Three nearby steps give the same truncation
+# error but independent rounding: their mean is the estimate, their spread
+# the estimate's rounding noise (1e-9 of the derivative for directions over
+# all components; a few 1e-6 for a direction in the density or momentum
+# alone, whose derivative is 1e-4 of the RHS terms it moves).
+FD_STEPS = (0.8e-7, 1e-7, 1.25e-7)
+
+
+def _fd_estimate(oracle_lib, cfg, st, mu, v):
+    """(mean, spread) of the central differences at FD_STEPS."""
+    vals = np.array([_fd(oracle_lib, cfg, st, mu, v, h) for h in FD_STEPS])
+    return float(vals.mean()), float(np.ptp(vals))
 
 
 def _local_direction(st, rng, ncells=6):
     """A direction confined to ncells seeded valid cells: each conserved
-    component of the cell scaled by its own seeded factor.  On grow(valid, 2)."""
+    component of the cell scaled by its own seeded factor.  On grow(valid, 2).
+
+    The cells avoid the first and last valid layer in z.  On the flames z is
+    an outflow direction, whose ghost cells are copies of those layers, and
+    the difference quotients here hold the ghosts fixed: moving a boundary
+    cell alone breaks the exact tie ghost = cell, which sits on kinks of the
+    forward (the limiter at mc(0, d), the Riemann solver's shock/rarefaction
+    switch at p* = p), so the central difference averages two branches there
+    (errors of 1e-2 of the derivative, the same for every step size).  A
+    trajectory refills the ghosts and keeps the tie."""
     v = np.zeros_like(st.S[:, 2:-2, 2:-2, 2:-2])
     nz, ny, nx = v.shape[1:]
     for _ in range(ncells):
-        k, j, i = (int(rng.integers(2, n - 2)) for n in (nz, ny, nx))
+        k = int(rng.integers(3, nz - 3))
+        j, i = (int(rng.integers(2, n - 2)) for n in (ny, nx))
         s = rng.normal(size=st.S.shape[0])
         s[abi.UEINT] = 0.0
         s[abi.UTEMP] = 0.0
@@ -116,9 +136,10 @@ def test_vjp_matches_oracle_finite_differences(cuda_lib, oracle_lib, kind):
     for trial in range(4):
         v = _local_direction(st, rng)
         ad = float((Ub * v).sum())
-        err = abs(_fd(oracle_lib, cfg, st, mu, v, FD_H) - ad) / abs(ad)
-        print(kind, "trial", trial, "adjoint", ad, "rel err vs FD:", err)
-        assert err <= FD_REL, err
+        fd, noise = _fd_estimate(oracle_lib, cfg, st, mu, v)
+        err = abs(fd - ad) / abs(ad)
+        print(kind, "trial", trial, "adjoint", ad, "rel err vs FD:", err, "FD noise", noise / abs(ad))
+        assert abs(fd - ad) <= FD_REL * abs(ad) + noise, (err, noise / abs(ad))
 
 
 def test_vjp_component_groups(cuda_lib, oracle_lib):
@@ -138,9 +159,10 @@ def test_vjp_component_groups(cuda_lib, oracle_lib):
         keep[comps] = True
         v[~keep] = 0.0
         ad = float((Ub * v).sum())
-        err = abs(_fd(oracle_lib, cfg, st, mu, v, FD_H) - ad) / abs(ad)
-        print("group", name, "adjoint", ad, "rel err", err)
-        assert err <= FD_REL, (name, err)
+        fd, noise = _fd_estimate(oracle_lib, cfg, st, mu, v)
+        err = abs(fd - ad) / abs(ad)
+        print("group", name, "adjoint", ad, "rel err", err, "FD noise", noise / abs(ad))
+        assert abs(fd - ad) <= FD_REL * abs(ad) + noise, (name, err, noise / abs(ad))
 
 
 def _jvp(mol, cfg, st, v):
