@@ -751,61 +751,71 @@ __device__ __forceinline__ void diffusion_face_f(const DevBox& b, const DevFlags
   if (ener) F[UEDEN] += fE;
 }
 
+// Shared-memory staging of the face fluxes of a tile, all three directions
+// at once: the FP64 total and internal energy fluxes first, then the other
+// components in FP32 (their widening to FP64 is exact, so it can wait for the
+// divergence).  Direction d's faces start at face slot base(d).
+template <int NS, class TL>
+struct FaceStage {
+  static constexpr int TOT = TL::F0 + TL::F1 + TL::F2;
+  double* e;  // [2][TOT]: UEDEN, UEINT
+  float* v;   // [7 + NS][TOT]
+  __device__ static constexpr int base(int d) { return d == 0 ? 0 : d == 1 ? TL::F0 : TL::F0 + TL::F1; }
+  __device__ double get(int n, int slot) const {
+    return n == UEDEN ? e[slot] : n == UEINT ? e[TOT + slot] : (double)v[n * TOT + slot];
+  }
+};
+
+// One face of direction d (index fi in the tile's face block of that
+// direction, nf0 x nf1 x nf2): hydrodynamic and diffusion fluxes, staged.
 template <int NS, bool MIX, int d, class TL>
-__device__ __forceinline__ void dir_pass_mixed(const DevBox& b, const MechF<NS>& m, const DevMech<NS>& md,
-                                               const DevFlags& f, const Geo& g,
-                                               const int o[3], const int ext[3], const long long stv[3], bool mine,
-                                               int tx, int ty, int tz, double* fbuf, double* acc, const double* U) {
+__device__ __forceinline__ void face_mixed(const DevBox& b, const MechF<NS>& m, const DevMech<NS>& md,
+                                           const DevFlags& f, const Geo& g, const int o[3], const long long stv[3],
+                                           int fi, int nf0, int nf1, bool diff, const double* U,
+                                           const FaceStage<NS, TL>& fs) {
   constexpr int NVAR = 7 + NS;
-  const bool diff = f.diffuse_vel || f.diffuse_temp || f.diffuse_spec || f.diffuse_enth;
-  const int nf0 = ext[0] + (d == 0), nf1 = ext[1] + (d == 1), nf2 = ext[2] + (d == 2);
-  const int nfaces = nf0 * nf1 * nf2;
-  for (int fi = threadIdx.x; fi < nfaces; fi += TL::NT) {
-    const int fx = fi % nf0, fy = (fi / nf0) % nf1, fz = fi / (nf0 * nf1);
-    const int i = o[0] + fx, j = o[1] + fy, k = o[2] + fz;
-    const long long cR = (i - b.g2lo[0]) + (j - b.g2lo[1]) * stv[1] + (k - b.g2lo[2]) * stv[2];
-    float F[NVAR];
-    double FE = 0.0, FEI = 0.0;
-    if (f.do_hydro) {
-      hydro_face_f<NS, MIX, d>(b, m, md, f, cR, stv[d], U, F, FE, FEI);
-    } else {
+  const int fx = fi % nf0, fy = (fi / nf0) % nf1, fz = fi / (nf0 * nf1);
+  const int i = o[0] + fx, j = o[1] + fy, k = o[2] + fz;
+  const long long cR = (i - b.g2lo[0]) + (j - b.g2lo[1]) * stv[1] + (k - b.g2lo[2]) * stv[2];
+  float F[NVAR];
+  double FE = 0.0, FEI = 0.0;
+  if (f.do_hydro) {
+    hydro_face_f<NS, MIX, d>(b, m, md, f, cR, stv[d], U, F, FE, FEI);
+  } else {
 #pragma unroll
-      for (int n = 0; n < NVAR; ++n) F[n] = 0.f;
-    }
-    if (diff) diffusion_face_f<NS, d>(b, f, g, cR, stv, U, F);
-#pragma unroll
-    for (int n = 0; n < NVAR; ++n) fbuf[n * TL::MAXF + fi] = (double)F[n];  // exact widening
-    fbuf[UEDEN * TL::MAXF + fi] = FE + (double)F[UEDEN];
-    fbuf[UEINT * TL::MAXF + fi] = FEI;
+    for (int n = 0; n < NVAR; ++n) F[n] = 0.f;
   }
-  __syncthreads();
-  if (mine) {
-    const int flo = tx + nf0 * (ty + nf1 * tz);
-    const int fhi = flo + ((d == 0) ? 1 : (d == 1) ? nf0 : nf0 * nf1);
-    const double s = g.dxinv[d];
+  if (diff) diffusion_face_f<NS, d>(b, f, g, cR, stv, U, F);
+  const int slot = FaceStage<NS, TL>::base(d) + fi;
 #pragma unroll
-    for (int n = 0; n < NVAR; ++n) acc[n] = fma(fbuf[n * TL::MAXF + flo] - fbuf[n * TL::MAXF + fhi], s, acc[n]);
-  }
-  __syncthreads();
+  for (int n = 0; n < NVAR; ++n)
+    if (n != UEDEN && n != UEINT) fs.v[n * FaceStage<NS, TL>::TOT + slot] = F[n];
+  fs.e[slot] = FE + (double)F[UEDEN];
+  fs.e[FaceStage<NS, TL>::TOT + slot] = FEI;
 }
 
 // Pass 2 over the tile list; CTA b takes tiles b, b + gridDim.x, ... (one
 // each with one CTA per tile; a persistent launch strides over the list).
+// The faces of all three directions of a tile form one list that the warps
+// take 32 at a time (a warp's faces share a direction), then one barrier,
+// then each cell sums its six faces: x, y, z in turn, each as
+// (F_lo - F_hi) / dx in FP64.  Per-direction barriers would leave most warps
+// idle while the last few faces of a direction finish (288 faces of 8x8x4
+// cells on 256 threads take two rounds).
 template <int NS, bool MIX, class TL = TileDefault>
 __global__ void __launch_bounds__(TL::NT, TL::MINB)
     flux_kernel_mixed(const DevBox* __restrict__ boxes, const int4* __restrict__ tiles, int ntiles,
                       const __grid_constant__ MechF<NS> m, const __grid_constant__ DevMech<NS> md, const DevFlags f,
                       const Geo g, unsigned long long* __restrict__ counters) {
   constexpr int NVAR = 7 + NS;
-  double* fbuf;
-  if constexpr (TL::DYN) {
-    extern __shared__ double flux_dyn_smem[];
-    fbuf = flux_dyn_smem;
-  } else {
-    __shared__ double flux_static_smem[NVAR * TL::MAXF];
-    fbuf = flux_static_smem;
-  }
+  constexpr int NW = TL::NT / 32;
+  extern __shared__ double flux_dyn_smem[];
+  FaceStage<NS, TL> fs;
+  fs.e = flux_dyn_smem;
+  fs.v = reinterpret_cast<float*>(flux_dyn_smem + 2 * FaceStage<NS, TL>::TOT);
+  const bool diff = f.diffuse_vel || f.diffuse_temp || f.diffuse_spec || f.diffuse_enth;
   const int tx = threadIdx.x % TL::TX, ty = (threadIdx.x / TL::TX) % TL::TY, tz = threadIdx.x / (TL::TX * TL::TY);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   for (int tb = blockIdx.x; tb < ntiles; tb += gridDim.x) {
     const int4 t = tiles[tb];
     const DevBox& b = boxes[t.x];
@@ -814,17 +824,40 @@ __global__ void __launch_bounds__(TL::NT, TL::MINB)
                         min(TL::TZ, b.hi[2] - o[2] + 1)};
     const bool mine = tx < ext[0] && ty < ext[1] && tz < ext[2];
     const long long stv[3] = {1, b.n2[0], (long long)b.n2[0] * b.n2[1]};
-    __shared__ double Us[3];  // the box's reference velocity (read before the first direction pass's barrier)
+    __shared__ double Us[3];  // the box's reference velocity
     if (threadIdx.x == 0) box_uref(b, Us);
     __syncthreads();
-    double acc[NVAR];
-#pragma unroll
-    for (int n = 0; n < NVAR; ++n) acc[n] = 0.0;
-    dir_pass_mixed<NS, MIX, 0, TL>(b, m, md, f, g, o, ext, stv, mine, tx, ty, tz, fbuf, acc, Us);
-    dir_pass_mixed<NS, MIX, 1, TL>(b, m, md, f, g, o, ext, stv, mine, tx, ty, tz, fbuf, acc, Us);
-    dir_pass_mixed<NS, MIX, 2, TL>(b, m, md, f, g, o, ext, stv, mine, tx, ty, tz, fbuf, acc, Us);
+    // faces of direction d: (ext + e_d) in each direction
+    const int n0 = (ext[0] + 1) * ext[1] * ext[2], n1 = ext[0] * (ext[1] + 1) * ext[2],
+              n2 = ext[0] * ext[1] * (ext[2] + 1);
+    const int c0 = (n0 + 31) >> 5, c1 = (n1 + 31) >> 5, c2 = (n2 + 31) >> 5;
+    for (int c = warp; c < c0 + c1 + c2; c += NW) {
+      if (c < c0) {
+        const int fi = (c << 5) + lane;
+        if (fi < n0) face_mixed<NS, MIX, 0, TL>(b, m, md, f, g, o, stv, fi, ext[0] + 1, ext[1], diff, Us, fs);
+      } else if (c < c0 + c1) {
+        const int fi = ((c - c0) << 5) + lane;
+        if (fi < n1) face_mixed<NS, MIX, 1, TL>(b, m, md, f, g, o, stv, fi, ext[0], ext[1] + 1, diff, Us, fs);
+      } else {
+        const int fi = ((c - c0 - c1) << 5) + lane;
+        if (fi < n2) face_mixed<NS, MIX, 2, TL>(b, m, md, f, g, o, stv, fi, ext[0], ext[1], diff, Us, fs);
+      }
+    }
+    __syncthreads();
     bool bad = false;
     if (mine) {
+      double acc[NVAR];
+#pragma unroll
+      for (int n = 0; n < NVAR; ++n) acc[n] = 0.0;
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        const int nf0 = ext[0] + (d == 0), nf1 = ext[1] + (d == 1);
+        const int flo = FaceStage<NS, TL>::base(d) + tx + nf0 * (ty + nf1 * tz);
+        const int fhi = flo + ((d == 0) ? 1 : (d == 1) ? nf0 : nf0 * nf1);
+        const double s = g.dxinv[d];
+#pragma unroll
+        for (int n = 0; n < NVAR; ++n) acc[n] = fma(fs.get(n, flo) - fs.get(n, fhi), s, acc[n]);
+      }
       const int i = o[0] + tx, j = o[1] + ty, k = o[2] + tz;
       double* r = b.R + (i - b.rb[0]) + (long long)(j - b.rb[1]) * b.rj + (long long)(k - b.rb[2]) * b.rk;
 #pragma unroll
@@ -835,6 +868,7 @@ __global__ void __launch_bounds__(TL::NT, TL::MINB)
     }
     if (f.check_output) warp_count(&counters[kCounterNonfinite], bad);
     if (threadIdx.x == 0) atomicAdd(&counters[kCounterCells], (unsigned long long)(ext[0] * ext[1] * ext[2]));
+    __syncthreads();  // the next tile's faces overwrite the staging
   }
 }
 
@@ -846,13 +880,13 @@ inline cudaError_t launch_flux_mixed_at(const DevBox* boxes, const int4* tiles, 
                                         unsigned long long* counters, cudaStream_t s, bool persistent) {
   static std::atomic<unsigned long long> opted{0};  // bit per device
   static std::atomic<int> resident[64];             // persistent grid per device (0: not known yet)
-  constexpr size_t smem = TL::DYN ? sizeof(double) * (7 + NS) * TL::MAXF : 0;
+  constexpr size_t smem = mixed_flux_smem_bytes<NS, TL>();
   if (ntiles <= 0) return cudaSuccess;
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
   const unsigned long long bit = (dev >= 0 && dev < 64) ? (1ull << dev) : 0ull;
-  if (TL::DYN && (!bit || !(opted.load() & bit))) {
+  if (!bit || !(opted.load() & bit)) {
     e = cudaFuncSetAttribute(flux_kernel_mixed<NS, MIX, TL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     opted.fetch_or(bit);

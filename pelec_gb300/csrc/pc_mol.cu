@@ -303,15 +303,15 @@ std::vector<int> tune_key(const pc_box_desc* boxes, int nboxes) {
 }
 
 // Dynamic shared memory of the flux pass at launch configuration t for the
-// handle's species count and precision (bytes).  The FP64 passes stage face
-// fluxes, cell slopes and the z carry; the mixed pass only the face fluxes,
-// and those in static shared memory for tiles of at most 256 cells.
+// handle's species count and precision (bytes).  The FP64 passes stage one
+// direction's face fluxes, cell slopes and the z carry; the mixed pass the
+// face fluxes of all three directions.
 size_t flux_pass_smem(const pc_mol_handle* h, int t) {
   return with_species(h->cfg.nspec, [&](auto sc) -> size_t {
     constexpr int NS = decltype(sc)::value;
     auto of = [&](auto tl) -> size_t {
       using TL = decltype(tl);
-      if (h->cfg.precision == PC_PRECISION_MIXED) return TL::DYN ? sizeof(double) * (7 + NS) * TL::MAXF : 0;
+      if (h->cfg.precision == PC_PRECISION_MIXED) return mixed_flux_smem_bytes<NS, TL>();
       return flux_smem_bytes<NS, TL>();
     };
     switch (t % kNumTiles) {
