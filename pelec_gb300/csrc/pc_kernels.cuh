@@ -753,14 +753,6 @@ constexpr size_t flux_smem_bytes() {
                            (size_t)(7 + NS + 4 + NS) * TL::TX * TL::TY);
 }
 
-// Dynamic shared memory of the mixed-precision flux pass (pc_mixed.cuh): the
-// face fluxes of all three directions of a tile at once, FP32 except the
-// total and internal energy fluxes (FP64).
-template <int NS, class TL>
-constexpr size_t mixed_flux_smem_bytes() {
-  return (size_t)(TL::F0 + TL::F1 + TL::F2) * (2 * sizeof(double) + sizeof(float) * (7 + NS));
-}
-
 // Pass 2 over the tile list.  CTA b takes the contiguous share
 // [b n / G, (b + 1) n / G) of the n tiles (G = gridDim.x): one tile each when
 // G = n; in a persistent launch (as many CTAs as fit on the GPU at once) a

@@ -751,6 +751,14 @@ __device__ __forceinline__ void diffusion_face_f(const DevBox& b, const DevFlags
   if (ener) F[UEDEN] += fE;
 }
 
+// Dynamic shared memory of the mixed-precision flux pass: the
+// face fluxes of all three directions of a tile at once, FP32 except the
+// total and internal energy fluxes (FP64).
+template <int NS, class TL>
+constexpr size_t mixed_flux_smem_bytes() {
+  return (size_t)(TL::F0 + TL::F1 + TL::F2) * (2 * sizeof(double) + sizeof(float) * (7 + NS));
+}
+
 // Shared-memory staging of the face fluxes of a tile, all three directions
 // at once: the FP64 total and internal energy fluxes first, then the other
 // components in FP32 (their widening to FP64 is exact, so it can wait for the

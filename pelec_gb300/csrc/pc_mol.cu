@@ -18,6 +18,7 @@
 #include "pc_adjoint.cuh"
 #include "pc_kernels.cuh"
 #include "pc_level.cuh"
+#include "pc_mixed.cuh"
 #include "pc_rcp.h"
 #include "pelec_mol.h"
 
