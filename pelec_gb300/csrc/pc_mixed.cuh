@@ -280,6 +280,152 @@ __device__ __forceinline__ float face_coeff(float a, float b, bool harmonic) {
   return 0.5f * (a + b);
 }
 
+// Double-float counterparts of IdealMixEos's mixture sums and polynomials:
+// R/Wbar = sum_k Y_k R/W_k, the mixture NASA-7 coefficients of range r,
+// e(T) = C5 + T ((C0 - R/Wbar) + T (C1/2 + T (C2/3 + T (C3/4 + T C4/5))))
+// and cv(T) = (C0 - R/Wbar) + T (C1 + T (C2 + T (C3 + T C4))).
+template <int NS>
+__device__ __forceinline__ ff mix_rw_ff(const MechF<NS>& m, const ff* Y) {
+  ff rw = ff_mul(Y[0], m.rWf[0]);
+#pragma unroll
+  for (int k = 1; k < NS; ++k) rw = ff_fma(Y[k], m.rWf[k], rw);
+  return rw;
+}
+template <int NS>
+__device__ __forceinline__ void mix_coefs_ff(const MechF<NS>& m, const ff* Y, int r, ff C[6]) {
+#pragma unroll
+  for (int n = 0; n < 6; ++n) {
+    ff c = ff_mul(Y[0], m.cpcf[r][n][0]);
+#pragma unroll
+    for (int k = 1; k < NS; ++k) c = ff_fma(Y[k], m.cpcf[r][n][k], c);
+    C[n] = c;
+  }
+}
+template <int NS>
+__device__ __forceinline__ ff e_of_ff(const MechF<NS>& m, const ff C[6], ff c0, ff T) {
+  ff q = ff_fma(T, ff_mul(C[4], m.fifth), ff_mul(C[3], 0.25f));
+  q = ff_fma(T, q, ff_mul(C[2], m.third));
+  q = ff_fma(T, q, ff_mul(C[1], 0.5f));
+  q = ff_fma(T, q, c0);
+  return ff_fma(T, q, C[5]);
+}
+__device__ __forceinline__ ff cv_of_ff(const ff C[6], ff c0, ff T) {
+  ff w = ff_fma(T, C[4], C[3]);
+  w = ff_fma(T, w, C[2]);
+  w = ff_fma(T, w, C[1]);
+  return ff_fma(T, w, c0);
+}
+
+// REY2T in double-float arithmetic: IdealMixEos::rey2t's Newton iteration
+// on e(T) = e from the guess (steps clamped to +-1000 K, T >= 10 K, stop
+// once |T_new - T| <= 1e-12 T_new, ok = false after maxit iterations).
+template <int NS>
+__device__ ff rey2t_ff(const MechF<NS>& m, const ff* Y, ff rw, ff ein, double Tguess, int maxit, bool& ok) {
+  ff t = (Tguess > 0.0 && isfinite(Tguess)) ? ff_of(Tguess) : ff_of(1000.f);
+  int r = t.hi < m.tmid ? 0 : 1;
+  ff C[6];
+  mix_coefs_ff<NS>(m, Y, r, C);
+  ok = false;
+  for (int it = 0; it < maxit; ++it) {
+    const int rn = t.hi < m.tmid ? 0 : 1;
+    if (rn != r) {
+      r = rn;
+      mix_coefs_ff<NS>(m, Y, r, C);
+    }
+    const ff c0 = ff_sub(C[0], rw);
+    ff dt = ff_div(ff_sub(ein, e_of_ff<NS>(m, C, c0, t)), cv_of_ff(C, c0, t));
+    if (dt.hi > 1000.f) dt = ff_of(1000.f);
+    if (dt.hi < -1000.f) dt = ff_of(-1000.f);
+    ff tn = ff_add(t, dt);
+    if (tn.hi < 10.f) tn = ff_of(10.f);
+    const bool conv = fabsf(ff_to_float(ff_sub(tn, t))) <= 1e-12f * tn.hi;
+    t = tn;
+    if (conv) {
+      ok = true;
+      break;
+    }
+  }
+  return t;
+}
+
+// One cell of the mixed cell pass with the ideal-mixture EOS, in
+// double-float arithmetic (pc_ff.cuh): the FP64 state read as hi + lo pairs,
+// then ctoprim (Y_k = rho Y_k / rho with the |Y| < 1e-4 eps zeroing of
+// Utilities.H:288-294, e = (rho E - rho |u|^2 / 2) / rho), the temperature
+// Newton solve, p = rho (R/Wbar) T and the mole fractions; the record's FP32
+// fields are those values rounded, its FP64 fields (X, T, rho, Y) the pairs.
+template <int NS, bool SIMPLE>
+__device__ __forceinline__ void cell_mixed_ff(const DevBox& b, const MechF<NS>& mf, const DevFlags& f, long long c,
+                                              const double* Us, bool& newton_fail, bool& nonpos) {
+  using RC = Rec<NS>;
+  const int nx = b.n2[0], ny = b.n2[1];
+  const int i = b.g2lo[0] + (int)(c % nx);
+  const int j = b.g2lo[1] + (int)((c / nx) % ny);
+  const int k = b.g2lo[2] + (int)(c / ((long long)nx * ny));
+  const double* s = b.S + (i - b.sb[0]) + (long long)(j - b.sb[1]) * b.sj + (long long)(k - b.sb[2]) * b.sk;
+  const long long sn = b.sn;
+  const ff rho = ff_of(__ldg(s + URHO * sn));
+  const ff ir = ff_div(ff_of(1.f), rho);
+  const ff vx = ff_mul(ff_of(__ldg(s + UMX * sn)), ir);
+  const ff vy = ff_mul(ff_of(__ldg(s + UMY * sn)), ir);
+  const ff vz = ff_mul(ff_of(__ldg(s + UMZ * sn)), ir);
+  const ff v2 = ff_fma(vz, vz, ff_fma(vy, vy, ff_mul(vx, vx)));
+  const ff e = ff_mul(ff_sub(ff_of(__ldg(s + UEDEN * sn)), ff_mul(ff_mul(rho, v2), 0.5f)), ir);
+  ff Y[NS];
+  float Yf[NS];
+#pragma unroll
+  for (int n = 0; n < NS; ++n) {
+    ff y = ff_mul(ff_of(__ldg(s + (UFS + n) * sn)), ir);
+    if (fabsf(y.hi) < 1e-4f * 2.220446049250313e-16f) y = ff_of(0.f);
+    Y[n] = y;
+    Yf[n] = ff_to_float(y);
+  }
+  const ff rw = mix_rw_ff<NS>(mf, Y);
+  bool ok = true;
+  const ff T = rey2t_ff<NS>(mf, Y, rw, e, __ldg(s + UTEMP * sn), f.newton_maxit, ok);
+  const ff p = ff_mul(ff_mul(rho, rw), T);
+  newton_fail = !ok;
+  nonpos = !(rho.hi > 0.f) || !(p.hi > 0.f) || !(T.hi > 0.f);
+  const float rhof = ff_to_float(rho), Tf = ff_to_float(T), pf = ff_to_float(p), rwf = ff_to_float(rw);
+  const float cs = EosF<NS, true>::cs_T(mf, Yf, rwf, rhof, Tf, pf);
+  float* r = reinterpret_cast<float*>(b.rec) + c;
+  const long long N = b.ncell;
+  r[RC::RHO * N] = rhof;
+  r[RC::U * N] = ff_to_float(ff_sub(vx, ff_of(Us[0])));  // velocity offsets from the box's reference velocity
+  r[RC::V * N] = ff_to_float(ff_sub(vy, ff_of(Us[1])));
+  r[RC::W * N] = ff_to_float(ff_sub(vz, ff_of(Us[2])));
+  r[RC::P * N] = ff_to_float(ff_sub(p, ff_of(mf.p_ref)));
+  r[RC::C * N] = cs;
+#pragma unroll
+  for (int n = 0; n < NS; ++n) r[(RC::Y + n) * N] = Yf[n];
+  const bool inner = i >= b.lo[0] - 1 && i <= b.hi[0] + 1 && j >= b.lo[1] - 1 && j <= b.hi[1] + 1 &&
+                     k >= b.lo[2] - 1 && k <= b.hi[2] + 1;
+  if (inner) {
+    float X[NS];
+    float2* xr = mixed_x<NS>(b) + c;
+    const ff irw = ff_div(ff_of(1.f), rw);
+#pragma unroll
+    for (int n = 0; n < NS; ++n) {
+      const ff x = ff_mul(ff_mul(Y[n], mf.rWf[n]), irw);
+      xr[n * N] = make_float2(x.hi, x.lo);
+      X[n] = ff_to_float(x);
+    }
+    xr[NS * N] = make_float2(T.hi, T.lo);
+    xr[kMixedRho<NS> * N] = make_float2(rho.hi, rho.lo);
+#pragma unroll
+    for (int n = 0; n < NS; ++n) xr[(kMixedRho<NS> + 1 + n) * N] = make_float2(Y[n].hi, Y[n].lo);
+    float out[NS + 3];
+    TransF<NS, SIMPLE>::eval(mf, Tf, rhof, pf, Yf, X, out);
+    r[RC::T * N] = Tf;
+    float h[NS];
+    EosF<NS, true>::hi(mf, Tf, h);
+#pragma unroll
+    for (int n = 0; n < NS; ++n) r[(RC::H + n) * N] = h[n];
+#pragma unroll
+    for (int n = 0; n < NS + 3; ++n) r[(RC::D + n) * N] = out[n];
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Pass 1, mixed precision.  Records are FP32, in the field order of Rec<NS>
 // (P holds p - p_ref).
@@ -297,7 +443,9 @@ __global__ void __launch_bounds__(kCellThreads)
   if (threadIdx.x == 0) box_uref(b, Us);
   __syncthreads();
   bool newton_fail = false, nonpos = false;
-  if (c < b.ncell) {
+  if constexpr (MIX) {
+    if (c < b.ncell) cell_mixed_ff<NS, SIMPLE>(b, mf, f, c, Us, newton_fail, nonpos);
+  } else if (c < b.ncell) {
     const int nx = b.n2[0], ny = b.n2[1];
     const int i = b.g2lo[0] + (int)(c % nx);
     const int j = b.g2lo[1] + (int)((c / nx) % ny);
@@ -374,25 +522,11 @@ __global__ void __launch_bounds__(kCellThreads)
 template <int NS, bool MIX>
 __device__ __forceinline__ ff e_rp_ff(const MechF<NS>& m, const ff* Y, ff rho, ff p) {
   if constexpr (MIX) {
-    ff rw = ff_mul(Y[0], m.rWf[0]);
-#pragma unroll
-    for (int k = 1; k < NS; ++k) rw = ff_fma(Y[k], m.rWf[k], rw);
+    const ff rw = mix_rw_ff<NS>(m, Y);
     const ff T = ff_div(p, ff_mul(rho, rw));
-    const int r = T.hi < m.tmid ? 0 : 1;
     ff C[6];
-#pragma unroll
-    for (int n = 0; n < 6; ++n) {
-      ff c = ff_mul(Y[0], m.cpcf[r][n][0]);
-#pragma unroll
-      for (int k = 1; k < NS; ++k) c = ff_fma(Y[k], m.cpcf[r][n][k], c);
-      C[n] = c;
-    }
-    // e = C5 + T ((C0 - rw) + T (C1/2 + T (C2/3 + T (C3/4 + T C4/5))))
-    ff q = ff_fma(T, ff_mul(C[4], m.fifth), ff_mul(C[3], 0.25f));
-    q = ff_fma(T, q, ff_mul(C[2], m.third));
-    q = ff_fma(T, q, ff_mul(C[1], 0.5f));
-    q = ff_fma(T, q, ff_sub(C[0], rw));
-    return ff_fma(T, q, C[5]);
+    mix_coefs_ff<NS>(m, Y, T.hi < m.tmid ? 0 : 1, C);
+    return e_of_ff<NS>(m, C, ff_sub(C[0], rw), T);
   } else {
     return ff_div(p, ff_mul(m.gm1f, rho));
   }
