@@ -13,7 +13,8 @@ all-reduce (min) for the time step (PeleC.cpp:939).  Here:
 * ``global_min`` — the time-step all-reduce over a torch.distributed group
   (NCCL between GPUs, gloo on CPU).
 
-The ghost exchange between ranks is not built: on one GPU the fill is a
+The ghost exchange between ranks is pelec_gb300/halo.py (a copy plan from
+the BoxArray, one packed message per peer pair); on one GPU the fill is a
 device kernel over the whole level (pc_mol_fill_ghosts).
 """
 from __future__ import annotations
