@@ -248,6 +248,39 @@ def fp64_roofline(prof: dict, ms_rhs: float, peaks: dict) -> dict:
                              + prof.get("source", "")}
 
 
+def algorithmic_flops(workload_name: str) -> dict:
+    """Exact algorithmic FP64 work of one RHS of the workload (flops and
+    transcendentals), counted by running the reference's own hot-path code and
+    the oracle's EOS and transport with a counting scalar type
+    (oracle/count_flops.py -> profiles/algorithmic_flops.txt); {} if absent."""
+    path = os.path.join(ROOT, "profiles", "algorithmic_flops.txt")
+    out = {}
+    if not os.path.exists(path):
+        return out
+    for ln in open(path):
+        if ln.startswith(workload_name + "_") and ":" in ln:
+            k, v = (x.strip() for x in ln.split(":", 1))
+            out[k[len(workload_name) + 1:]] = float(v)
+    return out
+
+
+def fp64_algorithmic(workload_name: str, ms_rhs: float, peaks: dict) -> dict:
+    """The algorithm's FP64 flops of one RHS over the RHS time against the
+    FP64 FMA rate measured in this run (the executed counts of fp64_roofline
+    also hold the extra instructions of divisions, square roots and
+    exponentials)."""
+    a = algorithmic_flops(workload_name)
+    peak = peaks.get("fp64_fma_tflops")
+    if not a or not peak:
+        return {"frac": None, "note": "no algorithmic count for this workload"}
+    achieved = a["flops_per_rhs"] / (ms_rhs * 1e-3) / 1e12
+    return {"unit": "TFLOP/s", "achieved": achieved, "peak": peak, "frac": achieved / peak,
+            "flops_per_rhs": a["flops_per_rhs"], "flops_per_cell": a["flops_per_cell"],
+            "transcendentals_per_cell": a["transcendentals_per_cell"],
+            "counts_source": "profiles/algorithmic_flops.txt (oracle/count_flops.py: the reference's hot-path code "
+                             "and the oracle's EOS/transport run with a counting double; add+mul+div+sqrt+2 fma)"}
+
+
 def launch_name(t: int) -> str:
     """'8x8x4', or '8x8x4/persistent', for flux-pass launch configuration t."""
     from pelec_gb300 import abi, mol
@@ -865,6 +898,7 @@ def run_gpu(args):
                      "alg_bytes_per_rhs": ab, "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)",
                      "binding_resource": "FP64 pipe",
                      "fp64": fp64_roofline(prof, ms_rhs, peaks_fp),
+                     "fp64_algorithmic": fp64_algorithmic(args.workload, ms_rhs, peaks_fp),
                      "fp64_pipe_active_pct": {"flux_kernel": prof.get("fp64_pipe_active_pct_flux_kernel"),
                                               "cell_kernel": prof.get("fp64_pipe_active_pct_cell_kernel"),
                                               "source": "ncu, " + prof.get("source", "no profile")},

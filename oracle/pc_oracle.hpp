@@ -119,16 +119,38 @@ inline void for_box(const Box& b, F&& f) {
 // exactly (IEEE fma, division and square root are correctly rounded), so an
 // implementation that performs the same operations reproduces these values
 // bit for bit.
-template <int NS>
-inline double mix_rw(const pc_mechanism* m, const double* Y) {
-  double s = 0.0;
+// The equation-of-state and transport code below is templated on its scalar
+// type R: double everywhere in the oracle, and a counting double in the
+// flop-counting build of the reference harness (ref_shim/flop_count.hpp).
+// exp and log are the shared pc_exp.h implementations (oexp / olog; the
+// counting type overloads them).
+inline double oexp(double x) { return pc_math::exp(x); }
+inline double olog(double x) { return pc_math::log(x); }
+#ifdef PC_COUNT_FLOPS
+}  // namespace orc
+namespace pcc {
+inline CReal oexp(CReal x) {
+  PCC_COUNT(exp);
+  return CReal(pc_math::exp(x.v));
+}
+inline CReal olog(CReal x) {
+  PCC_COUNT(log);
+  return CReal(pc_math::log(x.v));
+}
+}  // namespace pcc
+namespace orc {
+#endif
+
+template <int NS, class R>
+inline R mix_rw(const pc_mechanism* m, const R* Y) {
+  R s = 0.0;
   for (int k = 0; k < NS; ++k) s = std::fma(Y[k], RU / m->mw[k], s);
   return s;
 }
 // X_k = Y_k Wbar / W_k = Y_k (R/W_k) / rWbar.
-template <int NS>
-inline void mix_y2x(const pc_mechanism* m, const double* Y, double* X) {
-  const double rw = mix_rw<NS>(m, Y);
+template <int NS, class R>
+inline void mix_y2x(const pc_mechanism* m, const R* Y, R* X) {
+  const R rw = mix_rw<NS>(m, Y);
   for (int k = 0; k < NS; ++k) X[k] = Y[k] * (RU / m->mw[k]) / rw;
 }
 
@@ -136,30 +158,41 @@ inline void mix_y2x(const pc_mechanism* m, const double* Y, double* X) {
 template <int NS>
 struct GammaLaw {
   const pc_mechanism* m;
-  void Y2WBAR(const double* Y, double& wbar) const { wbar = RU / mix_rw<NS>(m, Y); }
-  void REY2T(double /*rho*/, double e, const double* Y, double& T, int& /*iters*/, bool& ok) const {
+  template <class R>
+  void Y2WBAR(const R* Y, R& wbar) const { wbar = RU / mix_rw<NS>(m, Y); }
+  template <class R>
+  void REY2T(R /*rho*/, R e, const R* Y, R& T, int& /*iters*/, bool& ok) const {
     T = e * (m->gamma - 1.0) / mix_rw<NS>(m, Y);
     ok = true;
   }
-  void RTY2P(double rho, double T, const double* Y, double& p) const { p = rho * mix_rw<NS>(m, Y) * T; }
-  void RTY2Cs(double rho, double T, const double* Y, double& cs) const {
-    double p;
+  template <class R>
+  void RTY2P(R rho, R T, const R* Y, R& p) const { p = rho * mix_rw<NS>(m, Y) * T; }
+  template <class R>
+  void RTY2Cs(R rho, R T, const R* Y, R& cs) const {
+    R p;
     RTY2P(rho, T, Y, p);
     cs = std::sqrt(m->gamma * p / rho);
   }
-  void RTY2G(double, double, const double*, double& g) const { g = m->gamma; }
-  void RTY2dpde_dpdre(double rho, double T, const double* Y, double& dpde, double& dpdr_e) const {
+  template <class R>
+  void RTY2G(R, R, const R*, R& g) const { g = m->gamma; }
+  template <class R>
+  void RTY2dpde_dpdre(R rho, R T, const R* Y, R& dpde, R& dpdr_e) const {
     dpde = (m->gamma - 1.0) * rho;
     dpdr_e = mix_rw<NS>(m, Y) * T;
   }
-  void RPY2Cs(double rho, double p, const double*, double& cs) const { cs = std::sqrt(m->gamma * p / rho); }
-  void RYP2E(double rho, const double*, double p, double& e) const { e = p / ((m->gamma - 1.0) * rho); }
-  void Y2X(const double* Y, double* X) const { mix_y2x<NS>(m, Y, X); }
-  void T2Hi(double T, double* h) const {
+  template <class R>
+  void RPY2Cs(R rho, R p, const R*, R& cs) const { cs = std::sqrt(m->gamma * p / rho); }
+  template <class R>
+  void RYP2E(R rho, const R*, R p, R& e) const { e = p / ((m->gamma - 1.0) * rho); }
+  template <class R>
+  void Y2X(const R* Y, R* X) const { mix_y2x<NS>(m, Y, X); }
+  template <class R>
+  void T2Hi(R T, R* h) const {
     for (int k = 0; k < NS; ++k) h[k] = (m->gamma / (m->gamma - 1.0) * RU / m->mw[k]) * T;
   }
-  void TY2CpCv(double, const double* Y, double& cp, double& cv) const {
-    const double rw = mix_rw<NS>(m, Y);
+  template <class R>
+  void TY2CpCv(R, const R* Y, R& cp, R& cv) const {
+    const R rw = mix_rw<NS>(m, Y);
     cv = rw / (m->gamma - 1.0);
     cp = cv + rw;
   }
@@ -176,34 +209,40 @@ template <int NS>
 struct IdealMix {
   const pc_mechanism* m;
   int maxit;
-  int range(double T) const { return (T < m->nasa_tmid[0]) ? 0 : 1; }
-  void coefs(const double* Y, int r, double C[6]) const {
+  template <class R>
+  int range(R T) const { return (T < m->nasa_tmid[0]) ? 0 : 1; }
+  template <class R>
+  void coefs(const R* Y, int r, R C[6]) const {
     const double(*a)[7] = r == 0 ? m->nasa_lo : m->nasa_hi;
     for (int n = 0; n < 6; ++n) {
-      double s = 0.0;
+      R s = 0.0;
       for (int k = 0; k < NS; ++k) s = std::fma(Y[k], (RU / m->mw[k]) * a[k][n], s);
       C[n] = s;
     }
   }
-  static double cv_of(const double C[6], double rw, double T) {
+  template <class R>
+  static R cv_of(const R C[6], R rw, R T) {
     return (C[0] - rw) + T * std::fma(T, std::fma(T, std::fma(T, C[4], C[3]), C[2]), C[1]);
   }
-  static double e_of(const double C[6], double rw, double T) {
-    const double p = std::fma(
+  template <class R>
+  static R e_of(const R C[6], R rw, R T) {
+    const R p = std::fma(
         T, std::fma(T, std::fma(T, std::fma(T, C[4] * 0.2, C[3] * 0.25), C[2] * (1.0 / 3.0)), C[1] * 0.5), C[0] - rw);
     return std::fma(T, p, C[5]);
   }
-  void Y2WBAR(const double* Y, double& wbar) const { wbar = RU / mix_rw<NS>(m, Y); }
+  template <class R>
+  void Y2WBAR(const R* Y, R& wbar) const { wbar = RU / mix_rw<NS>(m, Y); }
   // Temperature from internal energy by Newton's method on e(T) = e_in,
   // started from the caller's guess (U(UTEMP), Utilities.H:285).  Steps are
   // clamped to +-1000 K and T is kept >= 10 K; the solve stops once
   // |T_new - T| <= 1e-12 T_new, or fails after maxit iterations.
-  void REY2T(double /*rho*/, double ein, const double* Y, double& T, int& iters, bool& ok) const {
-    const double rw = mix_rw<NS>(m, Y);
-    double t = T;
+  template <class R>
+  void REY2T(R /*rho*/, R ein, const R* Y, R& T, int& iters, bool& ok) const {
+    const R rw = mix_rw<NS>(m, Y);
+    R t = T;
     if (!(t > 0.0) || !std::isfinite(t)) t = 1000.0;
     int r = range(t);
-    double C[6];
+    R C[6];
     coefs(Y, r, C);
     ok = false;
     int it = 0;
@@ -213,12 +252,12 @@ struct IdealMix {
         r = rn;
         coefs(Y, r, C);
       }
-      const double e = e_of(C, rw, t);
-      const double cv = cv_of(C, rw, t);
-      double dt = (ein - e) / cv;
+      const R e = e_of(C, rw, t);
+      const R cv = cv_of(C, rw, t);
+      R dt = (ein - e) / cv;
       if (dt > 1000.0) dt = 1000.0;
       if (dt < -1000.0) dt = -1000.0;
-      double tn = t + dt;
+      R tn = t + dt;
       if (tn < 10.0) tn = 10.0;
       const bool conv = std::fabs(tn - t) <= 1e-12 * tn;
       t = tn;
@@ -227,66 +266,78 @@ struct IdealMix {
     iters = it;
     T = t;
   }
-  void RTY2P(double rho, double T, const double* Y, double& p) const { p = rho * mix_rw<NS>(m, Y) * T; }
+  template <class R>
+  void RTY2P(R rho, R T, const R* Y, R& p) const { p = rho * mix_rw<NS>(m, Y) * T; }
   // c^2 = (cp/cv) p / rho with cp = cv + R/Wbar, evaluated as (cp p) / (cv rho).
-  double cs_at(double rho, double p, double T, const double* Y, double rw) const {
-    double C[6];
+  template <class R>
+  R cs_at(R rho, R p, R T, const R* Y, R rw) const {
+    R C[6];
     coefs(Y, range(T), C);
-    const double cv = cv_of(C, rw, T);
+    const R cv = cv_of(C, rw, T);
     return std::sqrt((cv + rw) * p / (cv * rho));
   }
-  void RTY2Cs(double rho, double T, const double* Y, double& cs) const {
-    const double rw = mix_rw<NS>(m, Y);
+  template <class R>
+  void RTY2Cs(R rho, R T, const R* Y, R& cs) const {
+    const R rw = mix_rw<NS>(m, Y);
     cs = cs_at(rho, rho * rw * T, T, Y, rw);
   }
-  void RTY2G(double, double T, const double* Y, double& g) const {
-    const double rw = mix_rw<NS>(m, Y);
-    double C[6];
+  template <class R>
+  void RTY2G(R, R T, const R* Y, R& g) const {
+    const R rw = mix_rw<NS>(m, Y);
+    R C[6];
     coefs(Y, range(T), C);
-    const double cv = cv_of(C, rw, T);
+    const R cv = cv_of(C, rw, T);
     g = (cv + rw) / cv;
   }
-  void RTY2dpde_dpdre(double rho, double T, const double* Y, double& dpde, double& dpdr_e) const {
-    const double rw = mix_rw<NS>(m, Y);
-    double C[6];
+  template <class R>
+  void RTY2dpde_dpdre(R rho, R T, const R* Y, R& dpde, R& dpdr_e) const {
+    const R rw = mix_rw<NS>(m, Y);
+    R C[6];
     coefs(Y, range(T), C);
     dpde = rho * rw / cv_of(C, rw, T);
     dpdr_e = rw * T;
   }
-  void RPY2Cs(double rho, double p, const double* Y, double& cs) const {
-    const double rw = mix_rw<NS>(m, Y);
+  template <class R>
+  void RPY2Cs(R rho, R p, const R* Y, R& cs) const {
+    const R rw = mix_rw<NS>(m, Y);
     cs = cs_at(rho, p, p / (rho * rw), Y, rw);
   }
-  void RYP2E(double rho, const double* Y, double p, double& e) const {
-    const double rw = mix_rw<NS>(m, Y);
-    const double T = p / (rho * rw);
-    double C[6];
+  template <class R>
+  void RYP2E(R rho, const R* Y, R p, R& e) const {
+    const R rw = mix_rw<NS>(m, Y);
+    const R T = p / (rho * rw);
+    R C[6];
     coefs(Y, range(T), C);
     e = e_of(C, rw, T);
   }
-  void Y2X(const double* Y, double* X) const { mix_y2x<NS>(m, Y, X); }
+  template <class R>
+  void Y2X(const R* Y, R* X) const { mix_y2x<NS>(m, Y, X); }
   // h_k = R/W_k T (h/RT)_k = e5_k + T (c0 + T (c1/2 + T (c2/3 + T (c3/4 + T c4/5)))), c = R/W_k a.
-  void T2Hi(double T, double* h) const {
+  template <class R>
+  void T2Hi(R T, R* h) const {
     const double(*a)[7] = range(T) == 0 ? m->nasa_lo : m->nasa_hi;
     for (int k = 0; k < NS; ++k) {
       const double r = RU / m->mw[k];
       const double c[6] = {r * a[k][0], r * a[k][1], r * a[k][2], r * a[k][3], r * a[k][4], r * a[k][5]};
-      const double p = std::fma(
-          T, std::fma(T, std::fma(T, std::fma(T, c[4] * 0.2, c[3] * 0.25), c[2] * (1.0 / 3.0)), c[1] * 0.5), c[0]);
-      h[k] = std::fma(T, p, c[5]);
+      const R p = std::fma(
+          T, std::fma(T, std::fma(T, std::fma(T, R(c[4] * 0.2), R(c[3] * 0.25)), R(c[2] * (1.0 / 3.0))), R(c[1] * 0.5)),
+          R(c[0]));
+      h[k] = std::fma(T, p, R(c[5]));
     }
   }
   // Mixture e and cv at T (used by tests).
-  void TY2E_Cv(double T, const double* Y, double& e, double& cv) const {
-    const double rw = mix_rw<NS>(m, Y);
-    double C[6];
+  template <class R>
+  void TY2E_Cv(R T, const R* Y, R& e, R& cv) const {
+    const R rw = mix_rw<NS>(m, Y);
+    R C[6];
     coefs(Y, range(T), C);
     e = e_of(C, rw, T);
     cv = cv_of(C, rw, T);
   }
-  void TY2CpCv(double T, const double* Y, double& cp, double& cv) const {
-    const double rw = mix_rw<NS>(m, Y);
-    double C[6];
+  template <class R>
+  void TY2CpCv(R T, const R* Y, R& cp, R& cv) const {
+    const R rw = mix_rw<NS>(m, Y);
+    R C[6];
     coefs(Y, range(T), C);
     cv = cv_of(C, rw, T);
     cp = cv + rw;
@@ -300,7 +351,8 @@ struct IdealMix {
 template <int NS, class EOS>
 struct ConstantTransport {
   const pc_mechanism* m;
-  void transport(const EOS&, double, double, const double*, double* Ddiag, double& mu, double& xi, double& lam) const {
+  template <class R>
+  void transport(const EOS&, R, R, const R*, R* Ddiag, R& mu, R& xi, R& lam) const {
     mu = m->const_mu;
     xi = m->const_xi;
     lam = m->const_lambda;
@@ -321,39 +373,40 @@ struct ConstantTransport {
 template <int NS, class EOS>
 struct SimpleTransport {
   const pc_mechanism* m;
-  static double fit(const double* c, double L) { return std::fma(L, std::fma(L, std::fma(L, c[3], c[2]), c[1]), c[0]); }
-  void transport(const EOS& eos, double T, double rho, const double* Y, double* Ddiag, double& mu, double& xi,
-                 double& lam) const {
-    double X[NS];
+  template <class R>
+  static R fit(const double* c, R L) { return std::fma(L, std::fma(L, std::fma(L, R(c[3]), R(c[2])), R(c[1])), R(c[0])); }
+  template <class R>
+  void transport(const EOS& eos, R T, R rho, const R* Y, R* Ddiag, R& mu, R& xi, R& lam) const {
+    R X[NS];
     eos.Y2X(Y, X);
-    double p;
+    R p;
     eos.RTY2P(rho, T, Y, p);
-    const double L = pc_math::log(T);
-    double smu = 0.0, slam = 0.0, sxi = 0.0;
+    const R L = olog(T);
+    R smu = 0.0, slam = 0.0, sxi = 0.0;
     for (int k = 0; k < NS; ++k) {
-      const double mk = pc_math::exp(fit(m->visc_fit[k], L));
-      const double m2 = mk * mk;
+      const R mk = oexp(fit(m->visc_fit[k], L));
+      const R m2 = mk * mk;
       smu = std::fma(X[k], m2 * m2 * m2, smu);
-      slam = std::fma(X[k], pc_math::exp(0.25 * fit(m->cond_fit[k], L)), slam);
+      slam = std::fma(X[k], oexp(0.25 * fit(m->cond_fit[k], L)), slam);
       sxi = std::fma(X[k], m->bulk_ratio[k] * mk, sxi);
     }
-    mu = pc_math::exp(pc_math::log(smu) * (1.0 / 6.0));
-    const double l2 = slam * slam;
+    mu = oexp(olog(smu) * (1.0 / 6.0));
+    const R l2 = slam * slam;
     lam = l2 * l2;
     xi = sxi;
     // 1/D_kj(T,p) = exp(-fit) p / p_ref, accumulated over j != k in order.
-    const double pr = p * (1.0 / m->diff_pref);
+    const R pr = p * (1.0 / m->diff_pref);
     for (int k = 0; k < NS; ++k) {
-      double s = 0.0;
+      R s = 0.0;
       for (int j = 0; j < NS; ++j) {
         if (j == k) continue;
-        const double invD = pc_math::exp(-fit(m->diff_fit[std::min(j, k)][std::max(j, k)], L)) * pr;
-        s = std::fma(std::max(X[j], 1e-15), invD, s);
+        const R invD = oexp(-fit(m->diff_fit[std::min(j, k)][std::max(j, k)], L)) * pr;
+        s = std::fma(std::max(X[j], R(1e-15)), invD, s);
       }
       // W_k / Wbar = (R/Wbar) / (R/W_k): rhoD_k grad X_k is then the
       // Hirschfelder-Curtiss mass flux rho (W_k/Wbar) D_k,mix grad X_k.
-      const double wrat = mix_rw<NS>(m, Y) / (RU / m->mw[k]);
-      Ddiag[k] = (s > 0.0) ? rho * (1.0 - Y[k]) * wrat / s : 0.0;
+      const R wrat = mix_rw<NS>(m, Y) / (RU / m->mw[k]);
+      Ddiag[k] = (s > 0.0) ? R(rho * (1.0 - Y[k]) * wrat / s) : R(0.0);
     }
   }
 };

@@ -1,7 +1,8 @@
 """ORACLE build recipe (test infrastructure): compiles PeleC's own hot-path
 source code, where it lies in the reference tree, into
-``oracle/_ref/libpc_ref_ns{1,9}.so`` — one library per species count, since
-NUM_SPECIES is a compile-time constant of the reference.
+``oracle/_ref/libpc_ref_ns{1,9,21}.so`` — one library per species count,
+since NUM_SPECIES is a compile-time constant of the reference — and, on
+request, the flop-counting builds ``libpc_ref_count_ns{1,9}.so``.
 
 What is compiled from the reference (unchanged): Source/MOL.cpp (with MOL.H
 and Riemann.H), Source/Diffterm.H, Source/Utilities.H, Source/TransCoeff.H,
@@ -32,6 +33,7 @@ REF_ROOT = os.environ.get("PC_REFERENCE_ROOT", "/root/reference")
 REF_SRC = os.path.join(REF_ROOT, "Source")
 OUTDIR = os.path.join(HERE, "_ref")
 SPECIES = (1, 9, 21)
+COUNT_SPECIES = (1, 9)
 REF_FILES = ("MOL.cpp", "MOL.H", "Riemann.H", "Diffterm.H", "Utilities.H", "TransCoeff.H", "Timestep.H", "IndexDefines.H",
              "Constants.H", "EBStencilTypes.H")
 
@@ -40,8 +42,8 @@ def available() -> bool:
     return all(os.path.exists(os.path.join(REF_SRC, f)) for f in REF_FILES)
 
 
-def lib_path(ns: int) -> str:
-    return os.path.join(OUTDIR, f"libpc_ref_ns{ns}.so")
+def lib_path(ns: int, count: bool = False) -> str:
+    return os.path.join(OUTDIR, f"libpc_ref_{'count_' if count else ''}ns{ns}.so")
 
 
 def _deps():
@@ -64,19 +66,24 @@ def _pstl_dir() -> list:
     return []
 
 
-def build(force: bool = False) -> list:
+def build(force: bool = False, count: bool = False) -> list:
+    """The reference-source libraries, one per species count; with count,
+    the flop-counting builds instead (amrex::Real a counting double,
+    ref_shim/flop_count.hpp; exported ref_count_mol_rhs)."""
     if not available():
         raise FileNotFoundError(f"reference sources not found under {REF_SRC}")
     os.makedirs(OUTDIR, exist_ok=True)
     newest = max(os.path.getmtime(p) for p in _deps())
     procs, outs = [], []
     pstl = _pstl_dir()
-    for ns in SPECIES:
-        out = lib_path(ns)
+    # the counting build runs serially (no -fopenmp): its tallies are plain counters
+    extra = ["-DPC_COUNT_FLOPS", "-fno-strict-aliasing"] if count else ["-fopenmp"]
+    for ns in (COUNT_SPECIES if count else SPECIES):
+        out = lib_path(ns, count)
         outs.append(out)
         if not force and os.path.exists(out) and os.path.getmtime(out) >= newest:
             continue
-        cmd = ["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared", "-w",
+        cmd = ["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-w", *extra,
                f"-DPC_REF_NS={ns}", "-I-", *pstl, "-I", os.path.join(HERE, "ref_shim"), "-I", REF_SRC,
                "-I", os.path.join(ROOT, "include"), "-I", HERE, "-I", os.path.join(ROOT, "pelec_gb300", "csrc"),
                "-o", out + ".tmp", os.path.join(HERE, "ref_harness.cpp"), os.path.join(HERE, "ref_physics.cpp")]
@@ -93,5 +100,5 @@ def build(force: bool = False) -> list:
 if __name__ == "__main__":
     import sys
 
-    for o in build(force="--force" in sys.argv):
+    for o in build(force="--force" in sys.argv, count="--count" in sys.argv):
         print(o)

@@ -37,7 +37,7 @@ namespace {
 template <class T>
 amrex::Array4<T> view(const pc_array4& a) {
   amrex::Array4<T> v;
-  v.p = a.p;
+  v.p = reinterpret_cast<decltype(v.p)>(a.p);  // the counting build's Real is one double wide
   v.jstride = a.jstride;
   v.kstride = a.kstride;
   v.nstride = a.nstride;
@@ -202,6 +202,19 @@ int ref_mol_rhs(const pc_mol_config* cfg, const pc_box_desc* boxes, int nboxes, 
   return PC_OK;
 }
 
+#ifdef PC_COUNT_FLOPS
+// The arithmetic of ref_mol_rhs on the boxes, counted by class
+// (flop_count.hpp): out = [add, mul, div, fma, sqrt, exp, log, pow, cmp].
+int ref_count_mol_rhs(const pc_mol_config* cfg, const pc_box_desc* boxes, int nboxes, const double dx[3],
+                      unsigned long long* out) {
+  pcc::tally() = pcc::Tally{};
+  const int rc = ref_mol_rhs(cfg, boxes, nboxes, dx, nullptr);
+  const pcc::Tally& t = pcc::tally();
+  const unsigned long long v[9] = {t.add, t.mul, t.div, t.fma, t.sqrt, t.exp, t.log, t.pow, t.cmp};
+  for (int q = 0; q < 9; ++q) out[q] = v[q];
+  return rc;
+}
+#else
 // pc_ctoprim on one cell: U[NVAR] -> q[QVAR], qaux[NQAUX].
 int ref_ctoprim_cell(const pc_mol_config* cfg, const double* U, double* qv, double* qa) {
   if (cfg->nspec != NUM_SPECIES) return PC_ERR_UNSUPPORTED;
@@ -281,5 +294,6 @@ int ref_est_dt_parts(const pc_mol_config* cfg, const pc_box_desc* boxes, int nbo
   }
   return PC_OK;
 }
+#endif  // PC_COUNT_FLOPS
 
 }  // extern "C"

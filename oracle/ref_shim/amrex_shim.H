@@ -34,9 +34,17 @@
     if (!(c)) amrex::Abort(m);                  \
   } while (0)
 
+#ifdef PC_COUNT_FLOPS
+#include "flop_count.hpp"
+#endif
+
 namespace amrex {
 
+#ifdef PC_COUNT_FLOPS
+using Real = pcc::CReal;  // the flop-counting build (flop_count.hpp)
+#else
 using Real = double;
+#endif
 
 // amrex::min / amrex::max (AMReX_Algorithm.H): std::min / std::max.
 template <class T>

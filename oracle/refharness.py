@@ -129,3 +129,40 @@ def est_dt_parts(cfg: abi.PcMolConfig, boxes) -> list:
     if rc != 0:
         raise RuntimeError(f"ref_est_dt_parts failed with code {rc}")
     return list(parts)
+
+
+FLOP_CLASSES = ("add", "mul", "div", "fma", "sqrt", "exp", "log", "pow", "cmp")
+_count_libs: dict = {}
+
+
+def count_library(nspec: int) -> ctypes.CDLL:
+    """The flop-counting build (amrex::Real a counting double)."""
+    if nspec not in _count_libs:
+        ref_build.build(count=True)
+        lib = ctypes.CDLL(ref_build.lib_path(nspec, count=True))
+        lib.ref_count_mol_rhs.argtypes = [POINTER(abi.PcMolConfig), POINTER(abi.PcBoxDesc), c_int, POINTER(c_double),
+                                          POINTER(ctypes.c_ulonglong)]
+        lib.ref_count_mol_rhs.restype = c_int
+        _count_libs[nspec] = lib
+    return _count_libs[nspec]
+
+
+def count_mol_rhs(cfg: abi.PcMolConfig, boxes):
+    """(counts, RHS list): the floating-point operations of the reference's
+    RHS of the BoxStates by class (FLOP_CLASSES), and the RHS it computed
+    (the same IEEE operations as mol_rhs)."""
+    lib = count_library(cfg.nspec)
+    descs, outs = [], []
+    for st in boxes:
+        S = np.ascontiguousarray(st.S, dtype=np.float64)
+        nx, ny, nz = st.shape
+        R = np.zeros((S.shape[0], nz, ny, nx))
+        descs.append(abi.box_desc(st.lo, st.hi, abi.array4(S.ctypes.data, S.shape, st.begin),
+                                  abi.array4(R.ctypes.data, R.shape, st.lo)))
+        outs.append((S, R))
+    out = (ctypes.c_ulonglong * len(FLOP_CLASSES))()
+    dx = (c_double * 3)(*boxes[0].dx)
+    rc = lib.ref_count_mol_rhs(ctypes.byref(cfg), abi.box_array(descs), len(descs), dx, out)
+    if rc != 0:
+        raise RuntimeError(f"ref_count_mol_rhs failed with code {rc}")
+    return dict(zip(FLOP_CLASSES, (int(v) for v in out))), [R for _, R in outs]
