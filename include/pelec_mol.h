@@ -421,7 +421,8 @@ int pc_mol_check_quotients(const double* a, const double* b, double* q, long lon
  * lists and counters live in one fixed 48 MiB device array that each GPU
  * reserves when the library is loaded and keeps until the process exits; a
  * box that does not fit (larger than about 46^3 valid cells with 9 species,
- * 67^3 with one) returns PC_ERR_TOO_LARGE before anything is launched.  The first call
+ * 67^3 with one, 36^3 with 21) returns PC_ERR_TOO_LARGE before anything is
+ * launched.  The first call
  * on each device does the one-time set-up — it looks up that array's device
  * address and raises the flux kernels' shared-memory limit — so make that
  * first call before any stream capture.  Every call reuses the same array: calls

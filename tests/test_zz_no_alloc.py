@@ -17,7 +17,7 @@ import pytest
 
 from conftest import rel_maxnorm
 from gpu_util import gpu_rhs
-from pelec_gb300 import abi, problems
+from pelec_gb300 import abi, mechanism, problems
 
 pytestmark = pytest.mark.gpu
 
@@ -52,8 +52,10 @@ def test_static_entry_matches_level_entry_on_consecutive_calls(cuda_lib):
     mech9, flameA, _ = problems.flame((20, 16, 12), seed=31)
     _, flameB, _ = problems.flame((24, 24, 24), seed=32)
     mech1, tgv = problems.tgv(32, seed=33)
+    mech21, flame21, _ = problems.flame((16, 12, 20), seed=35, mech=mechanism.drm_synthetic())
     cases = [(problems.make_config(mech9), flameA), (problems.make_config(mech9), flameB),
-             (problems.make_config(mech1), tgv), (problems.make_config(mech9), flameA)]
+             (problems.make_config(mech1), tgv), (problems.make_config(mech21), flame21),
+             (problems.make_config(mech9), flameA)]
     outs = []
     for cfg, st in cases:  # consecutive calls share the static array
         rc, R = _run_static(mol, cfg, st)
@@ -66,7 +68,7 @@ def test_static_entry_matches_level_entry_on_consecutive_calls(cuda_lib):
         assert err.max() <= RTOL, err
         np.testing.assert_array_equal(R, ref)  # the same kernels: the same bits
     # the repeated box gives the same answer after other boxes used the array
-    np.testing.assert_array_equal(outs[0], outs[3])
+    np.testing.assert_array_equal(outs[0], outs[4])
 
 
 def test_static_entry_rejects_a_box_that_does_not_fit(cuda_lib):
