@@ -26,8 +26,10 @@
 // internal energy of the Godunov state, whose formation-energy terms cancel
 // to ~1e-2 of their size, is evaluated in double-float arithmetic at a
 // double-float density and composition: the upwind cell's values plus FP32
-// increments (hydro_face_f); the energy fluxes formed from it are widened to
-// FP64 for the divergence.
+// increments (hydro_face_f).  The cell's part of the mixture sums (R/Wbar and
+// the NASA-7 coefficients of both ranges) is formed once per cell in the cell
+// pass; a face adds the FP32 sums over its composition increments.  The
+// energy fluxes formed from it are widened to FP64 for the divergence.
 #pragma once
 
 #include "pc_ff.cuh"
@@ -94,18 +96,20 @@ __host__ MechF<NS> to_float(const DevMech<NS>& m, double p_ref) {
   return f;
 }
 
-// FP64 fields stored after the FP32 fields of a mixed record, for the cells
-// whose faces the pass evaluates (the valid cells and one layer around
-// them): the mole fractions X_k (NS), the temperature, the density and the
-// mass fractions Y_k (NS), each a double-float pair (hi, lo) in an FP64-wide
-// slot, field n of cell c at [n N + c].  X and T enter the
-// diffusion fluxes only through differences between neighbouring cells,
-// which FP32 values would resolve to no better than 1e-4 K / 1e-7 (the
-// flame's second differences of T are a few K per cell).  rho and Y are the
-// base of the Godunov state's FP64 density and composition (energy fluxes,
-// hydro_face_f).  The fields start at the first 8-byte boundary after the
-// Rec<NS>::N FP32 fields of every cell (N ncell floats may be odd); with
-// 2 NS + 2 of them a mixed record stays within the FP64 record's size.
+// FP64-accuracy fields stored after the FP32 fields of a mixed record, for
+// the cells whose faces the pass evaluates (the valid cells and one layer
+// around them), each a double-float pair (hi, lo) in an FP64-wide slot,
+// field n of cell c at [n N + c]: the mole fractions X_k (NS), the
+// temperature and the density; with the ideal-mixture EOS then R/Wbar and
+// the mixture NASA-7 coefficients C_n = sum_k Y_k (R/W_k) a_{n,k} of both
+// temperature ranges (12).  X and T enter the diffusion fluxes only through
+// differences between neighbouring cells, which FP32 values would resolve to
+// no better than 1e-4 K / 1e-7 (the flame's second differences of T are a
+// few K per cell).  rho, R/Wbar and C are the cell's part of the Godunov
+// state's density and mixture sums (energy fluxes, hydro_face_f), to which a
+// face adds only FP32 increments.  The fields start at the first 8-byte
+// boundary after the Rec<NS>::N FP32 fields of every cell (N ncell floats
+// may be odd); a mixed record stays within the FP64 record's size.
 template <int NS>
 __device__ __forceinline__ float2* mixed_x(const DevBox& b) {
   const long long nf = ((long long)Rec<NS>::N * b.ncell + 1) & ~1LL;
@@ -124,10 +128,18 @@ __device__ __forceinline__ ff ld_pair(const float2* p) {
 __device__ __forceinline__ float pair_diff(ff a, ff b) {
   return __fadd_rn(__fsub_rn(a.hi, b.hi), __fsub_rn(a.lo, b.lo));
 }
-// field index of the density in the FP64 part; Y_k follow it
+// field indices in the pair part: the density, R/Wbar, C[r][n] at
+// kMixedCoef + 6 r + n; kMixedPairs fields in all
 template <int NS>
 constexpr int kMixedRho = NS + 1;
-static_assert(2 * 21 + 2 <= Rec<21>::N / 2 && 2 * 9 + 2 <= Rec<9>::N / 2 && 2 * 1 + 2 <= Rec<1>::N / 2,
+template <int NS>
+constexpr int kMixedRw = NS + 2;
+template <int NS>
+constexpr int kMixedCoef = NS + 3;
+template <int NS, bool MIX>
+constexpr int kMixedPairs = MIX ? NS + 15 : NS + 2;
+static_assert(kMixedPairs<21, true> <= Rec<21>::N / 2 && kMixedPairs<9, true> <= Rec<9>::N / 2 &&
+                  kMixedPairs<1, false> <= Rec<1>::N / 2,
               "mixed record exceeds the FP64 record");
 
 // Reference velocity of a box: the velocity of its first valid cell (lo
@@ -412,8 +424,14 @@ __device__ __forceinline__ void cell_mixed_ff(const DevBox& b, const MechF<NS>& 
     }
     xr[NS * N] = make_float2(T.hi, T.lo);
     xr[kMixedRho<NS> * N] = make_float2(rho.hi, rho.lo);
+    xr[kMixedRw<NS> * N] = make_float2(rw.hi, rw.lo);
 #pragma unroll
-    for (int n = 0; n < NS; ++n) xr[(kMixedRho<NS> + 1 + n) * N] = make_float2(Y[n].hi, Y[n].lo);
+    for (int range = 0; range < 2; ++range) {
+      ff C[6];
+      mix_coefs_ff<NS>(mf, Y, range, C);
+#pragma unroll
+      for (int n = 0; n < 6; ++n) xr[(kMixedCoef<NS> + 6 * range + n) * N] = make_float2(C[n].hi, C[n].lo);
+    }
     float out[NS + 3];
     TransF<NS, SIMPLE>::eval(mf, Tf, rhof, pf, Yf, X, out);
     r[RC::T * N] = Tf;
@@ -499,8 +517,6 @@ __global__ void __launch_bounds__(kCellThreads)
       }
       xr[NS * N] = to_pair(T);
       xr[kMixedRho<NS> * N] = to_pair(rho);
-#pragma unroll
-      for (int n = 0; n < NS; ++n) xr[(kMixedRho<NS> + 1 + n) * N] = to_pair(Y[n]);
       float out[NS + 3];
       TransF<NS, SIMPLE>::eval(mf, Tf, rhof, pf, Yf, X, out);
       r[RC::T * N] = Tf;
@@ -540,6 +556,32 @@ __device__ __forceinline__ ff e_rp_ff_rY(const MechF<NS>& m, const float* rY, fl
 #pragma unroll
   for (int n = 0; n < NS; ++n) Y[n] = ff_mul(ir, rY[n]);
   return e_rp_ff<NS, MIX>(m, Y, ff_of(rho), p);
+}
+
+// Internal energy of a Godunov state whose composition is that of the
+// upwind cell (pairs xr: R/Wbar and the mixture coefficients of both ranges,
+// from the cell pass) plus FP32 increments dY, at density rho and pressure p:
+// the sums of e_rp_ff with the cell's part in double-float and the
+// increments' part sum_k dY_k c_k in FP32 (its rounding falls on the
+// increments only).
+template <int NS>
+__device__ __forceinline__ ff e_godunov_ff(const MechF<NS>& m, const float2* xr, long long N, const float* dY, ff rho,
+                                           ff p) {
+  float drw = 0.f;
+#pragma unroll
+  for (int k = 0; k < NS; ++k) drw = fmaf(dY[k], m.rW[k], drw);
+  const ff rw = ff_add(ld_pair(xr + kMixedRw<NS> * N), drw);
+  const ff T = ff_div(p, ff_mul(rho, rw));
+  const int r = T.hi < m.tmid ? 0 : 1;
+  ff C[6];
+#pragma unroll
+  for (int n = 0; n < 6; ++n) {
+    float dc = 0.f;
+#pragma unroll
+    for (int k = 0; k < NS; ++k) dc = fmaf(dY[k], m.cpc[r][n][k], dc);
+    C[n] = ff_add(ld_pair(xr + (kMixedCoef<NS> + 6 * r + n) * N), dc);
+  }
+  return e_of_ff<NS>(m, C, ff_sub(C[0], rw), T);
 }
 
 // FP64 internal energy from FP32 mass fractions Y (for Lax-Friedrichs sides).
@@ -743,14 +785,19 @@ __device__ __forceinline__ void hydro_face_f(const DevBox& b, const MechF<NS>& m
       const float w = min_ ? 1.f : (mout ? 0.f : frac);
       const float H = mask ? HL : HR, irf = mask ? 1.f / rl : 1.f / rr;
       const ff rg = ff_add(ld_pair(xr + kMixedRho<NS> * N), H + w * drho);
-      ff Yg[NS];
+      if constexpr (MIX) {
+        // Y_k of the Godunov state = the cell's Y_k + d_k, d_k = (h_k - Y_k H) / rho
+        // in FP32; its mixture sums are the cell's (pairs) + sum_k d_k c_k (FP32)
+        float dY[NS];
 #pragma unroll
-      for (int n = 0; n < NS; ++n) {
-        const ff y = ld_pair(xr + (kMixedRho<NS> + 1 + n) * N);
-        const float h = mask ? hL[n] : hR[n];
-        Yg[n] = ff_add(y, (h - y.hi * H) * irf);
+        for (int n = 0; n < NS; ++n) {
+          const float h = mask ? hL[n] : hR[n];
+          dY[n] = (h - ld(RC::Y + n, cu) * H) * irf;
+        }
+        regd = ff_mul(rg, e_godunov_ff<NS>(m, xr, N, dY, rg, gdpa));
+      } else {
+        regd = ff_mul(rg, e_rp_ff<NS, false>(m, nullptr, rg, gdpa));
       }
-      regd = ff_mul(rg, e_rp_ff<NS, MIX>(m, Yg, rg, gdpa));
     } else {
       regd = ff_mul(e_rp_ff_rY<NS, MIX>(m, flY, rgd, gdpa), rgd);
     }
