@@ -157,21 +157,26 @@ def cpu_baseline(st, cfg, reps: int = 2) -> dict:
             "best_s": min(times), "median_s": statistics.median(times)}
 
 
-# Sources that define the FP64 cell and flux kernels (and their compile
-# flags) whose traffic and instruction counts a profile describes; a profile
-# records their hash, and a figure whose hash no longer matches is reported
-# as stale (null), not used.
+# Sources that define the FP64 cell and flux kernels whose traffic and
+# instruction counts a profile describes, and the unit that compiles them; a
+# profile records their hash (with the compile flags of that unit), and a
+# figure whose hash no longer matches is reported as stale (null), not used.
 PROFILED_SOURCES = ("pelec_gb300/csrc/pc_kernels.cuh", "pelec_gb300/csrc/pc_device.cuh", "pelec_gb300/csrc/pc_exp.h",
-                    "pelec_gb300/csrc/pc_exp_tables.h", "pelec_gb300/build.py")
+                    "pelec_gb300/csrc/pc_exp_tables.h")
+PROFILED_UNIT = "pc_mol.cu"
 
 
 def kernel_source_hash() -> str:
     import hashlib
 
+    from pelec_gb300 import build
+
     h = hashlib.sha256()
     for f in PROFILED_SOURCES:
         h.update(f.encode())
         h.update(open(os.path.join(ROOT, f), "rb").read())
+    flags = [fl for src, fl in build.LIBS["libpelec_mol.so"] if src == PROFILED_UNIT][0]
+    h.update(repr((build.ARCH, build.COMMON, PROFILED_UNIT, flags)).encode())
     return h.hexdigest()[:16]
 
 

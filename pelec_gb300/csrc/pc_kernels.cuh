@@ -598,9 +598,9 @@ __device__ __forceinline__ void diffusion_face(const RecAcc<R>& ra, const DevFla
 // Pass 2.  tiles[b] = (box index, tile origin i, j, k).
 // ---------------------------------------------------------------------------
 // Tile of the flux pass: TX x TY x TZ cells, one thread per cell, MINB CTAs
-// per SM requested from the register allocator.  The face buffer holds
-// NVAR x MAXF doubles; tiles whose buffer exceeds the 48 KB of static shared
-// memory use dynamic shared memory (DYN).
+// per SM requested from the register allocator.  MAXF and MAXC are the
+// largest face and slope-cell counts of one direction (the shared-memory
+// staging of the FP64 pass).
 template <int TX_, int TY_, int TZ_, int MINB_>
 struct Tile {
   static constexpr int TX = TX_, TY = TY_, TZ = TZ_, MINB = MINB_, NT = TX_ * TY_ * TZ_;
@@ -610,7 +610,6 @@ struct Tile {
   // each side in that direction
   static constexpr int C0 = (TX_ + 2) * TY_ * TZ_, C1 = TX_ * (TY_ + 2) * TZ_, C2 = TX_ * TY_ * (TZ_ + 2);
   static constexpr int MAXC = C0 > C1 ? (C0 > C2 ? C0 : C2) : (C1 > C2 ? C1 : C2);
-  static constexpr bool DYN = TX_ * TY_ * TZ_ > 256;
 };
 // The tile shapes the level autotuner chooses from (index = PC_TILE_* order).
 using TileDefault = Tile<8, 8, 4, 2>;
