@@ -201,11 +201,15 @@ struct EosF<NS, true> {
       C[n] = s;
     }
   }
+  // sound speed from the mixture coefficients C of T's range
+  __device__ static float cs_C(const float C[5], float rw, float rho, float T, float p) {
+    const float cv = (C[0] - rw) + T * fmaf(T, fmaf(T, fmaf(T, C[4], C[3]), C[2]), C[1]);
+    return sqrtf((cv + rw) * p / (cv * rho));
+  }
   __device__ static float cs_T(const MechF<NS>& m, const float* Y, float rw, float rho, float T, float p) {
     float C[5];
     coefs<5>(m, Y, T < m.tmid ? 0 : 1, C);
-    const float cv = (C[0] - rw) + T * fmaf(T, fmaf(T, fmaf(T, C[4], C[3]), C[2]), C[1]);
-    return sqrtf((cv + rw) * p / (cv * rho));
+    return cs_C(C, rw, rho, T, p);
   }
   __device__ static float cs_rp(const MechF<NS>& m, const float* Y, float rw, float rho, float p) {
     return cs_T(m, Y, rw, rho, p / (rho * rw), p);
@@ -688,8 +692,24 @@ __device__ __forceinline__ void hydro_face_f(const DevBox& b, const MechF<NS>& m
   const float pref = m.p_ref;
   const float cavg = 0.5f * (cRc + cLc);
   const float rwl = mix_rwf<NS>(m, spl), rwr = mix_rwf<NS>(m, spr);
-  const float cl = E::cs_rp(m, spl, rwl, rl, pl + pref);
-  const float cr = E::cs_rp(m, spr, rwr, rr, pr + pref);
+  // The mixture coefficients of the two face states are kept: the upwind
+  // state of the solver has one of their compositions, and so has the star
+  // state unless a species density is clamped.
+  float CLc[5], CRc[5];
+  int rgL = 0, rgR = 0;
+  float cl, cr;
+  if constexpr (MIX) {
+    const float TLs = (pl + pref) / (rl * rwl), TRs = (pr + pref) / (rr * rwr);
+    rgL = TLs < m.tmid ? 0 : 1;
+    rgR = TRs < m.tmid ? 0 : 1;
+    E::template coefs<5>(m, spl, rgL, CLc);
+    E::template coefs<5>(m, spr, rgR, CRc);
+    cl = E::cs_C(CLc, rwl, rl, TLs, pl + pref);
+    cr = E::cs_C(CRc, rwr, rr, TRs, pr + pref);
+  } else {
+    cl = E::cs_rp(m, spl, rwl, rl, pl + pref);
+    cr = E::cs_rp(m, spr, rwr, rr, pr + pref);
+  }
   float fl_rho, fl_un, fl_ut1, fl_ut2;
   double fl_E, fl_ei;
   float flY[NS];
@@ -722,7 +742,8 @@ __device__ __forceinline__ void hydro_face_f(const DevBox& b, const MechF<NS>& m
 #pragma unroll
       for (int n = 0; n < NS; ++n) Yt[n] = rspo[n] * y;
     }
-    const float co = E::cs_rp(m, Yt, mix_rwf<NS>(m, Yt), ro, po + pref);
+    // the upwind state is the upwind face state (u* != 0): its sound speed
+    const float co = (MIX && !m0) ? (mask ? cl : cr) : E::cs_rp(m, Yt, mix_rwf<NS>(m, Yt), ro, po + pref);
     const float drho = (pstar - po) / (co * co);
     float rspstar[NS];
     float rstar = 0.f;
@@ -734,12 +755,27 @@ __device__ __forceinline__ void hydro_face_f(const DevBox& b, const MechF<NS>& m
       rspstar[n] = fmaxf(0.f, v);
       rstar += rspstar[n];
     }
-    {
+    float cstar = 0.f;
+    bool star_done = false;
+    if constexpr (MIX) {
+      if (!m0 && !clamped) {  // the upwind face state's composition at (rstar, pstar)
+        const float rwo = mask ? rwl : rwr;
+        const float Ts = (pstar + pref) / (rstar * rwo);
+        if ((Ts < m.tmid ? 0 : 1) == (mask ? rgL : rgR)) {
+          float Co[5];
+#pragma unroll
+          for (int n = 0; n < 5; ++n) Co[n] = mask ? CLc[n] : CRc[n];
+          cstar = E::cs_C(Co, rwo, rstar, Ts, pstar + pref);
+          star_done = true;
+        }
+      }
+    }
+    if (!star_done) {
       const float y = 1.f / rstar;
 #pragma unroll
       for (int n = 0; n < NS; ++n) Yt[n] = rspstar[n] * y;
+      cstar = E::cs_rp(m, Yt, mix_rwf<NS>(m, Yt), rstar, pstar + pref);
     }
-    const float cstar = E::cs_rp(m, Yt, mix_rwf<NS>(m, Yt), rstar, pstar + pref);
     const float sgnm = copysignf(1.f, m0 ? 0.f : ustar + Unf);
     float spout = co - sgnm * (uo + Unf);
     float spin = cstar - sgnm * (m0 ? 0.f : ustar + Unf);
