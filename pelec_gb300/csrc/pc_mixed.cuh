@@ -2,13 +2,15 @@
 //
 // Same two passes as the FP64 form (pc_kernels.cuh) with the precision split
 // of PC_PRECISION_MIXED:
-//   FP64: conserved -> primitive conversion including the cell mass
-//         fractions Y_k = rho Y_k / rho, the EOS temperature Newton solve,
+//   FP64 accuracy, in double-float arithmetic (pc_ff.cuh, ~48 bits on the
+//         FP32 pipe; FP64 itself for the GammaLaw cell pass): conserved ->
+//         primitive conversion including the cell mass fractions
+//         Y_k = rho Y_k / rho, the EOS temperature Newton solve,
 //         p = rho (R/Wbar) T, mole fractions, the Godunov-state internal
-//         energy, and the flux-divergence accumulation (each FP32
-//         face flux is widened exactly to FP64 before the differences, so the
-//         telescoping sum conserves mass, momentum and energy to FP64
-//         round-off).
+//         energy and energy fluxes, and the flux-divergence accumulation (the
+//         difference of two FP32 face fluxes taken exactly, then scaled and
+//         summed in double-float and rounded to FP64 once, so the telescoping
+//         sum conserves mass, momentum and energy far below the form's error).
 //   FP32: sound speed, transport coefficients, MOL slopes and face states
 //         (including the face mass-fraction renormalisation), the Riemann
 //         solver and its EOS calls, and the diffusion fluxes.
@@ -601,12 +603,13 @@ __device__ __forceinline__ double e_rpY_fp64(const DevMech<NS>& md, const float*
     return GammaLawEos<NS>::e_rp(md, Y, rw, (double)rho, p);
 }
 
-// The total and internal energy fluxes (FE, FEI) are returned in FP64: their
-// divergence is ~1e-3 of their size, below what an FP32 flux can resolve.
+// The total and internal energy fluxes (FE, FEI) are returned in
+// double-float: their divergence is ~1e-3 of their size, below what an FP32
+// flux can resolve.
 template <int NS, bool MIX, int d>
 __device__ __forceinline__ void hydro_face_f(const DevBox& b, const MechF<NS>& m, const DevMech<NS>& md,
                                              const DevFlags& f, long long cR, long long st, const double* U,
-                                             float* F, double& FE, double& FEI) {
+                                             float* F, ff& FE, ff& FEI) {
   using RC = Rec<NS>;
   using E = EosF<NS, MIX>;
   const float* rec = reinterpret_cast<const float*>(b.rec);
@@ -711,7 +714,7 @@ __device__ __forceinline__ void hydro_face_f(const DevBox& b, const MechF<NS>& m
     cr = E::cs_rp(m, spr, rwr, rr, pr + pref);
   }
   float fl_rho, fl_un, fl_ut1, fl_ut2;
-  double fl_E, fl_ei;
+  ff fl_E, fl_ei;
   float flY[NS];
   if (!f.laxf) {
     const float wsmall = 1.17549435e-38f;
@@ -846,8 +849,8 @@ __device__ __forceinline__ void hydro_face_f(const DevBox& b, const MechF<NS>& m
     fl_ut2 = fl_rho * iv2a;
     const ff iud = ff_add(ff_of(Un), iu);  // U + u' in double-float
     const ff tot = ff_add(ff_add(regd, 0.5f * rgd * (iua * iua + iv1a * iv1a + iv2a * iv2a)), gdpa);
-    fl_E = ff_to_double(ff_mul(iud, tot));
-    fl_ei = ff_to_double(ff_mul(iud, regd));
+    fl_E = ff_mul(iud, tot);
+    fl_ei = ff_mul(iud, regd);
   } else {
     // Lax-Friedrichs on absolute velocities (U + u')
     const float unlA = unl + Unf, unrA = unr + Unf, ut1lA = ut1l + Ut1f, ut1rA = ut1r + Ut1f;
@@ -873,15 +876,16 @@ __device__ __forceinline__ void hydro_face_f(const DevBox& b, const MechF<NS>& m
     fl_ut1 = 0.5f * ((rl * ut1lA * unlA + rr * ut1rA * unrA) - mw * (rr * ut1rA - rl * ut1lA));
     fl_ut2 = 0.5f * ((rl * ut2lA * unlA + rr * ut2rA * unrA) - mw * (rr * ut2rA - rl * ut2lA));
     const double mwd = (double)mw;
-    fl_E = 0.5 * (((r_elt + pla) * (Un + (double)unl) + (r_ert + pra) * (Un + (double)unr)) - mwd * (r_ert - r_elt));
-    fl_ei = 0.5 * (((double)rl * el * (Un + (double)unl) + (double)rr * er * (Un + (double)unr)) -
-                   mwd * ((double)rr * er - (double)rl * el));
+    fl_E = ff_of(0.5 * (((r_elt + pla) * (Un + (double)unl) + (r_ert + pra) * (Un + (double)unr)) -
+                        mwd * (r_ert - r_elt)));
+    fl_ei = ff_of(0.5 * (((double)rl * el * (Un + (double)unl) + (double)rr * er * (Un + (double)unr)) -
+                         mwd * ((double)rr * er - (double)rl * el)));
   }
   F[URHO] = fl_rho;
   F[UMX + d] = fl_un;
   F[(d == 0) ? UMY : UMX] = fl_ut1;
   F[(d == 2) ? UMY : UMZ] = fl_ut2;
-  F[UEDEN] = 0.f;  // energy fluxes travel in FP64 (FE, FEI)
+  F[UEDEN] = 0.f;  // energy fluxes travel in double-float (FE, FEI)
   F[UEINT] = 0.f;
   F[UTEMP] = 0.f;
   FE = fl_E;
@@ -970,24 +974,30 @@ __device__ __forceinline__ void diffusion_face_f(const DevBox& b, const DevFlags
 
 // Dynamic shared memory of the mixed-precision flux pass: the
 // face fluxes of all three directions of a tile at once, FP32 except the
-// total and internal energy fluxes (FP64).
+// total and internal energy fluxes (double-float pairs).
 template <int NS, class TL>
 constexpr size_t mixed_flux_smem_bytes() {
   return (size_t)(TL::F0 + TL::F1 + TL::F2) * (2 * sizeof(double) + sizeof(float) * (7 + NS));
 }
 
 // Shared-memory staging of the face fluxes of a tile, all three directions
-// at once: the FP64 total and internal energy fluxes first, then the other
-// components in FP32 (their widening to FP64 is exact, so it can wait for the
-// divergence).  Direction d's faces start at face slot base(d).
+// at once: the total and internal energy fluxes first, as double-float
+// pairs, then the other components in FP32.  Direction d's faces start at
+// face slot base(d).
 template <int NS, class TL>
 struct FaceStage {
   static constexpr int TOT = TL::F0 + TL::F1 + TL::F2;
-  double* e;  // [2][TOT]: UEDEN, UEINT
+  float2* e;  // [2][TOT]: UEDEN, UEINT
   float* v;   // [7 + NS][TOT]
   __device__ static constexpr int base(int d) { return d == 0 ? 0 : d == 1 ? TL::F0 : TL::F0 + TL::F1; }
-  __device__ double get(int n, int slot) const {
-    return n == UEDEN ? e[slot] : n == UEINT ? e[TOT + slot] : (double)v[n * TOT + slot];
+  // F(slot, n) - F(slot2, n) for component n, exactly for the FP32
+  // components (TwoSum), to double-float accuracy for the energy fluxes
+  __device__ ff diff(int n, int slot, int slot2) const {
+    if (n == UEDEN || n == UEINT) {
+      const float2 a = e[(n == UEINT) * TOT + slot], c = e[(n == UEINT) * TOT + slot2];
+      return ff_sub(ff{a.x, a.y}, ff{c.x, c.y});
+    }
+    return ff_sum(v[n * TOT + slot], -v[n * TOT + slot2]);
   }
 };
 
@@ -1003,7 +1013,7 @@ __device__ __forceinline__ void face_mixed(const DevBox& b, const MechF<NS>& m, 
   const int i = o[0] + fx, j = o[1] + fy, k = o[2] + fz;
   const long long cR = (i - b.g2lo[0]) + (j - b.g2lo[1]) * stv[1] + (k - b.g2lo[2]) * stv[2];
   float F[NVAR];
-  double FE = 0.0, FEI = 0.0;
+  ff FE = ff_of(0.f), FEI = ff_of(0.f);
   if (f.do_hydro) {
     hydro_face_f<NS, MIX, d>(b, m, md, f, cR, stv[d], U, F, FE, FEI);
   } else {
@@ -1015,8 +1025,9 @@ __device__ __forceinline__ void face_mixed(const DevBox& b, const MechF<NS>& m, 
 #pragma unroll
   for (int n = 0; n < NVAR; ++n)
     if (n != UEDEN && n != UEINT) fs.v[n * FaceStage<NS, TL>::TOT + slot] = F[n];
-  fs.e[slot] = FE + (double)F[UEDEN];
-  fs.e[FaceStage<NS, TL>::TOT + slot] = FEI;
+  const ff fe = ff_add(FE, F[UEDEN]);
+  fs.e[slot] = make_float2(fe.hi, fe.lo);
+  fs.e[FaceStage<NS, TL>::TOT + slot] = make_float2(FEI.hi, FEI.lo);
 }
 
 // Pass 2 over the tile list; CTA b takes tiles b, b + gridDim.x, ... (one
@@ -1024,7 +1035,10 @@ __device__ __forceinline__ void face_mixed(const DevBox& b, const MechF<NS>& m, 
 // The faces of all three directions of a tile form one list that the warps
 // take 32 at a time (a warp's faces share a direction), then one barrier,
 // then each cell sums its six faces: x, y, z in turn, each as
-// (F_lo - F_hi) / dx in FP64.  Per-direction barriers would leave most warps
+// (F_lo - F_hi) / dx in double-float arithmetic on the FP32 pipe (the
+// difference of two FP32 fluxes exactly), rounded to FP64 once at the end;
+// about 48 significant bits, so the telescoping sum conserves to far below
+// the form's error.  Per-direction barriers would leave most warps
 // idle while the last few faces of a direction finish (288 faces of 8x8x4
 // cells on 256 threads take two rounds).
 template <int NS, bool MIX, class TL = TileDefault>
@@ -1036,11 +1050,12 @@ __global__ void __launch_bounds__(TL::NT, TL::MINB)
   constexpr int NW = TL::NT / 32;
   extern __shared__ double flux_dyn_smem[];
   FaceStage<NS, TL> fs;
-  fs.e = flux_dyn_smem;
+  fs.e = reinterpret_cast<float2*>(flux_dyn_smem);
   fs.v = reinterpret_cast<float*>(flux_dyn_smem + 2 * FaceStage<NS, TL>::TOT);
   const bool diff = f.diffuse_vel || f.diffuse_temp || f.diffuse_spec || f.diffuse_enth;
   const int tx = threadIdx.x % TL::TX, ty = (threadIdx.x / TL::TX) % TL::TY, tz = threadIdx.x / (TL::TX * TL::TY);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const ff dxi[3] = {ff_of(g.dxinv[0]), ff_of(g.dxinv[1]), ff_of(g.dxinv[2])};
   for (int tb = blockIdx.x; tb < ntiles; tb += gridDim.x) {
     const int4 t = tiles[tb];
     const DevBox& b = boxes[t.x];
@@ -1071,24 +1086,24 @@ __global__ void __launch_bounds__(TL::NT, TL::MINB)
     __syncthreads();
     bool bad = false;
     if (mine) {
-      double acc[NVAR];
+      ff acc[NVAR];
 #pragma unroll
-      for (int n = 0; n < NVAR; ++n) acc[n] = 0.0;
+      for (int n = 0; n < NVAR; ++n) acc[n] = ff_of(0.f);
 #pragma unroll
       for (int d = 0; d < 3; ++d) {
         const int nf0 = ext[0] + (d == 0), nf1 = ext[1] + (d == 1);
         const int flo = FaceStage<NS, TL>::base(d) + tx + nf0 * (ty + nf1 * tz);
         const int fhi = flo + ((d == 0) ? 1 : (d == 1) ? nf0 : nf0 * nf1);
-        const double s = g.dxinv[d];
 #pragma unroll
-        for (int n = 0; n < NVAR; ++n) acc[n] = fma(fs.get(n, flo) - fs.get(n, fhi), s, acc[n]);
+        for (int n = 0; n < NVAR; ++n) acc[n] = ff_add(ff_mul(fs.diff(n, flo, fhi), dxi[d]), acc[n]);
       }
       const int i = o[0] + tx, j = o[1] + ty, k = o[2] + tz;
       double* r = b.R + (i - b.rb[0]) + (long long)(j - b.rb[1]) * b.rj + (long long)(k - b.rb[2]) * b.rk;
 #pragma unroll
       for (int n = 0; n < NVAR; ++n) {
-        bad |= !isfinite(acc[n]);
-        r[n * b.rn] = acc[n];
+        const double v = ff_to_double(acc[n]);
+        bad |= !isfinite(v);
+        r[n * b.rn] = v;
       }
     }
     if (f.check_output) warp_count(&counters[kCounterNonfinite], bad);
