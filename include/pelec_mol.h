@@ -64,10 +64,11 @@ typedef enum pc_precision {
   PC_PRECISION_FP64 = 0,    /* every operation in FP64, each quotient
                                correctly rounded                           */
   PC_PRECISION_MIXED = 1,   /* FP32 reconstruction, Riemann and diffusion
-                               fluxes; FP64 EOS Newton solve, mass-fraction
-                               renormalisation and flux-divergence
-                               accumulation                                */
-  PC_PRECISION_FP64_RCP = 2 /* every operation in FP64; a quotient by a
+                               fluxes; the EOS Newton solve, the cell
+                               mass fractions, the Godunov energy and the
+                               flux-divergence accumulation in double-float
+                               arithmetic (~48 bits on the FP32 pipe)      */
+  PC_PRECISION_FP64_RCP = 2,/* every operation in FP64; a quotient by a
                                divisor shared by several numerators (Y_k =
                                rhoY_k / rho, the slopes' 1/c, the face-state
                                renormalisation, the Riemann weights, 1/V) is
@@ -78,6 +79,9 @@ typedef enum pc_precision {
                                rounding (as a build with multiply-add
                                contraction would be), about 1e-15 of each
                                component's flux scale |F|/V               */
+  PC_PRECISION_MIXED_FP64 = 3 /* PC_PRECISION_MIXED with the EOS Newton
+                                 solve, the cell mass fractions and the
+                                 flux-divergence accumulation in FP64     */
 } pc_precision;
 
 /* Species data.  Thermodynamics is NASA-7 per species:

@@ -30,6 +30,7 @@ PC_TRANSPORT_SIMPLE = 1
 PC_PRECISION_FP64 = 0
 PC_PRECISION_MIXED = 1
 PC_PRECISION_FP64_RCP = 2
+PC_PRECISION_MIXED_FP64 = 3
 
 # Conserved-state indices, Source/IndexDefines.H:6-13,60.
 URHO, UMX, UMY, UMZ, UEDEN, UEINT, UTEMP, UFS = range(8)

@@ -42,13 +42,14 @@ MIXED_FLAGS = ["-fmad=true", "-prec-div=false", "-prec-sqrt=false"]
 # (pc_unit_ns.h), so that the compilations run in parallel.
 _PER_NS = [(src, ["-fmad=false", f"-DPC_UNIT_NS={ns}"]) for src in ("pc_tiles_fp64.cu", "pc_adjoint.cu", "pc_tangent.cu")
            for ns in (1, 9, 21)]
+_PER_NS_MIXED = [("pc_tiles_mixed.cu", MIXED_FLAGS + [f"-DPC_UNIT_NS={ns}"]) for ns in (1, 9, 21)]
 LIBS = {
     # The mixed-precision units are checked by error norms, not bit for bit:
     # their FP32 divisions and square roots may be the approximate forms
     # (the double-float arithmetic uses explicit round-to-nearest intrinsics,
     # and denormals are kept).
     "libpelec_mol.so": [("pc_mol.cu", ["-fmad=false"]), ("pc_mol_mixed.cu", MIXED_FLAGS),
-                        ("pc_tiles_mixed.cu", MIXED_FLAGS), ("pc_rhs_rcp.cu", ["-fmad=false"])] + _PER_NS,
+                        ("pc_rhs_rcp.cu", ["-fmad=false"])] + _PER_NS + _PER_NS_MIXED,
     # arithmetic peak rates for bench.py's roofline (not part of the ABI)
     "libpc_peaks.so": [("pc_peaks.cu", ["-fmad=true"])],
 }

@@ -454,7 +454,7 @@ __device__ __forceinline__ void cell_mixed_ff(const DevBox& b, const MechF<NS>& 
 // Pass 1, mixed precision.  Records are FP32, in the field order of Rec<NS>
 // (P holds p - p_ref).
 // ---------------------------------------------------------------------------
-template <int NS, class EOSD, bool MIX, bool SIMPLE>
+template <int NS, class EOSD, bool MIX, bool SIMPLE, bool STRICT = false>
 __global__ void __launch_bounds__(kCellThreads)
     cell_kernel_mixed(const DevBox* __restrict__ boxes, const int2* __restrict__ items,
                       const __grid_constant__ DevMech<NS> m, const __grid_constant__ MechF<NS> mf, const DevFlags f,
@@ -467,9 +467,9 @@ __global__ void __launch_bounds__(kCellThreads)
   if (threadIdx.x == 0) box_uref(b, Us);
   __syncthreads();
   bool newton_fail = false, nonpos = false;
-  if constexpr (MIX) {
+  if constexpr (MIX && !STRICT) {
     if (c < b.ncell) cell_mixed_ff<NS, SIMPLE>(b, mf, f, c, Us, newton_fail, nonpos);
-  } else if (c < b.ncell) {
+  } else if (c < b.ncell) {  // FP64 (GammaLaw, or PC_PRECISION_MIXED_FP64)
     const int nx = b.n2[0], ny = b.n2[1];
     const int i = b.g2lo[0] + (int)(c % nx);
     const int j = b.g2lo[1] + (int)((c / nx) % ny);
@@ -523,6 +523,19 @@ __global__ void __launch_bounds__(kCellThreads)
       }
       xr[NS * N] = to_pair(T);
       xr[kMixedRho<NS> * N] = to_pair(rho);
+      if constexpr (MIX) {  // the cell's mixture sums for the Godunov energy, in double-float
+        xr[kMixedRw<NS> * N] = to_pair(rw);
+        ff Yp[NS];
+#pragma unroll
+        for (int n = 0; n < NS; ++n) Yp[n] = ff_of(Y[n]);
+#pragma unroll
+        for (int range = 0; range < 2; ++range) {
+          ff C[6];
+          mix_coefs_ff<NS>(mf, Yp, range, C);
+#pragma unroll
+          for (int n = 0; n < 6; ++n) xr[(kMixedCoef<NS> + 6 * range + n) * N] = make_float2(C[n].hi, C[n].lo);
+        }
+      }
       float out[NS + 3];
       TransF<NS, SIMPLE>::eval(mf, Tf, rhof, pf, Yf, X, out);
       r[RC::T * N] = Tf;
@@ -999,6 +1012,14 @@ struct FaceStage {
     }
     return ff_sum(v[n * TOT + slot], -v[n * TOT + slot2]);
   }
+  // the staged flux of component n as a double (the FP32 ones widened exactly)
+  __device__ double get(int n, int slot) const {
+    if (n == UEDEN || n == UEINT) {
+      const float2 a = e[(n == UEINT) * TOT + slot];
+      return ff_to_double(ff{a.x, a.y});
+    }
+    return (double)v[n * TOT + slot];
+  }
 };
 
 // One face of direction d (index fi in the tile's face block of that
@@ -1041,7 +1062,7 @@ __device__ __forceinline__ void face_mixed(const DevBox& b, const MechF<NS>& m, 
 // the form's error.  Per-direction barriers would leave most warps
 // idle while the last few faces of a direction finish (288 faces of 8x8x4
 // cells on 256 threads take two rounds).
-template <int NS, bool MIX, class TL = TileDefault>
+template <int NS, bool MIX, class TL = TileDefault, bool STRICT = false>
 __global__ void __launch_bounds__(TL::NT, TL::MINB)
     flux_kernel_mixed(const DevBox* __restrict__ boxes, const int4* __restrict__ tiles, int ntiles,
                       const __grid_constant__ MechF<NS> m, const __grid_constant__ DevMech<NS> md, const DevFlags f,
@@ -1086,24 +1107,43 @@ __global__ void __launch_bounds__(TL::NT, TL::MINB)
     __syncthreads();
     bool bad = false;
     if (mine) {
-      ff acc[NVAR];
-#pragma unroll
-      for (int n = 0; n < NVAR; ++n) acc[n] = ff_of(0.f);
-#pragma unroll
-      for (int d = 0; d < 3; ++d) {
-        const int nf0 = ext[0] + (d == 0), nf1 = ext[1] + (d == 1);
-        const int flo = FaceStage<NS, TL>::base(d) + tx + nf0 * (ty + nf1 * tz);
-        const int fhi = flo + ((d == 0) ? 1 : (d == 1) ? nf0 : nf0 * nf1);
-#pragma unroll
-        for (int n = 0; n < NVAR; ++n) acc[n] = ff_add(ff_mul(fs.diff(n, flo, fhi), dxi[d]), acc[n]);
-      }
       const int i = o[0] + tx, j = o[1] + ty, k = o[2] + tz;
       double* r = b.R + (i - b.rb[0]) + (long long)(j - b.rb[1]) * b.rj + (long long)(k - b.rb[2]) * b.rk;
+      if constexpr (STRICT) {  // PC_PRECISION_MIXED_FP64: each flux widened to FP64, summed in FP64
+        double acc[NVAR];
 #pragma unroll
-      for (int n = 0; n < NVAR; ++n) {
-        const double v = ff_to_double(acc[n]);
-        bad |= !isfinite(v);
-        r[n * b.rn] = v;
+        for (int n = 0; n < NVAR; ++n) acc[n] = 0.0;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+          const int nf0 = ext[0] + (d == 0), nf1 = ext[1] + (d == 1);
+          const int flo = FaceStage<NS, TL>::base(d) + tx + nf0 * (ty + nf1 * tz);
+          const int fhi = flo + ((d == 0) ? 1 : (d == 1) ? nf0 : nf0 * nf1);
+#pragma unroll
+          for (int n = 0; n < NVAR; ++n) acc[n] = fma(fs.get(n, flo) - fs.get(n, fhi), g.dxinv[d], acc[n]);
+        }
+#pragma unroll
+        for (int n = 0; n < NVAR; ++n) {
+          bad |= !isfinite(acc[n]);
+          r[n * b.rn] = acc[n];
+        }
+      } else {
+        ff acc[NVAR];
+#pragma unroll
+        for (int n = 0; n < NVAR; ++n) acc[n] = ff_of(0.f);
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+          const int nf0 = ext[0] + (d == 0), nf1 = ext[1] + (d == 1);
+          const int flo = FaceStage<NS, TL>::base(d) + tx + nf0 * (ty + nf1 * tz);
+          const int fhi = flo + ((d == 0) ? 1 : (d == 1) ? nf0 : nf0 * nf1);
+#pragma unroll
+          for (int n = 0; n < NVAR; ++n) acc[n] = ff_add(ff_mul(fs.diff(n, flo, fhi), dxi[d]), acc[n]);
+        }
+#pragma unroll
+        for (int n = 0; n < NVAR; ++n) {
+          const double v = ff_to_double(acc[n]);
+          bad |= !isfinite(v);
+          r[n * b.rn] = v;
+        }
       }
     }
     if (f.check_output) warp_count(&counters[kCounterNonfinite], bad);
@@ -1114,7 +1154,7 @@ __global__ void __launch_bounds__(TL::NT, TL::MINB)
 
 // Host: launch the mixed flux pass at tile shape TL, one CTA per tile or
 // (persistent) as many CTAs as are resident on the device at once.
-template <int NS, bool MIX, class TL>
+template <int NS, bool MIX, class TL, bool STRICT = false>
 inline cudaError_t launch_flux_mixed_at(const DevBox* boxes, const int4* tiles, int ntiles, const MechF<NS>& mf,
                                         const DevMech<NS>& md, const DevFlags& f, const Geo& g,
                                         unsigned long long* counters, cudaStream_t s, bool persistent) {
@@ -1127,7 +1167,7 @@ inline cudaError_t launch_flux_mixed_at(const DevBox* boxes, const int4* tiles, 
   if (e != cudaSuccess) return e;
   const unsigned long long bit = (dev >= 0 && dev < 64) ? (1ull << dev) : 0ull;
   if (!bit || !(opted.load() & bit)) {
-    e = cudaFuncSetAttribute(flux_kernel_mixed<NS, MIX, TL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    e = cudaFuncSetAttribute(flux_kernel_mixed<NS, MIX, TL, STRICT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     opted.fetch_or(bit);
   }
@@ -1135,12 +1175,12 @@ inline cudaError_t launch_flux_mixed_at(const DevBox* boxes, const int4* tiles, 
   if (persistent) {
     int r = bit ? resident[dev].load() : 0;
     if (r <= 0) {
-      r = resident_ctas(flux_kernel_mixed<NS, MIX, TL>, TL::NT, smem);
+      r = resident_ctas(flux_kernel_mixed<NS, MIX, TL, STRICT>, TL::NT, smem);
       if (bit && r > 0) resident[dev].store(r);
     }
     if (r > 0 && r < grid) grid = r;
   }
-  flux_kernel_mixed<NS, MIX, TL><<<grid, TL::NT, smem, s>>>(boxes, tiles, ntiles, mf, md, f, g, counters);
+  flux_kernel_mixed<NS, MIX, TL, STRICT><<<grid, TL::NT, smem, s>>>(boxes, tiles, ntiles, mf, md, f, g, counters);
   return cudaGetLastError();
 }
 

@@ -23,9 +23,10 @@
 #include "pelec_mol.h"
 
 namespace pcg {
-int launch_mixed(int nspec, int tile, bool persistent, const DevBox* boxes, const int2* items, int nitems,
-                 const int4* tiles, int ntiles, const MechSet& ms, const DevFlags& f, const Geo& g, double p_ref,
-                 unsigned long long* counters, cudaStream_t s, cudaEvent_t e0, cudaEvent_t e1, cudaEvent_t e2);
+int launch_mixed(int nspec, int tile, bool persistent, bool strict, const DevBox* boxes, const int2* items,
+                 int nitems, const int4* tiles, int ntiles, const MechSet& ms, const DevFlags& f, const Geo& g,
+                 double p_ref, unsigned long long* counters, cudaStream_t s, cudaEvent_t e0, cudaEvent_t e1,
+                 cudaEvent_t e2);
 cudaError_t launch_flux_fp64_tile(int tile, bool persistent, int nspec, const DevBox* boxes, const int4* tiles,
                                   int ntiles, const MechSet& ms, const DevFlags& f, const Geo& g,
                                   unsigned long long* counters, cudaStream_t s, const FluxBox* fx);
@@ -303,6 +304,8 @@ std::vector<int> tune_key(const pc_box_desc* boxes, int nboxes) {
   return k;
 }
 
+bool is_mixed(int precision) { return precision == PC_PRECISION_MIXED || precision == PC_PRECISION_MIXED_FP64; }
+
 // Dynamic shared memory of the flux pass at launch configuration t for the
 // handle's species count and precision (bytes).  The FP64 passes stage one
 // direction's face fluxes, cell slopes and the z carry; the mixed pass the
@@ -312,7 +315,7 @@ size_t flux_pass_smem(const pc_mol_handle* h, int t) {
     constexpr int NS = decltype(sc)::value;
     auto of = [&](auto tl) -> size_t {
       using TL = decltype(tl);
-      if (h->cfg.precision == PC_PRECISION_MIXED) return mixed_flux_smem_bytes<NS, TL>();
+      if (is_mixed(h->cfg.precision)) return mixed_flux_smem_bytes<NS, TL>();
       return flux_smem_bytes<NS, TL>();
     };
     switch (t % kNumTiles) {
@@ -469,7 +472,7 @@ int run(pc_mol_handle* h, const pc_box_desc* boxes, int nboxes, const double dx[
   const Layout& L = h->lay;
   const bool timed = h->cfg.time_passes != 0 && !per_box;
   h->timed = timed;
-  const bool mixed = h->cfg.precision == PC_PRECISION_MIXED;
+  const bool mixed = is_mixed(h->cfg.precision);
   const bool rcp = h->cfg.precision == PC_PRECISION_FP64_RCP;
   auto go = [&](int ib, int ie, int tb, int te) {
     if (rcp) {
@@ -504,7 +507,8 @@ int run(pc_mol_handle* h, const pc_box_desc* boxes, int nboxes, const double dx[
       const double p_ref = h->cfg.mixed_p_ref > 0.0 ? h->cfg.mixed_p_ref : 1013250.0;
       Geo gm = g;
       gm.p_ref = p_ref;
-      const int rc = launch_mixed(h->variant, h->lay_tile, h->tile >= kNumTiles, h->d_boxes, h->d_items + ib, ie - ib,
+      const int rc = launch_mixed(h->variant, h->lay_tile, h->tile >= kNumTiles,
+                                  h->cfg.precision == PC_PRECISION_MIXED_FP64, h->d_boxes, h->d_items + ib, ie - ib,
                                   h->d_tiles + tb, te - tb, h->mech, h->flags, gm, p_ref, h->d_counters, s,
                                   timed ? h->ev[0] : nullptr, timed ? h->ev[1] : nullptr, timed ? h->ev[2] : nullptr);
       return rc == 0 ? PC_OK : cuda_fail(h, cudaGetLastError());
@@ -548,7 +552,7 @@ int pc_mol_create(pc_mol_handle** out, const pc_mol_config* cfg) {
   *out = nullptr;
   const pc_mol_config& c = *cfg;
   if (c.nspec != c.mech.nspec) return PC_ERR_INVALID_ARGUMENT;
-  if (c.precision != PC_PRECISION_FP64 && c.precision != PC_PRECISION_MIXED && c.precision != PC_PRECISION_FP64_RCP)
+  if (c.precision != PC_PRECISION_FP64 && !is_mixed(c.precision) && c.precision != PC_PRECISION_FP64_RCP)
     return PC_ERR_INVALID_ARGUMENT;
   const int variant = compiled_variant(c);
   if (!variant) return PC_ERR_UNSUPPORTED;
@@ -1308,7 +1312,7 @@ extern "C" int pc_mol_rhs_level_fluxes(pc_mol_handle* h, const pc_box_desc* boxe
                                        const pc_array4* fluxes, void* stream) {
   if (!h) return PC_ERR_INVALID_ARGUMENT;
   if (nboxes < 0 || (nboxes > 0 && (!boxes || !fluxes))) return h->last_error = PC_ERR_INVALID_ARGUMENT;
-  if (h->cfg.precision == PC_PRECISION_MIXED) return h->last_error = PC_ERR_UNSUPPORTED;
+  if (is_mixed(h->cfg.precision)) return h->last_error = PC_ERR_UNSUPPORTED;
   const int nvar = 7 + h->cfg.nspec;
   std::vector<FluxBox> fb(nboxes);
   for (int b = 0; b < nboxes; ++b) {

@@ -5,31 +5,42 @@
 
 namespace pcg {
 
-cudaError_t launch_flux_mixed_tile(int tile, bool persistent, int nspec, const DevBox* boxes, const int4* tiles,
-                                   int ntiles, const MechSet& ms, const DevFlags& f, const Geo& g, double p_ref,
-                                   unsigned long long* counters, cudaStream_t s);
+cudaError_t launch_flux_mixed_tile(int tile, bool persistent, bool strict, int nspec, const DevBox* boxes,
+                                   const int4* tiles, int ntiles, const MechSet& ms, const DevFlags& f, const Geo& g,
+                                   double p_ref, unsigned long long* counters, cudaStream_t s);
 
 // Cell pass, then the flux pass at tile shape `tile` (0 = 8x8x4, launched
 // here; the others in pc_tiles_mixed.cu), persistent or one CTA per tile.
-int launch_mixed(int nspec, int tile, bool persistent, const DevBox* boxes, const int2* items, int nitems,
-                 const int4* tiles, int ntiles, const MechSet& ms, const DevFlags& f, const Geo& g, double p_ref,
-                 unsigned long long* counters, cudaStream_t s, cudaEvent_t e0, cudaEvent_t e1, cudaEvent_t e2) {
+// strict: PC_PRECISION_MIXED_FP64 (Newton solve, cell mass fractions and the
+// divergence in FP64) instead of their double-float forms.
+int launch_mixed(int nspec, int tile, bool persistent, bool strict, const DevBox* boxes, const int2* items,
+                 int nitems, const int4* tiles, int ntiles, const MechSet& ms, const DevFlags& f, const Geo& g,
+                 double p_ref, unsigned long long* counters, cudaStream_t s, cudaEvent_t e0, cudaEvent_t e1,
+                 cudaEvent_t e2) {
   if (e0) cudaEventRecord(e0, s);
   cudaError_t e = with_species(nspec, [&](auto ns) {
     constexpr int NS = decltype(ns)::value;
     using P = Physics<NS>;
     const DevMech<NS>& m = ms.get<NS>();
     const MechF<NS> mf = to_float(m, p_ref);
-    if (nitems > 0)
-      cell_kernel_mixed<NS, typename P::EOS, P::MIX, P::MIX><<<nitems, kCellThreads, 0, s>>>(boxes, items, m, mf, f,
-                                                                                            counters);
+    if (nitems > 0) {
+      if (strict)
+        cell_kernel_mixed<NS, typename P::EOS, P::MIX, P::MIX, true>
+            <<<nitems, kCellThreads, 0, s>>>(boxes, items, m, mf, f, counters);
+      else
+        cell_kernel_mixed<NS, typename P::EOS, P::MIX, P::MIX, false>
+            <<<nitems, kCellThreads, 0, s>>>(boxes, items, m, mf, f, counters);
+    }
     if (e1) cudaEventRecord(e1, s);
     if (tile == 0)
-      return launch_flux_mixed_at<NS, P::MIX, TileDefault>(boxes, tiles, ntiles, mf, m, f, g, counters, s,
-                                                             persistent);
+      return strict ? launch_flux_mixed_at<NS, P::MIX, TileDefault, true>(boxes, tiles, ntiles, mf, m, f, g, counters,
+                                                                          s, persistent)
+                    : launch_flux_mixed_at<NS, P::MIX, TileDefault, false>(boxes, tiles, ntiles, mf, m, f, g,
+                                                                           counters, s, persistent);
     return cudaSuccess;
   });
-  if (tile != 0) e = launch_flux_mixed_tile(tile, persistent, nspec, boxes, tiles, ntiles, ms, f, g, p_ref, counters, s);
+  if (tile != 0)
+    e = launch_flux_mixed_tile(tile, persistent, strict, nspec, boxes, tiles, ntiles, ms, f, g, p_ref, counters, s);
   if (e2) cudaEventRecord(e2, s);
   return e == cudaSuccess && cudaGetLastError() == cudaSuccess ? 0 : 3;
 }

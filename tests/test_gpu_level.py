@@ -40,7 +40,7 @@ def _ragged_level():
     return mech, boxes
 
 
-@pytest.mark.parametrize("precision", [abi.PC_PRECISION_FP64, abi.PC_PRECISION_MIXED])
+@pytest.mark.parametrize("precision", [abi.PC_PRECISION_FP64, abi.PC_PRECISION_MIXED, abi.PC_PRECISION_MIXED_FP64])
 def test_every_tile_shape_gives_identical_rhs(cuda_lib, oracle_lib, precision):
     mol = cuda_lib
     mech, boxes = _ragged_level()
@@ -68,7 +68,7 @@ def test_every_tile_shape_single_species(cuda_lib, oracle_lib):
     assert rel_maxnorm(outs[3], ref).max() <= 1e-12
 
 
-@pytest.mark.parametrize("precision", [abi.PC_PRECISION_FP64, abi.PC_PRECISION_MIXED])
+@pytest.mark.parametrize("precision", [abi.PC_PRECISION_FP64, abi.PC_PRECISION_MIXED, abi.PC_PRECISION_MIXED_FP64])
 def test_persistent_grid_strides_over_every_tile(cuda_lib, precision):
     """A 64^3 flame has more tiles than the GPU holds CTAs at any shape, so
     each CTA of a persistent launch takes a run of several tiles (handing the

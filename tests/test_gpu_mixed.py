@@ -1,10 +1,11 @@
-"""GPU tests of the mixed-precision form (PC_PRECISION_MIXED).
-
-FP32 reconstruction, Riemann and diffusion fluxes with FP64 EOS Newton,
-cell mass fractions and divergence accumulation.  The bar for the 9-species
-flame is 1e-5 relative L2 per component against the FP64 oracle (MIXED_L2
-below); the divergence is accumulated in FP64 from exactly widened face
-fluxes, so periodic domain totals vanish to FP64 round-off.
+"""GPU tests of the mixed-precision forms: PC_PRECISION_MIXED (FP32
+reconstruction, Riemann and diffusion fluxes; the EOS Newton solve, cell
+mass fractions, Godunov energy and divergence accumulation in double-float
+arithmetic) and PC_PRECISION_MIXED_FP64 (the same with the Newton solve,
+the cell mass fractions and the divergence accumulation in FP64).  The bar
+for the 9-species flame is 1e-5 relative L2 per component against the FP64
+oracle (MIXED_L2 below); the divergence telescopes from exact differences
+of the staged face fluxes, so periodic domain totals vanish to round-off.
 """
 import numpy as np
 import pytest
@@ -15,6 +16,7 @@ from pelec_gb300 import abi, mechanism, problems
 pytestmark = pytest.mark.gpu
 
 MIXED_L2 = 1e-5
+FORMS = [abi.PC_PRECISION_MIXED, abi.PC_PRECISION_MIXED_FP64]
 # Lax-Friedrichs adds |u|+c times the jump of the FP32 face states to every
 # flux, which amplifies their rounding by c/|u| ~ 1e3 in the energy equations.
 LAXF_L2 = 3e-4
@@ -45,25 +47,27 @@ def rel_max(a, b):
     return np.array(out)
 
 
-def test_mixed_flame_error_vs_fp64_oracle(cuda_lib, oracle_lib):
+@pytest.mark.parametrize("form", FORMS)
+def test_mixed_flame_error_vs_fp64_oracle(cuda_lib, oracle_lib, form):
     mech, st, _ = problems.flame((48, 40, 64), seed=41)
     ref, = oracle_lib.mol_rhs(problems.make_config(mech), [st])
-    (gpu,), status = gpu_rhs(cuda_lib, problems.make_config(mech, precision=abi.PC_PRECISION_MIXED), [st])
+    (gpu,), status = gpu_rhs(cuda_lib, problems.make_config(mech, precision=form), [st])
     l2, mx = rel_l2(gpu, ref), rel_max(gpu, ref)
-    print("mixed flame rel L2 per component:", l2)
+    print(form, "mixed flame rel L2 per component:", l2)
     print("mixed flame rel max per component:", mx)
     assert np.all(np.isfinite(gpu))
     assert np.all(l2 <= _tol()), l2
     assert status.nonfinite_output == 0
 
 
-def test_mixed_flame_128_vs_fp64_gpu(cuda_lib):
+@pytest.mark.parametrize("form", FORMS)
+def test_mixed_flame_128_vs_fp64_gpu(cuda_lib, form):
     """Full C2 size against the FP64 path (which matches the oracle bit for bit)."""
     mech, st, _ = problems.flame((128, 128, 128), seed=1)
     (r64,), _ = gpu_rhs(cuda_lib, problems.make_config(mech), [st])
-    (r32,), _ = gpu_rhs(cuda_lib, problems.make_config(mech, precision=abi.PC_PRECISION_MIXED), [st])
+    (r32,), _ = gpu_rhs(cuda_lib, problems.make_config(mech, precision=form), [st])
     l2 = rel_l2(r32, r64)
-    print("mixed flame 128^3 rel L2 per component:", l2)
+    print(form, "mixed flame 128^3 rel L2 per component:", l2)
     print("mixed flame 128^3 rel max per component:", rel_max(r32, r64))
     assert np.all(l2 <= _tol()), l2
 
@@ -78,10 +82,11 @@ def test_mixed_tgv_error(cuda_lib, oracle_lib):
     assert l2.max() <= 1e-4, l2
 
 
-def test_mixed_conserves_to_fp64_roundoff(cuda_lib):
+@pytest.mark.parametrize("form", FORMS)
+def test_mixed_conserves_to_roundoff(cuda_lib, form):
     mech, st, _ = problems.flame((32, 24, 40), seed=43)
     problems.fill_ghosts(st.S, 4, ("periodic",) * 3)
-    (gpu,), _ = gpu_rhs(cuda_lib, problems.make_config(mech, precision=abi.PC_PRECISION_MIXED), [st])
+    (gpu,), _ = gpu_rhs(cuda_lib, problems.make_config(mech, precision=form), [st])
     for n in [abi.URHO, abi.UMX, abi.UMY, abi.UMZ, abi.UEDEN] + [abi.UFS + k for k in range(9)]:
         assert abs(gpu[n].sum()) <= 1e-13 * np.abs(gpu[n]).sum(), n
 
@@ -117,11 +122,12 @@ def test_c4_mixed_256_against_fp64_oracle(cuda_lib, oracle_lib):
     torch.cuda.empty_cache()
 
 
-def test_mixed_21_species_error_vs_fp64_oracle(cuda_lib, oracle_lib):
-    """NUM_SPECIES = 21: the mixed form within MIXED_L2 of the FP64 oracle."""
+@pytest.mark.parametrize("form", FORMS)
+def test_mixed_21_species_error_vs_fp64_oracle(cuda_lib, oracle_lib, form):
+    """NUM_SPECIES = 21: the mixed forms within MIXED_L2 of the FP64 oracle."""
     mech, st, _ = problems.flame((24, 20, 32), seed=45, mech=mechanism.drm_synthetic())
     ref, = oracle_lib.mol_rhs(problems.make_config(mech), [st])
-    (gpu,), _ = gpu_rhs(cuda_lib, problems.make_config(mech, precision=abi.PC_PRECISION_MIXED), [st])
+    (gpu,), _ = gpu_rhs(cuda_lib, problems.make_config(mech, precision=form), [st])
     l2 = rel_l2(gpu, ref)
-    print("21 species mixed rel L2 per component:", l2)
+    print(form, "21 species mixed rel L2 per component:", l2)
     assert np.all(l2 <= MIXED_L2), l2
