@@ -100,49 +100,108 @@ __host__ MechF<NS> to_float(const DevMech<NS>& m, double p_ref) {
 
 // FP64-accuracy fields stored after the FP32 fields of a mixed record, for
 // the cells whose faces the pass evaluates (the valid cells and one layer
-// around them), each a double-float pair (hi, lo) in an FP64-wide slot,
-// field n of cell c at [n N + c]: the mole fractions X_k (NS), the
-// temperature and the density; with the ideal-mixture EOS then R/Wbar and
-// the mixture NASA-7 coefficients C_n = sum_k Y_k (R/W_k) a_{n,k} of both
-// temperature ranges (12).  X and T enter the diffusion fluxes only through
+// around them), each a double-float pair (hi, lo), two pairs to a 16-byte
+// group (hi, lo, hi, lo), group g of cell c at [g N + c] (MPair): the mole
+// fractions X_k and the temperature (X_0 X_1 | X_2 X_3 | ... | T last), then
+// (rho, R/Wbar) (R/Wbar with the ideal-mixture EOS only) and, with the
+// ideal-mixture EOS, the mixture NASA-7 coefficients C_n = sum_k Y_k (R/W_k)
+// a_{n,k} of both temperature ranges, three groups a range.  X and T enter the diffusion fluxes only through
 // differences between neighbouring cells, which FP32 values would resolve to
 // no better than 1e-4 K / 1e-7 (the flame's second differences of T are a
 // few K per cell).  rho, R/Wbar and C are the cell's part of the Godunov
 // state's density and mixture sums (energy fluxes, hydro_face_f), to which a
-// face adds only FP32 increments.  The fields start at the first 8-byte
-// boundary after the Rec<NS>::N FP32 fields of every cell (N ncell floats
-// may be odd); a mixed record stays within the FP64 record's size.
+// face adds only FP32 increments.  The fields start after the FP32 groups
+// (MRec) of every cell; a mixed record stays within the FP64 record's size.
+//
+// The FP32 fields of a mixed record are 16-byte groups (float4), group g of
+// cell c at [g N + c], so that a face reads four fields of a neighbour with
+// one load: G0 = (rho, u', v', w') (velocity offsets from the box's
+// reference velocity), G1 = (p', c, T, 0) (p' = p - p_ref); then the mass
+// fractions Y_k four to a group, the species enthalpies h_k four to a group,
+// and D_k, mu, xi, lambda (the transport coefficients, in that order) four to
+// a group, the last group of each padded with 0.  h_k and the transport
+// coefficients are written for the valid cells and one layer around them (the
+// cells whose faces carry diffusion fluxes) only.  The record arena of a box
+// starts on a 256-byte boundary.
 template <int NS>
-__device__ __forceinline__ float2* mixed_x(const DevBox& b) {
-  const long long nf = ((long long)Rec<NS>::N * b.ncell + 1) & ~1LL;
-  return reinterpret_cast<float2*>(reinterpret_cast<float*>(b.rec) + nf);
+struct MRec {
+  static constexpr int Q = (NS + 3) / 4, QD = (NS + 6) / 4;  // groups of Y / h, of the transport coefficients
+  static constexpr int G0 = 0, G1 = 1, Y = 2, H = 2 + Q, D = 2 + 2 * Q;
+  static constexpr int G = 2 + 2 * Q + QD;  // groups in all
+};
+template <int NS>
+struct MPair {
+  static constexpr int XT = 0, QX = (NS + 2) / 2;  // groups of X_k and T; T in group NS / 2, slot NS % 2
+  static constexpr int RHO = QX;           // (rho, R/Wbar)
+  static constexpr int COEF = QX + 1;      // C[r][n] in group COEF + 3 r + n / 2, slot n % 2
+  template <bool MIX>
+  static constexpr int G = MIX ? QX + 7 : QX + 1;  // groups in all
+};
+template <int NS>
+__device__ __forceinline__ float4* mixed_x(const DevBox& b) {
+  return reinterpret_cast<float4*>(b.rec) + (long long)MRec<NS>::G * b.ncell;
 }
-__device__ __forceinline__ float2 to_pair(double x) {
-  const ff v = ff_of(x);
-  return make_float2(v.hi, v.lo);
+// Loads / stores of the groups of a mixed record.
+__device__ __forceinline__ float4 ld_group(const float4* rec, int g, long long N, long long c) {
+  return __ldg(rec + (long long)g * N + c);
 }
-__device__ __forceinline__ ff ld_pair(const float2* p) {
-  const float2 v = __ldg(p);
-  return {v.x, v.y};
+__device__ __forceinline__ float grp(const float4& v, int i) {  // component i (a constant after unrolling)
+  return i == 0 ? v.x : (i == 1 ? v.y : (i == 2 ? v.z : v.w));
 }
+// n values v[0..n) of cell c from the groups starting at g
+template <int n>
+__device__ __forceinline__ void ld_groups(const float4* rec, int g, long long N, long long c, float* v) {
+#pragma unroll
+  for (int q = 0; q < (n + 3) / 4; ++q) {
+    const float4 t = ld_group(rec, g + q, N, c);
+#pragma unroll
+    for (int l = 0; l < 4; ++l)
+      if (4 * q + l < n) v[4 * q + l] = grp(t, l);
+  }
+}
+template <int n>
+__device__ __forceinline__ void st_groups(float4* r, int g, long long N, const float* v) {
+#pragma unroll
+  for (int q = 0; q < (n + 3) / 4; ++q) {
+    float t[4];
+#pragma unroll
+    for (int l = 0; l < 4; ++l) t[l] = 4 * q + l < n ? v[4 * q + l] : 0.f;
+    r[(long long)(g + q) * N] = make_float4(t[0], t[1], t[2], t[3]);
+  }
+}
+__device__ __forceinline__ ff pair_of(const float4& v, int slot) {  // slot 0 or 1 of a pair group
+  return slot == 0 ? ff{v.x, v.y} : ff{v.z, v.w};
+}
+__device__ __forceinline__ float4 pair_group(ff a, ff b) { return make_float4(a.hi, a.lo, b.hi, b.lo); }
 // x1 - x2 of two stored pairs, rounded to FP32 (the hi parts of nearby
 // values subtract exactly; the lo parts carry the rest)
 __device__ __forceinline__ float pair_diff(ff a, ff b) {
   return __fadd_rn(__fsub_rn(a.hi, b.hi), __fsub_rn(a.lo, b.lo));
 }
-// field indices in the pair part: the density, R/Wbar, C[r][n] at
-// kMixedCoef + 6 r + n; kMixedPairs fields in all
+// X_0..X_{NS-1} and T (NS + 1 pairs) from their groups at cell c
 template <int NS>
-constexpr int kMixedRho = NS + 1;
+__device__ __forceinline__ void st_xt(float4* xr, long long N, const ff* X, ff T) {
+#pragma unroll
+  for (int q = 0; q < MPair<NS>::QX; ++q) {
+    ff v[2];
+#pragma unroll
+    for (int l = 0; l < 2; ++l) {
+      const int n = 2 * q + l;
+      v[l] = n < NS ? X[n] : (n == NS ? T : ff_of(0.f));
+    }
+    xr[(long long)(MPair<NS>::XT + q) * N] = pair_group(v[0], v[1]);
+  }
+}
 template <int NS>
-constexpr int kMixedRw = NS + 2;
+__device__ __forceinline__ void st_coefs(float4* xr, long long N, int range, const ff* C) {
+#pragma unroll
+  for (int q = 0; q < 3; ++q) xr[(long long)(MPair<NS>::COEF + 3 * range + q) * N] = pair_group(C[2 * q], C[2 * q + 1]);
+}
 template <int NS>
-constexpr int kMixedCoef = NS + 3;
-template <int NS, bool MIX>
-constexpr int kMixedPairs = MIX ? NS + 15 : NS + 2;
-static_assert(kMixedPairs<21, true> <= Rec<21>::N / 2 && kMixedPairs<9, true> <= Rec<9>::N / 2 &&
-                  kMixedPairs<1, false> <= Rec<1>::N / 2,
-              "mixed record exceeds the FP64 record");
+constexpr bool mixed_fits() {  // FP32 groups and pair groups against the FP64 record (in floats)
+  return 4 * MRec<NS>::G + 4 * MPair<NS>::template G<Physics<NS>::MIX> <= 2 * Rec<NS>::N;
+}
+static_assert(mixed_fits<1>() && mixed_fits<9>() && mixed_fits<21>(), "mixed record exceeds the FP64 record");
 
 // Reference velocity of a box: the velocity of its first valid cell (lo
 // corner), in FP64 (0 where that is not finite).  The FP32 records hold the
@@ -375,7 +434,7 @@ __device__ ff rey2t_ff(const MechF<NS>& m, const ff* Y, ff rw, ff ein, double Tg
 template <int NS, bool SIMPLE>
 __device__ __forceinline__ void cell_mixed_ff(const DevBox& b, const MechF<NS>& mf, const DevFlags& f, long long c,
                                               const double* Us, bool& newton_fail, bool& nonpos) {
-  using RC = Rec<NS>;
+  using MR = MRec<NS>;
   const int nx = b.n2[0], ny = b.n2[1];
   const int i = b.g2lo[0] + (int)(c % nx);
   const int j = b.g2lo[1] + (int)((c / nx) % ny);
@@ -406,60 +465,52 @@ __device__ __forceinline__ void cell_mixed_ff(const DevBox& b, const MechF<NS>& 
   nonpos = !(rho.hi > 0.f) || !(p.hi > 0.f) || !(T.hi > 0.f);
   const float rhof = ff_to_float(rho), Tf = ff_to_float(T), pf = ff_to_float(p), rwf = ff_to_float(rw);
   const float cs = EosF<NS, true>::cs_T(mf, Yf, rwf, rhof, Tf, pf);
-  float* r = reinterpret_cast<float*>(b.rec) + c;
+  float4* r = reinterpret_cast<float4*>(b.rec) + c;
   const long long N = b.ncell;
-  r[RC::RHO * N] = rhof;
-  r[RC::U * N] = ff_to_float(ff_sub(vx, ff_of(Us[0])));  // velocity offsets from the box's reference velocity
-  r[RC::V * N] = ff_to_float(ff_sub(vy, ff_of(Us[1])));
-  r[RC::W * N] = ff_to_float(ff_sub(vz, ff_of(Us[2])));
-  r[RC::P * N] = ff_to_float(ff_sub(p, ff_of(mf.p_ref)));
-  r[RC::C * N] = cs;
-#pragma unroll
-  for (int n = 0; n < NS; ++n) r[(RC::Y + n) * N] = Yf[n];
+  // velocity offsets from the box's reference velocity
+  r[MR::G0 * N] = make_float4(rhof, ff_to_float(ff_sub(vx, ff_of(Us[0]))), ff_to_float(ff_sub(vy, ff_of(Us[1]))),
+                              ff_to_float(ff_sub(vz, ff_of(Us[2]))));
+  r[MR::G1 * N] = make_float4(ff_to_float(ff_sub(p, ff_of(mf.p_ref))), cs, Tf, 0.f);
+  st_groups<NS>(r, MR::Y, N, Yf);
   const bool inner = i >= b.lo[0] - 1 && i <= b.hi[0] + 1 && j >= b.lo[1] - 1 && j <= b.hi[1] + 1 &&
                      k >= b.lo[2] - 1 && k <= b.hi[2] + 1;
   if (inner) {
     float X[NS];
-    float2* xr = mixed_x<NS>(b) + c;
+    float4* xr = mixed_x<NS>(b) + c;
     const ff irw = ff_div(ff_of(1.f), rw);
+    ff Xp[NS];
 #pragma unroll
     for (int n = 0; n < NS; ++n) {
-      const ff x = ff_mul(ff_mul(Y[n], mf.rWf[n]), irw);
-      xr[n * N] = make_float2(x.hi, x.lo);
-      X[n] = ff_to_float(x);
+      Xp[n] = ff_mul(ff_mul(Y[n], mf.rWf[n]), irw);
+      X[n] = ff_to_float(Xp[n]);
     }
-    xr[NS * N] = make_float2(T.hi, T.lo);
-    xr[kMixedRho<NS> * N] = make_float2(rho.hi, rho.lo);
-    xr[kMixedRw<NS> * N] = make_float2(rw.hi, rw.lo);
+    st_xt<NS>(xr, N, Xp, T);
+    xr[MPair<NS>::RHO * N] = pair_group(rho, rw);
 #pragma unroll
     for (int range = 0; range < 2; ++range) {
       ff C[6];
       mix_coefs_ff<NS>(mf, Y, range, C);
-#pragma unroll
-      for (int n = 0; n < 6; ++n) xr[(kMixedCoef<NS> + 6 * range + n) * N] = make_float2(C[n].hi, C[n].lo);
+      st_coefs<NS>(xr, N, range, C);
     }
     float out[NS + 3];
     TransF<NS, SIMPLE>::eval(mf, Tf, rhof, pf, Yf, X, out);
-    r[RC::T * N] = Tf;
     float h[NS];
     EosF<NS, true>::hi(mf, Tf, h);
-#pragma unroll
-    for (int n = 0; n < NS; ++n) r[(RC::H + n) * N] = h[n];
-#pragma unroll
-    for (int n = 0; n < NS + 3; ++n) r[(RC::D + n) * N] = out[n];
+    st_groups<NS>(r, MR::H, N, h);
+    st_groups<NS + 3>(r, MR::D, N, out);
   }
 }
 
 // ---------------------------------------------------------------------------
-// Pass 1, mixed precision.  Records are FP32, in the field order of Rec<NS>
-// (P holds p - p_ref).
+// Pass 1, mixed precision.  Records: the FP32 groups of MRec<NS> (p - p_ref
+// in place of p), then the double-float pairs (mixed_x).
 // ---------------------------------------------------------------------------
 template <int NS, class EOSD, bool MIX, bool SIMPLE, bool STRICT = false>
 __global__ void __launch_bounds__(kCellThreads)
     cell_kernel_mixed(const DevBox* __restrict__ boxes, const int2* __restrict__ items,
                       const __grid_constant__ DevMech<NS> m, const __grid_constant__ MechF<NS> mf, const DevFlags f,
                       unsigned long long* __restrict__ counters) {
-  using RC = Rec<NS>;
+  using MR = MRec<NS>;
   const int2 it = items[blockIdx.x];
   const DevBox& b = boxes[it.x];
   const long long c = (long long)it.y + threadIdx.x;
@@ -499,32 +550,29 @@ __global__ void __launch_bounds__(kCellThreads)
     nonpos = !(rho > 0.0) || !(p > 0.0) || !(T > 0.0);
     const float rhof = (float)rho, Tf = (float)T, pf = (float)p, rwf = (float)rw;
     const float cs = EosF<NS, MIX>::cs_T(mf, Yf, rwf, rhof, Tf, pf);
-    float* r = reinterpret_cast<float*>(b.rec) + c;
+    float4* r = reinterpret_cast<float4*>(b.rec) + c;
     const long long N = b.ncell;
-    r[RC::RHO * N] = rhof;
-    r[RC::U * N] = (float)(vx - Us[0]);  // velocity offsets from the box's reference velocity
-    r[RC::V * N] = (float)(vy - Us[1]);
-    r[RC::W * N] = (float)(vz - Us[2]);
-    r[RC::P * N] = (float)(p - (double)mf.p_ref);
-    r[RC::C * N] = cs;
-#pragma unroll
-    for (int n = 0; n < NS; ++n) r[(RC::Y + n) * N] = Yf[n];
+    // velocity offsets from the box's reference velocity
+    r[MR::G0 * N] = make_float4(rhof, (float)(vx - Us[0]), (float)(vy - Us[1]), (float)(vz - Us[2]));
+    r[MR::G1 * N] = make_float4((float)(p - (double)mf.p_ref), cs, Tf, 0.f);
+    st_groups<NS>(r, MR::Y, N, Yf);
     const bool inner = i >= b.lo[0] - 1 && i <= b.hi[0] + 1 && j >= b.lo[1] - 1 && j <= b.hi[1] + 1 &&
                        k >= b.lo[2] - 1 && k <= b.hi[2] + 1;
     if (inner) {
       float X[NS];
-      float2* xr = mixed_x<NS>(b) + c;
+      float4* xr = mixed_x<NS>(b) + c;
       const double irw = 1.0 / rw;
+      ff Xp[NS];
 #pragma unroll
       for (int n = 0; n < NS; ++n) {
         const double x = Y[n] * m.rW[n] * irw;
-        xr[n * N] = to_pair(x);
+        Xp[n] = ff_of(x);
         X[n] = (float)x;
       }
-      xr[NS * N] = to_pair(T);
-      xr[kMixedRho<NS> * N] = to_pair(rho);
-      if constexpr (MIX) {  // the cell's mixture sums for the Godunov energy, in double-float
-        xr[kMixedRw<NS> * N] = to_pair(rw);
+      st_xt<NS>(xr, N, Xp, ff_of(T));
+      // the cell's mixture sums for the Godunov energy, in double-float (ideal mixture)
+      xr[MPair<NS>::RHO * N] = pair_group(ff_of(rho), MIX ? ff_of(rw) : ff_of(0.f));
+      if constexpr (MIX) {
         ff Yp[NS];
 #pragma unroll
         for (int n = 0; n < NS; ++n) Yp[n] = ff_of(Y[n]);
@@ -532,19 +580,15 @@ __global__ void __launch_bounds__(kCellThreads)
         for (int range = 0; range < 2; ++range) {
           ff C[6];
           mix_coefs_ff<NS>(mf, Yp, range, C);
-#pragma unroll
-          for (int n = 0; n < 6; ++n) xr[(kMixedCoef<NS> + 6 * range + n) * N] = make_float2(C[n].hi, C[n].lo);
+          st_coefs<NS>(xr, N, range, C);
         }
       }
       float out[NS + 3];
       TransF<NS, SIMPLE>::eval(mf, Tf, rhof, pf, Yf, X, out);
-      r[RC::T * N] = Tf;
       float h[NS];
       EosF<NS, MIX>::hi(mf, Tf, h);
-#pragma unroll
-      for (int n = 0; n < NS; ++n) r[(RC::H + n) * N] = h[n];
-#pragma unroll
-      for (int n = 0; n < NS + 3; ++n) r[(RC::D + n) * N] = out[n];
+      st_groups<NS>(r, MR::H, N, h);
+      st_groups<NS + 3>(r, MR::D, N, out);
     }
   }
   warp_count(&counters[kCounterNewton], newton_fail);
@@ -578,27 +622,33 @@ __device__ __forceinline__ ff e_rp_ff_rY(const MechF<NS>& m, const float* rY, fl
 }
 
 // Internal energy of a Godunov state whose composition is that of the
-// upwind cell (pairs xr: R/Wbar and the mixture coefficients of both ranges,
-// from the cell pass) plus FP32 increments dY, at density rho and pressure p:
+// upwind cell (its R/Wbar rw_cell and, in the pair groups xr, the mixture
+// coefficients of both ranges, from the cell pass) plus FP32 increments dY,
+// at density rho and pressure p:
 // the sums of e_rp_ff with the cell's part in double-float and the
 // increments' part sum_k dY_k c_k in FP32 (its rounding falls on the
 // increments only).
 template <int NS>
-__device__ __forceinline__ ff e_godunov_ff(const MechF<NS>& m, const float2* xr, long long N, const float* dY, ff rho,
-                                           ff p) {
+__device__ __forceinline__ ff e_godunov_ff(const MechF<NS>& m, const float4* xr, long long N, const float* dY, ff rho,
+                                           ff p, ff rw_cell) {
   float drw = 0.f;
 #pragma unroll
   for (int k = 0; k < NS; ++k) drw = fmaf(dY[k], m.rW[k], drw);
-  const ff rw = ff_add(ld_pair(xr + kMixedRw<NS> * N), drw);
+  const ff rw = ff_add(rw_cell, drw);
   const ff T = ff_div(p, ff_mul(rho, rw));
   const int r = T.hi < m.tmid ? 0 : 1;
   ff C[6];
 #pragma unroll
-  for (int n = 0; n < 6; ++n) {
-    float dc = 0.f;
+  for (int q = 0; q < 3; ++q) {
+    const float4 g = __ldg(xr + (long long)(MPair<NS>::COEF + 3 * r + q) * N);
 #pragma unroll
-    for (int k = 0; k < NS; ++k) dc = fmaf(dY[k], m.cpc[r][n][k], dc);
-    C[n] = ff_add(ld_pair(xr + (kMixedCoef<NS> + 6 * r + n) * N), dc);
+    for (int l = 0; l < 2; ++l) {
+      const int n = 2 * q + l;
+      float dc = 0.f;
+#pragma unroll
+      for (int k = 0; k < NS; ++k) dc = fmaf(dY[k], m.cpc[r][n][k], dc);
+      C[n] = ff_add(pair_of(g, l), dc);
+    }
   }
   return e_of_ff<NS>(m, C, ff_sub(C[0], rw), T);
 }
@@ -623,30 +673,32 @@ template <int NS, bool MIX, int d>
 __device__ __forceinline__ void hydro_face_f(const DevBox& b, const MechF<NS>& m, const DevMech<NS>& md,
                                              const DevFlags& f, long long cR, long long st, const double* U,
                                              float* F, ff& FE, ff& FEI) {
-  using RC = Rec<NS>;
+  using MR = MRec<NS>;
   using E = EosF<NS, MIX>;
-  const float* rec = reinterpret_cast<const float*>(b.rec);
+  const float4* rec = reinterpret_cast<const float4*>(b.rec);
   const long long N = b.ncell;
   const long long cL = cR - st, cLL = cL - st, cRR = cR + st;
-  auto ld = [&](int fld, long long c) { return __ldg(rec + (long long)fld * N + c); };
-  const int fun = RC::U + d;
-  const int fut1 = (d == 0) ? RC::V : RC::U;
-  const int fut2 = (d == 2) ? RC::V : RC::W;
+  // components of G0 = (rho, u', v', w'): the normal and the two transverse velocities
+  constexpr int iun = 1 + d, it1 = (d == 0) ? 2 : 1, it2 = (d == 2) ? 2 : 3;
   // reference velocity of the normal and the two transverse components (the
   // velocities below are offsets from them)
   const double Un = U[d], Ut1 = U[(d == 0) ? 1 : 0], Ut2 = U[(d == 2) ? 1 : 2];
   const float Unf = (float)Un, Ut1f = (float)Ut1, Ut2f = (float)Ut2;
-  const float rLL = ld(RC::RHO, cLL), rL = ld(RC::RHO, cL), rR = ld(RC::RHO, cR), rRR = ld(RC::RHO, cRR);
-  const float pLL = ld(RC::P, cLL), pL = ld(RC::P, cL), pR = ld(RC::P, cR), pRR = ld(RC::P, cRR);
-  const float uLL = ld(fun, cLL), uL = ld(fun, cL), uR = ld(fun, cR), uRR = ld(fun, cRR);
-  const float cLc = ld(RC::C, cL), cRc = ld(RC::C, cR);
-  const float t1L = ld(fut1, cL), t1R = ld(fut1, cR), t2L = ld(fut2, cL), t2R = ld(fut2, cR);
+  const float4 aLL = ld_group(rec, MR::G0, N, cLL), aL = ld_group(rec, MR::G0, N, cL);
+  const float4 aR = ld_group(rec, MR::G0, N, cR), aRR = ld_group(rec, MR::G0, N, cRR);
+  const float4 bL = ld_group(rec, MR::G1, N, cL), bR = ld_group(rec, MR::G1, N, cR);  // (p', c, T, 0)
+  const float* g1 = reinterpret_cast<const float*>(rec + (long long)MR::G1 * N);
+  const float rLL = aLL.x, rL = aL.x, rR = aR.x, rRR = aRR.x;
+  const float pLL = __ldg(g1 + 4 * cLL), pL = bL.x, pR = bR.x, pRR = __ldg(g1 + 4 * cRR);
+  const float uLL = grp(aLL, iun), uL = grp(aL, iun), uR = grp(aR, iun), uRR = grp(aRR, iun);
+  const float cLc = bL.y, cRc = bR.y;
+  const float t1L = grp(aL, it1), t1R = grp(aR, it1), t2L = grp(aL, it2), t2R = grp(aR, it2);
   const float icL = 1.f / cLc, icR = 1.f / cRc;
   float dqL[4] = {0.f, 0.f, 0.f, 0.f}, dqR[4] = {0.f, 0.f, 0.f, 0.f};
   const bool slopes = f.slopes != 0;
   const float dpl = pL - pLL, dpc = pR - pL, dpr = pRR - pR;
   if (slopes) {
-    const float t1LL = ld(fut1, cLL), t1RR = ld(fut1, cRR), t2LL = ld(fut2, cLL), t2RR = ld(fut2, cRR);
+    const float t1LL = grp(aLL, it1), t1RR = grp(aRR, it1), t2LL = grp(aLL, it2), t2RR = grp(aRR, it2);
     {
       const float a = 0.5f * dpl * icL, bb = 0.5f * rL * (uL - uLL);
       const float a2 = 0.5f * dpc * icL, b2 = 0.5f * rL * (uR - uL);
@@ -681,22 +733,29 @@ __device__ __forceinline__ void hydro_face_f(const DevBox& b, const MechF<NS>& m
     const float sL = (dqL[0] + dqL[1]) * icL, sR = (dqR[0] + dqR[1]) * icR;
     const float icL2 = icL * icL, icR2 = icR * icR;
 #pragma unroll
-    for (int n = 0; n < NS; ++n) {
-      const float yLL = ld(RC::Y + n, cLL), yL = ld(RC::Y + n, cL), yR = ld(RC::Y + n, cR), yRR = ld(RC::Y + n, cRR);
-      float dsL = 0.f, dsR = 0.f;
-      if (slopes) {
-        const float ryL = rL * yL, ryR = rR * yR;
-        dsL = mc_limitf(ryL - rLL * yLL - yL * dpl * icL2, ryR - ryL - yL * dpc * icL2);
-        dsR = mc_limitf(ryR - ryL - yR * dpc * icR2, rRR * yRR - ryR - yR * dpr * icR2);
+    for (int q = 0; q < MR::Q; ++q) {  // four species a group
+      const float4 gLL = ld_group(rec, MR::Y + q, N, cLL), gL = ld_group(rec, MR::Y + q, N, cL);
+      const float4 gR = ld_group(rec, MR::Y + q, N, cR), gRR = ld_group(rec, MR::Y + q, N, cRR);
+#pragma unroll
+      for (int l = 0; l < 4; ++l) {
+        const int n = 4 * q + l;
+        if (n >= NS) break;
+        const float yLL = grp(gLL, l), yL = grp(gL, l), yR = grp(gR, l), yRR = grp(gRR, l);
+        float dsL = 0.f, dsR = 0.f;
+        if (slopes) {
+          const float ryL = rL * yL, ryR = rR * yR;
+          dsL = mc_limitf(ryL - rLL * yLL - yL * dpl * icL2, ryR - ryL - yL * dpc * icL2);
+          dsR = mc_limitf(ryR - ryL - yR * dpc * icR2, rRR * yRR - ryR - yR * dpr * icR2);
+        }
+        hL[n] = 0.5f * (dsL + yL * sL);
+        hR[n] = -(0.5f * (dsR + yR * sR));
+        HL += hL[n];
+        HR += hR[n];
+        spl[n] = yL * rL + hL[n];
+        spr[n] = yR * rR + hR[n];
+        rl += spl[n];
+        rr += spr[n];
       }
-      hL[n] = 0.5f * (dsL + yL * sL);
-      hR[n] = -(0.5f * (dsR + yR * sR));
-      HL += hL[n];
-      HR += hR[n];
-      spl[n] = yL * rL + hL[n];
-      spr[n] = yR * rR + hR[n];
-      rl += spl[n];
-      rr += spr[n];
     }
     const float irl = 1.f / rl, irr = 1.f / rr;
 #pragma unroll
@@ -833,20 +892,22 @@ __device__ __forceinline__ void hydro_face_f(const DevBox& b, const MechF<NS>& m
       // energies, which turn a 6e-8 rounding of Y_k or of rho into far more
       // than rho e varies by across the flame.
       const long long cu = mask ? cL : cR;
-      const float2* xr = mixed_x<NS>(b) + cu;
+      const float4* xr = mixed_x<NS>(b) + cu;
       const float w = min_ ? 1.f : (mout ? 0.f : frac);
       const float H = mask ? HL : HR, irf = mask ? 1.f / rl : 1.f / rr;
-      const ff rg = ff_add(ld_pair(xr + kMixedRho<NS> * N), H + w * drho);
+      const float4 rr_cell = __ldg(xr + (long long)MPair<NS>::RHO * N);  // (rho, R/Wbar) of the upwind cell
+      const ff rg = ff_add(pair_of(rr_cell, 0), H + w * drho);
       if constexpr (MIX) {
         // Y_k of the Godunov state = the cell's Y_k + d_k, d_k = (h_k - Y_k H) / rho
         // in FP32; its mixture sums are the cell's (pairs) + sum_k d_k c_k (FP32)
         float dY[NS];
+        ld_groups<NS>(rec, MR::Y, N, cu, dY);  // the upwind cell's Y_k
 #pragma unroll
         for (int n = 0; n < NS; ++n) {
           const float h = mask ? hL[n] : hR[n];
-          dY[n] = (h - ld(RC::Y + n, cu) * H) * irf;
+          dY[n] = (h - dY[n] * H) * irf;
         }
-        regd = ff_mul(rg, e_godunov_ff<NS>(m, xr, N, dY, rg, gdpa));
+        regd = ff_mul(rg, e_godunov_ff<NS>(m, xr, N, dY, rg, gdpa, pair_of(rr_cell, 1)));
       } else {
         regd = ff_mul(rg, e_rp_ff<NS, false>(m, nullptr, rg, gdpa));
       }
@@ -911,19 +972,31 @@ __device__ __forceinline__ void hydro_face_f(const DevBox& b, const MechF<NS>& m
 template <int NS, int d>
 __device__ __forceinline__ void diffusion_face_f(const DevBox& b, const DevFlags& f, const Geo& g, long long cR,
                                                  const long long stv[3], const double* U, float* F) {
-  using RC = Rec<NS>;
-  const float* rec = reinterpret_cast<const float*>(b.rec);
+  using MR = MRec<NS>;
+  const float4* rec = reinterpret_cast<const float4*>(b.rec);
   const long long N = b.ncell;
-  auto ld = [&](int fld, long long c) { return __ldg(rec + (long long)fld * N + c); };
-  const float2* xrec = mixed_x<NS>(b);
+  const float4* xrec = mixed_x<NS>(b);
   const long long cL = cR - stv[d];
   const bool harm = f.harmonic != 0;
-  const float mu = face_coeff(ld(RC::MU, cR), ld(RC::MU, cL), harm);
-  const float xi = face_coeff(ld(RC::XI, cR), ld(RC::XI, cL), harm);
-  const float lam = face_coeff(ld(RC::LAM, cR), ld(RC::LAM, cL), harm);
+  // mu, xi, lambda follow D_k: the group holding mu (and the next one where
+  // they straddle two)
+  constexpr int gm = MR::D + NS / 4, lm = NS % 4;
+  const float4 tR0 = ld_group(rec, gm, N, cR), tL0 = ld_group(rec, gm, N, cL);
+  float4 tR1 = tR0, tL1 = tL0;
+  if constexpr (lm >= 2) {
+    tR1 = ld_group(rec, gm + 1, N, cR);
+    tL1 = ld_group(rec, gm + 1, N, cL);
+  }
+  auto coef = [&](const float4& t0, const float4& t1, int i) {
+    return lm + i < 4 ? grp(t0, lm + i) : grp(t1, lm + i - 4);
+  };
+  const float mu = face_coeff(coef(tR0, tR1, 0), coef(tL0, tL1, 0), harm);
+  const float xi = face_coeff(coef(tR0, tR1, 1), coef(tL0, tL1, 1), harm);
+  const float lam = face_coeff(coef(tR0, tR1, 2), coef(tL0, tL1, 2), harm);
   float grad[3][3];
-  const float uR[3] = {ld(RC::U, cR), ld(RC::V, cR), ld(RC::W, cR)};
-  const float uL[3] = {ld(RC::U, cL), ld(RC::V, cL), ld(RC::W, cL)};
+  const float4 aR = ld_group(rec, MR::G0, N, cR), aL = ld_group(rec, MR::G0, N, cL);
+  const float uR[3] = {aR.y, aR.z, aR.w};
+  const float uL[3] = {aL.y, aL.z, aL.w};
   const float dxi = (float)g.dxinv[d];
 #pragma unroll
   for (int c = 0; c < 3; ++c) grad[c][d] = dxi * (uR[c] - uL[c]);
@@ -932,9 +1005,10 @@ __device__ __forceinline__ void diffusion_face_f(const DevBox& b, const DevFlags
     if (a == d) continue;
     const long long sa = stv[a];
     const float q4 = 0.25f * (float)g.dxinv[a];
-    const int ca = RC::U + a, cd = RC::U + d;
-    grad[a][a] = (ld(ca, cR + sa) + ld(ca, cL + sa) - ld(ca, cR - sa) - ld(ca, cL - sa)) * q4;
-    grad[d][a] = (ld(cd, cR + sa) + ld(cd, cL + sa) - ld(cd, cR - sa) - ld(cd, cL - sa)) * q4;
+    const float4 vRp = ld_group(rec, MR::G0, N, cR + sa), vLp = ld_group(rec, MR::G0, N, cL + sa);
+    const float4 vRm = ld_group(rec, MR::G0, N, cR - sa), vLm = ld_group(rec, MR::G0, N, cL - sa);
+    grad[a][a] = (grp(vRp, 1 + a) + grp(vLp, 1 + a) - grp(vRm, 1 + a) - grp(vLm, 1 + a)) * q4;
+    grad[d][a] = (grp(vRp, 1 + d) + grp(vLp, 1 + d) - grp(vRm, 1 + d) - grp(vLm, 1 + d)) * q4;
   }
   const float divu = grad[0][0] + grad[1][1] + grad[2][2];
   float tau[3];
@@ -945,7 +1019,9 @@ __device__ __forceinline__ void diffusion_face_f(const DevBox& b, const DevFlags
     else
       tau[a] = mu * (grad[d][a] + grad[a][d]);
   }
-  const float dT = pair_diff(ld_pair(xrec + NS * N + cR), ld_pair(xrec + NS * N + cL));
+  constexpr int gT = MPair<NS>::XT + NS / 2;  // the pair group holding T
+  const float4 xtR = __ldg(xrec + gT * N + cR), xtL = __ldg(xrec + gT * N + cL);
+  const float dT = pair_diff(pair_of(xtR, NS % 2), pair_of(xtL, NS % 2));
   // the work term needs absolute velocities: the offsets plus the box's reference
   const float Uf[3] = {(float)U[0], (float)U[1], (float)U[2]};
   float fE = 0.5f * (-tau[0] * (uR[0] + uL[0] + 2.f * Uf[0]) - tau[1] * (uR[1] + uL[1] + 2.f * Uf[1]) -
@@ -954,23 +1030,41 @@ __device__ __forceinline__ void diffusion_face_f(const DevBox& b, const DevFlags
   const bool spec = f.diffuse_spec != 0;
   const bool ener = (f.diffuse_temp != 0) || (f.diffuse_enth != 0);
   {
-    const float pR = ld(RC::P, cR), pL = ld(RC::P, cL);
+    const float pR = __ldg(reinterpret_cast<const float*>(rec + (long long)MR::G1 * N + cR));
+    const float pL = __ldg(reinterpret_cast<const float*>(rec + (long long)MR::G1 * N + cL));
     // d ln p / dx from the offset pressure: p = p_ref + p'.
     const float dlnp = dxi * (pR - pL) / (0.5f * (pR + pL) + (float)g.p_ref);
     float Vd[NS], Yf[NS], hf[NS];
     float Vc = 0.f;
 #pragma unroll
-    for (int n = 0; n < NS; ++n) {
-      const ff x1 = ld_pair(xrec + n * N + cR), x2 = ld_pair(xrec + n * N + cL);
-      const float dX = pair_diff(x1, x2);
-      const float Xface = 0.5f * ((x1.hi + x2.hi) + (x1.lo + x2.lo));
-      const float y1 = ld(RC::Y + n, cR), y2 = ld(RC::Y + n, cL);
-      Yf[n] = 0.5f * (y1 + y2);
-      hf[n] = 0.5f * (ld(RC::H + n, cR) + ld(RC::H + n, cL));
-      const float D = face_coeff(ld(RC::D + n, cR), ld(RC::D + n, cL), harm);
-      Vd[n] = -D * (dxi * dX + (Xface - Yf[n]) * dlnp);
-      Vc += Vd[n];
-      fE += Vd[n] * hf[n];
+    for (int q = 0; q < MR::Q; ++q) {  // four species a group
+      const float4 yR = ld_group(rec, MR::Y + q, N, cR), yL = ld_group(rec, MR::Y + q, N, cL);
+      const float4 hR = ld_group(rec, MR::H + q, N, cR), hL = ld_group(rec, MR::H + q, N, cL);
+      const float4 dR = (MR::D + q == gm) ? tR0 : ld_group(rec, MR::D + q, N, cR);
+      const float4 dL = (MR::D + q == gm) ? tL0 : ld_group(rec, MR::D + q, N, cL);
+      // the pair groups of X_{4q} .. X_{4q+3}
+      float4 xR[2], xL[2];
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int gx = MPair<NS>::XT + 2 * q + h;
+        if (2 * (2 * q + h) >= NS) break;
+        xR[h] = gx == gT ? xtR : __ldg(xrec + gx * N + cR);
+        xL[h] = gx == gT ? xtL : __ldg(xrec + gx * N + cL);
+      }
+#pragma unroll
+      for (int l = 0; l < 4; ++l) {
+        const int n = 4 * q + l;
+        if (n >= NS) break;
+        const ff x1 = pair_of(xR[l / 2], l % 2), x2 = pair_of(xL[l / 2], l % 2);
+        const float dX = pair_diff(x1, x2);
+        const float Xface = 0.5f * ((x1.hi + x2.hi) + (x1.lo + x2.lo));
+        Yf[n] = 0.5f * (grp(yR, l) + grp(yL, l));
+        hf[n] = 0.5f * (grp(hR, l) + grp(hL, l));
+        const float D = face_coeff(grp(dR, l), grp(dL, l), harm);
+        Vd[n] = -D * (dxi * dX + (Xface - Yf[n]) * dlnp);
+        Vc += Vd[n];
+        fE += Vd[n] * hf[n];
+      }
     }
 #pragma unroll
     for (int n = 0; n < NS; ++n) {
