@@ -223,6 +223,28 @@ __device__ __forceinline__ void box_uref(const DevBox& b, double U[3]) {
   }
 }
 
+// Per-tile values of the face fluxes, formed once per tile by one thread:
+// conversions from FP64 run on the FP64 pipe, at a small fraction of the
+// FP32 rate, and would otherwise be repeated on every face.  The box's
+// reference velocity in FP64, double-float and FP32; 1/dx and p_ref in FP32.
+struct FaceConsts {
+  double Ud[3];
+  ff Uff[3];
+  float U[3];
+  float dxi[3];
+  float pref;
+};
+__device__ __forceinline__ void face_consts(const DevBox& b, const Geo& g, FaceConsts& fc) {
+  box_uref(b, fc.Ud);
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    fc.Uff[a] = ff_of(fc.Ud[a]);
+    fc.U[a] = (float)fc.Ud[a];
+    fc.dxi[a] = (float)g.dxinv[a];
+  }
+  fc.pref = (float)g.p_ref;
+}
+
 template <int NS>
 __device__ __forceinline__ float mix_rwf(const MechF<NS>& m, const float* Y) {
   float s = 0.f;
@@ -666,39 +688,47 @@ __device__ __forceinline__ double e_rpY_fp64(const DevMech<NS>& md, const float*
     return GammaLawEos<NS>::e_rp(md, Y, rw, (double)rho, p);
 }
 
-// The total and internal energy fluxes (FE, FEI) are returned in
-// double-float: their divergence is ~1e-3 of their size, below what an FP32
-// flux can resolve.
-template <int NS, bool MIX, int d>
+// (rho, normal velocity, first and second transverse velocity) of a G0
+// group for faces of direction d: the transverse axes are t1 = (d == 0 ? 1
+// : 0) and t2 = (d == 2 ? 1 : 2).
+__device__ __forceinline__ float4 rot_g0(const float4& a, int d) {
+  return make_float4(a.x, d == 0 ? a.y : (d == 1 ? a.z : a.w), d == 0 ? a.z : a.y, d == 2 ? a.z : a.w);
+}
+
+// The face code takes the direction d at run time, so that the pass holds
+// one copy of it rather than one per direction (its instruction footprint,
+// not its arithmetic, was what the warps waited on).  The momentum fluxes
+// are returned in rotated order: F[UMX] normal, F[UMY] along t1, F[UMZ]
+// along t2 (face_mixed stages them at their axes).  The total and internal
+// energy fluxes (FE, FEI) are returned in double-float: their divergence is
+// ~1e-3 of their size, below what an FP32 flux can resolve.
+template <int NS, bool MIX>
 __device__ __forceinline__ void hydro_face_f(const DevBox& b, const MechF<NS>& m, const DevMech<NS>& md,
-                                             const DevFlags& f, long long cR, long long st, const double* U,
-                                             float* F, ff& FE, ff& FEI) {
+                                             const DevFlags& f, int d, long long cR, long long st,
+                                             const FaceConsts& fc, float* F, ff& FE, ff& FEI) {
   using MR = MRec<NS>;
   using E = EosF<NS, MIX>;
   const float4* rec = reinterpret_cast<const float4*>(b.rec);
   const long long N = b.ncell;
   const long long cL = cR - st, cLL = cL - st, cRR = cR + st;
-  // components of G0 = (rho, u', v', w'): the normal and the two transverse velocities
-  constexpr int iun = 1 + d, it1 = (d == 0) ? 2 : 1, it2 = (d == 2) ? 2 : 3;
   // reference velocity of the normal and the two transverse components (the
   // velocities below are offsets from them)
-  const double Un = U[d], Ut1 = U[(d == 0) ? 1 : 0], Ut2 = U[(d == 2) ? 1 : 2];
-  const float Unf = (float)Un, Ut1f = (float)Ut1, Ut2f = (float)Ut2;
-  const float4 aLL = ld_group(rec, MR::G0, N, cLL), aL = ld_group(rec, MR::G0, N, cL);
-  const float4 aR = ld_group(rec, MR::G0, N, cR), aRR = ld_group(rec, MR::G0, N, cRR);
+  const float Unf = fc.U[d], Ut1f = fc.U[(d == 0) ? 1 : 0], Ut2f = fc.U[(d == 2) ? 1 : 2];
+  const float4 aLL = rot_g0(ld_group(rec, MR::G0, N, cLL), d), aL = rot_g0(ld_group(rec, MR::G0, N, cL), d);
+  const float4 aR = rot_g0(ld_group(rec, MR::G0, N, cR), d), aRR = rot_g0(ld_group(rec, MR::G0, N, cRR), d);
   const float4 bL = ld_group(rec, MR::G1, N, cL), bR = ld_group(rec, MR::G1, N, cR);  // (p', c, T, 0)
   const float* g1 = reinterpret_cast<const float*>(rec + (long long)MR::G1 * N);
   const float rLL = aLL.x, rL = aL.x, rR = aR.x, rRR = aRR.x;
   const float pLL = __ldg(g1 + 4 * cLL), pL = bL.x, pR = bR.x, pRR = __ldg(g1 + 4 * cRR);
-  const float uLL = grp(aLL, iun), uL = grp(aL, iun), uR = grp(aR, iun), uRR = grp(aRR, iun);
+  const float uLL = aLL.y, uL = aL.y, uR = aR.y, uRR = aRR.y;
   const float cLc = bL.y, cRc = bR.y;
-  const float t1L = grp(aL, it1), t1R = grp(aR, it1), t2L = grp(aL, it2), t2R = grp(aR, it2);
+  const float t1L = aL.z, t1R = aR.z, t2L = aL.w, t2R = aR.w;
   const float icL = 1.f / cLc, icR = 1.f / cRc;
   float dqL[4] = {0.f, 0.f, 0.f, 0.f}, dqR[4] = {0.f, 0.f, 0.f, 0.f};
   const bool slopes = f.slopes != 0;
   const float dpl = pL - pLL, dpc = pR - pL, dpr = pRR - pR;
   if (slopes) {
-    const float t1LL = grp(aLL, it1), t1RR = grp(aRR, it1), t2LL = grp(aLL, it2), t2RR = grp(aRR, it2);
+    const float t1LL = aLL.z, t1RR = aRR.z, t2LL = aLL.w, t2RR = aRR.w;
     {
       const float a = 0.5f * dpl * icL, bb = 0.5f * rL * (uL - uLL);
       const float a2 = 0.5f * dpc * icL, b2 = 0.5f * rL * (uR - uL);
@@ -921,12 +951,13 @@ __device__ __forceinline__ void hydro_face_f(const DevBox& b, const MechF<NS>& m
     fl_un = fl_rho * iua + gdp;  // p_ref dropped: zero divergence
     fl_ut1 = fl_rho * iv1a;
     fl_ut2 = fl_rho * iv2a;
-    const ff iud = ff_add(ff_of(Un), iu);  // U + u' in double-float
+    const ff iud = ff_add(fc.Uff[d], iu);  // U + u' in double-float
     const ff tot = ff_add(ff_add(regd, 0.5f * rgd * (iua * iua + iv1a * iv1a + iv2a * iv2a)), gdpa);
     fl_E = ff_mul(iud, tot);
     fl_ei = ff_mul(iud, regd);
   } else {
     // Lax-Friedrichs on absolute velocities (U + u')
+    const double Un = fc.Ud[d];
     const float unlA = unl + Unf, unrA = unr + Unf, ut1lA = ut1l + Ut1f, ut1rA = ut1r + Ut1f;
     const float ut2lA = ut2l + Ut2f, ut2rA = ut2r + Ut2f;
     const double pla = (double)pl + (double)pref, pra = (double)pr + (double)pref;
@@ -956,9 +987,9 @@ __device__ __forceinline__ void hydro_face_f(const DevBox& b, const MechF<NS>& m
                          mwd * ((double)rr * er - (double)rl * el)));
   }
   F[URHO] = fl_rho;
-  F[UMX + d] = fl_un;
-  F[(d == 0) ? UMY : UMX] = fl_ut1;
-  F[(d == 2) ? UMY : UMZ] = fl_ut2;
+  F[UMX] = fl_un;  // rotated order
+  F[UMY] = fl_ut1;
+  F[UMZ] = fl_ut2;
   F[UEDEN] = 0.f;  // energy fluxes travel in double-float (FE, FEI)
   F[UEINT] = 0.f;
   F[UTEMP] = 0.f;
@@ -968,15 +999,19 @@ __device__ __forceinline__ void hydro_face_f(const DevBox& b, const MechF<NS>& m
   for (int n = 0; n < NS; ++n) F[UFS + n] = flY[n];
 }
 
-// FP32 diffusion flux (not area-scaled), added to F.
-template <int NS, int d>
-__device__ __forceinline__ void diffusion_face_f(const DevBox& b, const DevFlags& f, const Geo& g, long long cR,
-                                                 const long long stv[3], const double* U, float* F) {
+// FP32 diffusion flux (not area-scaled), added to F (momentum in the rotated
+// order of hydro_face_f).  st: the cell stride of direction d; s1, s2: those
+// of the transverse axes t1, t2.
+template <int NS>
+__device__ __forceinline__ void diffusion_face_f(const DevBox& b, const DevFlags& f, int d, long long cR,
+                                                 long long st, long long s1, long long s2, const FaceConsts& fc,
+                                                 float* F) {
   using MR = MRec<NS>;
   const float4* rec = reinterpret_cast<const float4*>(b.rec);
   const long long N = b.ncell;
   const float4* xrec = mixed_x<NS>(b);
-  const long long cL = cR - stv[d];
+  const long long cL = cR - st;
+  const int t1 = (d == 0) ? 1 : 0, t2 = (d == 2) ? 1 : 2;
   const bool harm = f.harmonic != 0;
   // mu, xi, lambda follow D_k: the group holding mu (and the next one where
   // they straddle two)
@@ -993,37 +1028,36 @@ __device__ __forceinline__ void diffusion_face_f(const DevBox& b, const DevFlags
   const float mu = face_coeff(coef(tR0, tR1, 0), coef(tL0, tL1, 0), harm);
   const float xi = face_coeff(coef(tR0, tR1, 1), coef(tL0, tL1, 1), harm);
   const float lam = face_coeff(coef(tR0, tR1, 2), coef(tL0, tL1, 2), harm);
+  // velocity gradients in the rotated frame (0: normal, 1: t1, 2: t2),
+  // grad[c][a] = d u_c / d x_a
   float grad[3][3];
-  const float4 aR = ld_group(rec, MR::G0, N, cR), aL = ld_group(rec, MR::G0, N, cL);
+  const float4 aR = rot_g0(ld_group(rec, MR::G0, N, cR), d), aL = rot_g0(ld_group(rec, MR::G0, N, cL), d);
   const float uR[3] = {aR.y, aR.z, aR.w};
   const float uL[3] = {aL.y, aL.z, aL.w};
-  const float dxi = (float)g.dxinv[d];
+  const float dxi = fc.dxi[d];
 #pragma unroll
-  for (int c = 0; c < 3; ++c) grad[c][d] = dxi * (uR[c] - uL[c]);
+  for (int c = 0; c < 3; ++c) grad[c][0] = dxi * (uR[c] - uL[c]);
 #pragma unroll
-  for (int a = 0; a < 3; ++a) {
-    if (a == d) continue;
-    const long long sa = stv[a];
-    const float q4 = 0.25f * (float)g.dxinv[a];
+  for (int a = 1; a < 3; ++a) {
+    const long long sa = a == 1 ? s1 : s2;
+    const float q4 = 0.25f * fc.dxi[a == 1 ? t1 : t2];
     const float4 vRp = ld_group(rec, MR::G0, N, cR + sa), vLp = ld_group(rec, MR::G0, N, cL + sa);
     const float4 vRm = ld_group(rec, MR::G0, N, cR - sa), vLm = ld_group(rec, MR::G0, N, cL - sa);
-    grad[a][a] = (grp(vRp, 1 + a) + grp(vLp, 1 + a) - grp(vRm, 1 + a) - grp(vLm, 1 + a)) * q4;
-    grad[d][a] = (grp(vRp, 1 + d) + grp(vLp, 1 + d) - grp(vRm, 1 + d) - grp(vLm, 1 + d)) * q4;
+    // components of G0 = (rho, u, v, w) along axis a and along the normal
+    const int ia = 1 + (a == 1 ? t1 : t2), in = 1 + d;
+    grad[a][a] = (grp(vRp, ia) + grp(vLp, ia) - grp(vRm, ia) - grp(vLm, ia)) * q4;
+    grad[0][a] = (grp(vRp, in) + grp(vLp, in) - grp(vRm, in) - grp(vLm, in)) * q4;
   }
   const float divu = grad[0][0] + grad[1][1] + grad[2][2];
   float tau[3];
+  tau[0] = mu * (2.f * grad[0][0] - (2.f / 3.f) * divu) + xi * divu;
 #pragma unroll
-  for (int a = 0; a < 3; ++a) {
-    if (a == d)
-      tau[a] = mu * (2.f * grad[d][d] - (2.f / 3.f) * divu) + xi * divu;
-    else
-      tau[a] = mu * (grad[d][a] + grad[a][d]);
-  }
+  for (int a = 1; a < 3; ++a) tau[a] = mu * (grad[0][a] + grad[a][0]);
   constexpr int gT = MPair<NS>::XT + NS / 2;  // the pair group holding T
   const float4 xtR = __ldg(xrec + gT * N + cR), xtL = __ldg(xrec + gT * N + cL);
   const float dT = pair_diff(pair_of(xtR, NS % 2), pair_of(xtL, NS % 2));
   // the work term needs absolute velocities: the offsets plus the box's reference
-  const float Uf[3] = {(float)U[0], (float)U[1], (float)U[2]};
+  const float Uf[3] = {fc.U[d], fc.U[t1], fc.U[t2]};
   float fE = 0.5f * (-tau[0] * (uR[0] + uL[0] + 2.f * Uf[0]) - tau[1] * (uR[1] + uL[1] + 2.f * Uf[1]) -
                      tau[2] * (uR[2] + uL[2] + 2.f * Uf[2])) -
              lam * dxi * dT;
@@ -1033,7 +1067,7 @@ __device__ __forceinline__ void diffusion_face_f(const DevBox& b, const DevFlags
     const float pR = __ldg(reinterpret_cast<const float*>(rec + (long long)MR::G1 * N + cR));
     const float pL = __ldg(reinterpret_cast<const float*>(rec + (long long)MR::G1 * N + cL));
     // d ln p / dx from the offset pressure: p = p_ref + p'.
-    const float dlnp = dxi * (pR - pL) / (0.5f * (pR + pL) + (float)g.p_ref);
+    const float dlnp = dxi * (pR - pL) / (0.5f * (pR + pL) + fc.pref);
     float Vd[NS], Yf[NS], hf[NS];
     float Vc = 0.f;
 #pragma unroll
@@ -1117,32 +1151,41 @@ struct FaceStage {
 };
 
 // One face of direction d (index fi in the tile's face block of that
-// direction, nf0 x nf1 x nf2): hydrodynamic and diffusion fluxes, staged.
-template <int NS, bool MIX, int d, class TL>
+// direction, nf0 x nf1 x nf2): hydrodynamic and diffusion fluxes, staged
+// (the rotated momentum components at their axes).
+template <int NS, bool MIX, class TL>
 __device__ __forceinline__ void face_mixed(const DevBox& b, const MechF<NS>& m, const DevMech<NS>& md,
-                                           const DevFlags& f, const Geo& g, const int o[3], const long long stv[3],
-                                           int fi, int nf0, int nf1, bool diff, const double* U,
+                                           const DevFlags& f, const int o[3], const long long stv[3], int d, int fi,
+                                           int nf0, int nf1, bool diff, const FaceConsts& fc,
                                            const FaceStage<NS, TL>& fs) {
   constexpr int NVAR = 7 + NS;
   const int fx = fi % nf0, fy = (fi / nf0) % nf1, fz = fi / (nf0 * nf1);
   const int i = o[0] + fx, j = o[1] + fy, k = o[2] + fz;
   const long long cR = (i - b.g2lo[0]) + (j - b.g2lo[1]) * stv[1] + (k - b.g2lo[2]) * stv[2];
+  // strides of the normal and the two transverse axes
+  const long long st = d == 0 ? stv[0] : (d == 1 ? stv[1] : stv[2]);
+  const long long s1 = d == 0 ? stv[1] : stv[0], s2 = d == 2 ? stv[1] : stv[2];
   float F[NVAR];
   ff FE = ff_of(0.f), FEI = ff_of(0.f);
   if (f.do_hydro) {
-    hydro_face_f<NS, MIX, d>(b, m, md, f, cR, stv[d], U, F, FE, FEI);
+    hydro_face_f<NS, MIX>(b, m, md, f, d, cR, st, fc, F, FE, FEI);
   } else {
 #pragma unroll
     for (int n = 0; n < NVAR; ++n) F[n] = 0.f;
   }
-  if (diff) diffusion_face_f<NS, d>(b, f, g, cR, stv, U, F);
+  if (diff) diffusion_face_f<NS>(b, f, d, cR, st, s1, s2, fc, F);
   const int slot = FaceStage<NS, TL>::base(d) + fi;
+  constexpr int TOT = FaceStage<NS, TL>::TOT;
+  const int rowt1 = d == 0 ? UMY : UMX, rowt2 = d == 2 ? UMY : UMZ;  // rows of the transverse momenta
 #pragma unroll
-  for (int n = 0; n < NVAR; ++n)
-    if (n != UEDEN && n != UEINT) fs.v[n * FaceStage<NS, TL>::TOT + slot] = F[n];
+  for (int n = 0; n < NVAR; ++n) {
+    if (n == UEDEN || n == UEINT) continue;
+    const int row = n == UMX ? UMX + d : (n == UMY ? rowt1 : (n == UMZ ? rowt2 : n));
+    fs.v[row * TOT + slot] = F[n];
+  }
   const ff fe = ff_add(FE, F[UEDEN]);
   fs.e[slot] = make_float2(fe.hi, fe.lo);
-  fs.e[FaceStage<NS, TL>::TOT + slot] = make_float2(FEI.hi, FEI.lo);
+  fs.e[TOT + slot] = make_float2(FEI.hi, FEI.lo);
 }
 
 // Pass 2 over the tile list; CTA b takes tiles b, b + gridDim.x, ... (one
@@ -1179,24 +1222,18 @@ __global__ void __launch_bounds__(TL::NT, TL::MINB)
                         min(TL::TZ, b.hi[2] - o[2] + 1)};
     const bool mine = tx < ext[0] && ty < ext[1] && tz < ext[2];
     const long long stv[3] = {1, b.n2[0], (long long)b.n2[0] * b.n2[1]};
-    __shared__ double Us[3];  // the box's reference velocity
-    if (threadIdx.x == 0) box_uref(b, Us);
+    __shared__ FaceConsts fc;  // the box's reference velocity, 1/dx, p_ref
+    if (threadIdx.x == 0) face_consts(b, g, fc);
     __syncthreads();
     // faces of direction d: (ext + e_d) in each direction
     const int n0 = (ext[0] + 1) * ext[1] * ext[2], n1 = ext[0] * (ext[1] + 1) * ext[2],
               n2 = ext[0] * ext[1] * (ext[2] + 1);
     const int c0 = (n0 + 31) >> 5, c1 = (n1 + 31) >> 5, c2 = (n2 + 31) >> 5;
     for (int c = warp; c < c0 + c1 + c2; c += NW) {
-      if (c < c0) {
-        const int fi = (c << 5) + lane;
-        if (fi < n0) face_mixed<NS, MIX, 0, TL>(b, m, md, f, g, o, stv, fi, ext[0] + 1, ext[1], diff, Us, fs);
-      } else if (c < c0 + c1) {
-        const int fi = ((c - c0) << 5) + lane;
-        if (fi < n1) face_mixed<NS, MIX, 1, TL>(b, m, md, f, g, o, stv, fi, ext[0], ext[1] + 1, diff, Us, fs);
-      } else {
-        const int fi = ((c - c0 - c1) << 5) + lane;
-        if (fi < n2) face_mixed<NS, MIX, 2, TL>(b, m, md, f, g, o, stv, fi, ext[0], ext[1], diff, Us, fs);
-      }
+      const int d = c < c0 ? 0 : (c < c0 + c1 ? 1 : 2);
+      const int fi = ((c - (d == 0 ? 0 : (d == 1 ? c0 : c0 + c1))) << 5) + lane;
+      if (fi < (d == 0 ? n0 : (d == 1 ? n1 : n2)))
+        face_mixed<NS, MIX, TL>(b, m, md, f, o, stv, d, fi, ext[0] + (d == 0), ext[1] + (d == 1), diff, fc, fs);
     }
     __syncthreads();
     bool bad = false;
