@@ -420,7 +420,9 @@ __device__ __forceinline__ ff cv_of_ff(const ff C[6], ff c0, ff T) {
 // once |T_new - T| <= 1e-12 T_new, ok = false after maxit iterations).
 template <int NS>
 __device__ ff rey2t_ff(const MechF<NS>& m, const ff* Y, ff rw, ff ein, double Tguess, int maxit, bool& ok) {
-  ff t = (Tguess > 0.0 && isfinite(Tguess)) ? ff_of(Tguess) : ff_of(1000.f);
+  // Tguess > 0 and finite, tested on its bits (integer pipe)
+  const long long tb = __double_as_longlong(Tguess);
+  ff t = (tb > 0 && tb < 0x7ff0000000000000LL) ? ff_of(Tguess) : ff_of(1000.f);
   int r = t.hi < m.tmid ? 0 : 1;
   ff C[6];
   mix_coefs_ff<NS>(m, Y, r, C);
@@ -463,25 +465,48 @@ __device__ __forceinline__ void cell_mixed_ff(const DevBox& b, const MechF<NS>& 
   const int k = b.g2lo[2] + (int)(c / ((long long)nx * ny));
   const double* s = b.S + (i - b.sb[0]) + (long long)(j - b.sb[1]) * b.sj + (long long)(k - b.sb[2]) * b.sk;
   const long long sn = b.sn;
-  const ff rho = ff_of(__ldg(s + URHO * sn));
+  // the conserved state (rho, momenta, rho E, rho Y_k): every load first,
+  // then one warp-uniform choice of the conversion to double-float (the
+  // integer-pipe form unless a lane holds a value outside its range)
+  constexpr int NU = 5 + NS;
+  double u[NU];
+  u[0] = __ldg(s + URHO * sn);
+#pragma unroll
+  for (int a = 0; a < 3; ++a) u[1 + a] = __ldg(s + (UMX + a) * sn);
+  u[4] = __ldg(s + UEDEN * sn);
+#pragma unroll
+  for (int n = 0; n < NS; ++n) u[5 + n] = __ldg(s + (UFS + n) * sn);
+  const double Tguess = __ldg(s + UTEMP * sn);
+  bool fast = true;
+#pragma unroll
+  for (int n = 0; n < NU; ++n) fast &= ff_fast_ok(u[n]);
+  ff Uc[NU];
+  if (__all_sync(__activemask(), fast)) {
+#pragma unroll
+    for (int n = 0; n < NU; ++n) Uc[n] = ff_of_fast(u[n]);
+  } else {
+#pragma unroll
+    for (int n = 0; n < NU; ++n) Uc[n] = ff_of_conv(u[n]);
+  }
+  const ff rho = Uc[0];
   const ff ir = ff_div(ff_of(1.f), rho);
-  const ff vx = ff_mul(ff_of(__ldg(s + UMX * sn)), ir);
-  const ff vy = ff_mul(ff_of(__ldg(s + UMY * sn)), ir);
-  const ff vz = ff_mul(ff_of(__ldg(s + UMZ * sn)), ir);
+  const ff vx = ff_mul(Uc[1], ir);
+  const ff vy = ff_mul(Uc[2], ir);
+  const ff vz = ff_mul(Uc[3], ir);
   const ff v2 = ff_fma(vz, vz, ff_fma(vy, vy, ff_mul(vx, vx)));
-  const ff e = ff_mul(ff_sub(ff_of(__ldg(s + UEDEN * sn)), ff_mul(ff_mul(rho, v2), 0.5f)), ir);
+  const ff e = ff_mul(ff_sub(Uc[4], ff_mul(ff_mul(rho, v2), 0.5f)), ir);
   ff Y[NS];
   float Yf[NS];
 #pragma unroll
   for (int n = 0; n < NS; ++n) {
-    ff y = ff_mul(ff_of(__ldg(s + (UFS + n) * sn)), ir);
+    ff y = ff_mul(Uc[5 + n], ir);
     if (fabsf(y.hi) < 1e-4f * 2.220446049250313e-16f) y = ff_of(0.f);
     Y[n] = y;
     Yf[n] = ff_to_float(y);
   }
   const ff rw = mix_rw_ff<NS>(mf, Y);
   bool ok = true;
-  const ff T = rey2t_ff<NS>(mf, Y, rw, e, __ldg(s + UTEMP * sn), f.newton_maxit, ok);
+  const ff T = rey2t_ff<NS>(mf, Y, rw, e, Tguess, f.newton_maxit, ok);
   const ff p = ff_mul(ff_mul(rho, rw), T);
   newton_fail = !ok;
   nonpos = !(rho.hi > 0.f) || !(p.hi > 0.f) || !(T.hi > 0.f);
@@ -1269,11 +1294,23 @@ __global__ void __launch_bounds__(TL::NT, TL::MINB)
 #pragma unroll
           for (int n = 0; n < NVAR; ++n) acc[n] = ff_add(ff_mul(fs.diff(n, flo, fhi), dxi[d]), acc[n]);
         }
+        // to FP64: on the integer pipe (and one FP64 addition) unless a lane
+        // of the warp holds a subnormal, infinite or NaN part
+        bool fast = true;
+#pragma unroll
+        for (int n = 0; n < NVAR; ++n) fast &= f2d_fast_ok(acc[n].hi) && f2d_fast_ok(acc[n].lo);
+        double v[NVAR];
+        if (__all_sync(__activemask(), fast)) {
+#pragma unroll
+          for (int n = 0; n < NVAR; ++n) v[n] = ff_to_double_fast(acc[n]);
+        } else {
+#pragma unroll
+          for (int n = 0; n < NVAR; ++n) v[n] = ff_to_double(acc[n]);
+        }
 #pragma unroll
         for (int n = 0; n < NVAR; ++n) {
-          const double v = ff_to_double(acc[n]);
-          bad |= !isfinite(v);
-          r[n * b.rn] = v;
+          bad |= !isfinite(v[n]);
+          r[n * b.rn] = v[n];
         }
       }
     }
