@@ -1165,13 +1165,14 @@ struct FaceStage {
     }
     return ff_sum(v[n * TOT + slot], -v[n * TOT + slot2]);
   }
-  // the staged flux of component n as a double (the FP32 ones widened exactly)
+  // the staged flux of component n as a double (the FP32 ones widened
+  // exactly, on the integer pipe where they are normal or zero)
   __device__ double get(int n, int slot) const {
     if (n == UEDEN || n == UEINT) {
       const float2 a = e[(n == UEINT) * TOT + slot];
       return ff_to_double(ff{a.x, a.y});
     }
-    return (double)v[n * TOT + slot];
+    return f2d_exact(v[n * TOT + slot]);
   }
 };
 
