@@ -1231,14 +1231,12 @@ __global__ void __launch_bounds__(TL::NT, TL::MINB)
                       const __grid_constant__ MechF<NS> m, const __grid_constant__ DevMech<NS> md, const DevFlags f,
                       const Geo g, unsigned long long* __restrict__ counters) {
   constexpr int NVAR = 7 + NS;
-  constexpr int NW = TL::NT / 32;
   extern __shared__ double flux_dyn_smem[];
   FaceStage<NS, TL> fs;
   fs.e = reinterpret_cast<float2*>(flux_dyn_smem);
   fs.v = reinterpret_cast<float*>(flux_dyn_smem + 2 * FaceStage<NS, TL>::TOT);
   const bool diff = f.diffuse_vel || f.diffuse_temp || f.diffuse_spec || f.diffuse_enth;
   const int tx = threadIdx.x % TL::TX, ty = (threadIdx.x / TL::TX) % TL::TY, tz = threadIdx.x / (TL::TX * TL::TY);
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const ff dxi[3] = {ff_of(g.dxinv[0]), ff_of(g.dxinv[1]), ff_of(g.dxinv[2])};
   for (int tb = blockIdx.x; tb < ntiles; tb += gridDim.x) {
     const int4 t = tiles[tb];
@@ -1251,15 +1249,40 @@ __global__ void __launch_bounds__(TL::NT, TL::MINB)
     __shared__ FaceConsts fc;  // the box's reference velocity, 1/dx, p_ref
     if (threadIdx.x == 0) face_consts(b, g, fc);
     __syncthreads();
-    // faces of direction d: (ext + e_d) in each direction
-    const int n0 = (ext[0] + 1) * ext[1] * ext[2], n1 = ext[0] * (ext[1] + 1) * ext[2],
-              n2 = ext[0] * ext[1] * (ext[2] + 1);
-    const int c0 = (n0 + 31) >> 5, c1 = (n1 + 31) >> 5, c2 = (n2 + 31) >> 5;
-    for (int c = warp; c < c0 + c1 + c2; c += NW) {
-      const int d = c < c0 ? 0 : (c < c0 + c1 ? 1 : 2);
-      const int fi = ((c - (d == 0 ? 0 : (d == 1 ? c0 : c0 + c1))) << 5) + lane;
-      if (fi < (d == 0 ? n0 : (d == 1 ? n1 : n2)))
-        face_mixed<NS, MIX, TL>(b, m, md, f, o, stv, d, fi, ext[0] + (d == 0), ext[1] + (d == 1), diff, fc, fs);
+    // Cell-major face order: the faces of direction d form a block of
+    // (ext + e_d) faces.  In rounds 0-2 each thread evaluates the low x, y
+    // and z faces of its own cell (a warp revisits the same cells' records
+    // three times in a row); the later rounds spread the tile's high
+    // boundary faces (x = ext[0], y = ext[1], z = ext[2]) over all threads.
+    // One call site: the face code is inlined once.
+    {
+      const int nb0 = ext[1] * ext[2], nb1 = ext[0] * ext[2], nb2 = ext[0] * ext[1];
+      const int nrounds = 3 + (nb0 + nb1 + nb2 + TL::NT - 1) / TL::NT;
+#pragma unroll 1
+      for (int k = 0; k < nrounds; ++k) {
+        int d, c0, c1, c2;
+        bool act;
+        if (k < 3) {
+          d = k;
+          act = mine;
+          c0 = tx;
+          c1 = ty;
+          c2 = tz;
+        } else {
+          const int q = (k - 3) * TL::NT + threadIdx.x;
+          act = q < nb0 + nb1 + nb2;
+          d = q < nb0 ? 0 : (q < nb0 + nb1 ? 1 : 2);
+          const int r = q - (d == 0 ? 0 : (d == 1 ? nb0 : nb0 + nb1));
+          const int e1 = d == 0 ? ext[1] : ext[0];  // extent of the first of the other two axes
+          c0 = d == 0 ? ext[0] : r % e1;
+          c1 = d == 1 ? ext[1] : (d == 0 ? r % e1 : r / e1);
+          c2 = d == 2 ? ext[2] : r / e1;
+        }
+        if (act) {
+          const int nf0 = ext[0] + (d == 0), nf1 = ext[1] + (d == 1);
+          face_mixed<NS, MIX, TL>(b, m, md, f, o, stv, d, c0 + nf0 * (c1 + nf1 * c2), nf0, nf1, diff, fc, fs);
+        }
+      }
     }
     __syncthreads();
     bool bad = false;
