@@ -418,13 +418,15 @@ __device__ __forceinline__ ff cv_of_ff(const ff C[6], ff c0, ff T) {
 // REY2T in double-float arithmetic: IdealMixEos::rey2t's Newton iteration
 // on e(T) = e from the guess (steps clamped to +-1000 K, T >= 10 K, stop
 // once |T_new - T| <= 1e-12 T_new, ok = false after maxit iterations).
+// rC, C: the temperature range of the last iteration and the mixture
+// coefficients of that range (mix_coefs_ff), which the cell pass stores.
 template <int NS>
-__device__ ff rey2t_ff(const MechF<NS>& m, const ff* Y, ff rw, ff ein, double Tguess, int maxit, bool& ok) {
+__device__ ff rey2t_ff(const MechF<NS>& m, const ff* Y, ff rw, ff ein, double Tguess, int maxit, bool& ok, int& rC,
+                       ff C[6]) {
   // Tguess > 0 and finite, tested on its bits (integer pipe)
   const long long tb = __double_as_longlong(Tguess);
   ff t = (tb > 0 && tb < 0x7ff0000000000000LL) ? ff_of(Tguess) : ff_of(1000.f);
   int r = t.hi < m.tmid ? 0 : 1;
-  ff C[6];
   mix_coefs_ff<NS>(m, Y, r, C);
   ok = false;
   for (int it = 0; it < maxit; ++it) {
@@ -446,6 +448,7 @@ __device__ ff rey2t_ff(const MechF<NS>& m, const ff* Y, ff rw, ff ein, double Tg
       break;
     }
   }
+  rC = r;
   return t;
 }
 
@@ -506,21 +509,29 @@ __device__ __forceinline__ void cell_mixed_ff(const DevBox& b, const MechF<NS>& 
   }
   const ff rw = mix_rw_ff<NS>(mf, Y);
   bool ok = true;
-  const ff T = rey2t_ff<NS>(mf, Y, rw, e, Tguess, f.newton_maxit, ok);
+  int rC;
+  ff C[6];
+  const ff T = rey2t_ff<NS>(mf, Y, rw, e, Tguess, f.newton_maxit, ok, rC, C);
+  const bool inner = i >= b.lo[0] - 1 && i <= b.hi[0] + 1 && j >= b.lo[1] - 1 && j <= b.hi[1] + 1 &&
+                     k >= b.lo[2] - 1 && k <= b.hi[2] + 1;
+  const long long N = b.ncell;
+  if (inner) {  // the mixture coefficients of both ranges: the Newton solve's own, and the other's
+    float4* xr = mixed_x<NS>(b) + c;
+    st_coefs<NS>(xr, N, rC, C);
+    mix_coefs_ff<NS>(mf, Y, 1 - rC, C);
+    st_coefs<NS>(xr, N, 1 - rC, C);
+  }
   const ff p = ff_mul(ff_mul(rho, rw), T);
   newton_fail = !ok;
   nonpos = !(rho.hi > 0.f) || !(p.hi > 0.f) || !(T.hi > 0.f);
   const float rhof = ff_to_float(rho), Tf = ff_to_float(T), pf = ff_to_float(p), rwf = ff_to_float(rw);
   const float cs = EosF<NS, true>::cs_T(mf, Yf, rwf, rhof, Tf, pf);
   float4* r = reinterpret_cast<float4*>(b.rec) + c;
-  const long long N = b.ncell;
   // velocity offsets from the box's reference velocity
   r[MR::G0 * N] = make_float4(rhof, ff_to_float(ff_sub(vx, ff_of(Us[0]))), ff_to_float(ff_sub(vy, ff_of(Us[1]))),
                               ff_to_float(ff_sub(vz, ff_of(Us[2]))));
   r[MR::G1 * N] = make_float4(ff_to_float(ff_sub(p, ff_of(mf.p_ref))), cs, Tf, 0.f);
   st_groups<NS>(r, MR::Y, N, Yf);
-  const bool inner = i >= b.lo[0] - 1 && i <= b.hi[0] + 1 && j >= b.lo[1] - 1 && j <= b.hi[1] + 1 &&
-                     k >= b.lo[2] - 1 && k <= b.hi[2] + 1;
   if (inner) {
     float X[NS];
     float4* xr = mixed_x<NS>(b) + c;
@@ -533,12 +544,6 @@ __device__ __forceinline__ void cell_mixed_ff(const DevBox& b, const MechF<NS>& 
     }
     st_xt<NS>(xr, N, Xp, T);
     xr[MPair<NS>::RHO * N] = pair_group(rho, rw);
-#pragma unroll
-    for (int range = 0; range < 2; ++range) {
-      ff C[6];
-      mix_coefs_ff<NS>(mf, Y, range, C);
-      st_coefs<NS>(xr, N, range, C);
-    }
     float out[NS + 3];
     TransF<NS, SIMPLE>::eval(mf, Tf, rhof, pf, Yf, X, out);
     float h[NS];
