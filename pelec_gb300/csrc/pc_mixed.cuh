@@ -383,22 +383,37 @@ __device__ __forceinline__ float face_coeff(float a, float b, bool harmonic) {
 // R/Wbar = sum_k Y_k R/W_k, the mixture NASA-7 coefficients of range r,
 // e(T) = C5 + T ((C0 - R/Wbar) + T (C1/2 + T (C2/3 + T (C3/4 + T C4/5))))
 // and cv(T) = (C0 - R/Wbar) + T (C1 + T (C2 + T (C3 + T C4))).
+// sum_k a_k b_k of double-float operands as a compensated dot product
+// (Ogita, Rump and Oishi, "Accurate sum and dot product", SIAM J. Sci.
+// Comput. 26, 2005, Dot2): the products of the hi parts split exactly by
+// TwoProduct and summed by TwoSum, their errors, the cross terms and the
+// sums' errors gathered in one float, added by one TwoSum at the end.  About
+// 2^-48 of the terms' magnitude, like a chain of ff_fma, in fewer FP32
+// operations.
+template <int NS>
+__device__ __forceinline__ ff dot_ff(const ff* a, const ff* b) {
+  float s = __fmul_rn(a[0].hi, b[0].hi);
+  float c = fmaf(a[0].hi, b[0].hi, -s);
+  c = fmaf(a[0].hi, b[0].lo, fmaf(a[0].lo, b[0].hi, c));
+#pragma unroll
+  for (int k = 1; k < NS; ++k) {
+    const float p = __fmul_rn(a[k].hi, b[k].hi);
+    float e;
+    float t;
+    two_sum(s, p, t, e);
+    s = t;
+    c = __fadd_rn(c, __fadd_rn(e, fmaf(a[k].hi, b[k].lo, fmaf(a[k].lo, b[k].hi, fmaf(a[k].hi, b[k].hi, -p)))));
+  }
+  return ff_sum(s, c);  // TwoSum: exact even where the sum cancels below c
+}
 template <int NS>
 __device__ __forceinline__ ff mix_rw_ff(const MechF<NS>& m, const ff* Y) {
-  ff rw = ff_mul(Y[0], m.rWf[0]);
-#pragma unroll
-  for (int k = 1; k < NS; ++k) rw = ff_fma(Y[k], m.rWf[k], rw);
-  return rw;
+  return dot_ff<NS>(Y, m.rWf);
 }
 template <int NS>
 __device__ __forceinline__ void mix_coefs_ff(const MechF<NS>& m, const ff* Y, int r, ff C[6]) {
 #pragma unroll
-  for (int n = 0; n < 6; ++n) {
-    ff c = ff_mul(Y[0], m.cpcf[r][n][0]);
-#pragma unroll
-    for (int k = 1; k < NS; ++k) c = ff_fma(Y[k], m.cpcf[r][n][k], c);
-    C[n] = c;
-  }
+  for (int n = 0; n < 6; ++n) C[n] = dot_ff<NS>(Y, m.cpcf[r][n]);
 }
 template <int NS>
 __device__ __forceinline__ ff e_of_ff(const MechF<NS>& m, const ff C[6], ff c0, ff T) {
