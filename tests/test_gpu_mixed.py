@@ -61,6 +61,29 @@ def test_mixed_flame_error_vs_fp64_oracle(cuda_lib, oracle_lib, form):
 
 
 @pytest.mark.parametrize("form", FORMS)
+def test_mixed_tiny_and_zero_species(cuda_lib, oracle_lib, form):
+    """Species densities of 1e-30 rho (H, lower half of the box in z) and
+    exactly 0 (HO2, upper two thirds): the cell pass converts the FP64 state
+    to double-float pairs on the integer pipe where every value of a warp
+    lies in 2^-72 <= |x| < 2^116 or is zero, and by the FP64 conversions in
+    the warps that hold the tiny densities; the RHS stays within the bar
+    against the FP64 oracle either way."""
+    mech, st, _ = problems.flame((24, 20, 32), seed=43)
+    ufs = 7
+    k = {n: i for i, n in enumerate(mech.names)}
+    nz = st.S.shape[1]  # (component, z, y, x), ghosts included
+    st.S[ufs + k["H"], : nz // 2] = 1e-30 * st.S[0, : nz // 2]
+    st.S[ufs + k["HO2"], nz // 3 :] = 0.0
+    ref, = oracle_lib.mol_rhs(problems.make_config(mech), [st])
+    (gpu,), status = gpu_rhs(cuda_lib, problems.make_config(mech, precision=form), [st])
+    l2 = rel_l2(gpu, ref)
+    print(form, "tiny/zero species rel L2 per component:", l2)
+    assert np.all(np.isfinite(gpu))
+    assert np.all(l2 <= _tol()), l2
+    assert status.nonfinite_output == 0 and status.newton_nonconverged == 0
+
+
+@pytest.mark.parametrize("form", FORMS)
 def test_mixed_flame_128_vs_fp64_gpu(cuda_lib, form):
     """Full C2 size against the FP64 path (which matches the oracle bit for bit)."""
     mech, st, _ = problems.flame((128, 128, 128), seed=1)
