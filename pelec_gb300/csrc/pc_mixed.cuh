@@ -18,8 +18,9 @@
 // slopes, the Riemann star pressure and the pressure gradients only use
 // differences, the EOS calls add p_ref back, and the normal-momentum flux
 // drops the constant p_ref, whose divergence is zero on a uniform grid.
-// Records are FP32 except the mole fractions and the temperature, kept in
-// FP64 after the FP32 fields: diffusion is driven by their cell-to-cell
+// Records are FP32 (16-byte groups, MRec) except the mole fractions and the
+// temperature, kept at FP64 accuracy after the FP32 groups (MPair): diffusion
+// is driven by their cell-to-cell
 // differences, which in the far field are ~1e-6 of X itself and would be lost
 // in FP32, and whose second differences (the conduction term of the energy
 // RHS) are ~1e-3 of T.  Those FP64 values are stored as double-float pairs
@@ -31,7 +32,7 @@
 // increments (hydro_face_f).  The cell's part of the mixture sums (R/Wbar and
 // the NASA-7 coefficients of both ranges) is formed once per cell in the cell
 // pass; a face adds the FP32 sums over its composition increments.  The
-// energy fluxes formed from it are widened to FP64 for the divergence.
+// energy fluxes formed from it reach the divergence as double-float pairs.
 #pragma once
 
 #include "pc_ff.cuh"
