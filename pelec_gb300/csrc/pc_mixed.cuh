@@ -1237,15 +1237,16 @@ __device__ __forceinline__ void face_mixed(const DevBox& b, const MechF<NS>& m, 
 
 // Pass 2 over the tile list; CTA b takes tiles b, b + gridDim.x, ... (one
 // each with one CTA per tile; a persistent launch strides over the list).
-// The faces of all three directions of a tile form one list that the warps
-// take 32 at a time (a warp's faces share a direction), then one barrier,
-// then each cell sums its six faces: x, y, z in turn, each as
-// (F_lo - F_hi) / dx in double-float arithmetic on the FP32 pipe (the
-// difference of two FP32 fluxes exactly), rounded to FP64 once at the end;
-// about 48 significant bits, so the telescoping sum conserves to far below
-// the form's error.  Per-direction barriers would leave most warps
-// idle while the last few faces of a direction finish (288 faces of 8x8x4
-// cells on 256 threads take two rounds).
+// All faces of a tile, the three directions together, are evaluated before
+// one barrier (per-direction barriers would leave most warps idle while the
+// last faces of a direction finish: 288 faces of 8x8x4 cells on 256 threads
+// take two rounds): each thread the low x, y and z faces of its own cell,
+// then the tile's high boundary faces.  Then each cell sums its six faces,
+// each difference F_lo - F_hi of two staged FP32 fluxes taken exactly and
+// scaled by 1/dx in double-float arithmetic on the FP32 pipe (on cubic
+// cells the three differences summed first and scaled once), rounded to
+// FP64 once at the end: about 48 significant bits, so the telescoping sum
+// conserves to far below the form's error.
 template <int NS, bool MIX, class TL = TileDefault, bool STRICT = false>
 __global__ void __launch_bounds__(TL::NT, TL::MINB)
     flux_kernel_mixed(const DevBox* __restrict__ boxes, const int4* __restrict__ tiles, int ntiles,
@@ -1259,6 +1260,7 @@ __global__ void __launch_bounds__(TL::NT, TL::MINB)
   const bool diff = f.diffuse_vel || f.diffuse_temp || f.diffuse_spec || f.diffuse_enth;
   const int tx = threadIdx.x % TL::TX, ty = (threadIdx.x / TL::TX) % TL::TY, tz = threadIdx.x / (TL::TX * TL::TY);
   const ff dxi[3] = {ff_of(g.dxinv[0]), ff_of(g.dxinv[1]), ff_of(g.dxinv[2])};
+  const bool iso = g.dxinv[0] == g.dxinv[1] && g.dxinv[1] == g.dxinv[2];  // cubic cells
   for (int tb = blockIdx.x; tb < ntiles; tb += gridDim.x) {
     const int4 t = tiles[tb];
     const DevBox& b = boxes[t.x];
@@ -1331,13 +1333,24 @@ __global__ void __launch_bounds__(TL::NT, TL::MINB)
         ff acc[NVAR];
 #pragma unroll
         for (int n = 0; n < NVAR; ++n) acc[n] = ff_of(0.f);
+        int flo[3], fhi[3];
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
           const int nf0 = ext[0] + (d == 0), nf1 = ext[1] + (d == 1);
-          const int flo = FaceStage<NS, TL>::base(d) + tx + nf0 * (ty + nf1 * tz);
-          const int fhi = flo + ((d == 0) ? 1 : (d == 1) ? nf0 : nf0 * nf1);
+          flo[d] = FaceStage<NS, TL>::base(d) + tx + nf0 * (ty + nf1 * tz);
+          fhi[d] = flo[d] + ((d == 0) ? 1 : (d == 1) ? nf0 : nf0 * nf1);
+        }
+        if (iso) {  // one 1/dx: the three exact differences summed, then scaled once
 #pragma unroll
-          for (int n = 0; n < NVAR; ++n) acc[n] = ff_add(ff_mul(fs.diff(n, flo, fhi), dxi[d]), acc[n]);
+          for (int n = 0; n < NVAR; ++n)
+            acc[n] = ff_mul(ff_add(ff_add(fs.diff(n, flo[0], fhi[0]), fs.diff(n, flo[1], fhi[1])),
+                                   fs.diff(n, flo[2], fhi[2])),
+                            dxi[0]);
+        } else {
+#pragma unroll
+          for (int d = 0; d < 3; ++d)
+#pragma unroll
+            for (int n = 0; n < NVAR; ++n) acc[n] = ff_add(ff_mul(fs.diff(n, flo[d], fhi[d]), dxi[d]), acc[n]);
         }
         // to FP64: on the integer pipe (and one FP64 addition) unless a lane
         // of the warp holds a subnormal, infinite or NaN part
