@@ -1161,10 +1161,11 @@ __device__ __forceinline__ void diffusion_face_f(const DevBox& b, const DevFlags
 
 // Dynamic shared memory of the mixed-precision flux pass: the
 // face fluxes of all three directions of a tile at once, FP32 except the
-// total and internal energy fluxes (double-float pairs).
+// total and internal energy fluxes (double-float pairs); the temperature
+// component, whose flux is zero, is not staged.
 template <int NS, class TL>
 constexpr size_t mixed_flux_smem_bytes() {
-  return (size_t)(TL::F0 + TL::F1 + TL::F2) * (2 * sizeof(double) + sizeof(float) * (7 + NS));
+  return (size_t)(TL::F0 + TL::F1 + TL::F2) * (2 * sizeof(double) + sizeof(float) * (4 + NS));
 }
 
 // Shared-memory staging of the face fluxes of a tile, all three directions
@@ -1175,8 +1176,10 @@ template <int NS, class TL>
 struct FaceStage {
   static constexpr int TOT = TL::F0 + TL::F1 + TL::F2;
   float2* e;  // [2][TOT]: UEDEN, UEINT
-  float* v;   // [7 + NS][TOT]
+  float* v;   // [4 + NS][TOT]: rho, the momenta, the species (row()); UTEMP's flux is zero
   __device__ static constexpr int base(int d) { return d == 0 ? 0 : d == 1 ? TL::F0 : TL::F0 + TL::F1; }
+  // the row of v holding component n (not UEDEN, UEINT, UTEMP)
+  __device__ static constexpr int row(int n) { return n < UEDEN ? n : n - 3; }
   // F(slot, n) - F(slot2, n) for component n, exactly for the FP32
   // components (TwoSum), to double-float accuracy for the energy fluxes
   __device__ ff diff(int n, int slot, int slot2) const {
@@ -1184,7 +1187,8 @@ struct FaceStage {
       const float2 a = e[(n == UEINT) * TOT + slot], c = e[(n == UEINT) * TOT + slot2];
       return ff_sub(ff{a.x, a.y}, ff{c.x, c.y});
     }
-    return ff_sum(v[n * TOT + slot], -v[n * TOT + slot2]);
+    if (n == UTEMP) return ff_of(0.f);
+    return ff_sum(v[row(n) * TOT + slot], -v[row(n) * TOT + slot2]);
   }
   // the staged flux of component n as a double (the FP32 ones widened
   // exactly, on the integer pipe where they are normal or zero)
@@ -1193,7 +1197,8 @@ struct FaceStage {
       const float2 a = e[(n == UEINT) * TOT + slot];
       return ff_to_double(ff{a.x, a.y});
     }
-    return f2d_exact(v[n * TOT + slot]);
+    if (n == UTEMP) return 0.0;
+    return f2d_exact(v[row(n) * TOT + slot]);
   }
 };
 
@@ -1226,9 +1231,9 @@ __device__ __forceinline__ void face_mixed(const DevBox& b, const MechF<NS>& m, 
   const int rowt1 = d == 0 ? UMY : UMX, rowt2 = d == 2 ? UMY : UMZ;  // rows of the transverse momenta
 #pragma unroll
   for (int n = 0; n < NVAR; ++n) {
-    if (n == UEDEN || n == UEINT) continue;
-    const int row = n == UMX ? UMX + d : (n == UMY ? rowt1 : (n == UMZ ? rowt2 : n));
-    fs.v[row * TOT + slot] = F[n];
+    if (n == UEDEN || n == UEINT || n == UTEMP) continue;  // UTEMP's flux is zero
+    const int comp = n == UMX ? UMX + d : (n == UMY ? rowt1 : (n == UMZ ? rowt2 : n));
+    fs.v[FaceStage<NS, TL>::row(comp) * TOT + slot] = F[n];
   }
   const ff fe = ff_add(FE, F[UEDEN]);
   fs.e[slot] = make_float2(fe.hi, fe.lo);
