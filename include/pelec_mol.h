@@ -231,7 +231,10 @@ int pc_mol_rhs_level_per_box(pc_mol_handle* h, const pc_box_desc* boxes,
  * getMOLSrcTerm hands to the flux registers for refluxing on multi-level
  * runs (Diffusion.cpp:652-670).  fluxes[3*b + d] covers
  * surroundingNodes(valid_b, d); the RHS is the same as without the export.
- * PC_PRECISION_FP64 and PC_PRECISION_FP64_RCP.  Asynchronous on stream. */
+ * Every precision; with the mixed forms the fluxes are their FP32 face
+ * fluxes (the energy fluxes double-float; the normal-momentum flux with the
+ * reference pressure mixed_p_ref added back) times the area, in FP64, so that
+ * -sum_d (F(hi) - F(lo)) / V reproduces their RHS.  Asynchronous on stream. */
 int pc_mol_rhs_level_fluxes(pc_mol_handle* h, const pc_box_desc* boxes, int nboxes, const double dx[3],
                             const pc_array4* fluxes, void* stream);
 

@@ -1205,11 +1205,11 @@ struct FaceStage {
 // One face of direction d (index fi in the tile's face block of that
 // direction, nf0 x nf1 x nf2): hydrodynamic and diffusion fluxes, staged
 // (the rotated momentum components at their axes).
-template <int NS, bool MIX, class TL>
+template <int NS, bool MIX, class TL, bool EXPORT>
 __device__ __forceinline__ void face_mixed(const DevBox& b, const MechF<NS>& m, const DevMech<NS>& md,
                                            const DevFlags& f, const int o[3], const long long stv[3], int d, int fi,
                                            int nf0, int nf1, bool diff, const FaceConsts& fc,
-                                           const FaceStage<NS, TL>& fs) {
+                                           const FaceStage<NS, TL>& fs, const FluxBox* fxb, const Geo& g) {
   constexpr int NVAR = 7 + NS;
   const int fx = fi % nf0, fy = (fi / nf0) % nf1, fz = fi / (nf0 * nf1);
   const int i = o[0] + fx, j = o[1] + fy, k = o[2] + fz;
@@ -1238,6 +1238,25 @@ __device__ __forceinline__ void face_mixed(const DevBox& b, const MechF<NS>& m, 
   const ff fe = ff_add(FE, F[UEDEN]);
   fs.e[slot] = make_float2(fe.hi, fe.lo);
   fs.e[TOT + slot] = make_float2(FEI.hi, FEI.lo);
+  // Export (refluxing), times the face area, in FP64; the normal-momentum
+  // flux gets back the p_ref the FP32 form leaves out.  A face shared by two
+  // tiles is written twice, with the same values.  A separate instantiation
+  // (EXPORT), so that the plain pass carries none of it.
+  if constexpr (EXPORT) {
+    const double A = d == 0 ? g.area[0] : (d == 1 ? g.area[1] : g.area[2]);
+    double* q = fxb->p[d] + (i - fxb->b[d][0]) + (long long)(j - fxb->b[d][1]) * fxb->js[d] +
+                (long long)(k - fxb->b[d][2]) * fxb->ks[d];
+    const long long ns = fxb->ns[d];
+#pragma unroll
+    for (int n = 0; n < NVAR; ++n) {
+      if (n == UEDEN || n == UEINT || n == UTEMP) continue;
+      const int comp = n == UMX ? UMX + d : (n == UMY ? rowt1 : (n == UMZ ? rowt2 : n));
+      q[comp * ns] = (n == UMX ? f2d_exact(F[n]) + g.p_ref : f2d_exact(F[n])) * A;
+    }
+    q[UEDEN * ns] = ff_to_double(fe) * A;
+    q[UEINT * ns] = ff_to_double(FEI) * A;
+    q[UTEMP * ns] = 0.0;
+  }
 }
 
 // Pass 2 over the tile list; CTA b takes tiles b, b + gridDim.x, ... (one
@@ -1252,11 +1271,11 @@ __device__ __forceinline__ void face_mixed(const DevBox& b, const MechF<NS>& m, 
 // cells the three differences summed first and scaled once), rounded to
 // FP64 once at the end: about 48 significant bits, so the telescoping sum
 // conserves to far below the form's error.
-template <int NS, bool MIX, class TL = TileDefault, bool STRICT = false>
+template <int NS, bool MIX, class TL = TileDefault, bool STRICT = false, bool EXPORT = false>
 __global__ void __launch_bounds__(TL::NT, TL::MINB)
     flux_kernel_mixed(const DevBox* __restrict__ boxes, const int4* __restrict__ tiles, int ntiles,
                       const __grid_constant__ MechF<NS> m, const __grid_constant__ DevMech<NS> md, const DevFlags f,
-                      const Geo g, unsigned long long* __restrict__ counters) {
+                      const Geo g, unsigned long long* __restrict__ counters, const FluxBox* __restrict__ fluxes) {
   constexpr int NVAR = 7 + NS;
   extern __shared__ double flux_dyn_smem[];
   FaceStage<NS, TL> fs;
@@ -1274,6 +1293,7 @@ __global__ void __launch_bounds__(TL::NT, TL::MINB)
                         min(TL::TZ, b.hi[2] - o[2] + 1)};
     const bool mine = tx < ext[0] && ty < ext[1] && tz < ext[2];
     const long long stv[3] = {1, b.n2[0], (long long)b.n2[0] * b.n2[1]};
+    const FluxBox* fxb = EXPORT ? fluxes + t.x : nullptr;
     __shared__ FaceConsts fc;  // the box's reference velocity, 1/dx, p_ref
     if (threadIdx.x == 0) face_consts(b, g, fc);
     __syncthreads();
@@ -1308,7 +1328,8 @@ __global__ void __launch_bounds__(TL::NT, TL::MINB)
         }
         if (act) {
           const int nf0 = ext[0] + (d == 0), nf1 = ext[1] + (d == 1);
-          face_mixed<NS, MIX, TL>(b, m, md, f, o, stv, d, c0 + nf0 * (c1 + nf1 * c2), nf0, nf1, diff, fc, fs);
+          face_mixed<NS, MIX, TL, EXPORT>(b, m, md, f, o, stv, d, c0 + nf0 * (c1 + nf1 * c2), nf0, nf1, diff, fc,
+                                          fs, fxb, g);
         }
       }
     }
@@ -1384,21 +1405,23 @@ __global__ void __launch_bounds__(TL::NT, TL::MINB)
 }
 
 // Host: launch the mixed flux pass at tile shape TL, one CTA per tile or
-// (persistent) as many CTAs as are resident on the device at once.
-template <int NS, bool MIX, class TL, bool STRICT = false>
-inline cudaError_t launch_flux_mixed_at(const DevBox* boxes, const int4* tiles, int ntiles, const MechF<NS>& mf,
-                                        const DevMech<NS>& md, const DevFlags& f, const Geo& g,
-                                        unsigned long long* counters, cudaStream_t s, bool persistent) {
+// (persistent) as many CTAs as are resident on the device at once; with
+// fluxes, the instantiation that also exports the face fluxes.
+template <int NS, bool MIX, class TL, bool STRICT, bool EXPORT>
+inline cudaError_t launch_flux_mixed_kernel(const DevBox* boxes, const int4* tiles, int ntiles, const MechF<NS>& mf,
+                                            const DevMech<NS>& md, const DevFlags& f, const Geo& g,
+                                            unsigned long long* counters, cudaStream_t s, bool persistent,
+                                            const FluxBox* fluxes) {
   static std::atomic<unsigned long long> opted{0};  // bit per device
   static std::atomic<int> resident[64];             // persistent grid per device (0: not known yet)
   constexpr size_t smem = mixed_flux_smem_bytes<NS, TL>();
-  if (ntiles <= 0) return cudaSuccess;
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
   const unsigned long long bit = (dev >= 0 && dev < 64) ? (1ull << dev) : 0ull;
   if (!bit || !(opted.load() & bit)) {
-    e = cudaFuncSetAttribute(flux_kernel_mixed<NS, MIX, TL, STRICT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    e = cudaFuncSetAttribute(flux_kernel_mixed<NS, MIX, TL, STRICT, EXPORT>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     opted.fetch_or(bit);
   }
@@ -1406,13 +1429,25 @@ inline cudaError_t launch_flux_mixed_at(const DevBox* boxes, const int4* tiles, 
   if (persistent) {
     int r = bit ? resident[dev].load() : 0;
     if (r <= 0) {
-      r = resident_ctas(flux_kernel_mixed<NS, MIX, TL, STRICT>, TL::NT, smem);
+      r = resident_ctas(flux_kernel_mixed<NS, MIX, TL, STRICT, EXPORT>, TL::NT, smem);
       if (bit && r > 0) resident[dev].store(r);
     }
     if (r > 0 && r < grid) grid = r;
   }
-  flux_kernel_mixed<NS, MIX, TL, STRICT><<<grid, TL::NT, smem, s>>>(boxes, tiles, ntiles, mf, md, f, g, counters);
+  flux_kernel_mixed<NS, MIX, TL, STRICT, EXPORT><<<grid, TL::NT, smem, s>>>(boxes, tiles, ntiles, mf, md, f, g,
+                                                                              counters, fluxes);
   return cudaGetLastError();
+}
+template <int NS, bool MIX, class TL, bool STRICT = false>
+inline cudaError_t launch_flux_mixed_at(const DevBox* boxes, const int4* tiles, int ntiles, const MechF<NS>& mf,
+                                        const DevMech<NS>& md, const DevFlags& f, const Geo& g,
+                                        unsigned long long* counters, cudaStream_t s, bool persistent,
+                                        const FluxBox* fluxes = nullptr) {
+  if (ntiles <= 0) return cudaSuccess;
+  return fluxes ? launch_flux_mixed_kernel<NS, MIX, TL, STRICT, true>(boxes, tiles, ntiles, mf, md, f, g, counters, s,
+                                                                      persistent, fluxes)
+                : launch_flux_mixed_kernel<NS, MIX, TL, STRICT, false>(boxes, tiles, ntiles, mf, md, f, g, counters,
+                                                                       s, persistent, nullptr);
 }
 
 }  // namespace pcg

@@ -26,7 +26,7 @@ namespace pcg {
 int launch_mixed(int nspec, int tile, bool persistent, bool strict, const DevBox* boxes, const int2* items,
                  int nitems, const int4* tiles, int ntiles, const MechSet& ms, const DevFlags& f, const Geo& g,
                  double p_ref, unsigned long long* counters, cudaStream_t s, cudaEvent_t e0, cudaEvent_t e1,
-                 cudaEvent_t e2);
+                 cudaEvent_t e2, const FluxBox* fx);
 cudaError_t launch_flux_fp64_tile(int tile, bool persistent, int nspec, const DevBox* boxes, const int4* tiles,
                                   int ntiles, const MechSet& ms, const DevFlags& f, const Geo& g,
                                   unsigned long long* counters, cudaStream_t s, const FluxBox* fx);
@@ -510,7 +510,8 @@ int run(pc_mol_handle* h, const pc_box_desc* boxes, int nboxes, const double dx[
       const int rc = launch_mixed(h->variant, h->lay_tile, h->tile >= kNumTiles,
                                   h->cfg.precision == PC_PRECISION_MIXED_FP64, h->d_boxes, h->d_items + ib, ie - ib,
                                   h->d_tiles + tb, te - tb, h->mech, h->flags, gm, p_ref, h->d_counters, s,
-                                  timed ? h->ev[0] : nullptr, timed ? h->ev[1] : nullptr, timed ? h->ev[2] : nullptr);
+                                  timed ? h->ev[0] : nullptr, timed ? h->ev[1] : nullptr, timed ? h->ev[2] : nullptr,
+                                  fx);
       return rc == 0 ? PC_OK : cuda_fail(h, cudaGetLastError());
     }
     return with_species(h->variant, [&](auto ns) {
@@ -1312,7 +1313,6 @@ extern "C" int pc_mol_rhs_level_fluxes(pc_mol_handle* h, const pc_box_desc* boxe
                                        const pc_array4* fluxes, void* stream) {
   if (!h) return PC_ERR_INVALID_ARGUMENT;
   if (nboxes < 0 || (nboxes > 0 && (!boxes || !fluxes))) return h->last_error = PC_ERR_INVALID_ARGUMENT;
-  if (is_mixed(h->cfg.precision)) return h->last_error = PC_ERR_UNSUPPORTED;
   const int nvar = 7 + h->cfg.nspec;
   std::vector<FluxBox> fb(nboxes);
   for (int b = 0; b < nboxes; ++b) {

@@ -7,16 +7,17 @@ namespace pcg {
 
 cudaError_t launch_flux_mixed_tile(int tile, bool persistent, bool strict, int nspec, const DevBox* boxes,
                                    const int4* tiles, int ntiles, const MechSet& ms, const DevFlags& f, const Geo& g,
-                                   double p_ref, unsigned long long* counters, cudaStream_t s);
+                                   double p_ref, unsigned long long* counters, cudaStream_t s, const FluxBox* fx);
 
 // Cell pass, then the flux pass at tile shape `tile` (0 = 8x8x4, launched
 // here; the others in pc_tiles_mixed.cu), persistent or one CTA per tile.
 // strict: PC_PRECISION_MIXED_FP64 (Newton solve, cell mass fractions and the
-// divergence in FP64) instead of their double-float forms.
+// divergence in FP64) instead of their double-float forms.  fx: the face
+// fluxes' export (refluxing), or null.
 int launch_mixed(int nspec, int tile, bool persistent, bool strict, const DevBox* boxes, const int2* items,
                  int nitems, const int4* tiles, int ntiles, const MechSet& ms, const DevFlags& f, const Geo& g,
                  double p_ref, unsigned long long* counters, cudaStream_t s, cudaEvent_t e0, cudaEvent_t e1,
-                 cudaEvent_t e2) {
+                 cudaEvent_t e2, const FluxBox* fx) {
   if (e0) cudaEventRecord(e0, s);
   cudaError_t e = with_species(nspec, [&](auto ns) {
     constexpr int NS = decltype(ns)::value;
@@ -34,13 +35,14 @@ int launch_mixed(int nspec, int tile, bool persistent, bool strict, const DevBox
     if (e1) cudaEventRecord(e1, s);
     if (tile == 0)
       return strict ? launch_flux_mixed_at<NS, P::MIX, TileDefault, true>(boxes, tiles, ntiles, mf, m, f, g, counters,
-                                                                          s, persistent)
+                                                                          s, persistent, fx)
                     : launch_flux_mixed_at<NS, P::MIX, TileDefault, false>(boxes, tiles, ntiles, mf, m, f, g,
-                                                                           counters, s, persistent);
+                                                                           counters, s, persistent, fx);
     return cudaSuccess;
   });
   if (tile != 0)
-    e = launch_flux_mixed_tile(tile, persistent, strict, nspec, boxes, tiles, ntiles, ms, f, g, p_ref, counters, s);
+    e = launch_flux_mixed_tile(tile, persistent, strict, nspec, boxes, tiles, ntiles, ms, f, g, p_ref, counters, s,
+                               fx);
   if (e2) cudaEventRecord(e2, s);
   return e == cudaSuccess && cudaGetLastError() == cudaSuccess ? 0 : 3;
 }

@@ -10,7 +10,7 @@ of the staged face fluxes, so periodic domain totals vanish to round-off.
 import numpy as np
 import pytest
 
-from gpu_util import gpu_rhs
+from gpu_util import gpu_rhs, to_multifab
 from pelec_gb300 import abi, mechanism, problems
 
 pytestmark = pytest.mark.gpu
@@ -81,6 +81,35 @@ def test_mixed_tiny_and_zero_species(cuda_lib, oracle_lib, form):
     assert np.all(np.isfinite(gpu))
     assert np.all(l2 <= _tol()), l2
     assert status.nonfinite_output == 0 and status.newton_nonconverged == 0
+
+
+@pytest.mark.parametrize("form", FORMS)
+def test_mixed_flux_export(cuda_lib, form):
+    """The mixed forms export their face fluxes for refluxing: -sum_d (F(hi)
+    - F(lo)) / V of the exported fluxes reproduces their RHS cell by cell (to
+    round-off of the flux scale max |F| / V), and each component is within
+    1e-5 of its largest FP64 flux of the FP64 form's export (the normal
+    momentum flux with p_ref added back)."""
+    mech, st, _ = problems.flame((24, 20, 32), seed=44)
+    vol = float(np.prod(st.dx))
+
+    def run(prec):
+        op = cuda_lib.MOLOperator(problems.make_config(mech, precision=prec))
+        R = cuda_lib.MultiFab([(st.lo, st.hi)], st.S.shape[0], 0)
+        F, = op.rhs_level_fluxes(to_multifab(cuda_lib, [st], st.ng), R, st.dx)
+        return [f.cpu().numpy() for f in F], R.fabs[0].cpu().numpy()
+
+    Fm, Rm = run(form)
+    F64, _ = run(abi.PC_PRECISION_FP64)
+    # F[d]: (component, z, y, x) over the faces of direction d
+    div = -(np.diff(Fm[0], axis=3) + np.diff(Fm[1], axis=2) + np.diff(Fm[2], axis=1)) / vol
+    for n in range(Rm.shape[0]):
+        scale = max(np.abs(Fm[d][n]).max() for d in range(3)) / vol
+        err = np.abs(div[n] - Rm[n]).max()
+        assert err <= 1e-13 * max(scale, 1e-300), (n, err, scale)
+        big = max(np.abs(F64[d][n]).max() for d in range(3))
+        diff = max(np.abs(Fm[d][n] - F64[d][n]).max() for d in range(3))
+        assert diff <= 1e-5 * big or (big == 0.0 and diff == 0.0), (n, diff, big)
 
 
 @pytest.mark.parametrize("form", FORMS)
