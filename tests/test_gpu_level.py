@@ -126,17 +126,19 @@ def test_autotune_caches_choice_per_histogram(cuda_lib):
     assert op.current_tile() == 0
 
 
-def test_graph_replay_equals_direct_calls(cuda_lib):
+@pytest.mark.parametrize("precision", [abi.PC_PRECISION_FP64, abi.PC_PRECISION_MIXED])
+def test_graph_replay_equals_direct_calls(cuda_lib, precision):
     """Graph of ghost fill + RHS on a 2x2x2 split periodic flame: the replay
-    equals fill_ghosts + rhs_level, reads the arrays' current contents on
-    every replay, and is not disturbed by later calls through the handle."""
+    equals fill_ghosts + rhs_level (bit for bit, in either precision), reads
+    the arrays' current contents on every replay, and is not disturbed by
+    later calls through the handle."""
     import torch
 
     from test_gpu_advance import _split
 
     mol = cuda_lib
     mech, st, _ = problems.flame((24, 16, 16), seed=34)
-    cfg = problems.make_config(mech)
+    cfg = problems.make_config(mech, precision=precision)
     geom = abi.geometry((0, 0, 0), (23, 15, 15), (0, 0, 0), (0, 0, 0))
     boxes = _split(st, 2)
     op = mol.MOLOperator(cfg)

@@ -113,6 +113,21 @@ def test_mixed_flux_export(cuda_lib, form):
 
 
 @pytest.mark.parametrize("form", FORMS)
+def test_mixed_uneven_level_batched_vs_per_box(cuda_lib, form):
+    """An uneven BoxArray: one batched launch of the mixed passes equals
+    per-box launches bit for bit (a tile's faces and cells are computed the
+    same whatever else the launch holds)."""
+    mech, boxes = problems.level_boxes(nboxes=7, seed=21, edges=(8, 16, 24))
+    cfg = problems.make_config(mech, precision=form)
+    batched, st1 = gpu_rhs(cuda_lib, cfg, boxes)
+    perbox, _ = gpu_rhs(cuda_lib, cfg, boxes, per_box=True)
+    for g1, g2 in zip(batched, perbox):
+        np.testing.assert_array_equal(g1, g2)
+        assert np.all(np.isfinite(g1))
+    assert st1.cells == sum(b.ncells for b in boxes)
+
+
+@pytest.mark.parametrize("form", FORMS)
 def test_mixed_flame_128_vs_fp64_gpu(cuda_lib, form):
     """Full C2 size against the FP64 path (which matches the oracle bit for bit)."""
     mech, st, _ = problems.flame((128, 128, 128), seed=1)
