@@ -106,10 +106,10 @@ __host__ MechF<NS> to_float(const DevMech<NS>& m, double p_ref) {
 // fractions X_k and the temperature (X_0 X_1 | X_2 X_3 | ... | T last), then
 // (rho, R/Wbar) (R/Wbar with the ideal-mixture EOS only) and, with the
 // ideal-mixture EOS, the mixture NASA-7 coefficients C_n = sum_k Y_k (R/W_k)
-// a_{n,k} of both temperature ranges, three groups a range.  X and T enter the diffusion fluxes only through
-// differences between neighbouring cells, which FP32 values would resolve to
-// no better than 1e-4 K / 1e-7 (the flame's second differences of T are a
-// few K per cell).  rho, R/Wbar and C are the cell's part of the Godunov
+// a_{n,k} of both temperature ranges, three groups a range.  X and T enter
+// the diffusion fluxes only through differences between neighbouring cells,
+// which FP32 values would resolve to no better than 1e-4 K / 1e-7 (the
+// flame's second differences of T are a few K per cell).  rho, R/Wbar and C are the cell's part of the Godunov
 // state's density and mixture sums (energy fluxes, hydro_face_f), to which a
 // face adds only FP32 increments.  The fields start after the FP32 groups
 // (MRec) of every cell; a mixed record stays within the FP64 record's size.
@@ -179,7 +179,7 @@ __device__ __forceinline__ float4 pair_group(ff a, ff b) { return make_float4(a.
 __device__ __forceinline__ float pair_diff(ff a, ff b) {
   return __fadd_rn(__fsub_rn(a.hi, b.hi), __fsub_rn(a.lo, b.lo));
 }
-// X_0..X_{NS-1} and T (NS + 1 pairs) from their groups at cell c
+// X_0..X_{NS-1} and T (NS + 1 pairs) into their groups at cell c
 template <int NS>
 __device__ __forceinline__ void st_xt(float4* xr, long long N, const ff* X, ff T) {
 #pragma unroll
