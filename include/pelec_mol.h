@@ -430,12 +430,15 @@ int pc_mol_check_quotients(const double* a, const double* b, double* q, long lon
  * box that does not fit (larger than about 46^3 valid cells with 9 species,
  * 67^3 with one, 36^3 with 21) returns PC_ERR_TOO_LARGE before anything is
  * launched.  The first call
- * on each device does the one-time set-up — it looks up that array's device
- * address and raises the flux kernels' shared-memory limit — so make that
- * first call before any stream capture.  Every call reuses the same array: calls
- * whose work overlaps on the GPU (other streams, other host threads) race
- * and must be serialised by the caller.  Only PC_PRECISION_FP64 is
- * supported.  Asynchronous on stream; no diagnostic counters are returned. */
+ * on each device, and per precision, does the one-time set-up — it looks up
+ * that array's device address and raises the flux kernels' shared-memory
+ * limit — so make that first call before any stream capture.  Every call
+ * reuses the same array: calls whose work overlaps on the GPU (other
+ * streams, other host threads) race and must be serialised by the caller.
+ * PC_PRECISION_FP64, PC_PRECISION_MIXED and PC_PRECISION_MIXED_FP64 (the
+ * mixed records fit the same array); PC_PRECISION_FP64_RCP returns
+ * PC_ERR_UNSUPPORTED.  Asynchronous on stream; no diagnostic counters are
+ * returned. */
 int pc_mol_rhs_box_static(const pc_mol_config* cfg, const pc_box_desc* box, const double dx[3], void* stream);
 
 #ifdef __cplusplus

@@ -812,7 +812,7 @@ extern "C" int pc_mol_rhs_box_static(const pc_mol_config* cfg, const pc_box_desc
   if (!cfg || !box || !dx) return PC_ERR_INVALID_ARGUMENT;
   const pc_mol_config& c = *cfg;
   if (c.nspec != c.mech.nspec) return PC_ERR_INVALID_ARGUMENT;
-  if (c.precision != PC_PRECISION_FP64) return PC_ERR_UNSUPPORTED;
+  if (c.precision != PC_PRECISION_FP64 && !is_mixed(c.precision)) return PC_ERR_UNSUPPORTED;
   for (int d = 0; d < 3; ++d)
     if (!(dx[d] > 0.0) || !std::isfinite(dx[d])) return PC_ERR_INVALID_ARGUMENT;
   const int variant = compiled_variant(c);
@@ -893,6 +893,14 @@ extern "C" int pc_mol_rhs_box_static(const pc_mol_config* cfg, const pc_box_desc
   static_lists_kernel<<<(unsigned)((nlist + 255) / 256), 256, 0, s>>>(d, (int)nitems, (int)ntiles, nt[0], nt[1], dbox,
                                                                        items, tiles, ctr);
   const Geo g = make_geo(dx);
+  if (is_mixed(c.precision)) {  // the mixed passes on the same lists and scratch (its records are smaller)
+    const double p_ref = c.mixed_p_ref > 0.0 ? c.mixed_p_ref : 1013250.0;
+    Geo gm = g;
+    gm.p_ref = p_ref;
+    const int r = launch_mixed(variant, 0, false, c.precision == PC_PRECISION_MIXED_FP64, dbox, items, (int)nitems,
+                               tiles, (int)ntiles, ms, fl, gm, p_ref, ctr, s, nullptr, nullptr, nullptr, nullptr);
+    return r == 0 && cudaGetLastError() == cudaSuccess ? PC_OK : PC_ERR_CUDA;
+  }
   const bool ok = with_species(variant, [&](auto ns) {
     constexpr int NS = decltype(ns)::value;
     using P = Physics<NS>;

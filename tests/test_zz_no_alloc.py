@@ -4,7 +4,8 @@ example code running under a memory pool that forbids other allocations, or
 an application that reserved all device memory at start-up).
 
 It must give the same right-hand side as pc_mol_rhs_level on the same box —
-bit for bit, since it launches the same FP64 kernels — on consecutive calls
+bit for bit, since it launches the same kernels (FP64, and the mixed forms)
+— on consecutive calls
 that reuse its fixed device array, and must refuse a box that does not fit
 that array.  This file is collected last so that a run stopping at the first
 failure has already run every other test.
@@ -69,6 +70,25 @@ def test_static_entry_matches_level_entry_on_consecutive_calls(cuda_lib):
         np.testing.assert_array_equal(R, ref)  # the same kernels: the same bits
     # the repeated box gives the same answer after other boxes used the array
     np.testing.assert_array_equal(outs[0], outs[4])
+
+
+@pytest.mark.parametrize("precision", [abi.PC_PRECISION_MIXED, abi.PC_PRECISION_MIXED_FP64])
+def test_static_entry_mixed_matches_level_entry(cuda_lib, precision):
+    """The mixed forms through the static entry: the same kernels as
+    pc_mol_rhs_level, so the same bits, at 9 and 21 species and one species
+    (GammaLaw), on consecutive calls."""
+    mol = cuda_lib
+    mech9, flame, _ = problems.flame((20, 16, 12), seed=36)
+    mech1, tgv = problems.tgv(24, seed=37)
+    mech21, flame21, _ = problems.flame((16, 12, 20), seed=38, mech=mechanism.drm_synthetic())
+    cases = [(problems.make_config(m, precision=precision), st)
+             for m, st in ((mech9, flame), (mech1, tgv), (mech21, flame21))]
+    for cfg, st in cases:
+        rc, R = _run_static(mol, cfg, st)
+        assert rc == abi.PC_OK, mol.error_string(rc)
+        (ref,), _ = gpu_rhs(mol, cfg, [st])
+        assert np.all(np.isfinite(R))
+        np.testing.assert_array_equal(R, ref)
 
 
 def test_static_entry_rejects_a_box_that_does_not_fit(cuda_lib):
