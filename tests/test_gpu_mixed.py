@@ -128,6 +128,24 @@ def test_mixed_uneven_level_batched_vs_per_box(cuda_lib, form):
 
 
 @pytest.mark.parametrize("form", FORMS)
+def test_mixed_anisotropic_cells(cuda_lib, oracle_lib, form):
+    """Cells of unequal sides: the divergence takes its general form (a
+    double-float scaling by 1/dx per direction; cubic cells sum the three
+    differences first), within the bar of the FP64 oracle."""
+    import dataclasses
+
+    mech, st, _ = problems.flame((24, 20, 32), seed=45)
+    st = dataclasses.replace(st, dx=(1.0e-3, 1.25e-3, 0.8e-3))
+    ref, = oracle_lib.mol_rhs(problems.make_config(mech), [st])
+    (gpu,), status = gpu_rhs(cuda_lib, problems.make_config(mech, precision=form), [st])
+    l2 = rel_l2(gpu, ref)
+    print(form, "anisotropic cells rel L2 per component:", l2)
+    assert np.all(np.isfinite(gpu))
+    assert np.all(l2 <= _tol()), l2
+    assert status.nonfinite_output == 0
+
+
+@pytest.mark.parametrize("form", FORMS)
 def test_mixed_flame_128_vs_fp64_gpu(cuda_lib, form):
     """Full C2 size against the FP64 path (which matches the oracle bit for bit)."""
     mech, st, _ = problems.flame((128, 128, 128), seed=1)
